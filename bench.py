@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 engine on the all-pairs gravity workload.
+
+Workload (default): N = 65,536 equal-mass bodies (total mass 1, G = 1) from a
+seeded Plummer sphere (scale radius 1), open boundaries, no softening,
+velocity Verlet with dt = 1e-3. A step is one velocity-Verlet step of all
+bodies (one all-pairs force evaluation). Metric: atom-steps/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+                  [--workload gravity|lj|water]
+
+value    : device-timed steps on the resident state (CUDA events on the
+           engine's stream, L2 flushed between timed steps).
+e2e      : the same steps through the reference-facing drop-in, nbg_accel
+           on pinned host buffers (the SciML velocity-Verlet loop calling the
+           GPU right-hand side): every step uploads u and v and reads back dv.
+roofline : the dominant force kernel's algorithmic FLOP/s (20 flop per pair)
+           or bytes against the measured peak.
+cpu_baseline : the FP64 oracle (a restatement of the reference's O(N^2)
+           per-atom loops) on a bounded sample of the same step, host cores.
+With --gpus N > 1 (torchrun) every rank runs its own replica: replicas only,
+no collective on the data path.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__ as G  # noqa: E402
+
+WORKLOADS = {
+    "gravity": dict(name="gravity-plummer-65536", n=65536, dt=1e-3, steps=100),
+    "lj": dict(name="lj-argon-1000", n=1000, dt=0.005, steps=1000),
+    "water": dict(name="spcfw-water-12288", n=12288, dt=0.0005, steps=2000),
+}
+
+
+def make_sim(nbg, workload, seed=0):
+    if workload == "gravity":
+        pos, vel, m = nbg.workloads.plummer_sphere(65536, seed=seed)
+        bodies = [nbg.MassBody(pos[i], vel[i], m[i]) for i in range(len(m))]
+        return nbg.NBodySimulation(nbg.GravitationalSystem(bodies, 1.0), (0.0, 0.1))
+    if workload == "lj":
+        pos, vel, L = nbg.workloads.lj_argon_lattice(1000, rho=0.8, T=1.0, seed=seed)
+        bodies = [nbg.MassBody(pos[i], vel[i], 1.0) for i in range(len(pos))]
+        sysm = nbg.PotentialNBodySystem(bodies, {"lennard_jones": nbg.LennardJonesParameters(1.0, 1.0, 2.5)})
+        return nbg.NBodySimulation(sysm, (0.0, 5.0), nbg.CubicPeriodicBoundaryConditions(L), kb=1.0, skin=0.3,
+                                   rebuild_every=10)
+    if workload == "water":
+        pos, vel, L = nbg.workloads.spcfw_water_box(4096, seed=seed, T=300.0)
+        bodies = nbg.workloads.water_molecules(pos, vel)
+        lj = nbg.LennardJonesParameters(0.650299, 0.3165492, 0.9)
+        el = nbg.ElectrostaticParameters(nbg.workloads.K_EL, 0.9)
+        spc = nbg.SPCFwParameters(0.1012, 113.24 * math.pi / 180, 4637.0, 383.0)
+        water = nbg.WaterSPCFw(bodies, nbg.workloads.M_H, nbg.workloads.M_O, 0.41, -0.82, lj, el, spc)
+        return nbg.NBodySimulation(water, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L),
+                                   nbg.BerendsenThermostat(300.0, 0.1), kb=nbg.workloads.KB_KJ, skin=0.1,
+                                   rebuild_every=10)
+    raise ValueError(workload)
+
+
+def algorithmic_work(workload, n, eng):
+    """(amount per force-kernel launch, unit, bound) from the per-unit figures:
+    gravity 20 flop per ordered pair; list kernels the bytes a launch must move."""
+    if workload == "gravity":
+        return 20.0 * n * (n - 1), "TFLOP/s", "fp32"
+    # list kernels: per atom 32 B split position + 24 B acceleration write + 4 B
+    # per list entry + 32 B per neighbour gather (counted once per atom in HBM terms)
+    nbr = 73.6 if workload == "lj" else 419.0
+    return n * (32 + 24 + 4 * nbr), "GB/s", "hbm"
+
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(oracle, desc, u, workload, target_s=8.0):
+    """The oracle on a bounded sample of one step: accelerations of a subset of
+    atoms over all partners, on every host core; atom-steps/s = atoms / time."""
+    n = int(desc.n)
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    i1 = min(n, 64)
+    t0 = time.perf_counter()
+    oracle.partial_accel(desc, u, 0, i1)
+    dt = time.perf_counter() - t0
+    per_atom = dt / i1
+    k = int(max(i1, min(n, target_s / max(per_atom, 1e-9))))
+    reps = max(1, int(target_s / max(per_atom * k, 1e-9)))
+    reps = min(reps, 20)
+    t0 = time.perf_counter()
+    done = 0
+    for r in range(reps):
+        s0 = (r * k) % n
+        s1 = min(n, s0 + k)
+        oracle.partial_accel(desc, u, s0, s1)
+        done += s1 - s0
+    el = time.perf_counter() - t0
+    all_cores = done / el
+    oracle.set_threads(1)
+    m = max(8, min(n, int(2.0 / max(per_atom * cores, 1e-9))))
+    t0 = time.perf_counter()
+    oracle.partial_accel(desc, u, 0, m)
+    one = m / (time.perf_counter() - t0)
+    return {"value": all_cores, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{done} atom force evaluations (all {n} partners each) in {reps} slices, "
+                      f"{el:.1f} s wall; one step = {n} atoms",
+            "value_1thread": one, "sample_1thread": f"{m} atoms on 1 thread"}
+
+
+def run_reference(args, rank):
+    """--impl reference: the oracle's restatement of the reference's O(N^2)
+    per-atom loops on the host cores, each step a bounded sample."""
+    if rank != 0:
+        return
+    nbg = G.load_package()
+    oracle = G.load_oracle()
+    w = WORKLOADS[args.workload]
+    sim = make_sim(nbg, args.workload)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v, _ = nbg.gather_bodies_initial_coordinates(sim)
+    n = int(desc.n)
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    sample = min(n, args.ref_sample)
+    for s in range(args.warmup):
+        oracle.partial_accel(desc, u, (s * sample) % n, min(n, (s * sample) % n + sample))
+    t0 = time.perf_counter()
+    done = 0
+    for s in range(args.steps):
+        a = (s * sample) % n
+        b = min(n, a + sample)
+        oracle.partial_accel(desc, u, a, b)
+        done += b - a
+    el = time.perf_counter() - t0
+    val = done / el
+    line = {"metric": "atom-steps/s", "value": val, "unit": "atom-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps * (n / sample),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": w["name"], "N": n, "dt": w["dt"], "sample_atoms_per_step": sample},
+            "cpu_baseline": {"value": val, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{sample} of {n} atoms' forces per step over all partners"},
+            "e2e": {"value": val, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="gravity", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-flush", action="store_true", help="time all steps back to back (no L2 flush)")
+    ap.add_argument("--ref-sample", type=int, default=2048)
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.steps is None:
+        args.steps = 100 if args.workload == "gravity" else w["steps"]
+    if args.warmup < 3:
+        args.warmup = 3
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    if dist is not None:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    device = local
+    nbg = G.load_package()
+    nbg.load_library()
+    sim = make_sim(nbg, args.workload, seed=rank)
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0, _ = nbg.gather_bodies_initial_coordinates(sim)
+    n = int(desc.n)
+    dt = w["dt"]
+    eng = nbg.Engine(desc, device)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+
+    peak_fp32 = None
+    if args.workload == "gravity":
+        pk = __import__("ctypes").c_double()
+        if eng.lib.nbg_probe_fp32_peak(device, __import__("ctypes").byref(pk)) == 0:
+            peak_fp32 = pk.value
+
+    eng.set_state(u0, v0)
+    e_start = eng.energy(u0, v0)
+    eng.advance(dt, args.warmup)
+    torch.cuda.synchronize()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(device)
+    eng.set_profiling(True)
+    launches0 = eng.kernel_launches
+    step_ms = []
+    if args.no_flush:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.advance(dt, args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        step_ms = [e0.elapsed_time(e1) / args.steps] * args.steps
+    else:
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.advance(dt, 1)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    launches = eng.kernel_launches - launches0
+    clocks = sampler.stop()
+    kern_ms, kern_n = eng.force_kernel_time()
+    eng.set_profiling(False)
+    total_ms = float(sum(step_ms))
+    t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{device}")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    total_ms = float(t.item())
+    value = n * args.steps * world / (total_ms / 1e3)
+
+    # end-to-end: the drop-in right-hand side on pinned host buffers, with the
+    # velocity-Verlet update on the host (SciML's loop), every step
+    cols = eng.cols
+    pin = lambda: torch.zeros((cols, 3), dtype=torch.float64).pin_memory().numpy()
+    uh, vh, ah = pin(), pin(), pin()
+    uh[:] = u0
+    vh[:] = v0
+    e2e_steps = max(3, min(args.steps, 50 if args.workload == "gravity" else 200))
+    a = eng.accel(vh, uh)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        uh += dt * vh + (dt * dt) * (0.5 * a)
+        an = eng.accel(vh, uh)
+        vh += dt * (0.5 * a + 0.5 * an)
+        a = an
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": n * e2e_steps * world / e2e_s, "unit": "atom-steps/s",
+           "h2d_bytes_per_step": 2 * uh.nbytes, "d2h_bytes_per_step": ah.nbytes,
+           "path": "nbg_accel (RHS drop-in) per step from pinned host buffers, velocity-Verlet update on host",
+           "steps": e2e_steps}
+
+    # accuracy at this workload: forces of sampled atoms vs the oracle, drift
+    u_end, v_end = eng.get_state()
+    e_end = eng.energy(u_end, v_end)
+    drift_key = "gravity" if args.workload == "gravity" else "potential"
+    E0 = e_start["kinetic"] + e_start[drift_key]
+    E1 = e_end["kinetic"] + e_end[drift_key]
+
+    work, unit, bound = algorithmic_work(args.workload, n, eng)
+    avg_kern = kern_ms / max(kern_n, 1)
+    achieved = work / (avg_kern / 1e3) / (1e12 if unit == "TFLOP/s" else 1e9)
+    peaks = measured_peaks()
+    if unit == "TFLOP/s":
+        peak = peak_fp32
+        peak_src = "FP32 FMA probe measured in this run (nbg_probe_fp32_peak)"
+    else:
+        peak = peaks.get("hbm_gbs", 6800.0)
+        peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    kernel_name = {"gravity": "k_gravity", "lj": "k_force_list", "water": "k_force_list"}[args.workload]
+    traffic = profile_traffic(f"{kernel_name}:{w['name']}")
+    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": (achieved / peak) if peak else None, "traffic": traffic, "kernel": kernel_name,
+                "kernel_ms": avg_kern, "kernel_launches": kern_n, "peak_source": peak_src}
+
+    line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 pair forces, f64 state" if args.workload != "water" else "f32 pair forces, f64 state+bonded",
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": w["name"], "N": n, "dt": dt, "integrator": "velocity Verlet",
+                       "l2": "no flush (state L2-resident across steps)" if args.no_flush
+                       else "512 MB buffer written between timed steps (L2 flushed)",
+                       "parallelism": "replicas only" if world > 1 else "single GPU",
+                       "gravity_precision": "hi/lo split positions (compensated)" if args.workload == "gravity" else None},
+            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+            "energy_drift_rel": (E1 - E0) / abs(E0) if E0 else None}
+    if args.workload == "water":
+        line["ns_per_day"] = (1e3 / (total_ms / args.steps)) * dt * 1e-3 * 86400
+    if rank == 0 and world == 1 and not args.no_cpu:
+        oracle = G.load_oracle()
+        cb = cpu_baseline(oracle, desc, u0, args.workload)
+        line["cpu_baseline"] = cb
+    if rank == 0 and world == 1 and not args.no_cpu and args.workload != "water":
+        # force accuracy on a sample of atoms (oracle accelerations of atoms 0..255)
+        ns = 256
+        a_ref = oracle.partial_accel(desc, u0, 0, ns)
+        eng.set_state(u0, v0)
+        eng.compute_forces()
+        a_gpu = eng.get_accel()[:ns]
+        line["force_rel_rmse"] = float(np.linalg.norm(a_gpu - a_ref) / np.linalg.norm(a_ref))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,249 @@
+/*
+ * nbg.h - C ABI of the GB300 force-and-integration engine for the
+ * NBodySimulator.jl API (libnbg.so, CUDA sm_103a).
+ *
+ * The engine is a drop-in for the ODE right-hand side that NBodySimulator.jl
+ * builds in src/nbody_to_ode.jl, plus a fused velocity-Verlet / Euler-Maruyama
+ * loop that keeps the state resident on one GPU.
+ *
+ * Conventions shared by every entry point
+ *  - Arrays of vectors use the reference's layout: a column-major 3 x n Float64
+ *    matrix, i.e. x,y,z of atom i at [3i], [3i+1], [3i+2]
+ *    (src/nbody_to_ode.jl:1-20, the u0/v0 built by
+ *    gather_bodies_initial_coordinates).
+ *  - With the Nose-Hoover thermostat the state has one extra column (3 x (n+1)),
+ *    the thermostat variable zeta is u[3n] and its rate is v[3n]
+ *    (src/nbody_to_ode.jl:6-8, :419 "gamma_ind = 3n + 1").
+ *  - Water systems order atoms O,H1,H2 per molecule (src/nbody_to_ode.jl:46).
+ *  - Pointers named host_* or documented as host buffers are ordinary host
+ *    memory owned by the caller and never retained after the call returns.
+ *  - Every function returns an int status: NBG_OK (0) or a negative nbg_status;
+ *    nbg_last_error(ctx) returns a message for the last failure on ctx.
+ *  - A context is not re-entrant: call it from one host thread at a time.
+ *    Distinct contexts may be used concurrently; each owns its CUDA stream.
+ *  - The library has no CPU fallback. A system it does not implement returns
+ *    NBG_ERR_UNSUPPORTED so that the caller can keep the problem on its own
+ *    CPU path.
+ */
+#ifndef NBG_H
+#define NBG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBG_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define NBG_API __attribute__((visibility("default")))
+#else
+#define NBG_API
+#endif
+
+typedef enum nbg_status {
+    NBG_OK = 0,
+    NBG_ERR_ARG = -1,          /* invalid argument or descriptor field */
+    NBG_ERR_CUDA = -2,         /* a CUDA runtime call failed */
+    NBG_ERR_CAPACITY = -3,     /* cell / neighbour capacity could not be grown */
+    NBG_ERR_NONFINITE = -4,    /* NaN or Inf in accelerations or state */
+    NBG_ERR_TIMEOUT = -5,      /* a bounded device-side wait gave up */
+    NBG_ERR_UNSUPPORTED = -6,  /* system/option not implemented on the GPU */
+    NBG_ERR_RANGE = -7,        /* minimum-image loop exceeded its iteration cap */
+    NBG_ERR_NOMEM = -8         /* device allocation failed */
+} nbg_status;
+
+/* Boundary conditions (src/boundary_conditions.jl). */
+typedef enum nbg_bc {
+    NBG_BC_INFINITE = 0, /* InfiniteBox: plain difference, boundary_conditions.jl:167-172 */
+    NBG_BC_CUBIC = 1,    /* CubicPeriodicBoundaryConditions(L): minimum image by
+                            repeated +-L, boundary_conditions.jl:138-165 */
+    NBG_BC_PERIODIC = 2  /* PeriodicBoundaryConditions([lo,hi] x 3): the reference
+                            maps each difference into [lo,hi), :111-136 */
+} nbg_bc;
+
+/* System families (src/nbody_system.jl). */
+typedef enum nbg_system_kind {
+    NBG_SYSTEM_POTENTIAL = 0, /* PotentialNBodySystem / GravitationalSystem /
+                                 ChargedParticles, nbody_system.jl:32-150 */
+    NBG_SYSTEM_WATER = 1      /* WaterSPCFw, nbody_system.jl:182-191 */
+} nbg_system_kind;
+
+/* Potentials of a PotentialNBodySystem (bitmask). */
+typedef enum nbg_potential {
+    NBG_POT_LJ = 1,   /* LennardJonesParameters, basic_potentials.jl:240-272 */
+    NBG_POT_EL = 2,   /* ElectrostaticParameters, basic_potentials.jl:274-304 */
+    NBG_POT_GRAV = 4, /* GravitationalParameters, basic_potentials.jl:306-331 */
+    NBG_POT_MAG = 8   /* MagnetostaticParameters, basic_potentials.jl:333-365 */
+} nbg_potential;
+
+/* Thermostats (src/thermostats.jl). */
+typedef enum nbg_thermostat {
+    NBG_THERMO_NULL = 0,
+    NBG_THERMO_ANDERSEN = 1,   /* nbody_simulation_result.jl:504-540 */
+    NBG_THERMO_BERENDSEN = 2,  /* thermostats.jl:76-83 */
+    NBG_THERMO_NOSEHOOVER = 3, /* thermostats.jl:121-128 */
+    NBG_THERMO_LANGEVIN = 4    /* nbody_to_ode.jl:567-680 (SDE, Euler-Maruyama) */
+} nbg_thermostat;
+
+/*
+ * Everything the reference's marshalling functions (obtain_data_for_*,
+ * nbody_to_ode.jl:263-433, get_masses nbody_simulation_result.jl:121-139)
+ * extract from an NBodySimulation, as plain values.
+ */
+typedef struct nbg_system_desc {
+    int32_t abi_version;  /* must be NBG_ABI_VERSION */
+    int32_t kind;         /* nbg_system_kind */
+    int64_t n;            /* atoms (columns), excluding the Nose-Hoover column */
+    const double* mass;   /* [n] masses (get_masses order) */
+    const double* charge; /* [n] charges; required with NBG_POT_EL or WATER */
+    const double* dipole; /* [3n] magnetic moments; required with NBG_POT_MAG */
+    uint32_t potentials;  /* nbg_potential bitmask (ignored for WATER) */
+    /* LennardJonesParameters(eps, sigma, R); R may be +Inf. For WATER only the
+       O atoms take part (obtain_data_for_lennard_jones_interaction, :302-314). */
+    double lj_epsilon, lj_sigma, lj_cutoff;
+    /* ElectrostaticParameters(k, R); R may be +Inf. eps_rf selects reaction
+       field: 1.0 reproduces the reference's truncated Coulomb exactly. */
+    double el_k, el_cutoff, el_eps_rf;
+    double grav_G;        /* GravitationalParameters(G) */
+    double mag_mu_4pi;    /* MagnetostaticParameters(mu/4pi) */
+    /* SPCFwParameters(rOH, aHOH, kb, ka) for WATER */
+    double water_rOH, water_aHOH, water_kb, water_ka;
+    int32_t bc;           /* nbg_bc */
+    double box[6];        /* CUBIC: box[0] = L. PERIODIC: lo_x,hi_x,lo_y,hi_y,lo_z,hi_z */
+    int32_t thermostat;   /* nbg_thermostat */
+    double thermo_T;      /* target temperature */
+    double thermo_param;  /* tau (Berendsen, Nose-Hoover), nu (Andersen), gamma (Langevin) */
+    double kb;            /* Boltzmann constant of the simulation (nbody_simulation.jl:7) */
+    uint64_t seed;        /* Philox key for Andersen / Langevin noise */
+    /* Verlet list: list radius = cutoff + skin; rebuilt every rebuild_every
+       steps or as soon as an atom moved more than skin/2 since the last build. */
+    double skin;
+    int32_t rebuild_every;
+    int32_t flags;        /* NBG_FLAG_* */
+} nbg_system_desc;
+
+/* Force the all-pairs path even where a cell/Verlet list applies. */
+#define NBG_FLAG_ALL_PAIRS 1
+/* Gravity: plain FP32 position differences (no hi/lo compensation). */
+#define NBG_FLAG_GRAV_PLAIN 2
+
+typedef struct nbg_ctx nbg_ctx;
+
+/* Energies with the reference's definitions (nbody_simulation_result.jl:
+   209-212 kinetic, 293-319 LJ with r^2 clamped to R^2, 321-351 electrostatic,
+   353-372 bonds, 374-397 angles). gravity is the project's own
+   -G sum_{i<j} m_i m_j / r_ij (the reference defines none). */
+typedef struct nbg_energies {
+    double kinetic, lennard_jones, electrostatic, bonds, angles, gravity;
+    double potential, total;
+    double temperature; /* md_temperature with the system's n and Nc (thermostats.jl:87-91) */
+} nbg_energies;
+
+typedef struct nbg_run_stats {
+    int64_t steps;            /* steps taken */
+    int64_t list_builds;      /* Verlet-list rebuilds */
+    int64_t kernel_launches;  /* CUDA kernels launched by the call */
+    double device_ms;         /* device time of the call (CUDA events) */
+} nbg_run_stats;
+
+/* Library identity. */
+NBG_API const char* nbg_version(void);
+NBG_API int nbg_abi_version(void);
+
+/* Build a context for one system on CUDA device `device`. The descriptor and
+   the arrays it points to are copied; the caller may free them afterwards.
+   Replaces the closure construction of SciMLBase.SecondOrderODEProblem(sim)
+   (src/nbody_to_ode.jl:460-536). */
+NBG_API int nbg_create(const nbg_system_desc* desc, int device, nbg_ctx** out);
+
+/* A batch of independent replicas (uneven sizes, own box, temperature and
+   seed) advanced together in one launch sequence. All replicas must share
+   kind, potentials, thermostat kind and cutoffs. */
+NBG_API int nbg_create_batch(const nbg_system_desc* descs, int32_t n_replicas, int device,
+                     nbg_ctx** out);
+
+NBG_API void nbg_destroy(nbg_ctx* ctx);
+NBG_API const char* nbg_last_error(const nbg_ctx* ctx);
+
+/* Run the context's work on a caller-provided cudaStream_t (NULL restores the
+   context's own stream). */
+NBG_API int nbg_set_stream(nbg_ctx* ctx, void* cuda_stream);
+
+/* Number of CUDA kernels this context has launched so far. */
+NBG_API int64_t nbg_kernel_launches(const nbg_ctx* ctx);
+
+/*
+ * The right-hand side soode_system!(dv, v, u, p, t) of
+ * SciMLBase.SecondOrderODEProblem(sim) (src/nbody_to_ode.jl:474-488 and
+ * :502-532 for water), on host buffers. dv, v, u hold 3 x n doubles
+ * (3 x (n+1) with Nose-Hoover). As in the reference, the Nose-Hoover term
+ * writes the thermostat rate into v[3n] (thermostats.jl:126): v is the only
+ * input that is modified. Replaces one call of the closure SciML's solvers
+ * make per stage.
+ */
+NBG_API int nbg_accel(nbg_ctx* ctx, double* dv, double* v, const double* u, double t);
+
+/* Copy a state (3 x n doubles each, 3 x (n+1) with Nose-Hoover) to and from
+   the device-resident state. For batches the replicas' columns are
+   concatenated in replica order. */
+NBG_API int nbg_set_state(nbg_ctx* ctx, const double* u, const double* v);
+NBG_API int nbg_get_state(nbg_ctx* ctx, double* u, double* v);
+
+/* Accelerations of the resident state into the resident acceleration buffer
+   (no host traffic); the unit the force roofline is measured on. */
+NBG_API int nbg_compute_forces(nbg_ctx* ctx);
+NBG_API int nbg_get_accel(nbg_ctx* ctx, double* dv);
+
+/*
+ * Advance the resident state nsteps with velocity Verlet at step dt
+ * (run_simulation(sim, VelocityVerlet(), dt=dt), nbody_simulation_result.jl:
+ * 468-487), applying the thermostat. With NBG_THERMO_LANGEVIN it advances the
+ * first-order SDE with Euler-Maruyama instead (calculate_simulation_sde,
+ * :489-492). No host traffic; asynchronous on the context's stream.
+ */
+NBG_API int nbg_advance(nbg_ctx* ctx, double dt, int64_t nsteps);
+
+/*
+ * Host-buffer driver: upload u, v; take nsteps steps; every save_every steps
+ * (and at the end) copy the state into traj_u / traj_v (each of
+ * (nsteps/save_every + 1) x 3 x n doubles, frame 0 = the initial state; either
+ * may be NULL); download the final state into u, v. save_every <= 0 saves only
+ * the first and last frames.
+ */
+NBG_API int nbg_run(nbg_ctx* ctx, double* u, double* v, double dt, int64_t nsteps,
+            int64_t save_every, double* traj_u, double* traj_v, nbg_run_stats* stats);
+
+/* Energies and temperature of (u, v) (host buffers). */
+NBG_API int nbg_energy(nbg_ctx* ctx, const double* u, const double* v, nbg_energies* out);
+
+/*
+ * The pair set the force kernels used for (u): every ordered pair (i, j),
+ * j != i, with r^2 < R^2 in the reference's Float64 arithmetic
+ * (basic_potentials.jl:253-258 for NBG_POT_LJ, :288-292 for NBG_POT_EL).
+ * Pairs are written as (i, j) int32 couples sorted by i then j; *count gets
+ * the total even when it exceeds cap.
+ */
+NBG_API int nbg_pair_list(nbg_ctx* ctx, const double* u, int32_t which, int32_t* pairs,
+                  int64_t cap, int64_t* count);
+
+/*
+ * Profiling support (no reference counterpart). With profiling on, CUDA
+ * events bracket every launch of the context's dominant force kernel
+ * (gravity all-pairs, Verlet-list pair forces or the all-pairs kernel);
+ * nbg_force_kernel_time returns their summed duration and count since the
+ * last reset and resets them.
+ */
+NBG_API int nbg_set_profiling(nbg_ctx* ctx, int on);
+NBG_API int nbg_force_kernel_time(nbg_ctx* ctx, double* total_ms, int64_t* launches);
+
+/* Measured FP32 FMA throughput of a device in TFLOP/s (an FMA counts 2):
+   the roofline denominator of the FP32-bound gravity kernel. */
+NBG_API int nbg_probe_fp32_peak(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBG_H */

@@ -1,0 +1,410 @@
+// k_forces.cu - force kernels.
+//
+//  k_gravity<PLAIN>  all-pairs gravity (gravitational_acceleration!,
+//                    basic_potentials.jl:306-331): 256-body j-tiles of split
+//                    positions staged in shared memory, each i owned by S=4
+//                    lanes that split the tile and join by warp shuffles at the
+//                    end; the j range is cut into J chunks so the grid is a
+//                    near-exact multiple of the resident blocks (J partials per
+//                    atom in scratch, reduced in fixed order by k_gravity_reduce).
+//                    Per pair: FP32 differences of hi/lo split positions (exact
+//                    to ~2^-24 of |r_ij|, or plain FP32 positions when PLAIN),
+//                    one rsqrt, partial sums per tile folded into a compensated
+//                    (TwoSum) pair.
+//  k_allpairs        every other potential on small / unbounded systems, all
+//                    pairs through shared-memory tiles, same pair code as the
+//                    list kernel plus gravity and the magnetic dipole term.
+//  k_force_list      cutoff LJ + reaction-field electrostatics over a Verlet
+//                    list (one thread per atom, coalesced column-major list).
+//  k_bonded          SPC/Fw harmonic bonds and H-O-H angles in FP64, one thread
+//                    per molecule (basic_potentials.jl:367-433).
+#include "nbg_internal.cuh"
+
+#define GT 256       // gravity tile (j bodies per shared-memory stage)
+#define GS 4         // lanes per i
+#define GB 256       // gravity block size
+#define GI (GB / GS) // i per block
+
+template <bool PLAIN>
+__global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
+                                                int64_t n, int64_t npad, int jchunks, double* __restrict__ part)
+{
+    __shared__ float4 sh_hi[GT];
+    __shared__ float4 sh_lo[PLAIN ? 1 : GT];
+    const int64_t ntile = npad / GT;
+    const int64_t tiles_per_chunk = ntile / jchunks;
+    const int64_t unit = blockIdx.x;
+    const int64_t iblock = unit / jchunks;
+    const int jc = (int)(unit % jchunks);
+    const int lane = threadIdx.x % GS;
+    const int64_t i = iblock * GI + threadIdx.x / GS;
+    const float4 hi_i = phi[i < npad ? i : 0];
+    float4 lo_i = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!PLAIN) lo_i = plo[i < npad ? i : 0];
+    Acc2 ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f};
+    const int64_t t0 = jc * tiles_per_chunk;
+    const int64_t t1 = t0 + tiles_per_chunk;
+    const int64_t diag_tile = (iblock * GI) / GT;
+    for (int64_t t = t0; t < t1; ++t) {
+        __syncthreads();
+        sh_hi[threadIdx.x] = phi[t * GT + threadIdx.x];
+        if (!PLAIN) sh_lo[threadIdx.x] = plo[t * GT + threadIdx.x];
+        __syncthreads();
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (t != diag_tile) {
+#pragma unroll 8
+            for (int jj = lane; jj < GT; jj += GS) {
+                float4 hj = sh_hi[jj];
+                float dx = hi_i.x - hj.x, dy = hi_i.y - hj.y, dz = hi_i.z - hj.z;
+                if (!PLAIN) {
+                    float4 lj = sh_lo[jj];
+                    dx += lo_i.x - lj.x;
+                    dy += lo_i.y - lj.y;
+                    dz += lo_i.z - lj.z;
+                }
+                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                float ri = rsqrtf(r2);
+                float s = hj.w * ri * (ri * ri);
+                px = fmaf(s, dx, px);
+                py = fmaf(s, dy, py);
+                pz = fmaf(s, dz, pz);
+            }
+        } else {
+            for (int jj = lane; jj < GT; jj += GS) {
+                float4 hj = sh_hi[jj];
+                float dx = hi_i.x - hj.x, dy = hi_i.y - hj.y, dz = hi_i.z - hj.z;
+                if (!PLAIN) {
+                    float4 lj = sh_lo[jj];
+                    dx += lo_i.x - lj.x;
+                    dy += lo_i.y - lj.y;
+                    dz += lo_i.z - lj.z;
+                }
+                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                float ri = (t * GT + jj == i) ? 0.0f : rsqrtf(r2);  // j != i (:318)
+                float s = hj.w * ri * (ri * ri);
+                px = fmaf(s, dx, px);
+                py = fmaf(s, dy, py);
+                pz = fmaf(s, dz, pz);
+            }
+        }
+        ax.add(px);
+        ay.add(py);
+        az.add(pz);
+    }
+    double vx = ax.value(), vy = ay.value(), vz = az.value();
+#pragma unroll
+    for (int o = GS / 2; o > 0; o >>= 1) {
+        vx += __shfl_xor_sync(0xffffffffu, vx, o);
+        vy += __shfl_xor_sync(0xffffffffu, vy, o);
+        vz += __shfl_xor_sync(0xffffffffu, vz, o);
+    }
+    if (lane == 0 && i < n) {
+        double* p = part + ((int64_t)jc * n + i) * 3;
+        p[0] = vx;
+        p[1] = vy;
+        p[2] = vz;
+    }
+}
+
+// a_i = -G sum_chunks partial_i (fixed chunk order)
+__global__ void k_gravity_reduce(const double* __restrict__ part, int64_t n, int jchunks, double G,
+                                 double* __restrict__ A, unsigned* status)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < jchunks; ++c) s += part[(int64_t)c * 3 * n + e];
+        double a = -G * s;
+        if (!isfinite(a)) status_set(status, ST_NONFINITE);
+        A[e] = a;
+    }
+}
+
+struct GravPlan {
+    int jchunks;
+    int64_t units;
+};
+
+static GravPlan plan_gravity(nbg_ctx* c, int64_t npad)
+{
+    int dev = c->device, sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (c->d.grav_plain)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<true>, GB, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<false>, GB, 0);
+    if (sms < 1) sms = 1;
+    if (occ < 1) occ = 1;
+    int64_t slots = (int64_t)sms * occ;
+    int64_t ib = npad / GI;
+    int64_t ntile = npad / GT;
+    GravPlan best{1, ib};
+    double best_eff = -1.0;
+    for (int J = 1; J <= 64; J *= 2) {
+        if (ntile % J) break;
+        int64_t units = ib * J;
+        double waves = (double)units / (double)slots;
+        double eff = waves / ceil(waves);
+        // prefer fewer chunks unless the balance gain is real
+        if (eff > best_eff + 0.01) {
+            best_eff = eff;
+            best = GravPlan{J, units};
+        }
+    }
+    return best;
+}
+
+// Launch the gravity kernel and the chunk reduction into s.a_new. The
+// partials (grav_chunks * n * 3 doubles) live in c->grav_part.
+int launch_gravity(nbg_ctx* c, const StateView& s)
+{
+    int64_t units = (c->npad / GI) * c->grav_chunks;
+    prof_begin(c);
+    if (c->d.grav_plain)
+        k_gravity<true><<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks,
+                                                               c->grav_part);
+    else
+        k_gravity<false><<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks,
+                                                                c->grav_part);
+    prof_end(c);
+    NBG_LAUNCH_CHECK(c, "k_gravity");
+    k_gravity_reduce<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->grav_part, c->n, c->grav_chunks, c->d.G,
+                                                                      s.a_new, c->d.status);
+    NBG_LAUNCH_CHECK(c, "k_gravity_reduce");
+    return NBG_OK;
+}
+
+int gravity_plan_chunks(nbg_ctx* c, int64_t npad) { return plan_gravity(c, npad).jchunks; }
+
+// ---------------------------------------------------------------------
+// generic all-pairs kernel
+// ---------------------------------------------------------------------
+#define AT 128
+
+__global__ void __launch_bounds__(AT) k_allpairs(Dev d, StateView s)
+{
+    __shared__ float4 sh_hi[AT];
+    __shared__ float4 sh_lo[AT];
+    __shared__ float sh_m[AT];
+    __shared__ float3 sh_mm[AT];
+    const int64_t i = blockIdx.x * (int64_t)AT + threadIdx.x;
+    const bool active = i < d.n;
+    const int64_t ii = active ? i : 0;
+    const RepDev& R = d.reps[0];
+    float4 hi_i = d.phi[ii], lo_i = d.plo[ii];
+    float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[ii]) : 0.0f;
+    float3 mi = make_float3(0.f, 0.f, 0.f);
+    if (d.pots & NBG_POT_MAG) mi = make_float3((float)d.dipole[3 * ii], (float)d.dipole[3 * ii + 1], (float)d.dipole[3 * ii + 2]);
+    Acc2 fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};   // LJ + electrostatic force
+    Acc2 gx{0.f, 0.f}, gy{0.f, 0.f}, gz{0.f, 0.f};   // gravity sum m_j r / r^3
+    Acc2 mx{0.f, 0.f}, my{0.f, 0.f}, mz{0.f, 0.f};   // dipole sum
+    bool range_err = false;
+    const bool cutpots = (d.pots & (NBG_POT_LJ | NBG_POT_EL)) != 0;
+    for (int64_t t = 0; t < d.n; t += AT) {
+        __syncthreads();
+        int64_t j = t + threadIdx.x;
+        if (j < d.n) {
+            sh_hi[threadIdx.x] = d.phi[j];
+            sh_lo[threadIdx.x] = d.plo[j];
+            sh_m[threadIdx.x] = (float)d.mass[j];
+            if (d.pots & NBG_POT_MAG)
+                sh_mm[threadIdx.x] = make_float3((float)d.dipole[3 * j], (float)d.dipole[3 * j + 1], (float)d.dipole[3 * j + 2]);
+        }
+        __syncthreads();
+        int m = (int)((d.n - t) < AT ? (d.n - t) : AT);
+        float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f, wx = 0.f, wy = 0.f, wz = 0.f;
+        for (int k = 0; k < m; ++k) {
+            int64_t jg = t + k;
+            if (jg == ii) continue;
+            float4 hj = sh_hi[k], lj = sh_lo[k];
+            if (cutpots) {
+                PairOut o = pair_cutoff(d, R, ii, jg, hi_i, lo_i, hj, lj, kqi, s.x);
+                range_err |= o.range_err;
+                px += o.fx;
+                py += o.fy;
+                pz += o.fz;
+            }
+            if (d.pots & (NBG_POT_GRAV | NBG_POT_MAG)) {
+                // plain differences: gravity and dipoles ignore the boundary
+                float3 dr = split_diff(hi_i, lo_i, hj, lj, false, R);
+                float r2 = fmaf(dr.x, dr.x, fmaf(dr.y, dr.y, dr.z * dr.z));
+                float ri = rsqrtf(r2);
+                if (d.pots & NBG_POT_GRAV) {
+                    float sg = sh_m[k] * ri * ri * ri;
+                    qx = fmaf(sg, dr.x, qx);
+                    qy = fmaf(sg, dr.y, qy);
+                    qz = fmaf(sg, dr.z, qz);
+                }
+                if (d.pots & NBG_POT_MAG) {
+                    // (mi (mj.r) + mj (mi.r) + r (mi.mj) - 5 r (mi.r)(mj.r)) / |r|^4, r unit
+                    float3 u = make_float3(dr.x * ri, dr.y * ri, dr.z * ri);
+                    float3 mj = sh_mm[k];
+                    float mir = mi.x * u.x + mi.y * u.y + mi.z * u.z;
+                    float mjr = mj.x * u.x + mj.y * u.y + mj.z * u.z;
+                    float mimj = mi.x * mj.x + mi.y * mj.y + mi.z * mj.z;
+                    float inv4 = (ri * ri) * (ri * ri);
+                    wx += (mi.x * mjr + mj.x * mir + u.x * mimj - 5.0f * u.x * mir * mjr) * inv4;
+                    wy += (mi.y * mjr + mj.y * mir + u.y * mimj - 5.0f * u.y * mir * mjr) * inv4;
+                    wz += (mi.z * mjr + mj.z * mir + u.z * mimj - 5.0f * u.z * mir * mjr) * inv4;
+                }
+            }
+        }
+        fx.add(px); fy.add(py); fz.add(pz);
+        gx.add(qx); gy.add(qy); gz.add(qz);
+        mx.add(wx); my.add(wy); mz.add(wz);
+    }
+    if (range_err) status_set(d.status, ST_RANGE);
+    if (!active) return;
+    double im = 1.0 / d.mass[i];
+    double a[3] = {fx.value() * im, fy.value() * im, fz.value() * im};
+    if (d.pots & NBG_POT_GRAV) {
+        a[0] += -d.G * gx.value();
+        a[1] += -d.G * gy.value();
+        a[2] += -d.G * gz.value();
+    }
+    if (d.pots & NBG_POT_MAG) {
+        double cm = 3.0 * d.mu4pi / d.mass[i];
+        a[0] += cm * mx.value();
+        a[1] += cm * my.value();
+        a[2] += cm * mz.value();
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (!isfinite(a[k])) status_set(d.status, ST_NONFINITE);
+        s.a_new[3 * i + k] = a[k];
+    }
+}
+
+int launch_allpairs(nbg_ctx* c, const StateView& s)
+{
+    prof_begin(c);
+    k_allpairs<<<grid_for(c->n, AT), AT, 0, c->stream>>>(c->d, s);
+    prof_end(c);
+    NBG_LAUNCH_CHECK(c, "k_allpairs");
+    return NBG_OK;
+}
+
+// ---------------------------------------------------------------------
+// Verlet-list force kernel
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const RepDev& R = d.reps[d.rep_of[i]];
+        const float4 hi_i = d.phi[i], lo_i = d.plo[i];
+        const float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[i]) : 0.0f;
+        const int cnt = d.nbr_count[i];
+        Acc2 fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
+        float px = 0.f, py = 0.f, pz = 0.f;
+        bool range_err = false;
+        const int* nl = d.nbr + i;
+        for (int k = 0; k < cnt; ++k) {
+            int j = __ldg(nl + (int64_t)k * d.nbr_stride);
+            float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
+            PairOut o = pair_cutoff(d, R, i, j, hi_i, lo_i, hj, lj, kqi, s.x);
+            range_err |= o.range_err;
+            px += o.fx;
+            py += o.fy;
+            pz += o.fz;
+            if ((k & 31) == 31) {
+                fx.add(px); fy.add(py); fz.add(pz);
+                px = py = pz = 0.f;
+            }
+        }
+        fx.add(px); fy.add(py); fz.add(pz);
+        if (range_err) status_set(d.status, ST_RANGE);
+        double im = 1.0 / d.mass[i];
+        double a0 = fx.value() * im, a1 = fy.value() * im, a2 = fz.value() * im;
+        if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
+        s.a_new[3 * i] = a0;
+        s.a_new[3 * i + 1] = a1;
+        s.a_new[3 * i + 2] = a2;
+    }
+}
+
+int launch_force_list(nbg_ctx* c, const StateView& s)
+{
+    prof_begin(c);
+    k_force_list<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s);
+    prof_end(c);
+    NBG_LAUNCH_CHECK(c, "k_force_list");
+    return NBG_OK;
+}
+
+// ---------------------------------------------------------------------
+// SPC/Fw bonded terms (FP64), one thread per molecule (O, H1, H2)
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void cross3(const double* a, const double* b, double* c)
+{
+    c[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1]));
+    c[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2]));
+    c[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]));
+}
+
+__device__ __forceinline__ double norm3(const double* a)
+{
+    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a[0], a[0]), __dmul_rn(a[1], a[1])), __dmul_rn(a[2], a[2])));
+}
+
+__global__ void k_bonded(Dev d, StateView s)
+{
+    int64_t nm = d.n / 3;
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nm; m += (int64_t)gridDim.x * blockDim.x) {
+        int64_t o = 3 * m, h1 = o + 1, h2 = o + 2;
+        const double* X = s.x;
+        double ro[3] = {X[3 * o], X[3 * o + 1], X[3 * o + 2]};
+        double ra[3] = {X[3 * h1], X[3 * h1 + 1], X[3 * h1 + 2]};
+        double rc[3] = {X[3 * h2], X[3 * h2 + 1], X[3 * h2 + 2]};
+        // bonds (harmonic_bond_potential_acceleration!, :367-393): the force on
+        // O from bond O-H is the exact negative of the force on H.
+        double fO[3] = {0, 0, 0}, fH1[3], fH2[3];
+        const double* hs[2] = {ra, rc};
+        double* fh[2] = {fH1, fH2};
+        for (int b = 0; b < 2; ++b) {
+            double rij[3] = {__dsub_rn(ro[0], hs[b][0]), __dsub_rn(ro[1], hs[b][1]), __dsub_rn(ro[2], hs[b][2])};
+            double r = norm3(rij);
+            double dd = __dsub_rn(r, d.rOH);
+            double factor = __dmul_rn(-dd, d.kbond) / r;
+            for (int k = 0; k < 3; ++k) {
+                double f = __dmul_rn(factor, rij[k]);
+                fO[k] = __dadd_rn(fO[k], f);
+                fh[b][k] = -f;
+            }
+        }
+        // angle H1-O-H2 (valence_angle_potential_acceleration!, :395-433), a=H1, b=O, c=H2
+        double rba[3], rbc[3], rcb[3], x[3], pa[3], pc[3];
+        for (int k = 0; k < 3; ++k) {
+            rba[k] = __dsub_rn(ra[k], ro[k]);
+            rbc[k] = __dsub_rn(rc[k], ro[k]);
+            rcb[k] = __dsub_rn(ro[k], rc[k]);
+        }
+        cross3(rba, rbc, x);
+        cross3(rba, x, pa);
+        cross3(rcb, x, pc);
+        double npa = norm3(pa), npc = norm3(pc);
+        for (int k = 0; k < 3; ++k) {
+            pa[k] = pa[k] / npa;
+            pc[k] = pc[k] / npc;
+        }
+        double nba = norm3(rba), nbc = norm3(rbc);
+        double dot = __dadd_rn(__dadd_rn(__dmul_rn(rba[0], rbc[0]), __dmul_rn(rba[1], rbc[1])), __dmul_rn(rba[2], rbc[2]));
+        double cosine = dot / __dmul_rn(nba, nbc);
+        if (cosine > 1.0) cosine = 1.0;
+        else if (cosine < -1.0) cosine = -1.0;
+        double force = __dmul_rn(-d.kangle, __dsub_rn(acos(cosine), d.aHOH));
+        double iO = 1.0 / d.mass[o], iH1 = 1.0 / d.mass[h1], iH2 = 1.0 / d.mass[h2];
+        for (int k = 0; k < 3; ++k) {
+            double fa = __dmul_rn(pa[k], force) / nba;
+            double fc = __dmul_rn(pc[k], force) / nbc;
+            double fb = -__dadd_rn(fa, fc);
+            s.a_new[3 * o + k] = __dadd_rn(__dadd_rn(s.a_new[3 * o + k], __dmul_rn(iO, fO[k])), fb / d.mass[o]);
+            s.a_new[3 * h1 + k] = __dadd_rn(__dadd_rn(s.a_new[3 * h1 + k], __dmul_rn(iH1, fH1[k])), fa / d.mass[h1]);
+            s.a_new[3 * h2 + k] = __dadd_rn(__dadd_rn(s.a_new[3 * h2 + k], __dmul_rn(iH2, fH2[k])), fc / d.mass[h2]);
+        }
+    }
+}
+
+int launch_bonded(nbg_ctx* c, const StateView& s)
+{
+    k_bonded<<<grid_for(c->n / 3, 128), 128, 0, c->stream>>>(c->d, s);
+    NBG_LAUNCH_CHECK(c, "k_bonded");
+    return NBG_OK;
+}

@@ -1,0 +1,292 @@
+// k_integrate.cu - position packing, the fused velocity-Verlet drift/kick
+// with the Berendsen / Nose-Hoover terms, the temperature reduction, the
+// Andersen collisions and the Euler-Maruyama Langevin step.
+//
+// Velocity Verlet is the published method in the form
+//   u' = u + dt v + dt^2 (a/2);  a' = f(v, u');  v' = v + dt (a/2 + a'/2)
+// where f is soode_system! (nbody_to_ode.jl:474-488) including the
+// thermostat terms of thermostats.jl:76-128 evaluated at the start-of-step
+// velocity v. All FP64 arithmetic here uses explicit _rn intrinsics so that
+// no multiply-add is contracted (the reference's Julia arithmetic has none).
+#include "nbg_internal.cuh"
+
+// Split one atom's position into (hi, lo) floats; see nbg_internal.cuh.
+__device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double* X)
+{
+    const RepDev& R = d.reps[d.rep_of[i]];
+    double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+    float h[3], l[3];
+    if (d.bc == NBG_BC_CUBIC) {
+        for (int k = 0; k < 3; ++k) {
+            double w = p[k] - R.L * floor(p[k] * R.invL);
+            if (w < 0.0) w += R.L;
+            if (w >= R.L) w -= R.L;
+            double hq = rint(w * (double)R.qscale) * (double)R.qinv;
+            h[k] = (float)hq;
+            l[k] = (float)(w - hq);
+        }
+    } else {
+        for (int k = 0; k < 3; ++k) {
+            h[k] = (float)p[k];
+            l[k] = (float)(p[k] - (double)h[k]);
+        }
+    }
+    float4 hi = d.phi[i];
+    float4 lo = d.plo[i];
+    d.phi[i] = make_float4(h[0], h[1], h[2], hi.w);
+    d.plo[i] = make_float4(l[0], l[1], l[2], lo.w);
+}
+
+__global__ void k_pack(Dev d, const double* X)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x)
+        pack_atom(d, i, X);
+}
+
+int launch_pack(nbg_ctx* c, const StateView& s)
+{
+    k_pack<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s.x);
+    NBG_LAUNCH_CHECK(c, "k_pack");
+    return NBG_OK;
+}
+
+// u' = u + dt v + dt^2 (a/2) for every column (the Nose-Hoover column moves
+// zeta by dt * v_zeta since its acceleration is 0), then repack and flag a
+// Verlet-list rebuild when an atom moved more than skin/2.
+__global__ void k_drift(Dev d, StateView s, double dt, double dtsq)
+{
+    int64_t ncomp = 3 * d.cols;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x) {
+        double u = s.x[e];
+        s.x[e] = __dadd_rn(__dadd_rn(u, __dmul_rn(dt, s.v[e])), __dmul_rn(dtsq, __dmul_rn(0.5, s.a_old[e])));
+    }
+}
+
+__global__ void k_pack_disp(Dev d, const double* X, int check_disp, int parity)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        pack_atom(d, i, X);
+        if (check_disp) {
+            double dx = X[3 * i] - d.xref[3 * i];
+            double dy = X[3 * i + 1] - d.xref[3 * i + 1];
+            double dz = X[3 * i + 2] - d.xref[3 * i + 2];
+            double d2 = dx * dx + dy * dy + dz * dz;
+            if (!(d2 <= d.skin_half2)) d.rebuild_flag[parity] = 1;
+        }
+    }
+}
+
+int launch_drift(nbg_ctx* c, const StateView& s, double dt)
+{
+    k_drift<<<grid_for(3 * c->cols, 256), 256, 0, c->stream>>>(c->d, s, dt, dt * dt);
+    NBG_LAUNCH_CHECK(c, "k_drift");
+    k_pack_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s.x, c->path == PATH_LIST ? 1 : 0,
+                                                            (int)((c->step + 1) & 1));
+    NBG_LAUNCH_CHECK(c, "k_pack_disp");
+    return NBG_OK;
+}
+
+// Per-replica sum of m v^2 (md_temperature, thermostats.jl:87-91), grid
+// (slices, replicas); the last block of each replica adds the slice
+// partials in slice order, so the result is deterministic.
+__global__ void k_temperature(Dev d, const double* V)
+{
+    int r = blockIdx.y;
+    const RepDev& R = d.reps[r];
+    int64_t per = (R.n + gridDim.x - 1) / gridDim.x;
+    int64_t b = R.atom0 + blockIdx.x * per;
+    int64_t e = b + per;
+    if (e > R.atom0 + R.n) e = R.atom0 + R.n;
+    double acc = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        double sq = V[3 * i] * V[3 * i] + V[3 * i + 1] * V[3 * i + 1] + V[3 * i + 2] * V[3 * i + 2];
+        acc += d.mass[i] * sq;
+    }
+    __shared__ double sh[256];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        d.red_partial[(int64_t)r * gridDim.x + blockIdx.x] = sh[0];
+        __threadfence();
+        unsigned prev = atomicAdd(&d.red_counter[r], 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double tot = 0.0;
+        for (int k = 0; k < (int)gridDim.x; ++k) tot += ((volatile double*)d.red_partial)[(int64_t)r * gridDim.x + k];
+        d.red_T[r] = tot / (d.kb * R.ndf);
+        d.red_counter[r] = 0u;
+    }
+}
+
+int launch_temperature(nbg_ctx* c, const double* v)
+{
+    dim3 grid(c->d.red_slices, c->nrep);
+    k_temperature<<<grid, 256, 0, c->stream>>>(c->d, v);
+    NBG_LAUNCH_CHECK(c, "k_temperature");
+    return NBG_OK;
+}
+
+// Thermostat term of soode_system! for element e of atom i (i < n):
+// Berendsen dv += gamma (T0/T - 1) v (or gamma v when 1/T == Inf),
+// Nose-Hoover dv -= zeta v.
+__device__ __forceinline__ double thermo_term(const Dev& d, int64_t i, double v, double zeta)
+{
+    if (d.therm == NBG_THERMO_BERENDSEN) {
+        const RepDev& R = d.reps[d.rep_of[i]];
+        double T = d.red_T[d.rep_of[i]];
+        double g = 0.5 / R.tparam;
+        if (1.0 / T == INFINITY) return __dmul_rn(g, v);
+        return __dmul_rn(__dmul_rn(g, __dsub_rn(R.T0 / T, 1.0)), v);
+    }
+    if (d.therm == NBG_THERMO_NOSEHOOVER) return -__dmul_rn(zeta, v);
+    return 0.0;
+}
+
+// v' = v + dt (a/2 + a'/2) with a' = forces + thermostat term at v; stores a'
+// as the next step's a. Also sets the Nose-Hoover rate (thermostats.jl:126).
+__global__ void k_kick(Dev d, StateView s, double dt)
+{
+    int64_t ncomp = 3 * d.n;
+    double zeta = 0.0;
+    if (d.therm == NBG_THERMO_NOSEHOOVER) zeta = s.x[3 * d.n];
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x) {
+        double v = s.v[e];
+        double an = s.a_new[e];
+        if (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER)
+            an = __dadd_rn(an, thermo_term(d, e / 3, v, zeta));
+        if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+        s.v[e] = __dadd_rn(v, __dmul_rn(dt, __dadd_rn(__dmul_rn(0.5, s.a_old[e]), __dmul_rn(0.5, an))));
+        s.a_old[e] = an;
+    }
+    if (d.therm == NBG_THERMO_NOSEHOOVER && blockIdx.x == 0 && threadIdx.x < 3) {
+        int64_t z = 3 * d.n + threadIdx.x;
+        // dv[:, end] = 0; v[zeta] = tau^-2 (T/T0 - (ndf+1)/ndf)
+        s.a_old[z] = 0.0;
+        if (threadIdx.x == 0) {
+            const RepDev& R = d.reps[0];
+            double it = 1.0 / R.tparam;
+            double T = d.red_T[0];
+            s.v[z] = __dmul_rn(__dmul_rn(it, it), __dsub_rn(T / R.T0, (R.ndf + 1.0) / R.ndf));
+        }
+    }
+}
+
+int launch_kick(nbg_ctx* c, const StateView& s, double dt)
+{
+    k_kick<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->d, s, dt);
+    NBG_LAUNCH_CHECK(c, "k_kick");
+    return NBG_OK;
+}
+
+// The thermostat part of one RHS evaluation (nbg_accel): a_new += term(v);
+// Nose-Hoover also zeroes its column and writes the rate into v.
+__global__ void k_rhs_thermostat(Dev d, StateView s)
+{
+    int64_t ncomp = 3 * d.n;
+    double zeta = d.therm == NBG_THERMO_NOSEHOOVER ? s.x[3 * d.n] : 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x)
+        s.a_new[e] = __dadd_rn(s.a_new[e], thermo_term(d, e / 3, s.v[e], zeta));
+}
+
+__global__ void k_rhs_nh_column(Dev d, StateView s)
+{
+    int64_t z = 3 * d.n;
+    s.a_new[z] = 0.0;
+    s.a_new[z + 1] = 0.0;
+    s.a_new[z + 2] = 0.0;
+    const RepDev& R = d.reps[0];
+    double it = 1.0 / R.tparam;
+    s.v[z] = __dmul_rn(__dmul_rn(it, it), __dsub_rn(d.red_T[0] / R.T0, (R.ndf + 1.0) / R.ndf));
+}
+
+int launch_rhs_thermostat(nbg_ctx* c, const StateView& s)
+{
+    if (c->d.therm != NBG_THERMO_BERENDSEN && c->d.therm != NBG_THERMO_NOSEHOOVER) return NBG_OK;
+    int st = launch_temperature(c, s.v);
+    if (st) return st;
+    k_rhs_thermostat<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->d, s);
+    NBG_LAUNCH_CHECK(c, "k_rhs_thermostat");
+    if (c->d.therm == NBG_THERMO_NOSEHOOVER) {
+        k_rhs_nh_column<<<1, 1, 0, c->stream>>>(c->d, s);
+        NBG_LAUNCH_CHECK(c, "k_rhs_nh_column");
+    }
+    return NBG_OK;
+}
+
+// Andersen affect! after step `step` (nbody_simulation_result.jl:511-540):
+// with probability nu*dt an atom's velocity is redrawn as sqrt(kb T / m) z,
+// m = the first body's mass for potential systems, the site mass for water.
+__global__ void k_andersen(Dev d, StateView s, double dt, int64_t step)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        int r = d.rep_of[i];
+        const RepDev& R = d.reps[r];
+        int64_t li = i - R.atom0;
+        double prob = R.tparam * dt;
+        if (philox_u53(R.seed, (uint64_t)li, (uint64_t)step) < prob) {
+            double m = d.kind == NBG_SYSTEM_WATER ? d.mass[i] : d.mass[R.atom0];
+            double vdev = sqrt(d.kb * R.T0 / m);
+            double z[3];
+            philox_normals3<double>(R.seed, (uint64_t)li, (uint64_t)step, z);
+            s.v[3 * i] = vdev * z[0];
+            s.v[3 * i + 1] = vdev * z[1];
+            s.v[3 * i + 2] = vdev * z[2];
+        }
+    }
+}
+
+int launch_andersen(nbg_ctx* c, const StateView& s, double dt, int64_t step)
+{
+    k_andersen<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s, dt, step);
+    NBG_LAUNCH_CHECK(c, "k_andersen");
+    return NBG_OK;
+}
+
+// Euler-Maruyama step of the Langevin SDE (nbody_to_ode.jl:567-680):
+// u' = u + dt v;  v' = v + dt (a(u) - friction) + sigma sqrt(dt) z.
+// Potential systems: friction gamma v, sigma = sqrt(2 gamma kb T / m_1).
+// Water (the reference's terms): O rows lose gamma v / m_O and gamma v,
+// H rows gamma v; sigma = sqrt(2 gamma kb T) / m_site.
+__global__ void k_em(Dev d, StateView s, double dt, double sqdt, int64_t step)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        int r = d.rep_of[i];
+        const RepDev& R = d.reps[r];
+        int64_t li = i - R.atom0;
+        double g = R.tparam;
+        float z[3];
+        philox_normals3<float>(R.seed, (uint64_t)li, (uint64_t)step, z);
+        bool water = d.kind == NBG_SYSTEM_WATER;
+        bool oxy = water && (li % 3 == 0);
+        double sigma = water ? R.sigma_num / d.mass[i] : R.sigma;
+        for (int k = 0; k < 3; ++k) {
+            int64_t e = 3 * i + k;
+            double v = s.v[e];
+            double drift = s.a_new[e];
+            if (oxy) drift = __dsub_rn(drift, __dmul_rn(g, v) / d.mass[i]);
+            drift = __dsub_rn(drift, __dmul_rn(g, v));
+            if (!isfinite(drift)) status_set(d.status, ST_NONFINITE);
+            double vn = __dadd_rn(__dadd_rn(v, __dmul_rn(dt, drift)), __dmul_rn(sigma, __dmul_rn(sqdt, (double)z[k])));
+            s.x[e] = __dadd_rn(s.x[e], __dmul_rn(dt, v));
+            s.v[e] = vn;
+        }
+    }
+}
+
+int launch_em(nbg_ctx* c, const StateView& s, double dt, int64_t step)
+{
+    k_em<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s, dt, sqrt(dt), step);
+    NBG_LAUNCH_CHECK(c, "k_em");
+    k_pack_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s.x, c->path == PATH_LIST ? 1 : 0,
+                                                            (int)((step + 1) & 1));
+    NBG_LAUNCH_CHECK(c, "k_pack_disp");
+    return NBG_OK;
+}

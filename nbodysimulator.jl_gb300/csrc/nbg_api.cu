@@ -1,0 +1,933 @@
+// nbg_api.cu - the C ABI of include/nbg.h: context lifecycle, marshalling of
+// the system descriptor into device buffers, and the step loops.
+//
+// Step loops (all work asynchronous on the context's stream):
+//   velocity Verlet  drift -> [Verlet list] -> forces -> [bonded] ->
+//                    [temperature] -> kick -> [Andersen]
+//   Euler-Maruyama   [Verlet list] -> forces -> [bonded] -> EM update
+// nbg_advance runs the loop in chunks; after each chunk it reads the device
+// status word. A cell or neighbour capacity overflow restores the chunk's
+// starting state, grows the capacity and runs the chunk again; non-finite
+// accelerations or a minimum-image loop over its iteration cap end the call
+// with an error.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nbg_internal.cuh"
+
+static const char* kVersion = "libnbg 1.0 (sm_103a)";
+
+int cuda_fail(nbg_ctx* c, cudaError_t e, const char* what)
+{
+    if (c) c->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return NBG_ERR_CUDA;
+}
+
+static int fail(nbg_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call, what)                                        \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
+    } while (0)
+
+template <typename T>
+static int dalloc(nbg_ctx* c, T** p, size_t count)
+{
+    void* q = nullptr;
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, NBG_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    cudaMemset(q, 0, bytes);
+    c->allocs.push_back(q);
+    *p = (T*)q;
+    return NBG_OK;
+}
+
+static void dfree(nbg_ctx* c, void* p)
+{
+    if (!p) return;
+    auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
+    if (it != c->allocs.end()) c->allocs.erase(it);
+    cudaFree(p);
+}
+
+extern "C" const char* nbg_version(void) { return kVersion; }
+extern "C" int nbg_abi_version(void) { return NBG_ABI_VERSION; }
+
+extern "C" const char* nbg_last_error(const nbg_ctx* ctx)
+{
+    if (!ctx) return "null context";
+    return ctx->err.c_str();
+}
+
+extern "C" int64_t nbg_kernel_launches(const nbg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ---------------------------------------------------------------------
+// descriptor validation
+// ---------------------------------------------------------------------
+static int validate(const nbg_system_desc* d, std::string& why)
+{
+    if (!d) { why = "null descriptor"; return NBG_ERR_ARG; }
+    if (d->abi_version != NBG_ABI_VERSION) { why = "abi_version mismatch"; return NBG_ERR_ARG; }
+    if (d->n < 1) { why = "n must be >= 1"; return NBG_ERR_ARG; }
+    if (d->n > (1ll << 30)) { why = "n above 2^30 atoms"; return NBG_ERR_UNSUPPORTED; }
+    if (!d->mass) { why = "mass is required"; return NBG_ERR_ARG; }
+    for (int64_t i = 0; i < d->n; ++i)
+        if (!(d->mass[i] > 0.0) || !std::isfinite(d->mass[i])) { why = "masses must be finite and > 0"; return NBG_ERR_ARG; }
+    if (d->kind != NBG_SYSTEM_POTENTIAL && d->kind != NBG_SYSTEM_WATER) { why = "unknown system kind"; return NBG_ERR_ARG; }
+    uint32_t pots = d->kind == NBG_SYSTEM_WATER ? (NBG_POT_LJ | NBG_POT_EL) : d->potentials;
+    if (pots & ~15u) { why = "unknown potential bits"; return NBG_ERR_ARG; }
+    if (d->kind == NBG_SYSTEM_WATER && d->n % 3 != 0) { why = "water needs 3 atoms per molecule"; return NBG_ERR_ARG; }
+    if ((pots & NBG_POT_EL) && !d->charge) { why = "charges are required"; return NBG_ERR_ARG; }
+    if ((pots & NBG_POT_MAG) && !d->dipole) { why = "dipoles are required"; return NBG_ERR_ARG; }
+    if ((pots & NBG_POT_LJ) && !(d->lj_cutoff > 0.0)) { why = "LJ cutoff must be > 0"; return NBG_ERR_ARG; }
+    if ((pots & NBG_POT_EL) && !(d->el_cutoff > 0.0)) { why = "electrostatic cutoff must be > 0"; return NBG_ERR_ARG; }
+    if ((pots & NBG_POT_EL) && !(d->el_eps_rf >= 1.0)) { why = "eps_rf must be >= 1"; return NBG_ERR_ARG; }
+    if (d->bc == NBG_BC_CUBIC) {
+        if (!(d->box[0] > 0.0) || !std::isfinite(d->box[0])) { why = "cubic box needs finite L > 0"; return NBG_ERR_ARG; }
+    } else if (d->bc == NBG_BC_PERIODIC) {
+        for (int k = 0; k < 3; ++k)
+            if (!(d->box[2 * k + 1] > d->box[2 * k])) { why = "periodic box needs hi > lo"; return NBG_ERR_ARG; }
+    } else if (d->bc != NBG_BC_INFINITE) {
+        why = "unknown boundary";
+        return NBG_ERR_ARG;
+    }
+    if (d->thermostat < NBG_THERMO_NULL || d->thermostat > NBG_THERMO_LANGEVIN) { why = "unknown thermostat"; return NBG_ERR_ARG; }
+    if (d->thermostat != NBG_THERMO_NULL) {
+        if (!(d->thermo_param > 0.0)) { why = "thermostat parameter must be > 0"; return NBG_ERR_ARG; }
+        if (!(d->kb > 0.0)) { why = "kb must be > 0"; return NBG_ERR_ARG; }
+    }
+    return NBG_OK;
+}
+
+// ---------------------------------------------------------------------
+// context construction
+// ---------------------------------------------------------------------
+static float f_down(double x) { float f = (float)x; if ((double)f > x) f = nextafterf(f, 0.0f); return f; }
+static float f_up(double x)
+{
+    if (std::isinf(x)) return INFINITY;
+    float f = (float)x;
+    if ((double)f < x) f = nextafterf(f, INFINITY);
+    return f;
+}
+
+static double list_radius(const nbg_system_desc* d)
+{
+    uint32_t pots = d->kind == NBG_SYSTEM_WATER ? (NBG_POT_LJ | NBG_POT_EL) : d->potentials;
+    double rc = 0.0;
+    if (pots & NBG_POT_LJ) rc = std::max(rc, d->lj_cutoff);
+    if (pots & NBG_POT_EL) rc = std::max(rc, d->el_cutoff);
+    return rc + std::max(d->skin, 0.0);
+}
+
+static int choose_path(const nbg_system_desc* descs, int nrep)
+{
+    const nbg_system_desc* d = &descs[0];
+    uint32_t pots = d->kind == NBG_SYSTEM_WATER ? (NBG_POT_LJ | NBG_POT_EL) : d->potentials;
+    if (nrep == 1 && d->kind == NBG_SYSTEM_POTENTIAL && pots == NBG_POT_GRAV) return PATH_GRAVITY;
+    bool list_ok = !(d->flags & NBG_FLAG_ALL_PAIRS) && d->bc == NBG_BC_CUBIC && (pots & ~(uint32_t)(NBG_POT_LJ | NBG_POT_EL)) == 0 &&
+                   pots != 0;
+    if (list_ok) {
+        for (int r = 0; r < nrep; ++r) {
+            double rl = list_radius(&descs[r]);
+            if (!std::isfinite(rl)) { list_ok = false; break; }
+            int nc = (int)std::floor(descs[r].box[0] / (rl * (1.0 + 1e-4)));
+            if (nc < 3) { list_ok = false; break; }
+        }
+    }
+    if (list_ok) return PATH_LIST;
+    if (nrep == 1) return PATH_ALLPAIRS;
+    return -1;
+}
+
+static int alloc_lists(nbg_ctx* c, int cell_cap, int nbr_cap)
+{
+    int st;
+    if (c->d.cell_atoms) dfree(c, c->d.cell_atoms);
+    if (c->d.nbr) dfree(c, c->d.nbr);
+    c->d.cell_atoms = nullptr;
+    c->d.nbr = nullptr;
+    if ((st = dalloc(c, &c->d.cell_atoms, (size_t)c->d.ncell_total * cell_cap))) return st;
+    if ((st = dalloc(c, &c->d.nbr, (size_t)c->n * nbr_cap))) return st;
+    c->d.cell_cap = cell_cap;
+    c->d.nbr_cap = nbr_cap;
+    c->d.nbr_stride = c->n;
+    return NBG_OK;
+}
+
+static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
+{
+    const nbg_system_desc* d0 = &descs[0];
+    c->desc = *d0;
+    c->desc.mass = c->desc.charge = c->desc.dipole = nullptr;
+    c->nrep = nrep;
+    uint32_t pots = d0->kind == NBG_SYSTEM_WATER ? (NBG_POT_LJ | NBG_POT_EL) : d0->potentials;
+    int64_t n = 0;
+    for (int r = 0; r < nrep; ++r) n += descs[r].n;
+    c->n = n;
+    c->cols = n + ((nrep == 1 && d0->thermostat == NBG_THERMO_NOSEHOOVER) ? 1 : 0);
+    c->path = choose_path(descs, nrep);
+    if (c->path < 0) return fail(c, NBG_ERR_UNSUPPORTED, "a batch needs every replica on the cubic Verlet-list path");
+
+    // per-atom host arrays
+    c->mass_h.resize(n);
+    c->charge_h.assign(n, 0.0);
+    if (pots & NBG_POT_MAG) c->dipole_h.assign(3 * n, 0.0);
+    std::vector<int> rep_of(n);
+    int64_t off = 0;
+    for (int r = 0; r < nrep; ++r) {
+        const nbg_system_desc* d = &descs[r];
+        for (int64_t i = 0; i < d->n; ++i) {
+            c->mass_h[off + i] = d->mass[i];
+            if (pots & NBG_POT_EL) c->charge_h[off + i] = d->charge[i];
+            if (pots & NBG_POT_MAG)
+                for (int k = 0; k < 3; ++k) c->dipole_h[3 * (off + i) + k] = d->dipole[3 * i + k];
+            rep_of[off + i] = r;
+        }
+        off += d->n;
+    }
+
+    Dev& D = c->d;
+    D.n = n;
+    D.cols = c->cols;
+    D.kind = d0->kind;
+    D.bc = d0->bc;
+    D.therm = d0->thermostat;
+    D.nrep = nrep;
+    D.pots = pots;
+    D.lj_sig2_d = d0->lj_sigma * d0->lj_sigma;
+    D.lj_sig2 = (float)D.lj_sig2_d;
+    D.lj_eps = d0->lj_epsilon;
+    D.lj_eps24 = (float)(24.0 * d0->lj_epsilon);
+    D.lj_R2 = d0->lj_cutoff * d0->lj_cutoff;
+    D.el_k_d = d0->el_k;
+    D.el_k = (float)d0->el_k;
+    D.el_R = d0->el_cutoff;
+    D.el_R2 = d0->el_cutoff * d0->el_cutoff;
+    // reaction field with a vacuum (eps = 1) inside the cutoff
+    double eps_rf = d0->el_eps_rf;
+    if (std::isfinite(d0->el_cutoff) && eps_rf != 1.0) {
+        double R3 = d0->el_cutoff * d0->el_cutoff * d0->el_cutoff;
+        D.el_krf = std::isinf(eps_rf) ? 0.5 / R3 : (eps_rf - 1.0) / ((2.0 * eps_rf + 1.0) * R3);
+        D.el_crf = 1.0 / d0->el_cutoff + D.el_krf * d0->el_cutoff * d0->el_cutoff;
+    } else {
+        D.el_krf = 0.0;
+        D.el_crf = std::isfinite(d0->el_cutoff) ? 1.0 / d0->el_cutoff : 0.0;
+    }
+    D.el_krf2 = (float)(2.0 * D.el_krf);
+    D.G = d0->grav_G;
+    D.mu4pi = d0->mag_mu_4pi;
+    D.kb = d0->kb;
+    D.rOH = d0->water_rOH;
+    D.aHOH = d0->water_aHOH;
+    D.kbond = d0->water_kb;
+    D.kangle = d0->water_ka;
+    D.skin_half2 = 0.25 * std::max(d0->skin, 0.0) * std::max(d0->skin, 0.0);
+    D.grav_plain = (d0->flags & NBG_FLAG_GRAV_PLAIN) ? 1 : 0;
+
+    // replicas
+    c->reps_h.resize(nrep);
+    off = 0;
+    int cell0 = 0;
+    int max_cell_occ = 0;
+    double max_nbr = 0.0;
+    int64_t max_rep_n = 0;
+    for (int r = 0; r < nrep; ++r) {
+        const nbg_system_desc* d = &descs[r];
+        RepDev R{};
+        R.atom0 = off;
+        R.n = d->n;
+        max_rep_n = std::max(max_rep_n, d->n);
+        for (int k = 0; k < 6; ++k) R.box[k] = d->box[k];
+        double img2 = INFINITY;
+        if (d->bc == NBG_BC_CUBIC) {
+            double L = d->box[0];
+            R.L = L;
+            R.invL = 1.0 / L;
+            int e = (int)std::ceil(std::log2(L));
+            int k = 22 - e;
+            R.qscale = (float)std::ldexp(1.0, k);
+            R.qinv = (float)std::ldexp(1.0, -k);
+            double Lh = std::rint(L * std::ldexp(1.0, k)) * std::ldexp(1.0, -k);
+            R.Lh = (float)Lh;
+            R.Ll = (float)(L - Lh);
+            R.invLf = (float)(1.0 / L);
+            double h = 0.5 * L * (1.0 - CLASSIFY_MARGIN);
+            img2 = h * h;
+        }
+        double m = CLASSIFY_MARGIN;
+        if (pots & NBG_POT_LJ) {
+            double R2 = d0->lj_cutoff * d0->lj_cutoff;
+            R.lj_lo = f_down(std::min(R2 * (1.0 - m), img2));
+            R.lj_hi = f_up(R2 * (1.0 + m));
+        }
+        if (pots & NBG_POT_EL) {
+            double R2 = d0->el_cutoff * d0->el_cutoff;
+            R.el_lo = f_down(std::min(R2 * (1.0 - m), img2));
+            R.el_hi = f_up(R2 * (1.0 + m));
+        }
+        if (c->path == PATH_LIST) {
+            double rl = list_radius(d);
+            R.nc = (int)std::floor(d->box[0] / (rl * (1.0 + 1e-4)));
+            R.cell0 = cell0;
+            R.cell_inv = R.nc / d->box[0];
+            R.rl2 = f_up(rl * rl * (1.0 + 1e-5));
+            cell0 += R.nc * R.nc * R.nc;
+            double rho = d->n / (d->box[0] * d->box[0] * d->box[0]);
+            double cs = d->box[0] / R.nc;
+            max_cell_occ = std::max(max_cell_occ, (int)std::ceil(rho * cs * cs * cs));
+            max_nbr = std::max(max_nbr, 4.0 / 3.0 * M_PI * rl * rl * rl * rho);
+        }
+        R.T0 = d->thermo_T;
+        R.tparam = d->thermo_param;
+        if (d->thermostat == NBG_THERMO_LANGEVIN) {
+            R.sigma = std::sqrt(2.0 * d->thermo_param * d->kb * d->thermo_T / d->mass[0]);
+            R.sigma_num = std::sqrt(2.0 * d->thermo_param * d->kb * d->thermo_T);
+        }
+        int64_t Nc = d->kind == NBG_SYSTEM_WATER ? 2 * (d->n / 3) : 0;
+        R.ndf = (double)(3 * d->n - Nc);
+        R.seed = d->seed;
+        c->reps_h[r] = R;
+        off += d->n;
+    }
+    D.ncell_total = cell0;
+
+    int st;
+    // state
+    StateView* views[2] = {&c->st, &c->ev};
+    for (StateView* sv : views) {
+        if ((st = dalloc(c, &sv->x, 3 * c->cols))) return st;
+        if ((st = dalloc(c, &sv->v, 3 * c->cols))) return st;
+        if ((st = dalloc(c, &sv->a_old, 3 * c->cols))) return st;
+        if ((st = dalloc(c, &sv->a_new, 3 * c->cols))) return st;
+    }
+    c->npad = c->path == PATH_GRAVITY ? ((n + 255) / 256) * 256 : n;
+    double* dp;
+    if ((st = dalloc(c, &dp, n))) return st;
+    D.mass = dp;
+    CK(cudaMemcpy(dp, c->mass_h.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "mass upload");
+    std::vector<double> im(n);
+    for (int64_t i = 0; i < n; ++i) im[i] = 1.0 / c->mass_h[i];
+    if ((st = dalloc(c, &dp, n))) return st;
+    D.inv_mass = dp;
+    CK(cudaMemcpy(dp, im.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "inv_mass upload");
+    if ((st = dalloc(c, &dp, n))) return st;
+    D.charge = dp;
+    CK(cudaMemcpy(dp, c->charge_h.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "charge upload");
+    if (pots & NBG_POT_MAG) {
+        if ((st = dalloc(c, &dp, 3 * n))) return st;
+        D.dipole = dp;
+        CK(cudaMemcpy(dp, c->dipole_h.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice), "dipole upload");
+    }
+    int* ip;
+    if ((st = dalloc(c, &ip, n))) return st;
+    D.rep_of = ip;
+    CK(cudaMemcpy(ip, rep_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "rep_of upload");
+    RepDev* rp;
+    if ((st = dalloc(c, &rp, nrep))) return st;
+    D.reps = rp;
+    CK(cudaMemcpy(rp, c->reps_h.data(), sizeof(RepDev) * nrep, cudaMemcpyHostToDevice), "replica upload");
+
+    // split positions with their static w (charge or mass) and flags
+    if ((st = dalloc(c, &D.phi, c->npad))) return st;
+    if ((st = dalloc(c, &D.plo, c->npad))) return st;
+    {
+        std::vector<float4> hi(c->npad), lo(c->npad);
+        for (int64_t i = 0; i < c->npad; ++i) {
+            if (i >= n) {  // padding body: far away, massless
+                hi[i] = make_float4(1e18f, 1e18f, 1e18f, 0.0f);
+                lo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                continue;
+            }
+            float w = c->path == PATH_GRAVITY ? (float)c->mass_h[i] : (float)c->charge_h[i];
+            int flags = 0;
+            int64_t li = i - c->reps_h[rep_of[i]].atom0;
+            if ((pots & NBG_POT_LJ) && (d0->kind != NBG_SYSTEM_WATER || li % 3 == 0)) flags |= AF_LJ;
+            hi[i] = make_float4(0.f, 0.f, 0.f, w);
+            float wf;
+            memcpy(&wf, &flags, sizeof(float));
+            lo[i] = make_float4(0.f, 0.f, 0.f, wf);
+        }
+        CK(cudaMemcpy(D.phi, hi.data(), sizeof(float4) * c->npad, cudaMemcpyHostToDevice), "phi init");
+        CK(cudaMemcpy(D.plo, lo.data(), sizeof(float4) * c->npad, cudaMemcpyHostToDevice), "plo init");
+    }
+
+    if ((st = dalloc(c, &D.status, 4))) return st;
+    if ((st = dalloc(c, &D.rebuild_flag, 2))) return st;
+    if ((st = dalloc(c, &D.build_count, 1))) return st;
+    D.red_slices = (int)std::min<int64_t>(64, std::max<int64_t>(1, (max_rep_n + 4095) / 4096));
+    if ((st = dalloc(c, &D.red_partial, (size_t)nrep * D.red_slices))) return st;
+    if ((st = dalloc(c, &D.red_T, nrep))) return st;
+    if ((st = dalloc(c, &D.red_counter, nrep))) return st;
+
+    if (c->path == PATH_LIST) {
+        if ((st = dalloc(c, &D.cell_count, D.ncell_total))) return st;
+        if ((st = dalloc(c, &D.cell_n, D.ncell_total))) return st;
+        if ((st = dalloc(c, &D.nbr_count, n))) return st;
+        if ((st = dalloc(c, &D.xref, 3 * n))) return st;
+        int cell_cap = ((2 * max_cell_occ + 16 + 7) / 8) * 8;
+        int nbr_cap = ((int)std::ceil(1.3 * max_nbr + 32) + 7) / 8 * 8;
+        if ((st = alloc_lists(c, cell_cap, nbr_cap))) return st;
+    }
+    if (c->path == PATH_GRAVITY) {
+        c->grav_chunks = gravity_plan_chunks(c, c->npad);
+        if ((st = dalloc(c, &c->grav_part, (size_t)c->grav_chunks * 3 * n))) return st;
+    }
+    return NBG_OK;
+}
+
+void prof_begin(nbg_ctx* c)
+{
+    if (!c->profiling) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    c->prof_events.push_back(e);
+}
+
+void prof_end(nbg_ctx* c)
+{
+    if (!c->profiling) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    c->prof_events.push_back(e);
+}
+
+static void prof_drain(nbg_ctx* c)
+{
+    for (size_t k = 0; k + 1 < c->prof_events.size(); k += 2) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(c->prof_events[k + 1]) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, c->prof_events[k], c->prof_events[k + 1]) == cudaSuccess) {
+            c->prof_ms += ms;
+            c->prof_count++;
+        }
+        cudaEventDestroy(c->prof_events[k]);
+        cudaEventDestroy(c->prof_events[k + 1]);
+    }
+    c->prof_events.clear();
+}
+
+extern "C" int nbg_set_profiling(nbg_ctx* c, int on)
+{
+    if (!c) return NBG_ERR_ARG;
+    cudaSetDevice(c->device);
+    prof_drain(c);
+    c->profiling = on != 0;
+    c->prof_ms = 0.0;
+    c->prof_count = 0;
+    return NBG_OK;
+}
+
+extern "C" int nbg_force_kernel_time(nbg_ctx* c, double* total_ms, int64_t* launches)
+{
+    if (!c || !total_ms || !launches) return NBG_ERR_ARG;
+    cudaSetDevice(c->device);
+    prof_drain(c);
+    *total_ms = c->prof_ms;
+    *launches = c->prof_count;
+    c->prof_ms = 0.0;
+    c->prof_count = 0;
+    return NBG_OK;
+}
+
+static void release(nbg_ctx* c)
+{
+    prof_drain(c);
+    for (void* p : c->allocs) cudaFree(p);
+    c->allocs.clear();
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    c->own_stream = nullptr;
+}
+
+extern "C" int nbg_create_batch(const nbg_system_desc* descs, int32_t n_replicas, int device, nbg_ctx** out)
+{
+    if (!out) return NBG_ERR_ARG;
+    *out = nullptr;
+    if (!descs || n_replicas < 1) return NBG_ERR_ARG;
+    std::string why;
+    for (int r = 0; r < n_replicas; ++r) {
+        int v = validate(&descs[r], why);
+        if (v) {
+            fprintf(stderr, "nbg_create: replica %d: %s\n", r, why.c_str());
+            return v;
+        }
+    }
+    const nbg_system_desc* d0 = &descs[0];
+    for (int r = 1; r < n_replicas; ++r) {
+        const nbg_system_desc* d = &descs[r];
+        if (d->kind != d0->kind || d->potentials != d0->potentials || d->thermostat != d0->thermostat ||
+            d->bc != d0->bc || d->lj_cutoff != d0->lj_cutoff || d->el_cutoff != d0->el_cutoff ||
+            d->lj_sigma != d0->lj_sigma || d->lj_epsilon != d0->lj_epsilon || d->el_k != d0->el_k ||
+            d->skin != d0->skin || d->kb != d0->kb) {
+            fprintf(stderr, "nbg_create_batch: replica %d differs in kind/potentials/parameters\n", r);
+            return NBG_ERR_ARG;
+        }
+    }
+    if (n_replicas > 1 && d0->thermostat == NBG_THERMO_NOSEHOOVER) {
+        fprintf(stderr, "nbg_create_batch: Nose-Hoover batches are not supported\n");
+        return NBG_ERR_UNSUPPORTED;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        fprintf(stderr, "nbg_create: CUDA device %d not available\n", device);
+        return NBG_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return NBG_ERR_CUDA;
+    nbg_ctx* c = new nbg_ctx();
+    c->device = device;
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return NBG_ERR_CUDA;
+    }
+    c->stream = c->own_stream;
+    int st = build_context(c, descs, n_replicas);
+    if (st != NBG_OK) {
+        fprintf(stderr, "nbg_create: %s\n", c->err.c_str());
+        release(c);
+        delete c;
+        return st;
+    }
+    *out = c;
+    return NBG_OK;
+}
+
+extern "C" int nbg_create(const nbg_system_desc* desc, int device, nbg_ctx** out)
+{
+    return nbg_create_batch(desc, 1, device, out);
+}
+
+extern "C" void nbg_destroy(nbg_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    release(c);
+    delete c;
+}
+
+extern "C" int nbg_set_stream(nbg_ctx* c, void* s)
+{
+    if (!c) return NBG_ERR_ARG;
+    c->stream = s ? (cudaStream_t)s : c->own_stream;
+    return NBG_OK;
+}
+
+// ---------------------------------------------------------------------
+// forces and status
+// ---------------------------------------------------------------------
+static int read_status(nbg_ctx* c, unsigned* st)
+{
+    CK(cudaMemcpyAsync(st, c->d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream), "status read");
+    CK(cudaStreamSynchronize(c->stream), "stream sync");
+    return NBG_OK;
+}
+
+static int clear_status(nbg_ctx* c)
+{
+    CK(cudaMemsetAsync(c->d.status, 0, sizeof(unsigned), c->stream), "status clear");
+    return NBG_OK;
+}
+
+static int status_error(nbg_ctx* c, unsigned st)
+{
+    if (st & ST_NONFINITE) return fail(c, NBG_ERR_NONFINITE, "non-finite acceleration (NaN/Inf state or coincident bodies)");
+    if (st & ST_RANGE) return fail(c, NBG_ERR_RANGE, "minimum-image loop exceeded its iteration cap");
+    if (st & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) return fail(c, NBG_ERR_CAPACITY, "list capacity exceeded");
+    return NBG_OK;
+}
+
+// Potential accelerations of state s into s.a_new (no thermostat term).
+// parity: rebuild_flag word of the positions in s.
+static int forces(nbg_ctx* c, const StateView& s, bool force_build, int parity)
+{
+    int st = NBG_OK;
+    if (c->path == PATH_GRAVITY) {
+        st = launch_gravity(c, s);
+    } else if (c->path == PATH_LIST) {
+        if ((st = launch_list_build(c, s, force_build, parity))) return st;
+        st = launch_force_list(c, s);
+    } else {
+        st = launch_allpairs(c, s);
+    }
+    if (st) return st;
+    if (c->d.kind == NBG_SYSTEM_WATER) st = launch_bonded(c, s);
+    return st;
+}
+
+// grow the list capacities after an overflow
+static int grow_lists(nbg_ctx* c, unsigned st)
+{
+    int cell_cap = c->d.cell_cap, nbr_cap = c->d.nbr_cap;
+    if (st & ST_CELL_OVERFLOW) cell_cap *= 2;
+    if (st & ST_NBR_OVERFLOW) nbr_cap = nbr_cap + nbr_cap / 2 + 32;
+    return alloc_lists(c, cell_cap, nbr_cap);
+}
+
+// Evaluate forces on a one-off state (scratch view), retrying on overflow.
+static int forces_once(nbg_ctx* c, const StateView& s)
+{
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        int st;
+        if ((st = clear_status(c))) return st;
+        if ((st = launch_pack(c, s))) return st;
+        if ((st = forces(c, s, true, 0))) return st;
+        unsigned w = 0;
+        if ((st = read_status(c, &w))) return st;
+        if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
+            if ((st = grow_lists(c, w))) return st;
+            continue;
+        }
+        return status_error(c, w);
+    }
+    return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
+}
+
+static size_t state_bytes(const nbg_ctx* c) { return sizeof(double) * 3 * (size_t)c->cols; }
+
+// The scratch view shares the split positions and the lists with the
+// resident state: the next resident step rebuilds the lists (every step
+// repacks the positions anyway).
+static void resident_dirty(nbg_ctx* c) { c->steps_since_build = -1; }
+
+extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
+{
+    (void)t;
+    if (!c || !dv || !v || !u) return NBG_ERR_ARG;
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
+    CK(cudaMemsetAsync(c->ev.a_new, 0, state_bytes(c), c->stream), "dv clear");
+    resident_dirty(c);
+    int st = forces_once(c, c->ev);
+    if (st) return st;
+    if ((st = launch_rhs_thermostat(c, c->ev))) return st;
+    CK(cudaMemcpyAsync(dv, c->ev.a_new, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "dv download");
+    if (c->d.therm == NBG_THERMO_NOSEHOOVER)
+        CK(cudaMemcpyAsync(v + 3 * c->n, c->ev.v + 3 * c->n, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "v download");
+    CK(cudaStreamSynchronize(c->stream), "accel sync");
+    return NBG_OK;
+}
+
+extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
+{
+    if (!c || !u || !v) return NBG_ERR_ARG;
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(c->st.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    CK(cudaMemcpyAsync(c->st.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
+    c->state_valid = true;
+    c->accel_valid = false;
+    c->steps_since_build = -1;
+    return NBG_OK;
+}
+
+extern "C" int nbg_get_state(nbg_ctx* c, double* u, double* v)
+{
+    if (!c || (!u && !v)) return NBG_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (u) CK(cudaMemcpyAsync(u, c->st.x, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "u download");
+    if (v) CK(cudaMemcpyAsync(v, c->st.v, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "v download");
+    CK(cudaStreamSynchronize(c->stream), "state sync");
+    return NBG_OK;
+}
+
+extern "C" int nbg_compute_forces(nbg_ctx* c)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
+    cudaSetDevice(c->device);
+    int st;
+    if ((st = launch_pack(c, c->st))) return st;
+    if ((st = forces(c, c->st, c->steps_since_build < 0, (int)(c->step & 1)))) return st;
+    if (c->steps_since_build < 0) c->steps_since_build = 0;
+    return NBG_OK;
+}
+
+extern "C" int nbg_get_accel(nbg_ctx* c, double* dv)
+{
+    if (!c || !dv) return NBG_ERR_ARG;
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(dv, c->st.a_new, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "a download");
+    CK(cudaStreamSynchronize(c->stream), "accel sync");
+    unsigned w = 0;
+    int st = read_status(c, &w);
+    if (st) return st;
+    return status_error(c, w);
+}
+
+// ---------------------------------------------------------------------
+// the step loop
+// ---------------------------------------------------------------------
+struct Backup {
+    double *x = nullptr, *v = nullptr, *a = nullptr;
+};
+
+static int backup_alloc(nbg_ctx* c, Backup& b)
+{
+    int st;
+    if ((st = dalloc(c, &b.x, 3 * c->cols))) return st;
+    if ((st = dalloc(c, &b.v, 3 * c->cols))) return st;
+    if ((st = dalloc(c, &b.a, 3 * c->cols))) return st;
+    return NBG_OK;
+}
+
+static void backup_free(nbg_ctx* c, Backup& b)
+{
+    dfree(c, b.x);
+    dfree(c, b.v);
+    dfree(c, b.a);
+    b = Backup{};
+}
+
+// a_old = f(v, u) at the current resident state (SciML computes the first
+// acceleration before the first step; with Nose-Hoover this also writes the
+// rate into v, as the reference's RHS does).
+static int init_accel(nbg_ctx* c)
+{
+    int st;
+    if ((st = launch_pack(c, c->st))) return st;
+    if ((st = forces(c, c->st, true, (int)(c->step & 1)))) return st;
+    c->steps_since_build = 0;
+    if (c->d.therm != NBG_THERMO_LANGEVIN) {
+        if ((st = launch_rhs_thermostat(c, c->st))) return st;
+        CK(cudaMemcpyAsync(c->st.a_old, c->st.a_new, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "a init");
+    }
+    c->accel_valid = true;
+    return NBG_OK;
+}
+
+static int step_vv(nbg_ctx* c, double dt)
+{
+    int st;
+    const StateView& s = c->st;
+    if ((st = launch_drift(c, s, dt))) return st;
+    bool force = false;
+    if (c->path == PATH_LIST) {
+        int re = c->desc.rebuild_every;
+        force = c->steps_since_build < 0 || (re > 0 && c->steps_since_build + 1 >= re);
+    }
+    if ((st = forces(c, s, force, (int)((c->step + 1) & 1)))) return st;
+    c->steps_since_build = force ? 0 : c->steps_since_build + 1;
+    if (c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER)
+        if ((st = launch_temperature(c, s.v))) return st;
+    if ((st = launch_kick(c, s, dt))) return st;
+    if (c->d.therm == NBG_THERMO_ANDERSEN)
+        if ((st = launch_andersen(c, s, dt, c->step))) return st;
+    c->step++;
+    return NBG_OK;
+}
+
+static int step_em(nbg_ctx* c, double dt)
+{
+    int st;
+    const StateView& s = c->st;
+    bool force = false;
+    if (c->path == PATH_LIST) {
+        int re = c->desc.rebuild_every;
+        force = c->steps_since_build < 0 || (re > 0 && c->steps_since_build >= re);
+    }
+    if ((st = forces(c, s, force, (int)(c->step & 1)))) return st;
+    c->steps_since_build = force ? 1 : c->steps_since_build + 1;
+    if ((st = launch_em(c, s, dt, c->step))) return st;
+    c->step++;
+    return NBG_OK;
+}
+
+static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
+{
+    if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
+    if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
+    int st;
+    if ((st = clear_status(c))) return st;
+    const bool langevin = c->d.therm == NBG_THERMO_LANGEVIN;
+    if (!langevin && !c->accel_valid) {
+        if ((st = init_accel(c))) return st;
+    } else if (langevin) {
+        if ((st = launch_pack(c, c->st))) return st;
+    }
+    const bool can_overflow = c->path == PATH_LIST;
+    const int64_t chunk = can_overflow ? 512 : nsteps;
+    Backup b;
+    if (can_overflow && (st = backup_alloc(c, b))) return st;
+    int64_t done = 0;
+    int retries = 0;
+    while (done < nsteps) {
+        int64_t k = std::min<int64_t>(chunk > 0 ? chunk : nsteps, nsteps - done);
+        int64_t step0 = c->step, ssb0 = c->steps_since_build;
+        if (can_overflow) {
+            CK(cudaMemcpyAsync(b.x, c->st.x, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
+            CK(cudaMemcpyAsync(b.v, c->st.v, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
+            CK(cudaMemcpyAsync(b.a, c->st.a_old, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
+        }
+        for (int64_t s = 0; s < k; ++s) {
+            st = langevin ? step_em(c, dt) : step_vv(c, dt);
+            if (st) {
+                backup_free(c, b);
+                return st;
+            }
+        }
+        unsigned w = 0;
+        if ((st = read_status(c, &w))) { backup_free(c, b); return st; }
+        if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
+            if (++retries > 6) {
+                backup_free(c, b);
+                return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
+            }
+            if ((st = grow_lists(c, w))) { backup_free(c, b); return st; }
+            CK(cudaMemcpyAsync(c->st.x, b.x, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
+            CK(cudaMemcpyAsync(c->st.v, b.v, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
+            CK(cudaMemcpyAsync(c->st.a_old, b.a, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
+            c->step = step0;
+            c->steps_since_build = -1;
+            (void)ssb0;
+            if ((st = clear_status(c))) { backup_free(c, b); return st; }
+            if ((st = launch_pack(c, c->st))) { backup_free(c, b); return st; }
+            continue;
+        }
+        if ((st = status_error(c, w))) { backup_free(c, b); return st; }
+        done += k;
+    }
+    backup_free(c, b);
+    return NBG_OK;
+}
+
+extern "C" int nbg_advance(nbg_ctx* c, double dt, int64_t nsteps)
+{
+    if (!c) return NBG_ERR_ARG;
+    cudaSetDevice(c->device);
+    return advance_impl(c, dt, nsteps);
+}
+
+extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nsteps, int64_t save_every,
+                       double* traj_u, double* traj_v, nbg_run_stats* stats)
+{
+    if (!c || !u || !v) return NBG_ERR_ARG;
+    if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
+    cudaSetDevice(c->device);
+    int64_t launches0 = c->launches;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    CK(cudaEventRecord(e0, c->stream), "event");
+    unsigned long long builds0 = 0;
+    int st;
+    if ((st = nbg_set_state(c, u, v))) return st;
+    c->step = 0;
+    if (c->path == PATH_LIST) CK(cudaMemcpyAsync(&builds0, c->d.build_count, 8, cudaMemcpyDeviceToHost, c->stream), "builds");
+    size_t fb = state_bytes(c);
+    int64_t frame = 0;
+    if (traj_u) memcpy(traj_u, u, fb);
+    if (traj_v) memcpy(traj_v, v, fb);
+    ++frame;
+    int64_t done = 0;
+    while (done < nsteps) {
+        int64_t k = save_every > 0 ? std::min<int64_t>(save_every, nsteps - done) : nsteps - done;
+        if ((st = advance_impl(c, dt, k))) return st;
+        done += k;
+        if (traj_u || traj_v) {
+            if (traj_u) CK(cudaMemcpyAsync(traj_u + frame * 3 * c->cols, c->st.x, fb, cudaMemcpyDeviceToHost, c->stream), "traj");
+            if (traj_v) CK(cudaMemcpyAsync(traj_v + frame * 3 * c->cols, c->st.v, fb, cudaMemcpyDeviceToHost, c->stream), "traj");
+            ++frame;
+        }
+    }
+    CK(cudaMemcpyAsync(u, c->st.x, fb, cudaMemcpyDeviceToHost, c->stream), "u download");
+    CK(cudaMemcpyAsync(v, c->st.v, fb, cudaMemcpyDeviceToHost, c->stream), "v download");
+    CK(cudaEventRecord(e1, c->stream), "event");
+    CK(cudaStreamSynchronize(c->stream), "run sync");
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        unsigned long long builds1 = 0;
+        if (c->path == PATH_LIST) cudaMemcpy(&builds1, c->d.build_count, 8, cudaMemcpyDeviceToHost);
+        stats->steps = nsteps;
+        stats->list_builds = (int64_t)(builds1 - builds0);
+        stats->kernel_launches = c->launches - launches0;
+        stats->device_ms = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return NBG_OK;
+}
+
+extern "C" int nbg_energy(nbg_ctx* c, const double* u, const double* v, nbg_energies* out)
+{
+    if (!c || !u || !v || !out) return NBG_ERR_ARG;
+    if (c->nrep != 1) return fail(c, NBG_ERR_UNSUPPORTED, "energies are per system (create one context per replica)");
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
+    int st;
+    if ((st = clear_status(c))) return st;
+    double h[7];
+    if ((st = launch_energy(c, c->ev, h))) return st;
+    unsigned w = 0;
+    if ((st = read_status(c, &w))) return st;
+    if ((st = status_error(c, w))) return st;
+    out->kinetic = h[0];
+    out->lennard_jones = h[1];
+    out->electrostatic = h[2];
+    out->bonds = h[3];
+    out->angles = h[4];
+    out->gravity = h[5];
+    out->potential = h[1] + h[2] + h[3] + h[4];
+    out->total = out->kinetic + out->potential;
+    out->temperature = h[6] / (c->d.kb * c->reps_h[0].ndf);
+    return NBG_OK;
+}
+
+extern "C" int nbg_pair_list(nbg_ctx* c, const double* u, int32_t which, int32_t* pairs, int64_t cap, int64_t* count)
+{
+    if (!c || !u || !count || (which != NBG_POT_LJ && which != NBG_POT_EL)) return NBG_ERR_ARG;
+    if (!(c->d.pots & which)) return fail(c, NBG_ERR_ARG, "potential not present");
+    if (c->path == PATH_GRAVITY) return fail(c, NBG_ERR_UNSUPPORTED, "gravity has no pair list");
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    resident_dirty(c);
+    int st;
+    // build the lists for u (forces_once packs and rebuilds)
+    if ((st = forces_once(c, c->ev))) return st;
+    int64_t per = c->path == PATH_LIST ? c->d.nbr_cap : c->n;
+    int *dj = nullptr, *dc = nullptr;
+    CK(cudaMallocAsync((void**)&dj, sizeof(int) * per * c->n, c->stream), "pairs scratch");
+    CK(cudaMallocAsync((void**)&dc, sizeof(int) * c->n, c->stream), "pairs scratch");
+    if ((st = launch_pairs(c, c->ev, which, dj, dc, per))) return st;
+    std::vector<int> hj((size_t)per * c->n), hc(c->n);
+    CK(cudaMemcpyAsync(hj.data(), dj, sizeof(int) * per * c->n, cudaMemcpyDeviceToHost, c->stream), "pairs copy");
+    CK(cudaMemcpyAsync(hc.data(), dc, sizeof(int) * c->n, cudaMemcpyDeviceToHost, c->stream), "pairs copy");
+    cudaFreeAsync(dj, c->stream);
+    cudaFreeAsync(dc, c->stream);
+    CK(cudaStreamSynchronize(c->stream), "pairs sync");
+    unsigned w = 0;
+    if ((st = read_status(c, &w))) return st;
+    if ((st = status_error(c, w))) return st;
+    int64_t total = 0;
+    for (int64_t i = 0; i < c->n; ++i) {
+        int m = std::min<int64_t>(hc[i], per);
+        std::sort(hj.begin() + i * per, hj.begin() + i * per + m);
+        for (int k = 0; k < m; ++k) {
+            if (pairs && total < cap) {
+                pairs[2 * total] = (int32_t)i;
+                pairs[2 * total + 1] = hj[i * per + k];
+            }
+            ++total;
+        }
+    }
+    *count = total;
+    return NBG_OK;
+}

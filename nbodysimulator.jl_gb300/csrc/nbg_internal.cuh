@@ -1,0 +1,421 @@
+// nbg_internal.cuh - shared declarations and device helpers of libnbg.
+//
+// Data layout in device memory (one context = one system or a batch of
+// replicas, atoms of replica r at [atom0_r, atom0_r + n_r)):
+//   x, v, a_old, a_new : double[3 * cols]  (the reference's 3 x n column-major
+//                        state, Nose-Hoover column last for a single system)
+//   phi, plo           : float4[n] split positions: phi = (hi.xyz, w),
+//                        plo = (lo.xyz, flags) with x = hi + lo to ~2^-48
+//                        relative. Under cubic boundaries hi is the wrapped
+//                        position rounded to a 2^-k grid (k = 23 - ceil(log2 L))
+//                        so that hi_i - hi_j and the +-L image shift are exact
+//                        in FP32; w is the charge (pair path) or mass (gravity).
+//   cell_count/cell_atoms, nbr/nbr_count, xref : cell and Verlet lists.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/nbg.h"
+
+// device status word bits
+#define ST_CELL_OVERFLOW 1u
+#define ST_NBR_OVERFLOW 2u
+#define ST_NONFINITE 4u
+#define ST_RANGE 8u
+
+// atom flags (plo.w bits)
+#define AF_LJ 1
+
+// relative margin of the FP32 cutoff classification; pairs whose FP32 r^2 lies
+// within it of R^2 are classified again with the reference's FP64 arithmetic.
+#define CLASSIFY_MARGIN 1.0e-5
+
+// iteration cap of the reference's minimum-image while loops
+#define MINIMAGE_MAX_ITERS 65536
+
+struct RepDev {
+    int64_t atom0, n;   // atom range of the replica
+    double L, invL;     // cubic box
+    double box[6];      // general periodic box (lo,hi per axis)
+    float Lh, Ll;       // L split on the hi grid: L = Lh + Ll
+    float invLf;
+    float qscale, qinv; // 2^k and 2^-k of the hi grid
+    float lj_lo, lj_hi; // FP32 r^2 below lo: inside; >= hi: outside; else exact
+    float el_lo, el_hi;
+    float rl2;          // Verlet-list radius^2 (inflated)
+    int nc;             // cells per dimension
+    int cell0;          // first cell of the replica
+    double cell_inv;    // nc / L
+    double T0, tparam;  // thermostat target and tau / nu / gamma
+    double sigma;       // Langevin noise amplitude (potential systems)
+    double sigma_num;   // sqrt(2 gamma kb T) (water)
+    double ndf;         // 3N - Nc
+    uint64_t seed;
+};
+
+// Everything a kernel needs, passed by value.
+struct Dev {
+    int64_t n;          // atoms (all replicas)
+    int64_t cols;       // state columns (n, +1 with Nose-Hoover)
+    int kind, bc, therm, nrep;
+    uint32_t pots;
+    // parameters
+    float lj_sig2, lj_eps24;
+    double lj_sig2_d, lj_eps, lj_R2;
+    float el_k, el_krf2;          // k and 2 k_rf (reaction field)
+    double el_k_d, el_R, el_R2, el_krf, el_crf;
+    double G, mu4pi, kb;
+    double rOH, aHOH, kbond, kangle;
+    double skin_half2;            // (skin/2)^2
+    // per atom
+    const double* mass;
+    const double* inv_mass;
+    const double* charge;
+    const double* dipole;
+    const int* rep_of;
+    const RepDev* reps;
+    float4* phi;
+    float4* plo;
+    // lists
+    int* cell_count;
+    int* cell_n;
+    int* cell_atoms;
+    int cell_cap;
+    int ncell_total;
+    int* nbr;
+    int* nbr_count;
+    int nbr_cap;
+    int64_t nbr_stride;
+    double* xref;
+    int* rebuild_flag;          // [2], indexed by the parity of the position time index
+    unsigned long long* build_count;
+    unsigned* status;
+    // reductions
+    double* red_partial;
+    double* red_T;      // per replica temperature of the current velocities
+    unsigned* red_counter;
+    int red_slices;
+    // gravity
+    int grav_plain;
+};
+
+struct StateView {
+    double* x;
+    double* v;
+    double* a_old;
+    double* a_new;
+};
+
+struct nbg_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    nbg_system_desc desc{};
+    int nrep = 1;
+    std::vector<RepDev> reps_h;
+    std::vector<double> mass_h, charge_h, dipole_h;
+    int64_t n = 0, cols = 0;
+    int path = 0;          // PATH_*
+    Dev d{};
+    StateView st{};        // resident state
+    StateView ev{};        // scratch state for nbg_accel / nbg_energy / nbg_pair_list
+    bool state_valid = false;
+    bool accel_valid = false;
+    int64_t step = 0;      // steps taken on the resident state
+    int64_t steps_since_build = 0;
+    int64_t list_builds = 0;
+    int64_t launches = 0;
+    // gravity path: bodies padded to npad (multiple of the 256-body tile)
+    int64_t npad = 0;
+    int grav_chunks = 1;
+    double* grav_part = nullptr;
+    // profiling of the dominant force kernel
+    bool profiling = false;
+    std::vector<cudaEvent_t> prof_events;  // start/stop pairs not yet read
+    double prof_ms = 0.0;
+    int64_t prof_count = 0;
+    std::string err;
+    std::vector<void*> allocs;
+};
+
+enum { PATH_GRAVITY = 0, PATH_LIST = 1, PATH_ALLPAIRS = 2 };
+
+// ---------------------------------------------------------------------
+// host-side launchers (one translation unit each)
+// ---------------------------------------------------------------------
+int launch_pack(nbg_ctx* c, const StateView& s);
+int launch_gravity(nbg_ctx* c, const StateView& s);
+int launch_allpairs(nbg_ctx* c, const StateView& s);
+int launch_list_build(nbg_ctx* c, const StateView& s, bool force, int parity);
+int launch_force_list(nbg_ctx* c, const StateView& s);
+int launch_bonded(nbg_ctx* c, const StateView& s);
+int launch_drift(nbg_ctx* c, const StateView& s, double dt);
+int launch_temperature(nbg_ctx* c, const double* v);
+int launch_kick(nbg_ctx* c, const StateView& s, double dt);
+int launch_andersen(nbg_ctx* c, const StateView& s, double dt, int64_t step);
+int launch_em(nbg_ctx* c, const StateView& s, double dt, int64_t step);
+int launch_rhs_thermostat(nbg_ctx* c, const StateView& s);
+int gravity_plan_chunks(nbg_ctx* c, int64_t npad);
+int launch_energy(nbg_ctx* c, const StateView& s, double* out_host /*[8]*/);
+int launch_pairs(nbg_ctx* c, const StateView& s, int which, int* out_j, int* out_cnt, int64_t cap_per_atom);
+
+// events around the dominant force kernel when profiling is on
+void prof_begin(nbg_ctx* c);
+void prof_end(nbg_ctx* c);
+
+// record a CUDA error on the context; returns NBG_ERR_CUDA
+int cuda_fail(nbg_ctx* c, cudaError_t e, const char* what);
+
+#define NBG_LAUNCH_CHECK(c, what)                                  \
+    do {                                                           \
+        (c)->launches++;                                           \
+        cudaError_t _e = cudaGetLastError();                       \
+        if (_e != cudaSuccess) return cuda_fail((c), _e, (what));  \
+    } while (0)
+
+static inline int grid_for(int64_t work, int block)
+{
+    int64_t g = (work + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 1048576) g = 1048576;
+    return (int)g;
+}
+
+// ---------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------
+#ifdef __CUDACC__
+
+__device__ __forceinline__ void status_set(unsigned* st, unsigned bit) { atomicOr(st, bit); }
+
+// The reference's get_interparticle_distance in FP64, no contraction
+// (boundary_conditions.jl:111-172). Returns false when a while loop exceeded
+// MINIMAGE_MAX_ITERS (non-finite or absurdly distant coordinates).
+struct Dist64 {
+    double x, y, z, r2;
+};
+
+__device__ __forceinline__ bool wrap_cubic64(double& x, double size, double radius)
+{
+    int it = 0;
+    while (x >= radius) {
+        x = __dsub_rn(x, size);
+        if (++it > MINIMAGE_MAX_ITERS) return false;
+    }
+    while (x < -radius) {
+        x = __dadd_rn(x, size);
+        if (++it > MINIMAGE_MAX_ITERS) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool wrap_periodic64(double& x, double lo, double hi)
+{
+    int it = 0;
+    double w = __dsub_rn(hi, lo);
+    while (x < lo) {
+        x = __dadd_rn(x, w);
+        if (++it > MINIMAGE_MAX_ITERS) return false;
+    }
+    while (x >= hi) {
+        x = __dsub_rn(x, w);
+        if (++it > MINIMAGE_MAX_ITERS) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool distance64(const double* xi, const double* xj, int bc, const RepDev& R, Dist64& o)
+{
+    double x = __dsub_rn(xi[0], xj[0]);
+    double y = __dsub_rn(xi[1], xj[1]);
+    double z = __dsub_rn(xi[2], xj[2]);
+    bool ok = true;
+    if (bc == NBG_BC_CUBIC) {
+        double size = R.L;
+        double radius = __dmul_rn(0.5, size);
+        ok = wrap_cubic64(x, size, radius) && wrap_cubic64(y, size, radius) && wrap_cubic64(z, size, radius);
+    } else if (bc == NBG_BC_PERIODIC) {
+        ok = wrap_periodic64(x, R.box[0], R.box[1]) && wrap_periodic64(y, R.box[2], R.box[3]) &&
+             wrap_periodic64(z, R.box[4], R.box[5]);
+    }
+    o.x = x;
+    o.y = y;
+    o.z = z;
+    o.r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+    return ok;
+}
+
+// FP32 difference of two split positions; under cubic boundaries the hi
+// parts are exact multiples of the grid and the image shift is exact.
+__device__ __forceinline__ float3 split_diff(const float4& hi_i, const float4& lo_i, const float4& hi_j,
+                                             const float4& lo_j, bool cubic, const RepDev& R)
+{
+    float dxh = __fsub_rn(hi_i.x, hi_j.x);
+    float dyh = __fsub_rn(hi_i.y, hi_j.y);
+    float dzh = __fsub_rn(hi_i.z, hi_j.z);
+    float dxl = __fsub_rn(lo_i.x, lo_j.x);
+    float dyl = __fsub_rn(lo_i.y, lo_j.y);
+    float dzl = __fsub_rn(lo_i.z, lo_j.z);
+    if (cubic) {
+        // s = rint(dh / L) by the 1.5 * 2^23 trick, exact for |dh/L| <= 1
+        const float magic = 12582912.0f;
+        float sx = __fsub_rn(__fmaf_rn(dxh, R.invLf, magic), magic);
+        float sy = __fsub_rn(__fmaf_rn(dyh, R.invLf, magic), magic);
+        float sz = __fsub_rn(__fmaf_rn(dzh, R.invLf, magic), magic);
+        dxh = __fmaf_rn(-sx, R.Lh, dxh);
+        dyh = __fmaf_rn(-sy, R.Lh, dyh);
+        dzh = __fmaf_rn(-sz, R.Lh, dzh);
+        dxl = __fmaf_rn(-sx, R.Ll, dxl);
+        dyl = __fmaf_rn(-sy, R.Ll, dyl);
+        dzl = __fmaf_rn(-sz, R.Ll, dzl);
+    }
+    return make_float3(__fadd_rn(dxh, dxl), __fadd_rn(dyh, dyl), __fadd_rn(dzh, dzl));
+}
+
+// Electrostatic exclusion: self, or the same molecule for water
+// (nbody_to_ode.jl:316-351).
+__device__ __forceinline__ bool el_excluded(int kind, int64_t i, int64_t j)
+{
+    return kind == NBG_SYSTEM_WATER ? (i / 3 == j / 3) : (i == j);
+}
+
+// Result of classifying and evaluating one ordered pair (i, j).
+struct PairOut {
+    float fx, fy, fz;   // force contribution (already scaled by 24 eps / k q_i)
+    int lj_in, el_in;
+    bool range_err;
+};
+
+// One ordered pair of the cutoff potentials (LJ basic_potentials.jl:253-265,
+// electrostatics :288-297 generalised to reaction field). Classification:
+// FP32 r^2 decides clear cases, pairs within CLASSIFY_MARGIN of a cutoff (or
+// near the half-box image ambiguity) are decided by the reference's FP64
+// arithmetic on the unwrapped positions, so the pair set equals the
+// reference's bit for bit.
+__device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, int64_t i, int64_t j,
+                                               const float4& hi_i, const float4& lo_i, const float4& hi_j,
+                                               const float4& lo_j, float kqi, const double* X)
+{
+    PairOut o;
+    o.fx = o.fy = o.fz = 0.0f;
+    o.lj_in = o.el_in = 0;
+    o.range_err = false;
+    const bool cubic = d.bc == NBG_BC_CUBIC;
+    float3 dr = split_diff(hi_i, lo_i, hi_j, lo_j, cubic, R);
+    float r2 = __fmaf_rn(dr.x, dr.x, __fmaf_rn(dr.y, dr.y, __fmul_rn(dr.z, dr.z)));
+    const bool lj_pair = (d.pots & NBG_POT_LJ) && ((__float_as_int(lo_i.w) & __float_as_int(lo_j.w) & AF_LJ) != 0);
+    const bool el_pair = (d.pots & NBG_POT_EL) && !el_excluded(d.kind, i, j);
+    bool amb = false;
+    if (lj_pair) {
+        if (r2 < R.lj_lo) o.lj_in = 1;
+        else if (r2 < R.lj_hi) amb = true;
+    }
+    if (el_pair) {
+        if (r2 < R.el_lo) o.el_in = 1;
+        else if (r2 < R.el_hi) amb = true;
+    }
+    if (amb || d.bc == NBG_BC_PERIODIC) {
+        Dist64 q;
+        bool ok = distance64(X + 3 * i, X + 3 * j, d.bc, R, q);
+        if (!ok) {
+            o.range_err = true;
+            o.lj_in = o.el_in = 0;
+            return o;
+        }
+        o.lj_in = lj_pair && (q.r2 < d.lj_R2);
+        o.el_in = el_pair && (q.r2 < d.el_R2);
+        dr = make_float3((float)q.x, (float)q.y, (float)q.z);
+        r2 = (float)q.r2;
+    }
+    float factor = 0.0f;
+    if (o.lj_in) {
+        float s6 = __fdividef(d.lj_sig2, r2);
+        s6 = s6 * s6 * s6;
+        float s12 = s6 * s6;
+        factor = d.lj_eps24 * __fdividef(2.0f * s12 - s6, r2);
+    }
+    if (o.el_in) {
+        float rinv = rsqrtf(r2);
+        // reaction field: q_j (1/r^3 - 2 k_rf); k_rf = 0 for eps_rf = 1
+        factor += kqi * hi_j.w * (rinv * rinv * rinv - d.el_krf2);
+    }
+    o.fx = factor * dr.x;
+    o.fy = factor * dr.y;
+    o.fz = factor * dr.z;
+    return o;
+}
+
+// TwoSum: s + e = a + b exactly (Knuth).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Accumulator of float partials with a compensated (hi, lo) pair.
+struct Acc2 {
+    float hi, lo;
+    __device__ __forceinline__ void add(float p)
+    {
+        float s, e;
+        two_sum(hi, p, s, e);
+        hi = s;
+        lo = __fadd_rn(lo, e);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Philox4x32-10 (Salmon et al., SC'11); counter (atom, step lo, step hi, stream)
+__device__ __forceinline__ uint4 philox(uint64_t seed, uint64_t atom, uint64_t step, uint32_t stream)
+{
+    uint32_t c0 = (uint32_t)atom, c1 = (uint32_t)step, c2 = (uint32_t)(step >> 32), c3 = stream;
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return make_uint4(c0, c1, c2, c3);
+}
+
+__device__ __forceinline__ double philox_u53(uint64_t seed, uint64_t atom, uint64_t step)
+{
+    uint4 w = philox(seed, atom, step, 0u);
+    return ((double)(w.x >> 5) * 67108864.0 + (double)(w.y >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// Three normals from 24-bit uniforms (same draws as the oracle's).
+template <typename T>
+__device__ __forceinline__ void philox_normals3(uint64_t seed, uint64_t atom, uint64_t step, T out[3])
+{
+    uint4 w1 = philox(seed, atom, step, 1u);
+    uint4 w2 = philox(seed, atom, step, 2u);
+    const T two_pi = (T)6.283185307179586;
+    const T s24 = (T)(1.0 / 16777216.0);
+    T u1 = ((T)(w1.x >> 8) + (T)1) * s24;
+    T u2 = (T)(w1.y >> 8) * s24;
+    T rr = sqrt((T)-2 * log(u1));
+    T sn, cs;
+    sincos(two_pi * u2, &sn, &cs);
+    out[0] = rr * cs;
+    out[1] = rr * sn;
+    T u3 = ((T)(w2.x >> 8) + (T)1) * s24;
+    T u4 = (T)(w2.y >> 8) * s24;
+    out[2] = sqrt((T)-2 * log(u3)) * cos(two_pi * u4);
+}
+
+#endif  // __CUDACC__

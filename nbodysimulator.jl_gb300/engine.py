@@ -1,0 +1,137 @@
+"""Thin object wrapper over one libnbg context (include/nbg.h)."""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+
+
+def _check(lib, ctx, status):
+    if status != _abi.NBG_OK:
+        msg = lib.nbg_last_error(ctx) if ctx else b""
+        raise _abi.EngineError(status, (msg or b"").decode())
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.size != int(np.prod(shape)):
+        raise ValueError(f"expected {shape}, got {a.shape}")
+    return a
+
+
+class Engine:
+    """A device-resident system (or batch of replicas) on one GPU.
+
+    State arrays are (cols, 3) float64 in memory, i.e. the reference's 3 x n
+    column-major layout; cols = n, or n + 1 with the Nose-Hoover column."""
+
+    def __init__(self, descs, device=0):
+        self.lib = _abi.load_library()
+        ptr = ctypes.c_void_p()
+        if isinstance(descs, _abi.NbgSystemDesc):
+            descs = [descs]
+        arr = (_abi.NbgSystemDesc * len(descs))(*descs)
+        if len(descs) == 1:
+            st = self.lib.nbg_create(arr, int(device), ctypes.byref(ptr))
+        else:
+            st = self.lib.nbg_create_batch(arr, len(descs), int(device), ctypes.byref(ptr))
+        if st != _abi.NBG_OK:
+            raise _abi.EngineError(st, "nbg_create failed")
+        self.ctx = ptr
+        self.cols = sum(int(d.n) + (1 if d.thermostat == _abi.NBG_THERMO_NOSEHOOVER else 0) for d in descs)
+
+    def _chk(self, st):
+        _check(self.lib, self.ctx, st)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.nbg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def accel(self, v, u, t=0.0):
+        """soode_system!(dv, v, u, p, t); returns dv. With Nose-Hoover the
+        thermostat rate is written into v[-1, 0] as in the reference."""
+        u = _f64(u)
+        dv = np.zeros_like(u)
+        if not (isinstance(v, np.ndarray) and v.dtype == np.float64 and v.flags.c_contiguous):
+            raise TypeError("v must be a C-contiguous float64 array (it may be written)")
+        self._chk(self.lib.nbg_accel(self.ctx, _abi.as_dptr(dv), _abi.as_dptr(v), _abi.as_dptr(u), float(t)))
+        return dv
+
+    def set_state(self, u, v):
+        u, v = _f64(u), _f64(v)
+        self._chk(self.lib.nbg_set_state(self.ctx, _abi.as_dptr(u), _abi.as_dptr(v)))
+
+    def get_state(self):
+        u = np.zeros((self.cols, 3))
+        v = np.zeros((self.cols, 3))
+        self._chk(self.lib.nbg_get_state(self.ctx, _abi.as_dptr(u), _abi.as_dptr(v)))
+        return u, v
+
+    def compute_forces(self):
+        self._chk(self.lib.nbg_compute_forces(self.ctx))
+
+    def get_accel(self):
+        a = np.zeros((self.cols, 3))
+        self._chk(self.lib.nbg_get_accel(self.ctx, _abi.as_dptr(a)))
+        return a
+
+    def advance(self, dt, nsteps):
+        self._chk(self.lib.nbg_advance(self.ctx, float(dt), int(nsteps)))
+
+    def run(self, u, v, dt, nsteps, save_every=0, save_trajectory=True):
+        """Upload (u, v), run, download. Returns (u, v, traj_u, traj_v, stats);
+        traj arrays have shape (frames, cols, 3)."""
+        u = _f64(u).copy()
+        v = _f64(v).copy()
+        nframes = (nsteps // save_every + 1 if save_every > 0 else 1) + 1
+        tu = np.zeros((nframes, self.cols, 3)) if save_trajectory else None
+        tv = np.zeros((nframes, self.cols, 3)) if save_trajectory else None
+        stats = _abi.NbgRunStats()
+        self._chk(self.lib.nbg_run(self.ctx, _abi.as_dptr(u), _abi.as_dptr(v), float(dt), int(nsteps),
+                                   int(save_every), _abi.as_dptr(tu), _abi.as_dptr(tv), ctypes.byref(stats)))
+        if save_trajectory:
+            used = nsteps // save_every + 1 if save_every > 0 else 1
+            if nsteps > 0 and (save_every <= 0 or nsteps % save_every != 0):
+                used += 1
+            tu, tv = tu[:used], tv[:used]
+        return u, v, tu, tv, stats
+
+    def energy(self, u, v):
+        out = _abi.NbgEnergies()
+        u, v = _f64(u), _f64(v)
+        self._chk(self.lib.nbg_energy(self.ctx, _abi.as_dptr(u), _abi.as_dptr(v), ctypes.byref(out)))
+        return out.as_dict()
+
+    def pair_list(self, u, which):
+        u = _f64(u)
+        cnt = ctypes.c_int64()
+        self._chk(self.lib.nbg_pair_list(self.ctx, _abi.as_dptr(u), int(which), None, 0, ctypes.byref(cnt)))
+        pairs = np.zeros((max(cnt.value, 1), 2), dtype=np.int32)
+        self._chk(self.lib.nbg_pair_list(self.ctx, _abi.as_dptr(u), int(which),
+                                         pairs.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                         cnt.value, ctypes.byref(cnt)))
+        return pairs[: cnt.value]
+
+    def set_stream(self, stream_ptr):
+        self._chk(self.lib.nbg_set_stream(self.ctx, ctypes.c_void_p(stream_ptr)))
+
+    def set_profiling(self, on=True):
+        self._chk(self.lib.nbg_set_profiling(self.ctx, 1 if on else 0))
+
+    def force_kernel_time(self):
+        """(summed ms, launches) of the dominant force kernel since the last call."""
+        ms = ctypes.c_double()
+        cnt = ctypes.c_int64()
+        self._chk(self.lib.nbg_force_kernel_time(self.ctx, ctypes.byref(ms), ctypes.byref(cnt)))
+        return ms.value, cnt.value
+
+    @property
+    def kernel_launches(self):
+        return int(self.lib.nbg_kernel_launches(self.ctx))

@@ -1,0 +1,246 @@
+"""GPU engine (libnbg.so through the C ABI) against the FP64 oracle on the
+same seeded inputs: forces within the relative-RMSE tolerance of 1e-5, the
+cutoff pair sets bit for bit, energies, thermostat terms and trajectories."""
+import math
+
+import numpy as np
+import pytest
+
+import systems as S
+
+nbg = S.nbg
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5  # relative RMSE of accelerations vs the FP64 oracle
+
+
+def _accel_pair(gpu, oracle, sim, perturb=0.0, seed=0):
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    if perturb:
+        rng = np.random.default_rng(seed)
+        n = desc.n
+        u = u.copy()
+        u[:n] += rng.uniform(-perturb, perturb, size=(n, 3))
+    eng = nbg.Engine(desc, 0)
+    a_gpu = eng.accel(v.copy(), u)
+    a_ref, _ = oracle.accel(desc, v, u)
+    return eng, desc, keep, u, v, a_gpu, a_ref
+
+
+@pytest.mark.parametrize("flags", [0, nbg._abi.NBG_FLAG_GRAV_PLAIN])
+def test_gravity_forces(gpu, oracle, flags):
+    sim = S.plummer(3000, seed=5, flags=flags)
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    err = S.rel_rmse(ag, ar)
+    print(f"gravity {'plain' if flags else 'compensated'} rel RMSE {err:.3e}")
+    if not flags:
+        assert err <= FORCE_TOL
+    else:
+        assert err <= 1e-3
+    # Newton's third law in the sum: total force ~ 0
+    m = np.asarray(keep[0])
+    assert np.abs((m[:, None] * ag).sum(axis=0)).max() <= 1e-6 * np.abs(m[:, None] * ag).sum()
+
+
+def test_gravity_tile_edges(gpu, oracle):
+    """N not a multiple of the 256-body tile: padding bodies contribute nothing."""
+    for n in (3, 257, 511, 1000):
+        sim = S.plummer(n, seed=n)
+        eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+        assert S.rel_rmse(ag, ar) <= FORCE_TOL, n
+        eng.close()
+
+
+@pytest.mark.parametrize("flags", [0, nbg._abi.NBG_FLAG_ALL_PAIRS])
+def test_lj_forces_and_pair_set(gpu, oracle, flags):
+    sim = S.lj_liquid(1000, seed=2, jitter=0.15, flags=flags)
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    assert S.rel_rmse(ag, ar) <= FORCE_TOL
+    pg = eng.pair_list(u, nbg._abi.NBG_POT_LJ)
+    po = oracle.pair_list(desc, u, nbg._abi.NBG_POT_LJ)
+    assert pg.shape == po.shape and np.array_equal(pg, po)
+
+
+def test_lj_pair_set_at_cutoff_boundary(gpu, oracle):
+    """Pairs placed within a few ulps of r = R: the FP64 re-check decides."""
+    R = 2.5
+    L = 10.0
+    eps = np.finfo(np.float64).eps
+    pos = []
+    for k, d in enumerate([R * (1 - 4 * eps), R, R * (1 + 4 * eps), R * (1 - 1e-7), R * (1 + 1e-7)]):
+        base = np.array([1.0 + 1.9 * k, 0.5 + 1.9 * k, 2.0])
+        pos += [base, base + np.array([d, 0.0, 0.0])]
+    # across the periodic boundary as well
+    pos += [np.array([0.2, 7.0, 7.0]), np.array([0.2 + L - R, 7.0, 7.0])]
+    pos = np.array(pos)
+    bodies = [nbg.MassBody(p, (0, 0, 0), 1.0) for p in pos]
+    system = nbg.PotentialNBodySystem(bodies, {"lennard_jones": nbg.LennardJonesParameters(1.0, 1.0, R)})
+    sim = nbg.NBodySimulation(system, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), kb=1.0, skin=0.3)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    eng = nbg.Engine(desc, 0)
+    pg = eng.pair_list(u, nbg._abi.NBG_POT_LJ)
+    po = oracle.pair_list(desc, u, nbg._abi.NBG_POT_LJ)
+    assert np.array_equal(pg, po)
+
+
+def test_coulomb_unbounded_forces(gpu, oracle):
+    rng = np.random.default_rng(4)
+    n = 300
+    bodies = [nbg.ChargedParticle(rng.uniform(-1, 1, 3), (0, 0, 0), rng.uniform(0.5, 2), rng.choice([-1.0, 1.0]))
+              for _ in range(n)]
+    sim = nbg.NBodySimulation(nbg.ChargedParticles(bodies, 1.0), (0.0, 1.0))
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    assert S.rel_rmse(ag, ar) <= FORCE_TOL
+
+
+def test_lj_plus_coulomb_cubic(gpu, oracle):
+    """Both cutoff potentials on one system (distinct cutoffs) on the list path."""
+    pos, vel, L = nbg.workloads.lj_argon_lattice(1000, seed=9, jitter=0.1)
+    rng = np.random.default_rng(9)
+    bodies = [nbg.ChargedParticle(pos[i], vel[i], 1.0, rng.choice([-0.5, 0.5])) for i in range(len(pos))]
+    system = nbg.PotentialNBodySystem(bodies, {"lennard_jones": nbg.LennardJonesParameters(1.0, 1.0, 2.5),
+                                               "electrostatic": nbg.ElectrostaticParameters(1.0, 3.0)})
+    sim = nbg.NBodySimulation(system, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), kb=1.0, skin=0.3)
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    assert S.rel_rmse(ag, ar) <= FORCE_TOL
+    for which in (nbg._abi.NBG_POT_LJ, nbg._abi.NBG_POT_EL):
+        assert np.array_equal(eng.pair_list(u, which), oracle.pair_list(desc, u, which))
+
+
+def test_magnetic_dipoles(gpu, oracle):
+    rng = np.random.default_rng(5)
+    bodies = [nbg.MagneticParticle(rng.uniform(-1, 1, 3), (0, 0, 0), 1.0, rng.normal(size=3)) for _ in range(64)]
+    system = nbg.PotentialNBodySystem(bodies, {"magnetostatic": nbg.MagnetostaticParameters(1.0)})
+    sim = nbg.NBodySimulation(system, (0.0, 1.0))
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    assert S.rel_rmse(ag, ar) <= FORCE_TOL
+
+
+@pytest.mark.parametrize("n_mol", [3, 216, 1000])
+def test_water_forces_and_pair_sets(gpu, oracle, n_mol):
+    """SPC/Fw: O-O LJ, molecule-excluded electrostatics, bonds, angles (all-pairs
+    path for small boxes, Verlet-list path for 1000 molecules)."""
+    if n_mol == 3:
+        sim, _, _ = S.water3()
+    else:
+        sim = S.water_box(n_mol, seed=n_mol)
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    assert S.rel_rmse(ag, ar) <= FORCE_TOL
+    for which in (nbg._abi.NBG_POT_LJ, nbg._abi.NBG_POT_EL):
+        assert np.array_equal(eng.pair_list(u, which), oracle.pair_list(desc, u, which))
+
+
+def test_reaction_field_eps1_equals_truncated_coulomb(gpu):
+    """eps_rf = 1 is the reference's truncated Coulomb; eps_rf > 1 adds the
+    2 k_rf r term."""
+    s1 = S.water_box(1000, seed=1, eps_rf=1.0)
+    s2 = S.water_box(1000, seed=1, eps_rf=78.0)
+    d1, k1 = nbg.system_descriptor(s1)
+    d2, k2 = nbg.system_descriptor(s2)
+    u, v = S.state(s1)
+    a1 = nbg.Engine(d1, 0).accel(v.copy(), u)
+    a2 = nbg.Engine(d2, 0).accel(v.copy(), u)
+    assert S.rel_rmse(a2, a1) > 1e-4
+
+
+@pytest.mark.parametrize("kind", ["berendsen", "nosehoover"])
+def test_thermostat_rhs(gpu, oracle, kind):
+    th = nbg.BerendsenThermostat(0.8, 0.1) if kind == "berendsen" else nbg.NoseHooverThermostat(0.8, 0.1)
+    sim = S.lj_liquid(1000, seed=3, jitter=0.1, thermostat=th)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    if kind == "nosehoover":
+        u[-1, 0] = 0.37  # zeta
+    eng = nbg.Engine(desc, 0)
+    vg = v.copy()
+    ag = eng.accel(vg, u)
+    ar, vr = oracle.accel(desc, v, u)
+    assert S.rel_rmse(ag, ar) <= FORCE_TOL
+    if kind == "nosehoover":
+        assert vg[-1, 0] == pytest.approx(vr[-1, 0], rel=1e-12)
+        assert np.all(ag[-1] == 0)
+
+
+def test_energies_match_oracle(gpu, oracle):
+    for sim in (S.lj_liquid(1000, seed=4, jitter=0.1), S.water_box(216, seed=2), S.plummer(2000, seed=1),
+                S.water3()[0], S.charges8()[0]):
+        desc, keep = nbg.system_descriptor(sim)
+        u, v = S.state(sim)
+        eg = nbg.Engine(desc, 0).energy(u, v)
+        eo = oracle.energy(desc, u, v)
+        for k in ("kinetic", "lennard_jones", "electrostatic", "bonds", "angles", "gravity", "temperature"):
+            assert eg[k] == pytest.approx(eo[k], rel=1e-11, abs=1e-300), k
+
+
+@pytest.mark.parametrize("case", ["lj_list", "lj_berendsen", "lj_nosehoover", "water_list", "gravity"])
+def test_short_trajectories(gpu, oracle, case):
+    """A few velocity-Verlet steps on the GPU track the FP64 oracle (FP32 pair
+    forces, FP64 integration)."""
+    if case == "lj_list":
+        sim, dt, n, tol = S.lj_liquid(1000, seed=5), 0.005, 25, 1e-8
+    elif case == "lj_berendsen":
+        sim, dt, n, tol = S.lj_liquid(1000, seed=5, thermostat=nbg.BerendsenThermostat(1.5, 0.05)), 0.005, 25, 1e-8
+    elif case == "lj_nosehoover":
+        sim, dt, n, tol = S.lj_liquid(1000, seed=5, thermostat=nbg.NoseHooverThermostat(1.5, 0.05)), 0.005, 25, 1e-8
+    elif case == "water_list":
+        sim, dt, n, tol = S.water_box(1000, seed=6), 0.0005, 20, 1e-8
+    else:
+        sim, dt, n, tol = S.plummer(2048, seed=6), 1e-3, 20, 1e-8
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    eng = nbg.Engine(desc, 0)
+    ug, vg, _, _, stats = eng.run(u, v, dt, n, 0, save_trajectory=False)
+    uo, vo = oracle.run(desc, u, v, dt, n)
+    scale = np.abs(uo).max()
+    assert np.abs(ug - uo).max() <= tol * max(scale, 1.0), np.abs(ug - uo).max()
+    assert stats.kernel_launches > 0
+
+
+def test_langevin_em_one_step(gpu, oracle):
+    """Euler-Maruyama with the same Philox draws (FP32 Box-Muller on the GPU)."""
+    sim = S.lj_liquid(1000, seed=6, thermostat=nbg.LangevinThermostat(1.0, 1.0))
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    ug, vg, _, _, _ = nbg.Engine(desc, 0).run(u, v, 0.005, 1, 0, save_trajectory=False)
+    uo, vo = oracle.run(desc, u, v, 0.005, 1)
+    assert np.abs(ug - uo).max() <= 1e-12
+    assert np.abs(vg - vo).max() <= 1e-5 * np.abs(vo).max()
+
+
+def test_andersen_one_step(gpu, oracle):
+    sim = S.lj_liquid(1000, seed=7, thermostat=nbg.AndersenThermostat(1.0, 20.0))
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    ug, vg, _, _, _ = nbg.Engine(desc, 0).run(u, v, 0.005, 1, 0, save_trajectory=False)
+    uo, vo = oracle.run(desc, u, v, 0.005, 1)
+    changed = np.any(vo != S.state(sim)[1], axis=1)
+    assert changed.sum() > 20
+    assert np.abs(vg - vo).max() <= 1e-9
+
+
+def test_nonfinite_state_reported(gpu):
+    """NaN positions end the call with NBG_ERR_NONFINITE; the context stays usable."""
+    sim = S.plummer(512, seed=1)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    eng = nbg.Engine(desc, 0)
+    bad = u.copy()
+    bad[3, 0] = np.nan
+    with pytest.raises(nbg.EngineError) as ei:
+        eng.run(bad, v, 1e-3, 2, 0, save_trajectory=False)
+    assert ei.value.status == -4
+    eng.run(u, v, 1e-3, 2, 0, save_trajectory=False)
+
+
+def test_capacity_regrowth(gpu, oracle):
+    """A dense cluster overflows the initial cell and neighbour capacities;
+    the engine grows them and reruns, matching the oracle."""
+    pos, vel, L = nbg.workloads.lj_argon_lattice(1000, seed=8, jitter=0.1)
+    pos[:200] = pos[:200] * 0.35 + 0.5  # compress a fifth of the atoms into one corner
+    bodies = [nbg.MassBody(pos[i], vel[i] * 0.0, 1.0) for i in range(len(pos))]
+    system = nbg.PotentialNBodySystem(bodies, {"lennard_jones": nbg.LennardJonesParameters(1.0, 0.5, 2.5)})
+    sim = nbg.NBodySimulation(system, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), kb=1.0, skin=0.3)
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    assert S.rel_rmse(ag, ar) <= FORCE_TOL

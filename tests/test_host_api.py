@@ -1,0 +1,143 @@
+"""Host-side mirror of the reference API: constructors, show strings,
+marshalling of the system descriptor, and the C ABI's exported symbols.
+CPU only (no kernel is called)."""
+import ctypes
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+import systems as S
+
+nbg = S.nbg
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_parameter_defaults_and_show():
+    """lennard_jones_test.jl:152-166, electrostatics_test.jl:70-82, gravitational_test.jl:283-292."""
+    p = nbg.LennardJonesParameters()
+    assert (p.eps, p.sigma, p.R, p.sigma2, p.R2) == (1.0, 1.0, 2.5, 1.0, 6.25)
+    assert p.show() == "Lennard-Jones:\n\tϵ:1.0\n\tσ:1.0\n\tR:2.5\n"
+    assert nbg.LennardJonesParameters(2, 5, 10).show() == "Lennard-Jones:\n\tϵ:2\n\tσ:5\n\tR:10\n"
+    assert nbg.ElectrostaticParameters().k == 9.0e9
+    assert nbg.ElectrostaticParameters(9e9, 8.0).R2 == 64.0
+    assert nbg.ElectrostaticParameters().show() == "Electrostatic:\n\tk:9.0e9\n"
+    assert nbg.ElectrostaticParameters(1.0).show() == "Electrostatic:\n\tk:1.0\n"
+    assert nbg.GravitationalParameters().G == 6.67408e-11
+    assert nbg.GravitationalParameters().show() == "Gravitational:\n\tG:6.67408e-11\n"
+    assert nbg.GravitationalParameters(35.67).show() == "Gravitational:\n\tG:35.67\n"
+
+
+def test_potential_system_show():
+    """custom_potential_body.jl:49-59."""
+    p1 = nbg.MassBody((1, 0, 0), (0, 0, 0), 1.0)
+    p2 = nbg.MassBody((-1, 0, 0), (0, 0, 0), 1.0)
+    s = nbg.PotentialNBodySystem([p1, p2], [":lennard_jones", ":electrostatic", ":gravitational", ":magnetostatic"])
+    assert s.show() == ("Potentials: \nLennard-Jones:\n\tϵ:1.0\n\tσ:1.0\n\tR:2.5\nElectrostatic:\n\tk:9.0e9\n"
+                        "Magnetostatic:\n\tμ/4π:1.0e-7\nGravitational:\n\tG:6.67408e-11\n")
+
+
+def test_simulation_show():
+    """lennard_jones_test.jl:37-41."""
+    sim, _ = S.lj_two_body()
+    assert sim.system.show() == "Potentials: \nLennard-Jones:\n\tϵ:1.0\n\tσ:1.0\n\tR:Inf\n"
+    assert sim.show() == ("Timespan: (0.0, 1.0)\nBoundary conditions: InfiniteBox{Float64}([-Inf, Inf, -Inf, Inf, "
+                          "-Inf, Inf])\nPotentials: \nLennard-Jones:\n\tϵ:1.0\n\tσ:1.0\n\tR:Inf\n")
+
+
+def test_periodic_boundary_indexing():
+    """lennard_jones_test.jl:168-179."""
+    pbc = nbg.PeriodicBoundaryConditions(15.0e-6)
+    boundary = [0.0, 15.0e-6, 0.0, 15.0e-6, 0.0, 15.0e-6]
+    for i in range(1, 7):
+        assert boundary[i - 1] == pbc[i]
+
+
+def test_water_thermostat_data():
+    """water_test.jl:95-134: n = 6, nc = 4, Nose-Hoover index 19 (1-based)."""
+    L, lj, el, spc, mH2O = S.water_params()
+    b = [nbg.MassBody((L / 3, L / 3, 2 * L / 3), (0, 0, 0), mH2O), nbg.MassBody((L / 3, 2 * L / 3, L / 3), (0, 0, 0), mH2O)]
+    w = S.WATER
+    water = nbg.WaterSPCFw(b, w["mH"], w["mO"], w["qH"], w["qO"], lj, el, spc)
+    n, nc, ndf = nbg.get_degrees_of_freedom(water)
+    assert (n, nc) == (6, 4)
+    assert len(nbg.get_masses(water)) == n
+    sim = nbg.NBodySimulation(water, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L),
+                              nbg.NoseHooverThermostat(275, 0.1), S.KB_KJ)
+    u0, v0, _ = nbg.gather_bodies_initial_coordinates(sim)
+    assert u0.shape == (7, 3)
+    assert 3 * n + 1 == 19  # zeta at the first row of the extra column
+    desc, keep = nbg.system_descriptor(sim)
+    assert desc.n == 6 and desc.thermostat == nbg._abi.NBG_THERMO_NOSEHOOVER
+
+
+def test_water_hydrogen_placement():
+    """nbody_to_ode.jl:37-55: H1 = O + (rOH,0,0), H2 = O + (cos a rOH, 0, sin a rOH)."""
+    L, lj, el, spc, mH2O = S.water_params()
+    w = S.WATER
+    water = nbg.WaterSPCFw([nbg.MassBody((1, 2, 3), (0.1, 0, 0), mH2O)], w["mH"], w["mO"], w["qH"], w["qO"], lj, el, spc)
+    sim = nbg.NBodySimulation(water, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), S.KB_KJ)
+    u0, v0, _ = nbg.gather_bodies_initial_coordinates(sim)
+    assert np.allclose(u0[1], [1 + w["rOH"], 2, 3])
+    assert np.allclose(u0[2], [1 + math.cos(w["aHOH"]) * w["rOH"], 2, 3 + math.sin(w["aHOH"]) * w["rOH"]])
+    assert np.all(v0 == [0.1, 0, 0])
+
+
+def test_custom_potential_rejected():
+    """A Julia-side custom potential (test/shared/custom_potential_body.jl)
+    has no GPU kernel: the engine refuses it instead of computing on the CPU."""
+    class Custom(nbg.PotentialParameters):
+        pass
+    s = nbg.PotentialNBodySystem([nbg.MassBody((0, 0, 0), (0, 0, 0), 1.0)], {"custom_potential_params": Custom()})
+    sim = nbg.NBodySimulation(s, (0.0, 1.0))
+    with pytest.raises(nbg.EngineError):
+        nbg.system_descriptor(sim)
+
+
+def test_descriptor_layout_matches_header():
+    """The ctypes struct has the layout gcc gives the C struct of include/nbg.h."""
+    src = r'''
+    #include <stddef.h>
+    #include <stdio.h>
+    #include "nbg.h"
+    int main(void) {
+      printf("%zu %zu %zu %zu %zu %zu\n", sizeof(nbg_system_desc), offsetof(nbg_system_desc, box),
+             offsetof(nbg_system_desc, seed), offsetof(nbg_system_desc, flags), sizeof(nbg_energies),
+             sizeof(nbg_run_stats));
+      return 0; }
+    '''
+    import subprocess
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "t")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        vals = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    A = nbg._abi
+    assert vals == [ctypes.sizeof(A.NbgSystemDesc), A.NbgSystemDesc.box.offset, A.NbgSystemDesc.seed.offset,
+                    A.NbgSystemDesc.flags.offset, ctypes.sizeof(A.NbgEnergies), ctypes.sizeof(A.NbgRunStats)]
+
+
+def _header_functions():
+    text = open(os.path.join(ROOT, "include", "nbg.h")).read()
+    return sorted(set(re.findall(r"NBG_API[^;(]*?\b(nbg_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_header_symbol():
+    """libnbg.so (built for sm_103a) loads without a GPU and exports every
+    function include/nbg.h declares; the ctypes table covers them all."""
+    import __graft_entry__ as g
+    lib_build = g._load_by_path("nbg_lib_build", os.path.join(ROOT, "nbodysimulator.jl_gb300", "build.py"))
+    path = lib_build.build()
+    lib = ctypes.CDLL(path)
+    names = _header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(nbg._abi.SIGNATURES), set(names) ^ set(nbg._abi.SIGNATURES)
+    loaded = nbg.load_library()
+    assert loaded.nbg_abi_version() == nbg._abi.NBG_ABI_VERSION
+    assert b"sm_103a" in loaded.nbg_version()

@@ -1,0 +1,114 @@
+"""The FP64 oracle against the known answers of the reference's own tests
+(NBodySimulator.jl test/*.jl). These pin the oracle before it is used as
+the checker of the GPU engine. CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+import systems as S
+
+nbg = S.nbg
+
+
+def _run(oracle, sim, dt, nsteps, save_every=0):
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    u, v = oracle.run(desc, u0, v0, dt, nsteps, save_every)
+    return desc, keep, u0, v0, u, v
+
+
+def test_lj_two_body_speed(oracle):
+    """lennard_jones_test.jl:4-33: speed from energy conservation, 0.1 %."""
+    sim, r1 = S.lj_two_body()
+    desc, keep, u0, v0, u, v = _run(oracle, sim, 1e-3, 1000)
+    r2 = np.linalg.norm(u[1] - u[0])
+    v_expected = math.sqrt(4 * 1.0 / 1.0 * ((1 / r1) ** 12 - (1 / r2) ** 12 - ((1 / r1) ** 6 - (1 / r2) ** 6)))
+    assert abs(np.linalg.norm(v[1]) - v_expected) <= 0.001 * v_expected
+
+
+@pytest.mark.parametrize("bc", ["periodic", "cubic"])
+def test_argon3_temperature_energy(oracle, bc):
+    """lennard_jones_test.jl:47-97: T(0)=120 K, kinetic energy, 10 % energy drift."""
+    sim, m, v_dev = S.argon3(bc)
+    desc, keep, u0, v0, u, v = _run(oracle, sim, 0.5e-3, 100)
+    e0 = oracle.energy(desc, u0, v0)
+    assert abs(e0["temperature"] - 120.0) < 1e-6
+    assert e0["kinetic"] == pytest.approx(m * 3 * v_dev ** 2 / 2, rel=1e-14)
+    e1 = oracle.energy(desc, u, v)
+    assert abs(e1["total"] - e0["total"]) <= abs(0.1 * e0["total"])
+
+
+def test_coulomb_repulsion_speed(oracle):
+    """electrostatics_test.jl:42-68: speed from energy conservation, 0.1 %."""
+    sim, k, q = S.coulomb_pair()
+    desc, keep, u0, v0, u, v = _run(oracle, sim, 1e-3, 1000)
+    r2 = np.linalg.norm(u[1] - u[0])
+    v_expected = math.sqrt(k * q * q / 1.0 * (1 / 1.0 - 1 / r2))
+    assert abs(np.linalg.norm(v[1]) - v_expected) <= 0.001 * v_expected
+
+
+def test_charges8_energy_conservation(oracle):
+    """electrostatics_test.jl:84-119: 8 charges, cubic box, cutoff 0.45 L,
+    1000 VV steps, relative drift within 1e-3."""
+    sim, tau = S.charges8()
+    desc, keep, u0, v0, u, v = _run(oracle, sim, tau, 1000)
+    e0 = oracle.energy(desc, u0, v0)["total"]
+    e1 = oracle.energy(desc, u, v)["total"]
+    assert abs((e1 - e0) / e0) <= 1e-3
+
+
+def test_figure8_vv_closure(oracle):
+    """gravitational_test.jl:53-60 and :218-220: VV dt=pi/130 returns the
+    figure-eight to its start within 1e-3; KE(0) = 1.218 within 1e-3."""
+    sim = S.figure8()
+    desc, keep, u0, v0, u, v = _run(oracle, sim, math.pi / 130, 260)
+    assert np.abs(u - u0).max() <= 1e-3
+    assert oracle.energy(desc, u0, v0)["kinetic"] == pytest.approx(1.218, abs=1e-3)
+
+
+def test_water3_geometry_energy_temperature(oracle):
+    """water_test.jl:33-93: 3 SPC/Fw molecules, 10 VV steps: bonds and angle
+    within 1 %, total energy drift within 1 %, T(0) with ndf = 21."""
+    sim, v_dev, mH2O = S.water3()
+    w = S.WATER
+    desc, keep, u0, v0, u, v = _run(oracle, sim, w["tau"], 10)
+    for i in range(3):
+        o = 3 * i
+        for h in (1, 2):
+            assert abs(w["rOH"] - np.linalg.norm(u[o] - u[o + h])) / w["rOH"] <= 0.01
+        a, b = u[o] - u[o + 1], u[o] - u[o + 2]
+        ang = math.acos(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
+        assert abs(ang - w["aHOH"]) / w["aHOH"] <= 0.01
+    e0 = oracle.energy(desc, u0, v0)
+    e1 = oracle.energy(desc, u, v)
+    assert abs((e0["total"] - e1["total"]) / e0["total"]) <= 0.01
+    t_expected = 3 * v_dev ** 2 * mH2O / (S.KB_KJ * 21)
+    assert abs(e0["temperature"] - t_expected) / t_expected <= 0.01
+
+
+@pytest.mark.parametrize("kind", ["andersen", "berendsen", "nosehoover", "langevin"])
+def test_thermostats_argon125(oracle, kind):
+    """thermostat_test.jl:16-94: N=125 argon, 200 steps towards T0 = 90 K."""
+    T0 = 90.0
+    tau = 0.5e-3
+    if kind == "andersen":
+        th, bc, tol, scale = nbg.AndersenThermostat(T0, 0.1 / tau), "periodic", 0.5, T0
+    elif kind == "berendsen":
+        th, bc, tol, scale = nbg.BerendsenThermostat(T0, 10 * tau), "cubic", 0.1, 120.0
+    elif kind == "nosehoover":
+        th, bc, tol, scale = nbg.NoseHooverThermostat(T0, 20 * tau), "cubic", 0.5, T0
+    else:
+        th, bc, tol, scale = nbg.LangevinThermostat(T0, 10.0), "cubic", 0.5, T0
+    sim, tau = S.argon125(th, bc)
+    desc, keep, u0, v0, u, v = _run(oracle, sim, tau, 200)
+    T2 = oracle.energy(desc, u, v)["temperature"]
+    assert abs(T2 - T0) / scale <= tol
+
+
+def test_philox_streams_distinct(oracle):
+    """The counter-based RNG gives distinct, well-spread draws."""
+    us = np.array([oracle.uniform(7, i, 0) for i in range(2000)])
+    assert 0.45 < us.mean() < 0.55
+    zs = np.array([oracle.normals3(7, i, 3) for i in range(2000)]).ravel()
+    assert abs(zs.mean()) < 0.06 and abs(zs.std() - 1) < 0.05

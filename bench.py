@@ -44,9 +44,9 @@ WORKLOADS = {
 }
 
 
-def make_sim(nbg, workload, seed=0):
+def make_sim(nbg, workload, seed=0, n=None):
     if workload == "gravity":
-        pos, vel, m = nbg.workloads.plummer_sphere(65536, seed=seed)
+        pos, vel, m = nbg.workloads.plummer_sphere(n or 65536, seed=seed)
         bodies = [nbg.MassBody(pos[i], vel[i], m[i]) for i in range(len(m))]
         return nbg.NBodySimulation(nbg.GravitationalSystem(bodies, 1.0), (0.0, 0.1))
     if workload == "lj":
@@ -180,7 +180,7 @@ def run_reference(args, rank):
     nbg = G.load_package()
     oracle = G.load_oracle()
     w = WORKLOADS[args.workload]
-    sim = make_sim(nbg, args.workload)
+    sim = make_sim(nbg, args.workload, n=args.n)
     desc, keep = nbg.system_descriptor(sim)
     u, v, _ = nbg.gather_bodies_initial_coordinates(sim)
     n = int(desc.n)
@@ -219,6 +219,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-flush", action="store_true", help="time all steps back to back (no L2 flush)")
     ap.add_argument("--ref-sample", type=int, default=2048)
+    ap.add_argument("--n", type=int, default=None, help="gravity body count (smaller profiling captures)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--grav-plain", action="store_true", help="gravity with plain FP32 positions")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.steps is None:
@@ -244,7 +247,9 @@ def main():
     device = local
     nbg = G.load_package()
     nbg.load_library()
-    sim = make_sim(nbg, args.workload, seed=rank)
+    sim = make_sim(nbg, args.workload, seed=rank, n=args.n)
+    if args.grav_plain:
+        sim.flags |= nbg._abi.NBG_FLAG_GRAV_PLAIN
     desc, keep = nbg.system_descriptor(sim)
     u0, v0, _ = nbg.gather_bodies_initial_coordinates(sim)
     n = int(desc.n)
@@ -310,19 +315,21 @@ def main():
     uh[:] = u0
     vh[:] = v0
     e2e_steps = max(3, min(args.steps, 50 if args.workload == "gravity" else 200))
-    a = eng.accel(vh, uh)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s in range(e2e_steps):
-        uh += dt * vh + (dt * dt) * (0.5 * a)
-        an = eng.accel(vh, uh)
-        vh += dt * (0.5 * a + 0.5 * an)
-        a = an
-    e2e_s = time.perf_counter() - t0
-    e2e = {"value": n * e2e_steps * world / e2e_s, "unit": "atom-steps/s",
-           "h2d_bytes_per_step": 2 * uh.nbytes, "d2h_bytes_per_step": ah.nbytes,
-           "path": "nbg_accel (RHS drop-in) per step from pinned host buffers, velocity-Verlet update on host",
-           "steps": e2e_steps}
+    e2e = None
+    if not args.no_e2e:
+        a = eng.accel(vh, uh)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(e2e_steps):
+            uh += dt * vh + (dt * dt) * (0.5 * a)
+            an = eng.accel(vh, uh)
+            vh += dt * (0.5 * a + 0.5 * an)
+            a = an
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": n * e2e_steps * world / e2e_s, "unit": "atom-steps/s",
+               "h2d_bytes_per_step": 2 * uh.nbytes, "d2h_bytes_per_step": ah.nbytes,
+               "path": "nbg_accel (RHS drop-in) per step from pinned host buffers, velocity-Verlet update on host",
+               "steps": e2e_steps}
 
     # accuracy at this workload: forces of sampled atoms vs the oracle, drift
     u_end, v_end = eng.get_state()
@@ -356,7 +363,8 @@ def main():
                        "l2": "no flush (state L2-resident across steps)" if args.no_flush
                        else "512 MB buffer written between timed steps (L2 flushed)",
                        "parallelism": "replicas only" if world > 1 else "single GPU",
-                       "gravity_precision": "hi/lo split positions (compensated)" if args.workload == "gravity" else None},
+                       "gravity_precision": ("plain FP32 positions" if args.grav_plain else
+                                             "hi/lo split positions (compensated)") if args.workload == "gravity" else None},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "energy_drift_rel": (E1 - E0) / abs(E0) if E0 else None}
     if args.workload == "water":

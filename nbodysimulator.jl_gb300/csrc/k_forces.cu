@@ -1,12 +1,12 @@
 // k_forces.cu - force kernels.
 //
 //  k_gravity<PLAIN>  all-pairs gravity (gravitational_acceleration!,
-//                    basic_potentials.jl:306-331): 256-body j-tiles of split
-//                    positions staged in shared memory, each i owned by S=4
-//                    lanes that split the tile and join by warp shuffles at the
-//                    end; the j range is cut into J chunks so the grid is a
-//                    near-exact multiple of the resident blocks (J partials per
-//                    atom in scratch, reduced in fixed order by k_gravity_reduce).
+//                    basic_potentials.jl:306-331): 128-body j-tiles of split
+//                    positions staged in shared memory and read as warp-wide
+//                    broadcasts, two bodies i per thread; the j range is cut
+//                    into J chunks so the grid fills whole waves of resident
+//                    blocks (J partials per body in scratch, reduced in fixed
+//                    order by k_gravity_reduce).
 //                    Per pair: FP32 differences of hi/lo split positions (exact
 //                    to ~2^-24 of |r_ij|, or plain FP32 positions when PLAIN),
 //                    one rsqrt, partial sums per tile folded into a compensated
@@ -20,89 +20,93 @@
 //                    per molecule (basic_potentials.jl:367-433).
 #include "nbg_internal.cuh"
 
-#define GT 256       // gravity tile (j bodies per shared-memory stage)
-#define GS 4         // lanes per i
-#define GB 256       // gravity block size
-#define GI (GB / GS) // i per block
+#define GB 128         // gravity block size = j-tile size
+#define GI (2 * GB)    // bodies i per block (two per thread)
 
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// One body-body term: p += m_j (r_i - r_j) / |r_i - r_j|^3.
+template <bool PLAIN, bool CHECK>
+__device__ __forceinline__ void grav_term(const float4& hi, const float4& lo, const float4& hj, const float4& lj,
+                                          bool self, float& px, float& py, float& pz)
+{
+    float dx = hi.x - hj.x, dy = hi.y - hj.y, dz = hi.z - hj.z;
+    if (!PLAIN) {
+        dx += lo.x - lj.x;
+        dy += lo.y - lj.y;
+        dz += lo.z - lj.z;
+    }
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float ri = rsqrt_ftz(r2);
+    if (CHECK && self) ri = 0.0f;  // j != i (basic_potentials.jl:318)
+    float s = hj.w * ri * (ri * ri);
+    px = fmaf(s, dx, px);
+    py = fmaf(s, dy, py);
+    pz = fmaf(s, dz, pz);
+}
+
+// Grid: (i-block, j-chunk) units; each thread owns bodies i0 and i0 + GB of
+// its block and walks the chunk's j-tiles from shared memory (every lane of a
+// warp reads the same body: one broadcast load serves two pairs per thread).
 template <bool PLAIN>
 __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
                                                 int64_t n, int64_t npad, int jchunks, double* __restrict__ part)
 {
-    __shared__ float4 sh_hi[GT];
-    __shared__ float4 sh_lo[PLAIN ? 1 : GT];
-    const int64_t ntile = npad / GT;
-    const int64_t tiles_per_chunk = ntile / jchunks;
-    const int64_t unit = blockIdx.x;
-    const int64_t iblock = unit / jchunks;
-    const int jc = (int)(unit % jchunks);
-    const int lane = threadIdx.x % GS;
-    const int64_t i = iblock * GI + threadIdx.x / GS;
-    const float4 hi_i = phi[i < npad ? i : 0];
-    float4 lo_i = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!PLAIN) lo_i = plo[i < npad ? i : 0];
-    Acc2 ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f};
-    const int64_t t0 = jc * tiles_per_chunk;
-    const int64_t t1 = t0 + tiles_per_chunk;
-    const int64_t diag_tile = (iblock * GI) / GT;
+    __shared__ float4 sh_hi[GB];
+    __shared__ float4 sh_lo[PLAIN ? 1 : GB];
+    const int64_t ntile = npad / GB;
+    const int64_t iblock = blockIdx.x / jchunks;
+    const int jc = (int)(blockIdx.x % jchunks);
+    const int64_t t0 = (int64_t)jc * ntile / jchunks;
+    const int64_t t1 = (int64_t)(jc + 1) * ntile / jchunks;
+    const int64_t ib0 = iblock * GI;
+    const int64_t i0 = ib0 + threadIdx.x, i1 = i0 + GB;
+    const float4 hA = phi[i0], hB = phi[i1];
+    float4 lA = make_float4(0.f, 0.f, 0.f, 0.f), lB = lA;
+    if (!PLAIN) {
+        lA = plo[i0];
+        lB = plo[i1];
+    }
+    Acc2 ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, bx{0.f, 0.f}, by{0.f, 0.f}, bz{0.f, 0.f};
     for (int64_t t = t0; t < t1; ++t) {
+        const int64_t j0 = t * GB;
         __syncthreads();
-        sh_hi[threadIdx.x] = phi[t * GT + threadIdx.x];
-        if (!PLAIN) sh_lo[threadIdx.x] = plo[t * GT + threadIdx.x];
+        sh_hi[threadIdx.x] = phi[j0 + threadIdx.x];
+        if (!PLAIN) sh_lo[threadIdx.x] = plo[j0 + threadIdx.x];
         __syncthreads();
-        float px = 0.f, py = 0.f, pz = 0.f;
-        if (t != diag_tile) {
+        float pax = 0.f, pay = 0.f, paz = 0.f, pbx = 0.f, pby = 0.f, pbz = 0.f;
+        const bool diag = (j0 < ib0 + GI) && (j0 + GB > ib0);
+        if (!diag) {
 #pragma unroll 8
-            for (int jj = lane; jj < GT; jj += GS) {
-                float4 hj = sh_hi[jj];
-                float dx = hi_i.x - hj.x, dy = hi_i.y - hj.y, dz = hi_i.z - hj.z;
-                if (!PLAIN) {
-                    float4 lj = sh_lo[jj];
-                    dx += lo_i.x - lj.x;
-                    dy += lo_i.y - lj.y;
-                    dz += lo_i.z - lj.z;
-                }
-                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                float ri = rsqrtf(r2);
-                float s = hj.w * ri * (ri * ri);
-                px = fmaf(s, dx, px);
-                py = fmaf(s, dy, py);
-                pz = fmaf(s, dz, pz);
+            for (int jj = 0; jj < GB; ++jj) {
+                const float4 hj = sh_hi[jj];
+                const float4 lj = PLAIN ? hj : sh_lo[jj];
+                grav_term<PLAIN, false>(hA, lA, hj, lj, false, pax, pay, paz);
+                grav_term<PLAIN, false>(hB, lB, hj, lj, false, pbx, pby, pbz);
             }
         } else {
-            for (int jj = lane; jj < GT; jj += GS) {
-                float4 hj = sh_hi[jj];
-                float dx = hi_i.x - hj.x, dy = hi_i.y - hj.y, dz = hi_i.z - hj.z;
-                if (!PLAIN) {
-                    float4 lj = sh_lo[jj];
-                    dx += lo_i.x - lj.x;
-                    dy += lo_i.y - lj.y;
-                    dz += lo_i.z - lj.z;
-                }
-                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                float ri = (t * GT + jj == i) ? 0.0f : rsqrtf(r2);  // j != i (:318)
-                float s = hj.w * ri * (ri * ri);
-                px = fmaf(s, dx, px);
-                py = fmaf(s, dy, py);
-                pz = fmaf(s, dz, pz);
+            for (int jj = 0; jj < GB; ++jj) {
+                const float4 hj = sh_hi[jj];
+                const float4 lj = PLAIN ? hj : sh_lo[jj];
+                grav_term<PLAIN, true>(hA, lA, hj, lj, j0 + jj == i0, pax, pay, paz);
+                grav_term<PLAIN, true>(hB, lB, hj, lj, j0 + jj == i1, pbx, pby, pbz);
             }
         }
-        ax.add(px);
-        ay.add(py);
-        az.add(pz);
+        ax.add(pax); ay.add(pay); az.add(paz);
+        bx.add(pbx); by.add(pby); bz.add(pbz);
     }
-    double vx = ax.value(), vy = ay.value(), vz = az.value();
-#pragma unroll
-    for (int o = GS / 2; o > 0; o >>= 1) {
-        vx += __shfl_xor_sync(0xffffffffu, vx, o);
-        vy += __shfl_xor_sync(0xffffffffu, vy, o);
-        vz += __shfl_xor_sync(0xffffffffu, vz, o);
+    if (i0 < n) {
+        double* p = part + ((int64_t)jc * n + i0) * 3;
+        p[0] = ax.value(); p[1] = ay.value(); p[2] = az.value();
     }
-    if (lane == 0 && i < n) {
-        double* p = part + ((int64_t)jc * n + i) * 3;
-        p[0] = vx;
-        p[1] = vy;
-        p[2] = vz;
+    if (i1 < n) {
+        double* p = part + ((int64_t)jc * n + i1) * 3;
+        p[0] = bx.value(); p[1] = by.value(); p[2] = bz.value();
     }
 }
 
@@ -119,12 +123,9 @@ __global__ void k_gravity_reduce(const double* __restrict__ part, int64_t n, int
     }
 }
 
-struct GravPlan {
-    int jchunks;
-    int64_t units;
-};
-
-static GravPlan plan_gravity(nbg_ctx* c, int64_t npad)
+// Number of j-chunks: the smallest that makes (i-blocks x chunks) fill the
+// resident block slots (SMs x blocks per SM) in near-whole waves.
+static int plan_gravity(nbg_ctx* c, int64_t npad)
 {
     int dev = c->device, sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -134,21 +135,20 @@ static GravPlan plan_gravity(nbg_ctx* c, int64_t npad)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<false>, GB, 0);
     if (sms < 1) sms = 1;
     if (occ < 1) occ = 1;
-    int64_t slots = (int64_t)sms * occ;
-    int64_t ib = npad / GI;
-    int64_t ntile = npad / GT;
-    GravPlan best{1, ib};
+    const double slots = (double)sms * occ;
+    const int64_t ib = npad / GI;
+    const int64_t ntile = npad / GB;
+    int best = 1;
     double best_eff = -1.0;
-    for (int J = 1; J <= 64; J *= 2) {
-        if (ntile % J) break;
-        int64_t units = ib * J;
-        double waves = (double)units / (double)slots;
-        double eff = waves / ceil(waves);
-        // prefer fewer chunks unless the balance gain is real
-        if (eff > best_eff + 0.01) {
+    for (int J = 1; J <= 64 && J <= ntile; ++J) {
+        double waves = (double)(ib * J) / slots;
+        // whole-wave efficiency, with chunks of ceil(ntile/J) vs ntile/J tiles
+        double eff = waves / ceil(waves) * ((double)ntile / J) / (double)((ntile + J - 1) / J);
+        if (eff > best_eff + 0.005) {
             best_eff = eff;
-            best = GravPlan{J, units};
+            best = J;
         }
+        if (eff >= 0.97) break;
     }
     return best;
 }
@@ -173,7 +173,7 @@ int launch_gravity(nbg_ctx* c, const StateView& s)
     return NBG_OK;
 }
 
-int gravity_plan_chunks(nbg_ctx* c, int64_t npad) { return plan_gravity(c, npad).jchunks; }
+int gravity_plan_chunks(nbg_ctx* c, int64_t npad) { return plan_gravity(c, npad); }
 
 // ---------------------------------------------------------------------
 // generic all-pairs kernel

@@ -170,8 +170,10 @@ def test_energies_match_oracle(gpu, oracle):
         u, v = S.state(sim)
         eg = nbg.Engine(desc, 0).energy(u, v)
         eo = oracle.energy(desc, u, v)
-        for k in ("kinetic", "lennard_jones", "electrostatic", "bonds", "angles", "gravity", "temperature"):
-            assert eg[k] == pytest.approx(eo[k], rel=1e-11, abs=1e-300), k
+        scale = sum(abs(eo[k]) for k in ("kinetic", "lennard_jones", "electrostatic", "bonds", "angles", "gravity"))
+        for k in ("kinetic", "lennard_jones", "electrostatic", "bonds", "angles", "gravity"):
+            assert eg[k] == pytest.approx(eo[k], rel=1e-11, abs=1e-13 * scale), k
+        assert eg["temperature"] == pytest.approx(eo["temperature"], rel=1e-12)
 
 
 @pytest.mark.parametrize("case", ["lj_list", "lj_berendsen", "lj_nosehoover", "water_list", "gravity"])
@@ -215,9 +217,15 @@ def test_andersen_one_step(gpu, oracle):
     u, v = S.state(sim)
     ug, vg, _, _, _ = nbg.Engine(desc, 0).run(u, v, 0.005, 1, 0, save_trajectory=False)
     uo, vo = oracle.run(desc, u, v, 0.005, 1)
-    changed = np.any(vo != S.state(sim)[1], axis=1)
+    # atoms that collided got their velocity redrawn: FP64 normals on both
+    # sides; the rest went through the kick with FP32 pair forces
+    sim0 = S.lj_liquid(1000, seed=7)
+    d0, k0 = nbg.system_descriptor(sim0)
+    _, v_nocoll = oracle.run(d0, u, v, 0.005, 1)
+    changed = np.any(vo != v_nocoll, axis=1)
     assert changed.sum() > 20
-    assert np.abs(vg - vo).max() <= 1e-9
+    assert np.abs(vg[changed] - vo[changed]).max() <= 1e-12 * np.abs(vo).max()
+    assert np.abs(vg[~changed] - vo[~changed]).max() <= 1e-6 * np.abs(vo).max()
 
 
 def test_nonfinite_state_reported(gpu):

@@ -60,7 +60,7 @@ def make_sim(nbg, workload, seed=0, n=None):
         bodies = nbg.workloads.water_molecules(pos, vel)
         lj = nbg.LennardJonesParameters(0.650299, 0.3165492, 0.9)
         el = nbg.ElectrostaticParameters(nbg.workloads.K_EL, 0.9)
-        spc = nbg.SPCFwParameters(0.1012, 113.24 * math.pi / 180, 4637.0, 383.0)
+        spc = nbg.SPCFwParameters(0.1012, 113.24 * math.pi / 180, nbg.workloads.SPCFW_KB, nbg.workloads.SPCFW_KA)
         water = nbg.WaterSPCFw(bodies, nbg.workloads.M_H, nbg.workloads.M_O, 0.41, -0.82, lj, el, spc)
         return nbg.NBodySimulation(water, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L),
                                    nbg.BerendsenThermostat(300.0, 0.1), kb=nbg.workloads.KB_KJ, skin=0.1,

@@ -21,7 +21,7 @@
 #include "nbg_internal.cuh"
 
 #define GB 128         // gravity block size = j-tile size
-#define GI (2 * GB)    // bodies i per block (two per thread)
+#define GI_MAX (4 * GB)  // bodies i per block at most (TI <= 4)
 
 __device__ __forceinline__ float rsqrt_ftz(float x)
 {
@@ -30,33 +30,115 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
     return y;
 }
 
-// One body-body term: p += m_j (r_i - r_j) / |r_i - r_j|^3.
-template <bool PLAIN, bool CHECK>
-__device__ __forceinline__ void grav_term(const float4& hi, const float4& lo, const float4& hj, const float4& lj,
-                                          bool self, float& px, float& py, float& pz)
+// Grid: (i-block, j-chunk) units; each thread owns TI bodies i (strided by
+// GB within the block) and walks the chunk's j-tiles from shared memory:
+// every lane of a warp reads the same body j (one broadcast load serves TI
+// pairs). PACKED evaluates the TI bodies two at a time with the packed
+// FP32x2 instructions (__ffma2_rn / __fadd2_rn / __fmul2_rn), which halve the
+// issued FP32 instructions; both forms round every element identically.
+// Per pair: p += m_j (r_i - r_j) |r_i - r_j|^-3 (gravitational_acceleration!,
+// basic_potentials.jl:318-324), the j == i term skipped (:318).
+// Accumulate one j-tile (sh_hi / sh_lo) into the per-body partials.
+// DIAG: the tile holds some of this thread's own bodies (j == i skipped).
+template <bool PLAIN, int TI, bool PACKED, bool DIAG>
+__device__ __forceinline__ void grav_tile(const float4* sh_hi, const float4* sh_lo, int64_t j0, const int64_t* ii,
+                                          const float* hx, const float* hy, const float* hz, const float* lx,
+                                          const float* ly, const float* lz, float* px, float* py, float* pz)
 {
-    float dx = hi.x - hj.x, dy = hi.y - hj.y, dz = hi.z - hj.z;
-    if (!PLAIN) {
-        dx += lo.x - lj.x;
-        dy += lo.y - lj.y;
-        dz += lo.z - lj.z;
+    constexpr int NP = PACKED ? TI / 2 : 1;
+    if (!PACKED) {
+#pragma unroll 4
+        for (int jj = 0; jj < GB; ++jj) {
+            const float4 hj = sh_hi[jj];
+            float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!PLAIN) lj = sh_lo[jj];
+#pragma unroll
+            for (int k = 0; k < TI; ++k) {
+                float dx = hx[k] - hj.x, dy = hy[k] - hj.y, dz = hz[k] - hj.z;
+                if (!PLAIN) {
+                    dx += lx[k] - lj.x;
+                    dy += ly[k] - lj.y;
+                    dz += lz[k] - lj.z;
+                }
+                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                float ri = rsqrt_ftz(r2);
+                if (DIAG && j0 + jj == ii[k]) ri = 0.0f;
+                float sc = hj.w * ri * (ri * ri);
+                px[k] = fmaf(sc, dx, px[k]);
+                py[k] = fmaf(sc, dy, py[k]);
+                pz[k] = fmaf(sc, dz, pz[k]);
+            }
+        }
+        return;
     }
-    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    float ri = rsqrt_ftz(r2);
-    if (CHECK && self) ri = 0.0f;  // j != i (basic_potentials.jl:318)
-    float s = hj.w * ri * (ri * ri);
-    px = fmaf(s, dx, px);
-    py = fmaf(s, dy, py);
-    pz = fmaf(s, dz, pz);
+    float2 hx2[NP], hy2[NP], hz2[NP], lx2[NP], ly2[NP], lz2[NP], px2[NP], py2[NP], pz2[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        hx2[q] = make_float2(hx[2 * q], hx[2 * q + 1]);
+        hy2[q] = make_float2(hy[2 * q], hy[2 * q + 1]);
+        hz2[q] = make_float2(hz[2 * q], hz[2 * q + 1]);
+        lx2[q] = make_float2(lx[2 * q], lx[2 * q + 1]);
+        ly2[q] = make_float2(ly[2 * q], ly[2 * q + 1]);
+        lz2[q] = make_float2(lz[2 * q], lz[2 * q + 1]);
+        px2[q] = py2[q] = pz2[q] = make_float2(0.f, 0.f);
+    }
+    const float2 m1 = make_float2(-1.f, -1.f);
+#pragma unroll 4
+    for (int jj = 0; jj < GB; ++jj) {
+        const float4 hj = sh_hi[jj];
+        const float2 jx = make_float2(hj.x, hj.x), jy = make_float2(hj.y, hj.y), jz = make_float2(hj.z, hj.z);
+        const float2 jm = make_float2(hj.w, hj.w);
+        float2 kx = m1, ky = m1, kz = m1;
+        if (!PLAIN) {
+            const float4 lj = sh_lo[jj];
+            kx = make_float2(lj.x, lj.x);
+            ky = make_float2(lj.y, lj.y);
+            kz = make_float2(lj.z, lj.z);
+        }
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            float2 dx = __ffma2_rn(jx, m1, hx2[q]);  // hi_i - hi_j (scaling by -1 is exact)
+            float2 dy = __ffma2_rn(jy, m1, hy2[q]);
+            float2 dz = __ffma2_rn(jz, m1, hz2[q]);
+            if (!PLAIN) {
+                dx = __fadd2_rn(dx, __ffma2_rn(kx, m1, lx2[q]));
+                dy = __fadd2_rn(dy, __ffma2_rn(ky, m1, ly2[q]));
+                dz = __fadd2_rn(dz, __ffma2_rn(kz, m1, lz2[q]));
+            }
+            float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+            if (DIAG) {
+                if (j0 + jj == ii[2 * q]) ri.x = 0.0f;
+                if (j0 + jj == ii[2 * q + 1]) ri.y = 0.0f;
+            }
+            float2 sc = __fmul2_rn(__fmul2_rn(jm, ri), __fmul2_rn(ri, ri));
+            px2[q] = __ffma2_rn(sc, dx, px2[q]);
+            py2[q] = __ffma2_rn(sc, dy, py2[q]);
+            pz2[q] = __ffma2_rn(sc, dz, pz2[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        px[2 * q] = px2[q].x; px[2 * q + 1] = px2[q].y;
+        py[2 * q] = py2[q].x; py[2 * q + 1] = py2[q].y;
+        pz[2 * q] = pz2[q].x; pz[2 * q + 1] = pz2[q].y;
+    }
 }
 
-// Grid: (i-block, j-chunk) units; each thread owns bodies i0 and i0 + GB of
-// its block and walks the chunk's j-tiles from shared memory (every lane of a
-// warp reads the same body: one broadcast load serves two pairs per thread).
-template <bool PLAIN>
+// Grid: (i-block, j-chunk) units; each thread owns TI bodies i (strided by
+// GB within the block) and walks the chunk's j-tiles from shared memory:
+// every lane of a warp reads the same body j (one broadcast load serves TI
+// pairs). PACKED evaluates the TI bodies two at a time with the packed
+// FP32x2 instructions (__ffma2_rn / __fadd2_rn / __fmul2_rn), which halve the
+// issued FP32 instructions; both forms round every element identically.
+// Per pair: p += m_j (r_i - r_j) |r_i - r_j|^-3 (gravitational_acceleration!,
+// basic_potentials.jl:318-324), the j == i term skipped (:318).
+template <bool PLAIN, int TI, bool PACKED>
 __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
                                                 int64_t n, int64_t npad, int jchunks, double* __restrict__ part)
 {
+    static_assert(TI == 1 || TI == 2 || TI == 4, "TI");
+    static_assert(!PACKED || TI >= 2, "packed needs pairs");
     __shared__ float4 sh_hi[GB];
     __shared__ float4 sh_lo[PLAIN ? 1 : GB];
     const int64_t ntile = npad / GB;
@@ -64,51 +146,66 @@ __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, 
     const int jc = (int)(blockIdx.x % jchunks);
     const int64_t t0 = (int64_t)jc * ntile / jchunks;
     const int64_t t1 = (int64_t)(jc + 1) * ntile / jchunks;
-    const int64_t ib0 = iblock * GI;
-    const int64_t i0 = ib0 + threadIdx.x, i1 = i0 + GB;
-    const float4 hA = phi[i0], hB = phi[i1];
-    float4 lA = make_float4(0.f, 0.f, 0.f, 0.f), lB = lA;
-    if (!PLAIN) {
-        lA = plo[i0];
-        lB = plo[i1];
+    const int64_t ib0 = iblock * (TI * GB);
+    float hx[TI], hy[TI], hz[TI], lx[TI], ly[TI], lz[TI];
+    int64_t ii[TI];
+#pragma unroll
+    for (int k = 0; k < TI; ++k) {
+        ii[k] = ib0 + threadIdx.x + k * GB;
+        float4 h = phi[ii[k]];
+        hx[k] = h.x; hy[k] = h.y; hz[k] = h.z;
+        float4 l = PLAIN ? make_float4(0.f, 0.f, 0.f, 0.f) : plo[ii[k]];
+        lx[k] = l.x; ly[k] = l.y; lz[k] = l.z;
     }
-    Acc2 ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f}, bx{0.f, 0.f}, by{0.f, 0.f}, bz{0.f, 0.f};
+    Acc2 ax[TI], ay[TI], az[TI];
+#pragma unroll
+    for (int k = 0; k < TI; ++k) ax[k] = ay[k] = az[k] = Acc2{0.f, 0.f};
     for (int64_t t = t0; t < t1; ++t) {
         const int64_t j0 = t * GB;
         __syncthreads();
         sh_hi[threadIdx.x] = phi[j0 + threadIdx.x];
         if (!PLAIN) sh_lo[threadIdx.x] = plo[j0 + threadIdx.x];
         __syncthreads();
-        float pax = 0.f, pay = 0.f, paz = 0.f, pbx = 0.f, pby = 0.f, pbz = 0.f;
-        const bool diag = (j0 < ib0 + GI) && (j0 + GB > ib0);
-        if (!diag) {
-#pragma unroll 8
-            for (int jj = 0; jj < GB; ++jj) {
-                const float4 hj = sh_hi[jj];
-                const float4 lj = PLAIN ? hj : sh_lo[jj];
-                grav_term<PLAIN, false>(hA, lA, hj, lj, false, pax, pay, paz);
-                grav_term<PLAIN, false>(hB, lB, hj, lj, false, pbx, pby, pbz);
-            }
-        } else {
-            for (int jj = 0; jj < GB; ++jj) {
-                const float4 hj = sh_hi[jj];
-                const float4 lj = PLAIN ? hj : sh_lo[jj];
-                grav_term<PLAIN, true>(hA, lA, hj, lj, j0 + jj == i0, pax, pay, paz);
-                grav_term<PLAIN, true>(hB, lB, hj, lj, j0 + jj == i1, pbx, pby, pbz);
-            }
+        float px[TI], py[TI], pz[TI];
+#pragma unroll
+        for (int k = 0; k < TI; ++k) px[k] = py[k] = pz[k] = 0.f;
+        if ((j0 < ib0 + TI * GB) && (j0 + GB > ib0))
+            grav_tile<PLAIN, TI, PACKED, true>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
+        else
+            grav_tile<PLAIN, TI, PACKED, false>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
+#pragma unroll
+        for (int k = 0; k < TI; ++k) {
+            ax[k].add(px[k]);
+            ay[k].add(py[k]);
+            az[k].add(pz[k]);
         }
-        ax.add(pax); ay.add(pay); az.add(paz);
-        bx.add(pbx); by.add(pby); bz.add(pbz);
     }
-    if (i0 < n) {
-        double* p = part + ((int64_t)jc * n + i0) * 3;
-        p[0] = ax.value(); p[1] = ay.value(); p[2] = az.value();
-    }
-    if (i1 < n) {
-        double* p = part + ((int64_t)jc * n + i1) * 3;
-        p[0] = bx.value(); p[1] = by.value(); p[2] = bz.value();
+#pragma unroll
+    for (int k = 0; k < TI; ++k) {
+        if (ii[k] < n) {
+            double* p = part + ((int64_t)jc * n + ii[k]) * 3;
+            p[0] = ax[k].value();
+            p[1] = ay[k].value();
+            p[2] = az[k].value();
+        }
     }
 }
+
+typedef void (*grav_kernel_t)(const float4*, const float4*, int64_t, int64_t, int, double*);
+
+// Kernel variants: bodies per thread (TI) x packed FP32x2; index
+// 0: TI=2 scalar, 1: TI=2 packed, 2: TI=4 scalar, 3: TI=4 packed, 4: TI=1 scalar.
+static grav_kernel_t grav_variant(bool plain, int v)
+{
+    switch (v) {
+    case 0: return plain ? k_gravity<true, 2, false> : k_gravity<false, 2, false>;
+    case 2: return plain ? k_gravity<true, 4, false> : k_gravity<false, 4, false>;
+    case 3: return plain ? k_gravity<true, 4, true> : k_gravity<false, 4, true>;
+    case 4: return plain ? k_gravity<true, 1, false> : k_gravity<false, 1, false>;
+    default: return plain ? k_gravity<true, 2, true> : k_gravity<false, 2, true>;
+    }
+}
+static int grav_ti(int v) { return v == 2 || v == 3 ? 4 : (v == 4 ? 1 : 2); }
 
 // a_i = -G sum_chunks partial_i (fixed chunk order)
 __global__ void k_gravity_reduce(const double* __restrict__ part, int64_t n, int jchunks, double G,
@@ -129,14 +226,11 @@ static int plan_gravity(nbg_ctx* c, int64_t npad)
 {
     int dev = c->device, sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (c->d.grav_plain)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<true>, GB, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<false>, GB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, grav_variant(c->d.grav_plain, c->grav_variant), GB, 0);
     if (sms < 1) sms = 1;
     if (occ < 1) occ = 1;
     const double slots = (double)sms * occ;
-    const int64_t ib = npad / GI;
+    const int64_t ib = npad / (grav_ti(c->grav_variant) * GB);
     const int64_t ntile = npad / GB;
     int best = 1;
     double best_eff = -1.0;
@@ -157,14 +251,10 @@ static int plan_gravity(nbg_ctx* c, int64_t npad)
 // partials (grav_chunks * n * 3 doubles) live in c->grav_part.
 int launch_gravity(nbg_ctx* c, const StateView& s)
 {
-    int64_t units = (c->npad / GI) * c->grav_chunks;
+    int64_t units = (c->npad / (grav_ti(c->grav_variant) * GB)) * c->grav_chunks;
+    grav_kernel_t kern = grav_variant(c->d.grav_plain, c->grav_variant);
     prof_begin(c);
-    if (c->d.grav_plain)
-        k_gravity<true><<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks,
-                                                               c->grav_part);
-    else
-        k_gravity<false><<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks,
-                                                                c->grav_part);
+    kern<<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks, c->grav_part);
     prof_end(c);
     NBG_LAUNCH_CHECK(c, "k_gravity");
     k_gravity_reduce<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->grav_part, c->n, c->grav_chunks, c->d.G,
@@ -408,3 +498,4 @@ int launch_bonded(nbg_ctx* c, const StateView& s)
     NBG_LAUNCH_CHECK(c, "k_bonded");
     return NBG_OK;
 }
+

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -315,7 +316,8 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         if ((st = dalloc(c, &sv->a_old, 3 * c->cols))) return st;
         if ((st = dalloc(c, &sv->a_new, 3 * c->cols))) return st;
     }
-    c->npad = c->path == PATH_GRAVITY ? ((n + 255) / 256) * 256 : n;
+    // gravity bodies padded to a multiple of the largest i-block (4 x 128)
+    c->npad = c->path == PATH_GRAVITY ? ((n + 511) / 512) * 512 : n;
     double* dp;
     if ((st = dalloc(c, &dp, n))) return st;
     D.mass = dp;
@@ -384,6 +386,8 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         if ((st = alloc_lists(c, cell_cap, nbr_cap))) return st;
     }
     if (c->path == PATH_GRAVITY) {
+        const char* gv = getenv("NBG_GRAVITY_VARIANT");  // kernel-form override for tuning sweeps
+        if (gv) c->grav_variant = atoi(gv);
         c->grav_chunks = gravity_plan_chunks(c, c->npad);
         if ((st = dalloc(c, &c->grav_part, (size_t)c->grav_chunks * 3 * n))) return st;
     }
@@ -577,6 +581,9 @@ static int grow_lists(nbg_ctx* c, unsigned st)
     int cell_cap = c->d.cell_cap, nbr_cap = c->d.nbr_cap;
     if (st & ST_CELL_OVERFLOW) cell_cap *= 2;
     if (st & ST_NBR_OVERFLOW) nbr_cap = nbr_cap + nbr_cap / 2 + 32;
+    // the per-cell sort stages a cell in 48 KB of shared memory
+    if (cell_cap > 12288)
+        return fail(c, NBG_ERR_CAPACITY, "more than 12288 atoms in one cell: the configuration has collapsed");
     return alloc_lists(c, cell_cap, nbr_cap);
 }
 
@@ -590,6 +597,7 @@ static int forces_once(nbg_ctx* c, const StateView& s)
         if ((st = forces(c, s, true, 0))) return st;
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
+        if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if ((st = grow_lists(c, w))) return st;
             continue;
@@ -784,6 +792,10 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
         }
         unsigned w = 0;
         if ((st = read_status(c, &w))) { backup_free(c, b); return st; }
+        if (w & (ST_NONFINITE | ST_RANGE)) {
+            backup_free(c, b);
+            return status_error(c, w);
+        }
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if (++retries > 6) {
                 backup_free(c, b);

@@ -133,6 +133,7 @@ struct nbg_ctx {
     // gravity path: bodies padded to npad (multiple of the 256-body tile)
     int64_t npad = 0;
     int grav_chunks = 1;
+    int grav_variant = 1;     // k_gravity form (bodies per thread, packed FP32x2)
     double* grav_part = nullptr;
     // profiling of the dominant force kernel
     bool profiling = false;

@@ -22,6 +22,11 @@ from .bodies import MassBody, WaterMolecule
 
 # SPC/Fw water in kJ/mol, nm, ps, Da (the units of the reference's water tests)
 KB_KJ = 8.3144598e-3
+# SPC/Fw force constants of the benchmark workload: bond 4637 kJ/mol/A^2
+# (= 463,700 kJ/mol/nm^2, read per square angstrom: per nm^2 the O-H bond is too
+# soft to hold an H against a neighbouring O's Coulomb pull), angle 383 kJ/mol/rad^2
+SPCFW_KB = 4637.0 * 100.0
+SPCFW_KA = 383.0
 M_O = 15.999
 M_H = 1.00794
 K_EL = 138.935458
@@ -85,9 +90,35 @@ def _random_rotations(rng, k):
     ], axis=1)
 
 
+def _lattice_contacts(O, H1, H2, side, n_mol, L, d_ho, d_hh):
+    """Molecules whose H lies closer than d_ho to a neighbouring site's O or
+    closer than d_hh to its H (26 lattice neighbours, periodic)."""
+    idx = np.arange(n_mol)
+    ix, iy, iz = idx // (side * side), (idx // side) % side, idx % side
+    bad = np.zeros(n_mol, dtype=bool)
+    for ox in (-1, 0, 1):
+        for oy in (-1, 0, 1):
+            for oz in (-1, 0, 1):
+                if ox == oy == oz == 0:
+                    continue
+                nb = (((ix + ox) % side) * side + (iy + oy) % side) * side + (iz + oz) % side
+                ok = nb < n_mol
+                nbv = np.where(ok, nb, 0)
+                for H in (H1, H2):
+                    for other, lim in ((O, d_ho), (H1, d_hh), (H2, d_hh)):
+                        d = H - other[nbv]
+                        d -= L * np.round(d / L)
+                        bad |= ok & ((d * d).sum(axis=1) < lim * lim)
+    return bad
+
+
 def spcfw_water_box(n_mol, density_g_cm3=0.997, T=300.0, seed=0, rOH=0.1012,
-                    aHOH=113.24 * math.pi / 180, jitter=0.1):
-    """Atom positions (3 n_mol, 3) ordered O,H1,H2, velocities, box L (nm)."""
+                    aHOH=113.24 * math.pi / 180, jitter=0.05):
+    """Atom positions (3 n_mol, 3) ordered O,H1,H2, velocities, box L (nm).
+    Orientations are uniform random, re-drawn (up to 200 times) for any
+    molecule whose H lands within 0.17 nm of a neighbouring O or 0.15 nm of a
+    neighbouring H, so that the start holds no H-O contact that Coulomb
+    attraction would collapse."""
     rng = np.random.default_rng(seed)
     m_mol = M_O + 2 * M_H
     # 1 g/cm^3 = 602.214 Da/nm^3
@@ -104,6 +135,13 @@ def spcfw_water_box(n_mol, density_g_cm3=0.997, T=300.0, seed=0, rOH=0.1012,
     R = _random_rotations(rng, n_mol)
     H1 = O + R @ h1
     H2 = O + R @ h2
+    for _ in range(200):
+        bad = _lattice_contacts(O, H1, H2, side, n_mol, L, 0.17, 0.15)
+        if not bad.any():
+            break
+        Rb = _random_rotations(rng, int(bad.sum()))
+        H1[bad] = O[bad] + Rb @ h1
+        H2[bad] = O[bad] + Rb @ h2
     pos = np.empty((3 * n_mol, 3))
     pos[0::3], pos[1::3], pos[2::3] = O, H1, H2
     vmol = rng.standard_normal((n_mol, 3)) * math.sqrt(KB_KJ * T / m_mol)

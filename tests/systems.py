@@ -149,7 +149,7 @@ def water_box(n_mol, seed=0, eps_rf=1.0, thermostat=None, R=0.9, skin=0.1):
     bodies = nbg.workloads.water_molecules(pos, vel)
     lj = nbg.LennardJonesParameters(0.650299, 0.3165492, R)
     el = nbg.ElectrostaticParameters(nbg.workloads.K_EL, R, eps_rf=eps_rf)
-    spc = nbg.SPCFwParameters(0.1012, 113.24 * math.pi / 180, 4637.0, 383.0)
+    spc = nbg.SPCFwParameters(0.1012, 113.24 * math.pi / 180, nbg.workloads.SPCFW_KB, nbg.workloads.SPCFW_KA)
     water = nbg.WaterSPCFw(bodies, nbg.workloads.M_H, nbg.workloads.M_O, 0.41, -0.82, lj, el, spc)
     args = [nbg.CubicPeriodicBoundaryConditions(L)]
     if thermostat is not None:

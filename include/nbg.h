@@ -238,6 +238,26 @@ NBG_API int nbg_pair_list(nbg_ctx* ctx, const double* u, int32_t which, int32_t*
 NBG_API int nbg_set_profiling(nbg_ctx* ctx, int on);
 NBG_API int nbg_force_kernel_time(nbg_ctx* ctx, double* total_ms, int64_t* launches);
 
+/*
+ * All-pairs gravity accelerations that allocate no device memory. It has no
+ * counterpart in the reference: it is for callers that cannot let a library
+ * allocate (a host integrator calling the right-hand side at a high rate,
+ * where cudaMalloc/cudaFree would synchronise the device, or a process whose
+ * device memory is owned by another allocator). x (3 x n, the reference's
+ * column-major layout), mass (n) and a (3 x n) are device buffers of the
+ * current device; a_i = -G sum_{j != i} m_j (x_i - x_j) / |x_i - x_j|^3.
+ * The scratch is a fixed device array of the library, held by every GPU that
+ * loads it until the process exits, and sized for n <= 16384 bodies; larger n
+ * returns NBG_ERR_CAPACITY. The first call on a device looks up that array's
+ * device address, so make the first call before any stream capture. All calls
+ * share the array: calls that overlap on the GPU (other streams or threads)
+ * race and must be serialised by the caller. Synchronous on `stream` (a
+ * cudaStream_t, NULL for the default stream). Errors are described by
+ * nbg_last_error(NULL).
+ */
+NBG_API int nbg_gravity_accel_noalloc(const double* x, const double* mass, int64_t n, double G, double* a,
+                                      void* stream);
+
 /* Measured FP32 FMA throughput of a device in TFLOP/s (an FMA counts 2):
    the roofline denominator of the FP32-bound gravity kernel. */
 NBG_API int nbg_probe_fp32_peak(int device, double* tflops);

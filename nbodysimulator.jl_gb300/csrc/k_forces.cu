@@ -499,3 +499,40 @@ int launch_bonded(nbg_ctx* c, const StateView& s)
     return NBG_OK;
 }
 
+// ---------------------------------------------------------------------
+// Raw launcher of the gravity kernel (default form) and its chunk reduction
+// on caller-provided buffers, for entry points that own their scratch.
+// ---------------------------------------------------------------------
+int gravity_raw_chunks(int device, int64_t npad, int max_chunks)
+{
+    int sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<false, 2, true>, GB, 0);
+    if (sms < 1) sms = 1;
+    if (occ < 1) occ = 1;
+    const double slots = (double)sms * occ;
+    const int64_t ib = npad / (2 * GB);
+    const int64_t ntile = npad / GB;
+    int best = 1;
+    double best_eff = -1.0;
+    for (int J = 1; J <= max_chunks && J <= ntile; ++J) {
+        double waves = (double)(ib * J) / slots;
+        double eff = waves / ceil(waves) * ((double)ntile / J) / (double)((ntile + J - 1) / J);
+        if (eff > best_eff + 0.005) {
+            best_eff = eff;
+            best = J;
+        }
+    }
+    return best;
+}
+
+cudaError_t gravity_raw_launch(const float4* phi, const float4* plo, int64_t n, int64_t npad, int jchunks,
+                               double* part, double G, double* a, unsigned* status, cudaStream_t stream)
+{
+    int64_t units = (npad / (2 * GB)) * jchunks;
+    k_gravity<false, 2, true><<<(unsigned)units, GB, 0, stream>>>(phi, plo, n, npad, jchunks, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_gravity_reduce<<<grid_for(3 * n, 256), 256, 0, stream>>>(part, n, jchunks, G, a, status);
+    return cudaGetLastError();
+}

@@ -68,9 +68,11 @@ static void dfree(nbg_ctx* c, void* p)
 extern "C" const char* nbg_version(void) { return kVersion; }
 extern "C" int nbg_abi_version(void) { return NBG_ABI_VERSION; }
 
+const char* noalloc_last_error();
+
 extern "C" const char* nbg_last_error(const nbg_ctx* ctx)
 {
-    if (!ctx) return "null context";
+    if (!ctx) return noalloc_last_error();  // errors of the context-free entry points
     return ctx->err.c_str();
 }
 

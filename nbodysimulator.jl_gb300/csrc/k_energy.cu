@@ -170,7 +170,7 @@ __global__ void k_pairs(Dev d, StateView s, int which, int use_list, int* out_j,
         int64_t cnt = 0;
         int64_t m = use_list ? d.nbr_count[i] : (R.atom0 + R.n);
         for (int64_t k = use_list ? 0 : R.atom0; k < m; ++k) {
-            int64_t j = use_list ? d.nbr[k * d.nbr_stride + i] : k;
+            int64_t j = use_list ? d.nbr[k * d.nbr_kstride + i * d.nbr_istride] : k;
             if (j == i) continue;
             PairOut o = pair_cutoff(d, R, i, j, hi, lo, d.phi[j], d.plo[j], 0.0f, s.x);
             if (o.range_err) status_set(d.status, ST_RANGE);

@@ -373,8 +373,10 @@ int launch_allpairs(nbg_ctx* c, const StateView& s)
 }
 
 // ---------------------------------------------------------------------
-// Verlet-list force kernel
+// Verlet-list force kernels
 // ---------------------------------------------------------------------
+// Thread per atom over a column-major list (coalesced across the atoms of a
+// warp): for large systems, where every SM has thousands of atoms.
 __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -385,9 +387,9 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
         Acc2 fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
         float px = 0.f, py = 0.f, pz = 0.f;
         bool range_err = false;
-        const int* nl = d.nbr + i;
+        const int* nl = d.nbr + i * d.nbr_istride;
         for (int k = 0; k < cnt; ++k) {
-            int j = __ldg(nl + (int64_t)k * d.nbr_stride);
+            int j = __ldg(nl + (int64_t)k * d.nbr_kstride);
             float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
             PairOut o = pair_cutoff(d, R, i, j, hi_i, lo_i, hj, lj, kqi, s.x);
             range_err |= o.range_err;
@@ -410,10 +412,68 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
     }
 }
 
+// LPA lanes per atom over a row-major list: the group reads its atom's
+// entries coalesced, each lane keeps an FP32 partial of every LPA-th entry,
+// and the partials are joined by an xor butterfly of shuffles in FP64 (a
+// fixed order: deterministic). For small systems, where one atom per thread
+// leaves the GPU waiting on memory latency.
+template <int LPA>
+__global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
+{
+    // one atom per group of LPA lanes; groups past n keep running (with no
+    // entries) so that every lane of the warp takes part in the shuffles
+    const int lane = threadIdx.x % LPA;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPA;
+    const bool active = i < d.n;
+    const int64_t ia = active ? i : 0;
+    const RepDev& R = d.reps[d.rep_of[ia]];
+    const float4 hi_i = d.phi[ia], lo_i = d.plo[ia];
+    const float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[ia]) : 0.0f;
+    const int cnt = active ? d.nbr_count[ia] : 0;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    bool range_err = false;
+    const int* nl = d.nbr + ia * d.nbr_istride;
+    for (int k = lane; k < cnt; k += LPA) {
+        int j = __ldg(nl + k);
+        float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
+        PairOut o = pair_cutoff(d, R, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
+        range_err |= o.range_err;
+        px += o.fx;
+        py += o.fy;
+        pz += o.fz;
+    }
+    double vx = px, vy = py, vz = pz;
+#pragma unroll
+    for (int o = LPA / 2; o > 0; o >>= 1) {
+        vx += __shfl_xor_sync(0xffffffffu, vx, o, LPA);
+        vy += __shfl_xor_sync(0xffffffffu, vy, o, LPA);
+        vz += __shfl_xor_sync(0xffffffffu, vz, o, LPA);
+    }
+    if (range_err) status_set(d.status, ST_RANGE);
+    if (active && lane == 0) {
+        double im = 1.0 / d.mass[i];
+        double a0 = vx * im, a1 = vy * im, a2 = vz * im;
+        if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
+        s.a_new[3 * i] = a0;
+        s.a_new[3 * i + 1] = a1;
+        s.a_new[3 * i + 2] = a2;
+    }
+}
+
 int launch_force_list(nbg_ctx* c, const StateView& s)
 {
+    const int lpa = c->list_lpa;
     prof_begin(c);
-    k_force_list<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s);
+    if (lpa <= 1) {
+        k_force_list<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s);
+    } else {
+        const int per_block = 256 / lpa;  // one atom per group, whole groups per block
+        int grid = (int)((c->n + per_block - 1) / per_block);
+        if (lpa == 4) k_force_list_lanes<4><<<grid, 256, 0, c->stream>>>(c->d, s);
+        else if (lpa == 8) k_force_list_lanes<8><<<grid, 256, 0, c->stream>>>(c->d, s);
+        else if (lpa == 16) k_force_list_lanes<16><<<grid, 256, 0, c->stream>>>(c->d, s);
+        else k_force_list_lanes<32><<<grid, 256, 0, c->stream>>>(c->d, s);
+    }
     prof_end(c);
     NBG_LAUNCH_CHECK(c, "k_force_list");
     return NBG_OK;
@@ -494,7 +554,8 @@ __global__ void k_bonded(Dev d, StateView s)
 
 int launch_bonded(nbg_ctx* c, const StateView& s)
 {
-    k_bonded<<<grid_for(c->n / 3, 128), 128, 0, c->stream>>>(c->d, s);
+    // FP64-heavy and short: small blocks spread the molecules over every SM
+    k_bonded<<<grid_for(c->n / 3, 32), 32, 0, c->stream>>>(c->d, s);
     NBG_LAUNCH_CHECK(c, "k_bonded");
     return NBG_OK;
 }

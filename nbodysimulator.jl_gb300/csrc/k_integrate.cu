@@ -50,20 +50,39 @@ int launch_pack(nbg_ctx* c, const StateView& s)
     return NBG_OK;
 }
 
-// u' = u + dt v + dt^2 (a/2) for every column (the Nose-Hoover column moves
-// zeta by dt * v_zeta since its acceleration is 0), then repack and flag a
-// Verlet-list rebuild when an atom moved more than skin/2.
-__global__ void k_drift(Dev d, StateView s, double dt, double dtsq)
+// u' = u + dt v + dt^2 (a/2) for one atom's three components, then its split
+// position, then the Verlet-list displacement check (moved more than skin/2
+// since the last build: flag a rebuild). One thread per atom; the thread after
+// the last atom moves the Nose-Hoover column (zeta += dt v_zeta, a = 0).
+__device__ __forceinline__ double drift1(double u, double v, double a, double dt, double dtsq)
 {
-    int64_t ncomp = 3 * d.cols;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x) {
-        double u = s.x[e];
-        s.x[e] = __dadd_rn(__dadd_rn(u, __dmul_rn(dt, s.v[e])), __dmul_rn(dtsq, __dmul_rn(0.5, s.a_old[e])));
+    return __dadd_rn(__dadd_rn(u, __dmul_rn(dt, v)), __dmul_rn(dtsq, __dmul_rn(0.5, a)));
+}
+
+__global__ void k_drift_pack(Dev d, StateView s, double dt, double dtsq, int check_disp, StepRef pos)
+{
+    const int parity = (int)(step_of(pos) & 1);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.cols; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int k = 0; k < 3; ++k) {
+            const int64_t e = 3 * i + k;
+            s.x[e] = drift1(s.x[e], s.v[e], s.a_old[e], dt, dtsq);
+        }
+        if (i >= d.n) continue;
+        pack_atom(d, i, s.x);
+        if (check_disp) {
+            double dx = s.x[3 * i] - d.xref[3 * i];
+            double dy = s.x[3 * i + 1] - d.xref[3 * i + 1];
+            double dz = s.x[3 * i + 2] - d.xref[3 * i + 2];
+            double d2 = dx * dx + dy * dy + dz * dz;
+            if (!(d2 <= d.skin_half2)) d.rebuild_flag[parity] = 1;
+        }
     }
 }
 
-__global__ void k_pack_disp(Dev d, const double* X, int check_disp, int parity)
+// The rebuild flag written is the one of the positions' time index `pos`.
+__global__ void k_pack_disp(Dev d, const double* X, int check_disp, StepRef pos)
 {
+    const int parity = (int)(step_of(pos) & 1);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         pack_atom(d, i, X);
         if (check_disp) {
@@ -76,13 +95,11 @@ __global__ void k_pack_disp(Dev d, const double* X, int check_disp, int parity)
     }
 }
 
-int launch_drift(nbg_ctx* c, const StateView& s, double dt)
+int launch_drift(nbg_ctx* c, const StateView& s, double dt, StepRef pos)
 {
-    k_drift<<<grid_for(3 * c->cols, 256), 256, 0, c->stream>>>(c->d, s, dt, dt * dt);
-    NBG_LAUNCH_CHECK(c, "k_drift");
-    k_pack_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s.x, c->path == PATH_LIST ? 1 : 0,
-                                                            (int)((c->step + 1) & 1));
-    NBG_LAUNCH_CHECK(c, "k_pack_disp");
+    k_drift_pack<<<grid_for(c->cols, 128), 128, 0, c->stream>>>(c->d, s, dt, dt * dt,
+                                                                 c->path == PATH_LIST ? 1 : 0, pos);
+    NBG_LAUNCH_CHECK(c, "k_drift_pack");
     return NBG_OK;
 }
 
@@ -224,8 +241,9 @@ int launch_rhs_thermostat(nbg_ctx* c, const StateView& s)
 // Andersen affect! after step `step` (nbody_simulation_result.jl:511-540):
 // with probability nu*dt an atom's velocity is redrawn as sqrt(kb T / m) z,
 // m = the first body's mass for potential systems, the site mass for water.
-__global__ void k_andersen(Dev d, StateView s, double dt, int64_t step)
+__global__ void k_andersen(Dev d, StateView s, double dt, StepRef sr)
 {
+    const int64_t step = step_of(sr);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         int r = d.rep_of[i];
         const RepDev& R = d.reps[r];
@@ -243,7 +261,7 @@ __global__ void k_andersen(Dev d, StateView s, double dt, int64_t step)
     }
 }
 
-int launch_andersen(nbg_ctx* c, const StateView& s, double dt, int64_t step)
+int launch_andersen(nbg_ctx* c, const StateView& s, double dt, StepRef step)
 {
     k_andersen<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s, dt, step);
     NBG_LAUNCH_CHECK(c, "k_andersen");
@@ -255,8 +273,9 @@ int launch_andersen(nbg_ctx* c, const StateView& s, double dt, int64_t step)
 // Potential systems: friction gamma v, sigma = sqrt(2 gamma kb T / m_1).
 // Water (the reference's terms): O rows lose gamma v / m_O and gamma v,
 // H rows gamma v; sigma = sqrt(2 gamma kb T) / m_site.
-__global__ void k_em(Dev d, StateView s, double dt, double sqdt, int64_t step)
+__global__ void k_em(Dev d, StateView s, double dt, double sqdt, StepRef sr)
 {
+    const int64_t step = step_of(sr);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         int r = d.rep_of[i];
         const RepDev& R = d.reps[r];
@@ -281,12 +300,29 @@ __global__ void k_em(Dev d, StateView s, double dt, double sqdt, int64_t step)
     }
 }
 
-int launch_em(nbg_ctx* c, const StateView& s, double dt, int64_t step)
+int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step)
 {
     k_em<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s, dt, sqrt(dt), step);
     NBG_LAUNCH_CHECK(c, "k_em");
-    k_pack_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s.x, c->path == PATH_LIST ? 1 : 0,
-                                                            (int)((step + 1) & 1));
+    StepRef pos{step.off + 1, step.base};
+    k_pack_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, s.x, c->path == PATH_LIST ? 1 : 0, pos);
     NBG_LAUNCH_CHECK(c, "k_pack_disp");
+    return NBG_OK;
+}
+
+__global__ void k_step_advance(int64_t* step, int64_t by) { *step += by; }
+__global__ void k_set_step(int64_t* step, int64_t value) { *step = value; }
+
+int launch_step_advance(nbg_ctx* c, int64_t by)
+{
+    k_step_advance<<<1, 1, 0, c->stream>>>(c->d.step_dev, by);
+    NBG_LAUNCH_CHECK(c, "k_step_advance");
+    return NBG_OK;
+}
+
+int launch_set_step(nbg_ctx* c, int64_t value)
+{
+    k_set_step<<<1, 1, 0, c->stream>>>(c->d.step_dev, value);
+    NBG_LAUNCH_CHECK(c, "k_set_step");
     return NBG_OK;
 }

@@ -168,7 +168,13 @@ static int alloc_lists(nbg_ctx* c, int cell_cap, int nbr_cap)
     if ((st = dalloc(c, &c->d.nbr, (size_t)c->n * nbr_cap))) return st;
     c->d.cell_cap = cell_cap;
     c->d.nbr_cap = nbr_cap;
-    c->d.nbr_stride = c->n;
+    if (c->list_lpa <= 1) {  // column-major for thread per atom
+        c->d.nbr_kstride = c->n;
+        c->d.nbr_istride = 1;
+    } else {                 // row-major for lanes per atom
+        c->d.nbr_kstride = 1;
+        c->d.nbr_istride = nbr_cap;
+    }
     return NBG_OK;
 }
 
@@ -373,7 +379,9 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     if ((st = dalloc(c, &D.status, 4))) return st;
     if ((st = dalloc(c, &D.rebuild_flag, 2))) return st;
     if ((st = dalloc(c, &D.build_count, 1))) return st;
-    D.red_slices = (int)std::min<int64_t>(64, std::max<int64_t>(1, (max_rep_n + 4095) / 4096));
+    if ((st = dalloc(c, &D.step_dev, 1))) return st;
+    // slices of 256 atoms per replica (the last block adds them in order)
+    D.red_slices = (int)std::min<int64_t>(512, std::max<int64_t>(1, (max_rep_n + 255) / 256));
     if ((st = dalloc(c, &D.red_partial, (size_t)nrep * D.red_slices))) return st;
     if ((st = dalloc(c, &D.red_T, nrep))) return st;
     if ((st = dalloc(c, &D.red_counter, nrep))) return st;
@@ -385,8 +393,29 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         if ((st = dalloc(c, &D.xref, 3 * n))) return st;
         int cell_cap = ((2 * max_cell_occ + 16 + 7) / 8) * 8;
         int nbr_cap = ((int)std::ceil(1.3 * max_nbr + 32) + 7) / 8 * 8;
+        // lanes per atom of the list force kernel: a group of lanes per atom
+        // until the GPU holds ~64 resident lanes per SM-thread slot, then one
+        // thread per atom (column-major list)
+        const char* lv = getenv("NBG_LIST_LPA");  // override for tuning sweeps
+        if (lv) {
+            c->list_lpa = atoi(lv);
+        } else {
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+            double threads_wanted = (double)std::max(sms, 1) * 2048.0;
+            int lpa = 1;
+            while (lpa < 32 && (double)n * lpa < threads_wanted && lpa * 4 <= max_nbr) lpa *= 2;
+            c->list_lpa = lpa;
+        }
+        // supported group sizes: 1 (thread per atom), 4, 8, 16, 32
+        if (c->list_lpa <= 1) c->list_lpa = 1;
+        else if (c->list_lpa <= 4) c->list_lpa = 4;
+        else if (c->list_lpa <= 8) c->list_lpa = 8;
+        else if (c->list_lpa <= 16) c->list_lpa = 16;
+        else c->list_lpa = 32;
         if ((st = alloc_lists(c, cell_cap, nbr_cap))) return st;
     }
+    if (getenv("NBG_NO_GRAPHS")) c->use_graphs = false;  // direct launches, for comparisons
     if (c->path == PATH_GRAVITY) {
         const char* gv = getenv("NBG_GRAVITY_VARIANT");  // kernel-form override for tuning sweeps
         if (gv) c->grav_variant = atoi(gv);
@@ -455,6 +484,8 @@ extern "C" int nbg_force_kernel_time(nbg_ctx* c, double* total_ms, int64_t* laun
 static void release(nbg_ctx* c)
 {
     prof_drain(c);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
     for (void* p : c->allocs) cudaFree(p);
     c->allocs.clear();
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -560,14 +591,14 @@ static int status_error(nbg_ctx* c, unsigned st)
 }
 
 // Potential accelerations of state s into s.a_new (no thermostat term).
-// parity: rebuild_flag word of the positions in s.
-static int forces(nbg_ctx* c, const StateView& s, bool force_build, int parity)
+// pos: time index of the positions in s (its parity picks the rebuild flag).
+static int forces(nbg_ctx* c, const StateView& s, bool force_build, StepRef pos)
 {
     int st = NBG_OK;
     if (c->path == PATH_GRAVITY) {
         st = launch_gravity(c, s);
     } else if (c->path == PATH_LIST) {
-        if ((st = launch_list_build(c, s, force_build, parity))) return st;
+        if ((st = launch_list_build(c, s, force_build, pos))) return st;
         st = launch_force_list(c, s);
     } else {
         st = launch_allpairs(c, s);
@@ -586,6 +617,10 @@ static int grow_lists(nbg_ctx* c, unsigned st)
     // the per-cell sort stages a cell in 48 KB of shared memory
     if (cell_cap > 12288)
         return fail(c, NBG_ERR_CAPACITY, "more than 12288 atoms in one cell: the configuration has collapsed");
+    if (c->graph) {  // the captured kernels hold the old list pointers
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
     return alloc_lists(c, cell_cap, nbr_cap);
 }
 
@@ -596,7 +631,7 @@ static int forces_once(nbg_ctx* c, const StateView& s)
         int st;
         if ((st = clear_status(c))) return st;
         if ((st = launch_pack(c, s))) return st;
-        if ((st = forces(c, s, true, 0))) return st;
+        if ((st = forces(c, s, true, StepRef{0, nullptr}))) return st;
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
         if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
@@ -664,7 +699,7 @@ extern "C" int nbg_compute_forces(nbg_ctx* c)
     cudaSetDevice(c->device);
     int st;
     if ((st = launch_pack(c, c->st))) return st;
-    if ((st = forces(c, c->st, c->steps_since_build < 0, (int)(c->step & 1)))) return st;
+    if ((st = forces(c, c->st, c->steps_since_build < 0, StepRef{c->step, nullptr}))) return st;
     if (c->steps_since_build < 0) c->steps_since_build = 0;
     return NBG_OK;
 }
@@ -712,7 +747,7 @@ static int init_accel(nbg_ctx* c)
 {
     int st;
     if ((st = launch_pack(c, c->st))) return st;
-    if ((st = forces(c, c->st, true, (int)(c->step & 1)))) return st;
+    if ((st = forces(c, c->st, true, StepRef{c->step, nullptr}))) return st;
     c->steps_since_build = 0;
     if (c->d.therm != NBG_THERMO_LANGEVIN) {
         if ((st = launch_rhs_thermostat(c, c->st))) return st;
@@ -722,40 +757,128 @@ static int init_accel(nbg_ctx* c)
     return NBG_OK;
 }
 
-static int step_vv(nbg_ctx* c, double dt)
+// Is the host-forced list rebuild due at this step? (VV: positions advance
+// before the forces; EM: the forces use the current positions.)
+static bool rebuild_due(const nbg_ctx* c, bool vv)
+{
+    if (c->path != PATH_LIST) return false;
+    int re = c->desc.rebuild_every;
+    if (c->steps_since_build < 0) return true;
+    return re > 0 && (vv ? c->steps_since_build + 1 : c->steps_since_build) >= re;
+}
+
+// One step. sr: the step index (absolute, or an offset from the device step
+// counter inside a captured graph).
+static int step_vv(nbg_ctx* c, double dt, StepRef sr)
 {
     int st;
     const StateView& s = c->st;
-    if ((st = launch_drift(c, s, dt))) return st;
-    bool force = false;
-    if (c->path == PATH_LIST) {
-        int re = c->desc.rebuild_every;
-        force = c->steps_since_build < 0 || (re > 0 && c->steps_since_build + 1 >= re);
-    }
-    if ((st = forces(c, s, force, (int)((c->step + 1) & 1)))) return st;
+    StepRef pos{sr.off + 1, sr.base};
+    if ((st = launch_drift(c, s, dt, pos))) return st;
+    bool force = rebuild_due(c, true);
+    if ((st = forces(c, s, force, pos))) return st;
     c->steps_since_build = force ? 0 : c->steps_since_build + 1;
     if (c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER)
         if ((st = launch_temperature(c, s.v))) return st;
     if ((st = launch_kick(c, s, dt))) return st;
     if (c->d.therm == NBG_THERMO_ANDERSEN)
-        if ((st = launch_andersen(c, s, dt, c->step))) return st;
+        if ((st = launch_andersen(c, s, dt, sr))) return st;
+    return NBG_OK;
+}
+
+static int step_em(nbg_ctx* c, double dt, StepRef sr)
+{
+    int st;
+    const StateView& s = c->st;
+    bool force = rebuild_due(c, false);
+    if ((st = forces(c, s, force, sr))) return st;
+    c->steps_since_build = force ? 1 : c->steps_since_build + 1;
+    if ((st = launch_em(c, s, dt, sr))) return st;
+    return NBG_OK;
+}
+
+static int step_direct(nbg_ctx* c, double dt)
+{
+    int st = c->d.therm == NBG_THERMO_LANGEVIN ? step_em(c, dt, StepRef{c->step, nullptr})
+                                               : step_vv(c, dt, StepRef{c->step, nullptr});
+    if (st) return st;
     c->step++;
     return NBG_OK;
 }
 
-static int step_em(nbg_ctx* c, double dt)
+// Steps per captured graph: one rebuild period (so the host-forced rebuilds
+// fall on the same graph steps every replay), at least 8.
+static int64_t graph_period(const nbg_ctx* c)
 {
-    int st;
-    const StateView& s = c->st;
-    bool force = false;
-    if (c->path == PATH_LIST) {
-        int re = c->desc.rebuild_every;
-        force = c->steps_since_build < 0 || (re > 0 && c->steps_since_build >= re);
+    int64_t g = c->path == PATH_LIST && c->desc.rebuild_every > 0 ? c->desc.rebuild_every : 1;
+    while (g < 8) g *= 2;
+    return g;
+}
+
+// A replay starts where the host pattern of forced rebuilds matches the
+// capture: right after a rebuild period (or with a rebuild pending).
+static bool graph_aligned(const nbg_ctx* c)
+{
+    if (c->path != PATH_LIST) return true;
+    // displacement-only rebuilds: capture once the first (forced) build is done
+    if (c->desc.rebuild_every <= 0) return c->steps_since_build >= 0;
+    bool vv = c->d.therm != NBG_THERMO_LANGEVIN;
+    int re = c->desc.rebuild_every;
+    int64_t s = c->steps_since_build;
+    return vv ? (s < 0 || s + 1 >= re) : (s < 0 || s >= re);
+}
+
+// Capture graph_period() steps on the context stream (kernels read the step
+// counter from device memory, the last node advances it) and instantiate.
+static int capture_graph(nbg_ctx* c, double dt)
+{
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
     }
-    if ((st = forces(c, s, force, (int)(c->step & 1)))) return st;
-    c->steps_since_build = force ? 1 : c->steps_since_build + 1;
-    if ((st = launch_em(c, s, dt, c->step))) return st;
-    c->step++;
+    const int64_t G = graph_period(c);
+    const int64_t launches0 = c->launches;
+    const int64_t ssb0 = c->steps_since_build;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
+    int st = NBG_OK;
+    for (int64_t k = 0; k < G && st == NBG_OK; ++k)
+        st = c->d.therm == NBG_THERMO_LANGEVIN ? step_em(c, dt, StepRef{k, c->d.step_dev})
+                                               : step_vv(c, dt, StepRef{k, c->d.step_dev});
+    if (st == NBG_OK) st = launch_step_advance(c, G);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->steps_since_build = ssb0;  // capture only recorded the steps
+    if (st != NBG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph capture");
+    e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->graph = nullptr;
+        return cuda_fail(c, e, "graph instantiate");
+    }
+    c->graph_steps = G;
+    c->graph_launches = c->launches - launches0;
+    c->launches = launches0;
+    c->graph_dt = dt;
+    return NBG_OK;
+}
+
+// Replay the step graph once: graph_period() steps.
+static int replay_graph(nbg_ctx* c)
+{
+    CK(cudaGraphLaunch(c->graph, c->stream), "graph launch");
+    c->launches += c->graph_launches;
+    c->step += c->graph_steps;
+    // the forced-rebuild pattern repeats: after a period the host state is as at capture
+    bool vv = c->d.therm != NBG_THERMO_LANGEVIN;
+    if (c->path == PATH_LIST && c->desc.rebuild_every > 0) {
+        int64_t re = c->desc.rebuild_every;
+        c->steps_since_build = vv ? re - 1 : re;
+        (void)re;
+    }
     return NBG_OK;
 }
 
@@ -773,24 +896,42 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
     }
     const bool can_overflow = c->path == PATH_LIST;
     const int64_t chunk = can_overflow ? 512 : nsteps;
+    // graphs pay off for short steps; events around kernels (profiling) stay direct
+    const bool graphs = c->use_graphs && !c->profiling && nsteps >= 2 * graph_period(c);
     Backup b;
     if (can_overflow && (st = backup_alloc(c, b))) return st;
     int64_t done = 0;
     int retries = 0;
     while (done < nsteps) {
         int64_t k = std::min<int64_t>(chunk > 0 ? chunk : nsteps, nsteps - done);
-        int64_t step0 = c->step, ssb0 = c->steps_since_build;
+        int64_t step0 = c->step;
         if (can_overflow) {
             CK(cudaMemcpyAsync(b.x, c->st.x, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
             CK(cudaMemcpyAsync(b.v, c->st.v, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
             CK(cudaMemcpyAsync(b.a, c->st.a_old, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
         }
-        for (int64_t s = 0; s < k; ++s) {
-            st = langevin ? step_em(c, dt) : step_vv(c, dt);
-            if (st) {
-                backup_free(c, b);
-                return st;
+        int64_t s = 0;
+        bool counter_set = false;
+        while (s < k) {
+            if (graphs && graph_aligned(c) && k - s >= graph_period(c)) {
+                if (!c->graph || c->graph_dt != dt) {
+                    if ((st = capture_graph(c, dt))) break;
+                }
+                if (!counter_set) {
+                    if ((st = launch_set_step(c, c->step))) break;
+                    counter_set = true;
+                }
+                if ((st = replay_graph(c))) break;
+                s += c->graph_steps;
+            } else {
+                if ((st = step_direct(c, dt))) break;
+                counter_set = false;
+                ++s;
             }
+        }
+        if (st) {
+            backup_free(c, b);
+            return st;
         }
         unsigned w = 0;
         if ((st = read_status(c, &w))) { backup_free(c, b); return st; }
@@ -809,7 +950,6 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
             CK(cudaMemcpyAsync(c->st.a_old, b.a, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
             c->step = step0;
             c->steps_since_build = -1;
-            (void)ssb0;
             if ((st = clear_status(c))) { backup_free(c, b); return st; }
             if ((st = launch_pack(c, c->st))) { backup_free(c, b); return st; }
             continue;

@@ -87,14 +87,16 @@ struct Dev {
     int* cell_atoms;
     int cell_cap;
     int ncell_total;
-    int* nbr;
+    int* nbr;           // entry k of atom i at nbr[k * nbr_kstride + i * nbr_istride]
     int* nbr_count;
     int nbr_cap;
-    int64_t nbr_stride;
+    int64_t nbr_kstride;  // n (column-major, thread per atom) or 1 (row-major, lanes per atom)
+    int64_t nbr_istride;  // 1 or nbr_cap
     double* xref;
     int* rebuild_flag;          // [2], indexed by the parity of the position time index
     unsigned long long* build_count;
     unsigned* status;
+    int64_t* step_dev;          // step counter read by graph-captured kernels
     // reductions
     double* red_partial;
     double* red_T;      // per replica temperature of the current velocities
@@ -134,9 +136,16 @@ struct nbg_ctx {
     int64_t npad = 0;
     int grav_chunks = 1;
     int grav_variant = 1;     // k_gravity form (bodies per thread, packed FP32x2)
+    int list_lpa = 0;         // lanes per atom of k_force_list (1 = thread per atom)
     double* grav_part = nullptr;
     // profiling of the dominant force kernel
     bool profiling = false;
+    // captured step graphs (velocity Verlet / Euler-Maruyama)
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_steps = 0;     // steps per replay
+    int64_t graph_launches = 0;  // kernels per replay
+    double graph_dt = 0.0;
+    bool use_graphs = true;
     std::vector<cudaEvent_t> prof_events;  // start/stop pairs not yet read
     double prof_ms = 0.0;
     int64_t prof_count = 0;
@@ -149,17 +158,26 @@ enum { PATH_GRAVITY = 0, PATH_LIST = 1, PATH_ALLPAIRS = 2 };
 // ---------------------------------------------------------------------
 // host-side launchers (one translation unit each)
 // ---------------------------------------------------------------------
+// Step index of a launch: off + *base (base = the device step counter in a
+// captured graph, NULL for a direct launch where off is the absolute step).
+struct StepRef {
+    int64_t off;
+    const int64_t* base;
+};
+
 int launch_pack(nbg_ctx* c, const StateView& s);
 int launch_gravity(nbg_ctx* c, const StateView& s);
 int launch_allpairs(nbg_ctx* c, const StateView& s);
-int launch_list_build(nbg_ctx* c, const StateView& s, bool force, int parity);
+int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
 int launch_force_list(nbg_ctx* c, const StateView& s);
 int launch_bonded(nbg_ctx* c, const StateView& s);
-int launch_drift(nbg_ctx* c, const StateView& s, double dt);
+int launch_drift(nbg_ctx* c, const StateView& s, double dt, StepRef pos);
 int launch_temperature(nbg_ctx* c, const double* v);
 int launch_kick(nbg_ctx* c, const StateView& s, double dt);
-int launch_andersen(nbg_ctx* c, const StateView& s, double dt, int64_t step);
-int launch_em(nbg_ctx* c, const StateView& s, double dt, int64_t step);
+int launch_andersen(nbg_ctx* c, const StateView& s, double dt, StepRef step);
+int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step);
+int launch_step_advance(nbg_ctx* c, int64_t by);
+int launch_set_step(nbg_ctx* c, int64_t value);
 int launch_rhs_thermostat(nbg_ctx* c, const StateView& s);
 int gravity_plan_chunks(nbg_ctx* c, int64_t npad);
 int launch_energy(nbg_ctx* c, const StateView& s, double* out_host /*[8]*/);
@@ -191,6 +209,8 @@ static inline int grid_for(int64_t work, int block)
 // device helpers
 // ---------------------------------------------------------------------
 #ifdef __CUDACC__
+
+__device__ __forceinline__ int64_t step_of(StepRef r) { return r.off + (r.base ? *r.base : 0); }
 
 __device__ __forceinline__ void status_set(unsigned* st, unsigned bit) { atomicOr(st, bit); }
 

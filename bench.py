@@ -22,6 +22,7 @@ With --gpus N > 1 (torchrun) every rank runs its own replica: replicas only,
 no collective on the data path.
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -41,7 +42,41 @@ WORKLOADS = {
     "gravity": dict(name="gravity-plummer-65536", n=65536, dt=1e-3, steps=100),
     "lj": dict(name="lj-argon-1000", n=1000, dt=0.005, steps=1000),
     "water": dict(name="spcfw-water-12288", n=12288, dt=0.0005, steps=2000),
+    "ensemble": dict(name="lj-langevin-ensemble-256", n=None, dt=0.005, steps=5000),
 }
+
+
+class Workload:
+    """Engine inputs of one benchmark workload: descriptors (one per replica),
+    the initial state in the reference layout, and oracle descriptors."""
+
+    def __init__(self, nbg, name, seed=0, n=None):
+        self.name = name
+        self.keep = []
+        if name == "ensemble":
+            reps = nbg.workloads.lj_ensemble(seed=seed)
+            self.descs = []
+            for r, rep in enumerate(reps):
+                d, k = nbg.lennard_jones_descriptor(np.ones(rep["n"]), rep["L"],
+                                                    thermostat=nbg.LangevinThermostat(rep["T"], 1.0),
+                                                    seed=1000 + r, skin=0.3, rebuild_every=10)
+                # Euler-Maruyama (the reference's Langevin integrator) diverges
+                # for an LJ liquid at dt = 0.005: BAOAB keeps velocity-Verlet stability
+                d.flags |= nbg._abi.NBG_FLAG_LANGEVIN_BAOAB
+                self.descs.append(d)
+                self.keep.append(k)
+            self.u0 = np.concatenate([rep["pos"] for rep in reps])
+            self.v0 = np.concatenate([rep["vel"] for rep in reps])
+            self.sizes = [rep["n"] for rep in reps]
+        else:
+            sim = make_sim(nbg, name, seed=seed, n=n)
+            self.sim = sim
+            d, k = nbg.system_descriptor(sim)
+            self.descs = [d]
+            self.keep.append(k)
+            self.u0, self.v0, _ = nbg.gather_bodies_initial_coordinates(sim)
+            self.sizes = [int(d.n)]
+        self.n = int(sum(self.sizes))
 
 
 def make_sim(nbg, workload, seed=0, n=None):
@@ -138,20 +173,39 @@ def profile_traffic(kernel):
         return None
 
 
-def cpu_baseline(oracle, desc, u, workload, target_s=8.0):
-    """The oracle on a bounded sample of one step: accelerations of a subset of
-    atoms over all partners, on every host core; atom-steps/s = atoms / time."""
-    n = int(desc.n)
+def cpu_baseline(oracle, wl, target_s=8.0):
+    """The oracle on a bounded sample of one step, on every host core:
+    accelerations of a subset of atoms over all their partners (the
+    reference's per-atom loops), atom-steps/s = atoms / time. For the ensemble,
+    a stratified sample of replicas, timed whole, fitted to c N^2 and summed
+    over all replicas (the reference's cost is all-pairs per replica)."""
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
+    if wl.name == "ensemble":
+        order = np.argsort(wl.sizes)
+        pick = order[np.linspace(0, len(order) - 1, 6).astype(int)]
+        offs = np.concatenate([[0], np.cumsum(wl.sizes)])
+        cs, done, el = [], 0, 0.0
+        for r in pick:
+            u = wl.u0[offs[r]:offs[r + 1]]
+            t0 = time.perf_counter()
+            oracle.partial_accel(wl.descs[r], u, 0, wl.sizes[r])
+            dt = time.perf_counter() - t0
+            cs.append(dt / wl.sizes[r] ** 2)
+            done += wl.sizes[r]
+            el += dt
+        c = float(np.mean(cs))
+        step_s = c * float(np.sum(np.asarray(wl.sizes, dtype=np.float64) ** 2))
+        return {"value": wl.n / step_s, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                "sample": f"{len(pick)} replicas (sizes {sorted(int(wl.sizes[r]) for r in pick)}) timed whole, "
+                          f"{el:.1f} s; step time = c * sum N_r^2 over all {len(wl.sizes)} replicas"}
+    desc, u, n = wl.descs[0], wl.u0, wl.n
     i1 = min(n, 64)
     t0 = time.perf_counter()
     oracle.partial_accel(desc, u, 0, i1)
-    dt = time.perf_counter() - t0
-    per_atom = dt / i1
+    per_atom = (time.perf_counter() - t0) / i1
     k = int(max(i1, min(n, target_s / max(per_atom, 1e-9))))
-    reps = max(1, int(target_s / max(per_atom * k, 1e-9)))
-    reps = min(reps, 20)
+    reps = min(20, max(1, int(target_s / max(per_atom * k, 1e-9))))
     t0 = time.perf_counter()
     done = 0
     for r in range(reps):
@@ -174,37 +228,48 @@ def cpu_baseline(oracle, desc, u, workload, target_s=8.0):
 
 def run_reference(args, rank):
     """--impl reference: the oracle's restatement of the reference's O(N^2)
-    per-atom loops on the host cores, each step a bounded sample."""
+    per-atom loops on the host cores, each step a bounded sample of the
+    workload's force evaluation (atoms over all partners)."""
     if rank != 0:
         return
     nbg = G.load_package()
     oracle = G.load_oracle()
     w = WORKLOADS[args.workload]
-    sim = make_sim(nbg, args.workload, n=args.n)
-    desc, keep = nbg.system_descriptor(sim)
-    u, v, _ = nbg.gather_bodies_initial_coordinates(sim)
-    n = int(desc.n)
+    wl = Workload(nbg, args.workload, n=args.n)
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    sample = min(n, args.ref_sample)
+    offs = np.concatenate([[0], np.cumsum(wl.sizes)])
+
+    def sample_step(s):
+        """one bounded sample: `ref_sample` atoms of one system / replica"""
+        r = s % len(wl.sizes)
+        n_r = wl.sizes[r]
+        a = (s * args.ref_sample) % n_r
+        b = min(n_r, a + args.ref_sample)
+        oracle.partial_accel(wl.descs[r], wl.u0[offs[r]:offs[r + 1]], a, b)
+        return b - a
+
     for s in range(args.warmup):
-        oracle.partial_accel(desc, u, (s * sample) % n, min(n, (s * sample) % n + sample))
+        sample_step(s)
     t0 = time.perf_counter()
     done = 0
     for s in range(args.steps):
-        a = (s * sample) % n
-        b = min(n, a + sample)
-        oracle.partial_accel(desc, u, a, b)
-        done += b - a
+        done += sample_step(s)
     el = time.perf_counter() - t0
     val = done / el
+    if wl.name == "ensemble":
+        # all-pairs cost grows with N_r: rescale the sampled rate to the ensemble's mix
+        sz = np.asarray(wl.sizes, dtype=np.float64)
+        sampled = np.asarray([wl.sizes[s % len(sz)] for s in range(args.steps)], dtype=np.float64)
+        val = val * sampled.mean() / (np.sum(sz ** 2) / np.sum(sz))
     line = {"metric": "atom-steps/s", "value": val, "unit": "atom-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps * (n / sample),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wl.n / val,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": w["name"], "N": n, "dt": w["dt"], "sample_atoms_per_step": sample},
+            "config": {"workload": w["name"], "N": wl.n, "dt": w["dt"], "sample_atoms_per_step": args.ref_sample},
             "cpu_baseline": {"value": val, "unit": "atom-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{sample} of {n} atoms' forces per step over all partners"},
+                             "sample": f"{args.ref_sample} atoms' forces per step over all partners "
+                                       "(the FP64 restatement of the reference's per-atom loops)"},
             "e2e": {"value": val, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -225,7 +290,7 @@ def main():
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.steps is None:
-        args.steps = 100 if args.workload == "gravity" else w["steps"]
+        args.steps = w["steps"]
     if args.warmup < 3:
         args.warmup = 3
 
@@ -247,25 +312,26 @@ def main():
     device = local
     nbg = G.load_package()
     nbg.load_library()
-    sim = make_sim(nbg, args.workload, seed=rank, n=args.n)
+    wl = Workload(nbg, args.workload, seed=rank, n=args.n)
     if args.grav_plain:
-        sim.flags |= nbg._abi.NBG_FLAG_GRAV_PLAIN
-    desc, keep = nbg.system_descriptor(sim)
-    u0, v0, _ = nbg.gather_bodies_initial_coordinates(sim)
-    n = int(desc.n)
+        wl.descs[0].flags |= nbg._abi.NBG_FLAG_GRAV_PLAIN
+    u0, v0, n = wl.u0, wl.v0, wl.n
     dt = w["dt"]
-    eng = nbg.Engine(desc, device)
+    eng = nbg.Engine(wl.descs, device)
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
+    batch = len(wl.descs) > 1
+    # the ensemble's working set (~0.5 GB) exceeds L2 by itself
+    flush_steps = not args.no_flush and not batch
 
     peak_fp32 = None
     if args.workload == "gravity":
-        pk = __import__("ctypes").c_double()
-        if eng.lib.nbg_probe_fp32_peak(device, __import__("ctypes").byref(pk)) == 0:
+        pk = ctypes.c_double()
+        if eng.lib.nbg_probe_fp32_peak(device, ctypes.byref(pk)) == 0:
             peak_fp32 = pk.value
 
     eng.set_state(u0, v0)
-    e_start = eng.energy(u0, v0)
+    e_start = None if batch else eng.energy(u0, v0)
     eng.advance(dt, args.warmup)
     torch.cuda.synchronize()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
@@ -276,8 +342,9 @@ def main():
     sampler = ClockSampler(device)
     launches0 = eng.kernel_launches
     step_ms = []
-    if args.no_flush:
+    if not flush_steps:
         # all K steps back to back (the step loop replays captured CUDA graphs)
+        flush.fill_(0.0)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -298,7 +365,7 @@ def main():
     launches = eng.kernel_launches - launches0
     clocks = sampler.stop()
     # the dominant force kernel's launch time: a separate pass with CUDA events
-    # around every launch (direct launches, same state continuing)
+    # around every launch (direct launches, the same state continuing)
     eng.set_profiling(True)
     eng.advance(dt, min(args.steps, 20 if args.workload == "gravity" else 200))
     kern_ms, kern_n = eng.force_kernel_time()
@@ -313,14 +380,14 @@ def main():
 
     # end-to-end: the drop-in right-hand side on pinned host buffers, with the
     # velocity-Verlet update on the host (SciML's loop), every step
-    cols = eng.cols
-    pin = lambda: torch.zeros((cols, 3), dtype=torch.float64).pin_memory().numpy()
-    uh, vh, ah = pin(), pin(), pin()
-    uh[:] = u0
-    vh[:] = v0
-    e2e_steps = max(3, min(args.steps, 50 if args.workload == "gravity" else 200))
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and not batch:
+        cols = eng.cols
+        pin = lambda: torch.zeros((cols, 3), dtype=torch.float64).pin_memory().numpy()
+        uh, vh, ah = pin(), pin(), pin()
+        uh[:] = u0
+        vh[:] = v0
+        e2e_steps = max(3, min(args.steps, 50 if args.workload == "gravity" else 200))
         a = eng.accel(vh, uh)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -334,14 +401,16 @@ def main():
                "h2d_bytes_per_step": 2 * uh.nbytes, "d2h_bytes_per_step": ah.nbytes,
                "path": "nbg_accel (RHS drop-in) per step from pinned host buffers, velocity-Verlet update on host",
                "steps": e2e_steps}
+    elif not args.no_e2e and batch:
+        # the batch's public call: nbg_run from (pageable) host buffers, state in and out
+        t0 = time.perf_counter()
+        ug, vg, _, _, st = eng.run(u0, v0, dt, args.steps, 0, save_trajectory=False)
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": n * args.steps * world / e2e_s, "unit": "atom-steps/s",
+               "h2d_bytes_per_step": 2 * u0.nbytes / args.steps, "d2h_bytes_per_step": 2 * u0.nbytes / args.steps,
+               "path": "nbg_run: host state uploaded, K steps, host state downloaded", "steps": args.steps}
 
-    # accuracy at this workload: forces of sampled atoms vs the oracle, drift
     u_end, v_end = eng.get_state()
-    e_end = eng.energy(u_end, v_end)
-    drift_key = "gravity" if args.workload == "gravity" else "potential"
-    E0 = e_start["kinetic"] + e_start[drift_key]
-    E1 = e_end["kinetic"] + e_end[drift_key]
-
     work, unit, bound = algorithmic_work(args.workload, n, eng)
     avg_kern = kern_ms / max(kern_n, 1)
     achieved = work / (avg_kern / 1e3) / (1e12 if unit == "TFLOP/s" else 1e9)
@@ -352,42 +421,54 @@ def main():
     else:
         peak = peaks.get("hbm_gbs", 6800.0)
         peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    kernel_name = {"gravity": "k_gravity", "lj": "k_force_list", "water": "k_force_list"}[args.workload]
+    kernel_name = "k_gravity" if args.workload == "gravity" else "k_force_list"
     traffic = profile_traffic(f"{kernel_name}:{w['name']}")
     roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
                 "frac": (achieved / peak) if peak else None, "traffic": traffic, "kernel": kernel_name,
                 "kernel_ms": avg_kern, "kernel_launches": kern_n, "peak_source": peak_src}
-
+    config = {"workload": w["name"], "N": n, "dt": dt, "integrator": "velocity Verlet",
+              "l2": ("512 MB buffer written between timed steps (L2 flushed)" if flush_steps else
+                     "working set larger than L2" if batch else "no flush (state L2-resident across steps)"),
+              "parallelism": "replicas only" if world > 1 else "single GPU"}
+    if args.workload == "gravity":
+        config["gravity_precision"] = "plain FP32 positions" if args.grav_plain else "hi/lo split positions (compensated)"
+    if batch:
+        config.update(integrator="BAOAB Langevin (gamma=1)", replicas=len(wl.sizes),
+                      atoms_min=int(min(wl.sizes)), atoms_max=int(max(wl.sizes)))
     line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 pair forces, f64 state" if args.workload != "water" else "f32 pair forces, f64 state+bonded",
-            "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": w["name"], "N": n, "dt": dt, "integrator": "velocity Verlet",
-                       "l2": "no flush (state L2-resident across steps)" if args.no_flush
-                       else "512 MB buffer written between timed steps (L2 flushed)",
-                       "parallelism": "replicas only" if world > 1 else "single GPU",
-                       "gravity_precision": ("plain FP32 positions" if args.grav_plain else
-                                             "hi/lo split positions (compensated)") if args.workload == "gravity" else None},
-            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-            "energy_drift_rel": (E1 - E0) / abs(E0) if E0 else None}
+            "dtype": "f32 pair forces, f64 state" + ("+bonded" if args.workload == "water" else ""),
+            "data": "synthetic (seeded generator, no dataset)", "config": config,
+            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+    if not batch:
+        e_end = eng.energy(u_end, v_end)
+        drift_key = "gravity" if args.workload == "gravity" else "potential"
+        E0 = e_start["kinetic"] + e_start[drift_key]
+        E1 = e_end["kinetic"] + e_end[drift_key]
+        line["energy_drift_rel"] = (E1 - E0) / abs(E0) if E0 else None
+        if args.workload != "gravity":
+            line["temperature_start"] = e_start["temperature"]
+            line["temperature_end"] = e_end["temperature"]
+    else:
+        offs = np.concatenate([[0], np.cumsum(wl.sizes)])
+        T_end = [float((v_end[offs[r]:offs[r + 1]] ** 2).sum() / (3 * wl.sizes[r])) for r in range(len(wl.sizes))]
+        T_tgt = [float(d.thermo_T) for d in wl.descs]
+        line["temperature_rel_err_mean"] = float(np.mean(np.abs(np.array(T_end) / np.array(T_tgt) - 1)))
     if args.workload == "water":
         line["ns_per_day"] = (1e3 / (total_ms / args.steps)) * dt * 1e-3 * 86400
-    if args.workload != "gravity":
-        line["temperature_start"] = e_start["temperature"]
-        line["temperature_end"] = e_end["temperature"]
     if rank == 0 and world == 1 and not args.no_cpu:
         oracle = G.load_oracle()
-        cb = cpu_baseline(oracle, desc, u0, args.workload)
-        line["cpu_baseline"] = cb
-    if rank == 0 and world == 1 and not args.no_cpu and args.workload != "water":
-        # force accuracy on a sample of atoms (oracle accelerations of atoms 0..255)
-        ns = 256
-        a_ref = oracle.partial_accel(desc, u0, 0, ns)
-        eng.set_state(u0, v0)
-        eng.compute_forces()
-        a_gpu = eng.get_accel()[:ns]
-        line["force_rel_rmse"] = float(np.linalg.norm(a_gpu - a_ref) / np.linalg.norm(a_ref))
+        line["cpu_baseline"] = cpu_baseline(oracle, wl)
+        if args.workload in ("gravity", "lj"):
+            # force accuracy on atoms 0..255 of the end state (a thermalised
+            # liquid: on the starting lattice the LJ forces cancel to ~0)
+            ns = min(256, n)
+            a_ref = oracle.partial_accel(wl.descs[0], u_end, 0, ns)
+            eng.set_state(u_end, v_end)
+            eng.compute_forces()
+            a_gpu = eng.get_accel()[:ns]
+            line["force_rel_rmse"] = float(np.linalg.norm(a_gpu - a_ref) / np.linalg.norm(a_ref))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -128,6 +128,10 @@ typedef struct nbg_system_desc {
 #define NBG_FLAG_ALL_PAIRS 1
 /* Gravity: plain FP32 position differences (no hi/lo compensation). */
 #define NBG_FLAG_GRAV_PLAIN 2
+/* Langevin thermostat integrated by BAOAB (velocity-Verlet splitting with an
+   exact Ornstein-Uhlenbeck step, Leimkuhler & Matthews 2013) instead of the
+   reference's Euler-Maruyama; stable at the step sizes of velocity Verlet. */
+#define NBG_FLAG_LANGEVIN_BAOAB 4
 
 typedef struct nbg_ctx nbg_ctx;
 

@@ -20,11 +20,12 @@ from .parameters import (AndersenThermostat, BerendsenThermostat,
                          NoseHooverThermostat, NullThermostat,
                          PeriodicBoundaryConditions, PotentialParameters,
                          SPCFwParameters)
-from .simulation import (EM, NBodySimulation, SecondOrderODEProblem,
+from .simulation import (BAOAB, EM, NBodySimulation, SecondOrderODEProblem,
                          SimulationResult, VelocityVerlet,
                          gather_bodies_initial_coordinates, get_masses,
                          get_degrees_of_freedom, get_position, get_velocity,
                          gravitational_energy, initial_energy, kinetic_energy,
+                         lennard_jones_descriptor,
                          msd, potential_energy, rdf, run_simulation,
                          system_descriptor, temperature, total_energy, kb_SI)
 from .systems import (ChargedParticles, GravitationalSystem,

@@ -30,6 +30,7 @@ NBG_POT_LJ, NBG_POT_EL, NBG_POT_GRAV, NBG_POT_MAG = 1, 2, 4, 8
  NBG_THERMO_NOSEHOOVER, NBG_THERMO_LANGEVIN) = 0, 1, 2, 3, 4
 NBG_FLAG_ALL_PAIRS = 1
 NBG_FLAG_GRAV_PLAIN = 2
+NBG_FLAG_LANGEVIN_BAOAB = 4
 
 _dp = ctypes.POINTER(ctypes.c_double)
 

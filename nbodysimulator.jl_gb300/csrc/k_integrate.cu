@@ -310,6 +310,65 @@ int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step)
     return NBG_OK;
 }
 
+// BAOAB first half (Leimkuhler & Matthews 2013): B half kick with the old
+// forces, A half drift, O exact Ornstein-Uhlenbeck step with each atom's own
+// mass, A half drift; then the split position and the displacement check.
+__global__ void k_baoab_drift(Dev d, StateView s, double dt, StepRef sr)
+{
+    const int64_t step = step_of(sr);
+    const int parity = (int)((step + 1) & 1);
+    const double hdt = 0.5 * dt;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const RepDev& R = d.reps[d.rep_of[i]];
+        const int64_t li = i - R.atom0;
+        const double c1 = exp(-R.tparam * dt);
+        const double sd = sqrt(1.0 - c1 * c1) * sqrt(d.kb * R.T0 / d.mass[i]);
+        float z[3];
+        philox_normals3<float>(R.seed, (uint64_t)li, (uint64_t)step, z);
+        for (int k = 0; k < 3; ++k) {
+            const int64_t e = 3 * i + k;
+            double vh = __dadd_rn(s.v[e], __dmul_rn(hdt, s.a_old[e]));
+            double x = __dadd_rn(s.x[e], __dmul_rn(hdt, vh));
+            double vo = __dadd_rn(__dmul_rn(c1, vh), __dmul_rn(sd, (double)z[k]));
+            s.x[e] = __dadd_rn(x, __dmul_rn(hdt, vo));
+            s.v[e] = vo;
+        }
+        pack_atom(d, i, s.x);
+        if (d.xref) {
+            double dx = s.x[3 * i] - d.xref[3 * i];
+            double dy = s.x[3 * i + 1] - d.xref[3 * i + 1];
+            double dz = s.x[3 * i + 2] - d.xref[3 * i + 2];
+            if (!(dx * dx + dy * dy + dz * dz <= d.skin_half2)) d.rebuild_flag[parity] = 1;
+        }
+    }
+}
+
+// BAOAB last B: v += dt/2 a(x'); the new forces become the next step's.
+__global__ void k_baoab_kick(Dev d, StateView s, double dt)
+{
+    const double hdt = 0.5 * dt;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * d.n; e += (int64_t)gridDim.x * blockDim.x) {
+        double an = s.a_new[e];
+        if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+        s.v[e] = __dadd_rn(s.v[e], __dmul_rn(hdt, an));
+        s.a_old[e] = an;
+    }
+}
+
+int launch_baoab_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step)
+{
+    k_baoab_drift<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s, dt, step);
+    NBG_LAUNCH_CHECK(c, "k_baoab_drift");
+    return NBG_OK;
+}
+
+int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt)
+{
+    k_baoab_kick<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->d, s, dt);
+    NBG_LAUNCH_CHECK(c, "k_baoab_kick");
+    return NBG_OK;
+}
+
 __global__ void k_step_advance(int64_t* step, int64_t by) { *step += by; }
 __global__ void k_set_step(int64_t* step, int64_t value) { *step = value; }
 

@@ -87,15 +87,16 @@ __global__ void k_list_build(Dev d, ListCtl L, const double* X)
         int cx = cell_coord(hi.x, R), cy = cell_coord(hi.y, R), cz = cell_coord(hi.z, R);
         int cnt = 0;
         const bool water = d.kind == NBG_SYSTEM_WATER;
-        for (int ox = -1; ox <= 1; ++ox) {
+        const int o0 = R.nc >= 3 ? -1 : 0, o1 = R.nc >= 3 ? 1 : 0;
+        for (int ox = o0; ox <= o1; ++ox) {
             int nx = cx + ox;
             nx += (nx < 0) ? R.nc : 0;
             nx -= (nx >= R.nc) ? R.nc : 0;
-            for (int oy = -1; oy <= 1; ++oy) {
+            for (int oy = o0; oy <= o1; ++oy) {
                 int ny = cy + oy;
                 ny += (ny < 0) ? R.nc : 0;
                 ny -= (ny >= R.nc) ? R.nc : 0;
-                for (int oz = -1; oz <= 1; ++oz) {
+                for (int oz = o0; oz <= o1; ++oz) {
                     int nz = cz + oz;
                     nz += (nz < 0) ? R.nc : 0;
                     nz -= (nz >= R.nc) ? R.nc : 0;
@@ -149,15 +150,16 @@ __global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, cons
     const bool water = d.kind == NBG_SYSTEM_WATER;
     int cnt = 0;
     int* out = d.nbr + i * d.nbr_istride;
-    for (int ox = -1; ox <= 1; ++ox) {
+    const int o0 = R.nc >= 3 ? -1 : 0, o1 = R.nc >= 3 ? 1 : 0;
+    for (int ox = o0; ox <= o1; ++ox) {
         int nx = cx + ox;
         nx += (nx < 0) ? R.nc : 0;
         nx -= (nx >= R.nc) ? R.nc : 0;
-        for (int oy = -1; oy <= 1; ++oy) {
+        for (int oy = o0; oy <= o1; ++oy) {
             int ny = cy + oy;
             ny += (ny < 0) ? R.nc : 0;
             ny -= (ny >= R.nc) ? R.nc : 0;
-            for (int oz = -1; oz <= 1; ++oz) {
+            for (int oz = o0; oz <= o1; ++oz) {
                 int nz = cz + oz;
                 nz += (nz < 0) ? R.nc : 0;
                 nz -= (nz >= R.nc) ? R.nc : 0;

@@ -145,11 +145,13 @@ static int choose_path(const nbg_system_desc* descs, int nrep)
     bool list_ok = !(d->flags & NBG_FLAG_ALL_PAIRS) && d->bc == NBG_BC_CUBIC && (pots & ~(uint32_t)(NBG_POT_LJ | NBG_POT_EL)) == 0 &&
                    pots != 0;
     if (list_ok) {
+        // a single system needs at least 3 cells per side to gain from cells;
+        // a batch keeps small replicas on the list path as one cell each
         for (int r = 0; r < nrep; ++r) {
             double rl = list_radius(&descs[r]);
             if (!std::isfinite(rl)) { list_ok = false; break; }
             int nc = (int)std::floor(descs[r].box[0] / (rl * (1.0 + 1e-4)));
-            if (nc < 3) { list_ok = false; break; }
+            if (nc < 3 && nrep == 1) { list_ok = false; break; }
         }
     }
     if (list_ok) return PATH_LIST;
@@ -247,6 +249,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     D.kangle = d0->water_ka;
     D.skin_half2 = 0.25 * std::max(d0->skin, 0.0) * std::max(d0->skin, 0.0);
     D.grav_plain = (d0->flags & NBG_FLAG_GRAV_PLAIN) ? 1 : 0;
+    c->baoab = d0->thermostat == NBG_THERMO_LANGEVIN && (d0->flags & NBG_FLAG_LANGEVIN_BAOAB);
 
     // replicas
     c->reps_h.resize(nrep);
@@ -292,6 +295,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         if (c->path == PATH_LIST) {
             double rl = list_radius(d);
             R.nc = (int)std::floor(d->box[0] / (rl * (1.0 + 1e-4)));
+            if (R.nc < 3) R.nc = 1;  // one cell holding the whole replica
             R.cell0 = cell0;
             R.cell_inv = R.nc / d->box[0];
             R.rl2 = f_up(rl * rl * (1.0 + 1e-5));
@@ -740,6 +744,10 @@ static void backup_free(nbg_ctx* c, Backup& b)
     b = Backup{};
 }
 
+// EM is the reference's Langevin integrator; BAOAB (flag) and velocity
+// Verlet share the kick-drift structure.
+static bool is_em(const nbg_ctx* c) { return c->d.therm == NBG_THERMO_LANGEVIN && !c->baoab; }
+
 // a_old = f(v, u) at the current resident state (SciML computes the first
 // acceleration before the first step; with Nose-Hoover this also writes the
 // rate into v, as the reference's RHS does).
@@ -749,7 +757,7 @@ static int init_accel(nbg_ctx* c)
     if ((st = launch_pack(c, c->st))) return st;
     if ((st = forces(c, c->st, true, StepRef{c->step, nullptr}))) return st;
     c->steps_since_build = 0;
-    if (c->d.therm != NBG_THERMO_LANGEVIN) {
+    if (!is_em(c)) {
         if ((st = launch_rhs_thermostat(c, c->st))) return st;
         CK(cudaMemcpyAsync(c->st.a_old, c->st.a_new, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "a init");
     }
@@ -786,6 +794,18 @@ static int step_vv(nbg_ctx* c, double dt, StepRef sr)
     return NBG_OK;
 }
 
+static int step_baoab(nbg_ctx* c, double dt, StepRef sr)
+{
+    int st;
+    const StateView& s = c->st;
+    StepRef pos{sr.off + 1, sr.base};
+    if ((st = launch_baoab_drift(c, s, dt, sr))) return st;
+    bool force = rebuild_due(c, true);
+    if ((st = forces(c, s, force, pos))) return st;
+    c->steps_since_build = force ? 0 : c->steps_since_build + 1;
+    return launch_baoab_kick(c, s, dt);
+}
+
 static int step_em(nbg_ctx* c, double dt, StepRef sr)
 {
     int st;
@@ -797,10 +817,16 @@ static int step_em(nbg_ctx* c, double dt, StepRef sr)
     return NBG_OK;
 }
 
+static int step_any(nbg_ctx* c, double dt, StepRef sr)
+{
+    if (is_em(c)) return step_em(c, dt, sr);
+    if (c->baoab) return step_baoab(c, dt, sr);
+    return step_vv(c, dt, sr);
+}
+
 static int step_direct(nbg_ctx* c, double dt)
 {
-    int st = c->d.therm == NBG_THERMO_LANGEVIN ? step_em(c, dt, StepRef{c->step, nullptr})
-                                               : step_vv(c, dt, StepRef{c->step, nullptr});
+    int st = step_any(c, dt, StepRef{c->step, nullptr});
     if (st) return st;
     c->step++;
     return NBG_OK;
@@ -822,7 +848,7 @@ static bool graph_aligned(const nbg_ctx* c)
     if (c->path != PATH_LIST) return true;
     // displacement-only rebuilds: capture once the first (forced) build is done
     if (c->desc.rebuild_every <= 0) return c->steps_since_build >= 0;
-    bool vv = c->d.therm != NBG_THERMO_LANGEVIN;
+    bool vv = !is_em(c);
     int re = c->desc.rebuild_every;
     int64_t s = c->steps_since_build;
     return vv ? (s < 0 || s + 1 >= re) : (s < 0 || s >= re);
@@ -842,9 +868,7 @@ static int capture_graph(nbg_ctx* c, double dt)
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
     int st = NBG_OK;
-    for (int64_t k = 0; k < G && st == NBG_OK; ++k)
-        st = c->d.therm == NBG_THERMO_LANGEVIN ? step_em(c, dt, StepRef{k, c->d.step_dev})
-                                               : step_vv(c, dt, StepRef{k, c->d.step_dev});
+    for (int64_t k = 0; k < G && st == NBG_OK; ++k) st = step_any(c, dt, StepRef{k, c->d.step_dev});
     if (st == NBG_OK) st = launch_step_advance(c, G);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->steps_since_build = ssb0;  // capture only recorded the steps
@@ -873,7 +897,7 @@ static int replay_graph(nbg_ctx* c)
     c->launches += c->graph_launches;
     c->step += c->graph_steps;
     // the forced-rebuild pattern repeats: after a period the host state is as at capture
-    bool vv = c->d.therm != NBG_THERMO_LANGEVIN;
+    bool vv = !is_em(c);
     if (c->path == PATH_LIST && c->desc.rebuild_every > 0) {
         int64_t re = c->desc.rebuild_every;
         c->steps_since_build = vv ? re - 1 : re;
@@ -888,10 +912,10 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
     if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
     int st;
     if ((st = clear_status(c))) return st;
-    const bool langevin = c->d.therm == NBG_THERMO_LANGEVIN;
-    if (!langevin && !c->accel_valid) {
+    const bool em = is_em(c);
+    if (!em && !c->accel_valid) {
         if ((st = init_accel(c))) return st;
-    } else if (langevin) {
+    } else if (em) {
         if ((st = launch_pack(c, c->st))) return st;
     }
     const bool can_overflow = c->path == PATH_LIST;

@@ -146,6 +146,7 @@ struct nbg_ctx {
     int64_t graph_launches = 0;  // kernels per replay
     double graph_dt = 0.0;
     bool use_graphs = true;
+    bool baoab = false;          // Langevin by BAOAB instead of Euler-Maruyama
     std::vector<cudaEvent_t> prof_events;  // start/stop pairs not yet read
     double prof_ms = 0.0;
     int64_t prof_count = 0;
@@ -177,6 +178,8 @@ int launch_kick(nbg_ctx* c, const StateView& s, double dt);
 int launch_andersen(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_step_advance(nbg_ctx* c, int64_t by);
+int launch_baoab_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step);
+int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt);
 int launch_set_step(nbg_ctx* c, int64_t value);
 int launch_rhs_thermostat(nbg_ctx* c, const StateView& s);
 int gravity_plan_chunks(nbg_ctx* c, int64_t npad);

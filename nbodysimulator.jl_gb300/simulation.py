@@ -12,9 +12,9 @@ from .bodies import MassBody, WaterMolecule
 from .engine import Engine
 from .parameters import (AndersenThermostat, BerendsenThermostat,
                          CubicPeriodicBoundaryConditions, InfiniteBox,
-                         LangevinThermostat, NoseHooverThermostat,
-                         NullThermostat, PeriodicBoundaryConditions,
-                         Thermostat, _jl)
+                         LangevinThermostat, LennardJonesParameters,
+                         NoseHooverThermostat, NullThermostat,
+                         PeriodicBoundaryConditions, Thermostat, _jl)
 from .systems import (ChargedParticles, GravitationalSystem,
                       PotentialNBodySystem, WaterSPCFw)
 
@@ -28,6 +28,12 @@ class VelocityVerlet:
 
 class EM:
     """Euler-Maruyama (StochasticDiffEq.EM), used with LangevinThermostat."""
+
+
+class BAOAB:
+    """Langevin dynamics by the BAOAB splitting (Leimkuhler & Matthews 2013):
+    an engine integrator with no reference counterpart, stable at
+    velocity-Verlet step sizes where Euler-Maruyama diverges."""
 
 
 class NBodySimulation:
@@ -83,6 +89,8 @@ class NBodySimulation:
 
 def get_masses(system):
     """get_masses (nbody_simulation_result.jl:121-139)."""
+    if isinstance(system.bodies, _MassView):
+        return system.bodies._m
     if isinstance(system, WaterSPCFw):
         n = len(system.bodies)
         ms = np.empty(3 * n)
@@ -228,6 +236,37 @@ def system_descriptor(simulation):
     return d, keep
 
 
+def lennard_jones_descriptor(masses, L, eps=1.0, sigma=1.0, R=2.5, skin=0.3, thermostat=None, kb=1.0,
+                             seed=0, rebuild_every=10):
+    """nbg_system_desc of a Lennard-Jones PotentialNBodySystem in a cubic box,
+    built straight from a mass array (what system_descriptor extracts from
+    the bodies), for large replica ensembles. Returns (desc, keepalive)."""
+    masses = np.ascontiguousarray(masses, dtype=np.float64)
+    sim = NBodySimulation(PotentialNBodySystem([], {"lennard_jones": LennardJonesParameters(eps, sigma, R)}),
+                          (0.0, 1.0), CubicPeriodicBoundaryConditions(L),
+                          *( [thermostat] if thermostat is not None else []), kb=kb, skin=skin,
+                          rebuild_every=rebuild_every, seed=seed)
+    sim.system.bodies = _MassView(masses)
+    return system_descriptor(sim)
+
+
+class _MassView(list):
+    """Stand-in body list for lennard_jones_descriptor: only masses are read."""
+
+    class _B:
+        __slots__ = ("m",)
+
+        def __init__(self, m):
+            self.m = m
+
+    def __init__(self, masses):
+        super().__init__()
+        self._m = masses
+
+    def __len__(self):
+        return len(self._m)
+
+
 class SecondOrderODEProblem:
     """SciMLBase.SecondOrderODEProblem(sim) (nbody_to_ode.jl:460-536): the
     right-hand side f(dv, v, u, p, t) evaluated by nbg_accel on the GPU, the
@@ -360,7 +399,16 @@ def run_simulation(simulation, alg=None, dt=None, save_everystep=True, save_ever
     save_everystep=False (first and last frame) or save_every=k."""
     if dt is None:
         raise ValueError("dt is required: the GPU integrators take fixed steps")
-    if alg is not None and not isinstance(alg, (VelocityVerlet, EM)):
+    if isinstance(alg, BAOAB):
+        if not isinstance(simulation.thermostat, LangevinThermostat):
+            raise ValueError("BAOAB integrates a LangevinThermostat simulation")
+        if not simulation.flags & _abi.NBG_FLAG_LANGEVIN_BAOAB:
+            simulation.flags |= _abi.NBG_FLAG_LANGEVIN_BAOAB
+            simulation._engine = None
+    elif isinstance(simulation.thermostat, LangevinThermostat) and simulation.flags & _abi.NBG_FLAG_LANGEVIN_BAOAB:
+        simulation.flags &= ~_abi.NBG_FLAG_LANGEVIN_BAOAB
+        simulation._engine = None
+    if alg is not None and not isinstance(alg, (VelocityVerlet, EM, BAOAB)):
         raise _abi.EngineError(-6, f"{type(alg).__name__} is not fused on the GPU; use "
                                    "SecondOrderODEProblem(sim) with a host integrator")
     t0, t1 = simulation.tspan

@@ -158,3 +158,17 @@ def water_molecules(pos, vel):
         out.append(WaterMolecule(MassBody(pos[o], vel[o], M_O), MassBody(pos[o + 1], vel[o + 1], M_H),
                                  MassBody(pos[o + 2], vel[o + 2], M_H)))
     return out
+
+
+def lj_ensemble(n_rep=256, n_min=256, n_max=8192, T_min=0.7, T_max=1.5, rho=0.8, seed=0, jitter=0.02):
+    """Uneven replica ensemble of LJ liquids: N_r ~ U[n_min, n_max] and
+    T_r ~ U[T_min, T_max] (seeded), each on its own jittered lattice at
+    density rho. Returns a list of dicts with pos, vel, L, T, n."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(n_min, n_max + 1, size=n_rep)
+    Ts = rng.uniform(T_min, T_max, size=n_rep)
+    out = []
+    for r in range(n_rep):
+        pos, vel, L = lj_argon_lattice(int(ns[r]), rho=rho, T=float(Ts[r]), seed=seed * 100003 + r, jitter=jitter)
+        out.append(dict(pos=pos, vel=vel, L=L, T=float(Ts[r]), n=int(ns[r])))
+    return out

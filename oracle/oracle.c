@@ -24,6 +24,10 @@
  * are this project's reading of those packages: parity there is unpinned by
  * the reference tree and only checked statistically by its thermostat tests.
  *
+ * With NBG_FLAG_LANGEVIN_BAOAB the Langevin thermostat is integrated by BAOAB
+ * (Leimkuhler & Matthews 2013) instead of Euler-Maruyama: an engine option
+ * with no reference counterpart, restated here from the published scheme.
+ *
  * Random numbers (Andersen collisions, Langevin noise) come from Philox4x32-10
  * (Salmon, Moraes, Dror, Shaw, SC'11) keyed by the descriptor's seed, with the
  * same counter layout as the CUDA engine; the reference uses Julia's unseeded
@@ -49,28 +53,39 @@ int oracle_get_threads(void) { return g_threads; }
 /* ------------------------------------------------------------------ */
 typedef struct { double x, y, z, r, r2; } pairdist;
 
+/* The reference's loops never end on coordinates that diverged to huge or
+   infinite values; here each loop gives up after OR_MAX_ITERS passes (far
+   beyond any physical input) and leaves the difference unwrapped. */
+#define OR_MAX_ITERS (1 << 20)
+int oracle_range_errors = 0;
+
 static pairdist distance(const double* ri, const double* rj, const nbg_system_desc* d)
 {
     pairdist p;
     double x = ri[0] - rj[0], y = ri[1] - rj[1], z = ri[2] - rj[2];
+    long it = 0;
+#define OR_LOOP(cond, stmt) \
+    for (it = 0; (cond) && it < OR_MAX_ITERS; ++it) stmt; \
+    if (it == OR_MAX_ITERS) oracle_range_errors++;
     if (d->bc == NBG_BC_CUBIC) { /* :138-165 */
         double size = d->box[0];
         double radius = 0.5 * size;
-        while (x >= radius) x -= size;
-        while (x < -radius) x += size;
-        while (y >= radius) y -= size;
-        while (y < -radius) y += size;
-        while (z >= radius) z -= size;
-        while (z < -radius) z += size;
+        OR_LOOP(x >= radius, x -= size)
+        OR_LOOP(x < -radius, x += size)
+        OR_LOOP(y >= radius, y -= size)
+        OR_LOOP(y < -radius, y += size)
+        OR_LOOP(z >= radius, z -= size)
+        OR_LOOP(z < -radius, z += size)
     } else if (d->bc == NBG_BC_PERIODIC) { /* :111-136, maps into [lo, hi) */
         const double* b = d->box;
-        while (x < b[0]) x += b[1] - b[0];
-        while (x >= b[1]) x -= b[1] - b[0];
-        while (y < b[2]) y += b[3] - b[2];
-        while (y >= b[3]) y -= b[3] - b[2];
-        while (z < b[4]) z += b[5] - b[4];
-        while (z >= b[5]) z -= b[5] - b[4];
+        OR_LOOP(x < b[0], x += b[1] - b[0])
+        OR_LOOP(x >= b[1], x -= b[1] - b[0])
+        OR_LOOP(y < b[2], y += b[3] - b[2])
+        OR_LOOP(y >= b[3], y -= b[3] - b[2])
+        OR_LOOP(z < b[4], z += b[5] - b[4])
+        OR_LOOP(z >= b[5], z -= b[5] - b[4])
     }
+#undef OR_LOOP
     p.x = x; p.y = y; p.z = z;
     p.r2 = x * x + y * y + z * z; /* rij[1]^2 + rij[2]^2 + rij[3]^2 */
     p.r = sqrt(p.r2);
@@ -524,6 +539,32 @@ static void em_step(double* u, double* v, double* work, double dt, uint64_t step
     }
 }
 
+/* BAOAB step (Leimkuhler & Matthews, Appl. Math. Res. eXpress 2013): B half
+   kick, A half drift, O exact Ornstein-Uhlenbeck v = c1 v + c2 sqrt(kb T/m) z
+   with c1 = exp(-gamma dt), c2 = sqrt(1 - c1^2), A half drift, forces, B half
+   kick. Each atom uses its own mass. a holds the forces at u on entry and exit. */
+static void baoab_step(double* u, double* v, double* a, double dt, uint64_t step, const nbg_system_desc* d)
+{
+    int64_t n = d->n;
+    double c1 = exp(-d->thermo_param * dt);
+    double c2 = sqrt(1.0 - c1 * c1);
+    for (int64_t i = 0; i < n; ++i) {
+        double z[3];
+        oracle_normals3(d->seed, (uint64_t)i, step, z);
+        double s = c2 * sqrt(d->kb * d->thermo_T / d->mass[i]);
+        for (int k = 0; k < 3; ++k) {
+            int64_t e = 3 * i + k;
+            double vh = v[e] + (0.5 * dt) * a[e];
+            double x = u[e] + (0.5 * dt) * vh;
+            double vo = c1 * vh + s * z[k];
+            u[e] = x + (0.5 * dt) * vo;
+            v[e] = vo;
+        }
+    }
+    body_accelerations(a, u, d);
+    for (int64_t e = 0; e < 3 * n; ++e) v[e] = v[e] + (0.5 * dt) * a[e];
+}
+
 static void save_frame(double* traj, const double* x, int64_t cols, int64_t frame)
 {
     if (traj) memcpy(traj + frame * 3 * cols, x, sizeof(double) * 3 * cols);
@@ -544,6 +585,20 @@ int64_t oracle_run(const nbg_system_desc* d, double* u, double* v, double dt, in
     save_frame(traj_u, u, cols, frame);
     save_frame(traj_v, v, cols, frame);
     ++frame;
+    if (d->thermostat == NBG_THERMO_LANGEVIN && (d->flags & NBG_FLAG_LANGEVIN_BAOAB)) {
+        body_accelerations(a, u, d);
+        for (int64_t s = 0; s < nsteps; ++s) {
+            baoab_step(u, v, a, dt, (uint64_t)s, d);
+            if ((save_every > 0 && (s + 1) % save_every == 0) || s + 1 == nsteps) {
+                save_frame(traj_u, u, cols, frame);
+                save_frame(traj_v, v, cols, frame);
+                ++frame;
+            }
+        }
+        free(a);
+        free(an);
+        return frame;
+    }
     if (d->thermostat == NBG_THERMO_LANGEVIN) {
         for (int64_t s = 0; s < nsteps; ++s) {
             em_step(u, v, a, dt, (uint64_t)s, d);

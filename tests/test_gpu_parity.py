@@ -211,6 +211,31 @@ def test_langevin_em_one_step(gpu, oracle):
     assert np.abs(vg - vo).max() <= 1e-5 * np.abs(vo).max()
 
 
+def test_baoab_one_step_and_batch(gpu, oracle):
+    """BAOAB Langevin steps with the same Philox draws (FP32 Box-Muller on the
+    GPU), single system and a batch of uneven replicas."""
+    sim = S.lj_liquid(1000, seed=6, thermostat=nbg.LangevinThermostat(1.0, 1.0),
+                      flags=nbg._abi.NBG_FLAG_LANGEVIN_BAOAB)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    ug, vg, _, _, _ = nbg.Engine(desc, 0).run(u, v, 0.005, 3, 0, save_trajectory=False)
+    uo, vo = oracle.run(desc, u, v, 0.005, 3)
+    assert np.abs(ug - uo).max() <= 1e-6 * desc.box[0]
+    assert np.abs(vg - vo).max() <= 1e-5 * np.abs(vo).max()
+    sizes = [256, 1000, 1500]
+    descs, keep, us, vs = _ensemble(nbg, sizes, lambda r: nbg.LangevinThermostat(0.9 + 0.3 * r, 1.0))
+    for d in descs:
+        d.flags |= nbg._abi.NBG_FLAG_LANGEVIN_BAOAB
+    ug, vg, _, _, _ = nbg.Engine(descs, 0).run(np.concatenate(us), np.concatenate(vs), 0.005, 1, 0,
+                                               save_trajectory=False)
+    off = 0
+    for r, n in enumerate(sizes):
+        uo, vo = oracle.run(descs[r], us[r], vs[r], 0.005, 1)
+        assert np.abs(ug[off:off + n] - uo).max() <= 1e-6 * descs[r].box[0]
+        assert np.abs(vg[off:off + n] - vo).max() <= 1e-5 * np.abs(vo).max()
+        off += n
+
+
 def test_andersen_one_step(gpu, oracle):
     sim = S.lj_liquid(1000, seed=7, thermostat=nbg.AndersenThermostat(1.0, 20.0))
     desc, keep = nbg.system_descriptor(sim)
@@ -252,3 +277,50 @@ def test_capacity_regrowth(gpu, oracle):
     sim = nbg.NBodySimulation(system, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), kb=1.0, skin=0.3)
     eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
     assert S.rel_rmse(ag, ar) <= FORCE_TOL
+
+
+def _ensemble(nbg, sizes, thermostat_of):
+    descs, keep, us, vs = [], [], [], []
+    for r, n in enumerate(sizes):
+        pos, vel, L = nbg.workloads.lj_argon_lattice(n, seed=40 + r, jitter=0.1, T=0.8 + 0.2 * r)
+        d, k = nbg.lennard_jones_descriptor(np.ones(n), L, thermostat=thermostat_of(r), seed=77 + r, skin=0.3)
+        descs.append(d)
+        keep.append(k)
+        us.append(pos)
+        vs.append(vel)
+    return descs, keep, us, vs
+
+
+def test_batch_langevin_matches_oracle(gpu, oracle):
+    """Uneven replicas (one of them a single cell) in one context: one
+    Euler-Maruyama step per replica against the oracle per replica."""
+    sizes = [256, 1000, 1500]
+    descs, keep, us, vs = _ensemble(nbg, sizes, lambda r: nbg.LangevinThermostat(0.9 + 0.3 * r, 1.0))
+    eng = nbg.Engine(descs, 0)
+    ug, vg, _, _, _ = eng.run(np.concatenate(us), np.concatenate(vs), 0.005, 1, 0, save_trajectory=False)
+    off = 0
+    for r, n in enumerate(sizes):
+        uo, vo = oracle.run(descs[r], us[r], vs[r], 0.005, 1)
+        assert np.abs(ug[off:off + n] - uo).max() <= 1e-12
+        assert np.abs(vg[off:off + n] - vo).max() <= 1e-5 * np.abs(vo).max()
+        off += n
+
+
+def test_batch_nve_matches_single_contexts(gpu):
+    """The same replicas without thermostat: a batch of 3 gives the
+    accelerations of 3 separate contexts (replicas do not interact), and short
+    velocity-Verlet runs agree to the FP32 summation-order level."""
+    sizes = [256, 1000, 1500]
+    descs, keep, us, vs = _ensemble(nbg, sizes, lambda r: None)
+    eng = nbg.Engine(descs, 0)
+    U, V = np.concatenate(us), np.concatenate(vs)
+    ab = eng.accel(V.copy(), U)
+    ug, vg, _, _, _ = eng.run(U, V, 0.005, 10, 0, save_trajectory=False)
+    off = 0
+    for r, n in enumerate(sizes):
+        single = nbg.Engine(descs[r], 0)
+        a1 = single.accel(vs[r].copy(), us[r])
+        assert S.rel_rmse(ab[off:off + n], a1) <= 1e-6
+        u1, v1, _, _, _ = single.run(us[r], vs[r], 0.005, 10, 0, save_trajectory=False)
+        assert np.abs(ug[off:off + n] - u1).max() <= 1e-7 * descs[r].box[0]
+        off += n

@@ -106,6 +106,17 @@ def test_thermostats_argon125(oracle, kind):
     assert abs(T2 - T0) / scale <= tol
 
 
+def test_baoab_thermostat_argon125(oracle):
+    """The BAOAB Langevin option reaches T0 on the thermostat test's argon
+    (gamma = 10, as thermostat_test.jl:197-214)."""
+    th = nbg.LangevinThermostat(90.0, 10.0)
+    sim, tau = S.argon125(th, "cubic")
+    sim.flags |= nbg._abi.NBG_FLAG_LANGEVIN_BAOAB
+    desc, keep, u0, v0, u, v = _run(oracle, sim, tau, 200)
+    T2 = oracle.energy(desc, u, v)["temperature"]
+    assert abs(T2 - 90.0) / 90.0 <= 0.5
+
+
 def test_philox_streams_distinct(oracle):
     """The counter-based RNG gives distinct, well-spread draws."""
     us = np.array([oracle.uniform(7, i, 0) for i in range(2000)])

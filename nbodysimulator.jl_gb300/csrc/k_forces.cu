@@ -16,8 +16,9 @@
 //                    list kernel plus gravity and the magnetic dipole term.
 //  k_force_list      cutoff LJ + reaction-field electrostatics over a Verlet
 //                    list (one thread per atom, coalesced column-major list).
-//  k_bonded          SPC/Fw harmonic bonds and H-O-H angles in FP64, one thread
-//                    per molecule (basic_potentials.jl:367-433).
+//  k_bonded          SPC/Fw harmonic bonds and H-O-H angles, one thread per
+//                    molecule (basic_potentials.jl:367-433), FP32 terms from
+//                    FP64 intramolecular differences.
 #include "nbg_internal.cuh"
 
 #define GB 128         // gravity block size = j-tile size
@@ -482,80 +483,72 @@ int launch_force_list(nbg_ctx* c, const StateView& s)
 // ---------------------------------------------------------------------
 // SPC/Fw bonded terms (FP64), one thread per molecule (O, H1, H2)
 // ---------------------------------------------------------------------
-__device__ __forceinline__ void cross3(const double* a, const double* b, double* c)
+__device__ __forceinline__ void cross3f(const float* a, const float* b, float* c)
 {
-    c[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1]));
-    c[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2]));
-    c[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]));
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-__device__ __forceinline__ double norm3(const double* a)
-{
-    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a[0], a[0]), __dmul_rn(a[1], a[1])), __dmul_rn(a[2], a[2])));
-}
+__device__ __forceinline__ float norm3f(const float* a) { return sqrtf(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
 
+// Bonds and angle of one molecule. The intramolecular differences are taken
+// in FP64 from the unwrapped positions and rounded once to FP32 (relative
+// error 2^-24); the terms themselves are FP32, like the pair forces (the bond
+// stretch r - rOH and the angle offset then carry ~1e-6 relative error). The
+// accelerations are added to a_new in FP64.
 __global__ void k_bonded(Dev d, StateView s)
 {
     int64_t nm = d.n / 3;
+    const float rOH = (float)d.rOH, kb = (float)d.kbond, ka = (float)d.kangle, a0 = (float)d.aHOH;
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < nm; m += (int64_t)gridDim.x * blockDim.x) {
         int64_t o = 3 * m, h1 = o + 1, h2 = o + 2;
         const double* X = s.x;
-        double ro[3] = {X[3 * o], X[3 * o + 1], X[3 * o + 2]};
-        double ra[3] = {X[3 * h1], X[3 * h1 + 1], X[3 * h1 + 2]};
-        double rc[3] = {X[3 * h2], X[3 * h2 + 1], X[3 * h2 + 2]};
-        // bonds (harmonic_bond_potential_acceleration!, :367-393): the force on
-        // O from bond O-H is the exact negative of the force on H.
-        double fO[3] = {0, 0, 0}, fH1[3], fH2[3];
-        const double* hs[2] = {ra, rc};
-        double* fh[2] = {fH1, fH2};
+        float r1[3], r2[3];  // H1 - O, H2 - O
+        for (int k = 0; k < 3; ++k) {
+            r1[k] = (float)(X[3 * h1 + k] - X[3 * o + k]);
+            r2[k] = (float)(X[3 * h2 + k] - X[3 * o + k]);
+        }
+        // bonds (harmonic_bond_potential_acceleration!, :367-393): on O from
+        // bond O-H, -(r - rOH) k / r (r_O - r_H); on H the exact negative.
+        float fO[3] = {0.f, 0.f, 0.f}, fH1[3], fH2[3];
+        const float* hs[2] = {r1, r2};
+        float* fh[2] = {fH1, fH2};
         for (int b = 0; b < 2; ++b) {
-            double rij[3] = {__dsub_rn(ro[0], hs[b][0]), __dsub_rn(ro[1], hs[b][1]), __dsub_rn(ro[2], hs[b][2])};
-            double r = norm3(rij);
-            double dd = __dsub_rn(r, d.rOH);
-            double factor = __dmul_rn(-dd, d.kbond) / r;
+            float r = norm3f(hs[b]);
+            float factor = -(r - rOH) * kb / r;
             for (int k = 0; k < 3; ++k) {
-                double f = __dmul_rn(factor, rij[k]);
-                fO[k] = __dadd_rn(fO[k], f);
+                float f = factor * -hs[b][k];  // rij = r_O - r_H
+                fO[k] += f;
                 fh[b][k] = -f;
             }
         }
         // angle H1-O-H2 (valence_angle_potential_acceleration!, :395-433), a=H1, b=O, c=H2
-        double rba[3], rbc[3], rcb[3], x[3], pa[3], pc[3];
-        for (int k = 0; k < 3; ++k) {
-            rba[k] = __dsub_rn(ra[k], ro[k]);
-            rbc[k] = __dsub_rn(rc[k], ro[k]);
-            rcb[k] = __dsub_rn(ro[k], rc[k]);
-        }
-        cross3(rba, rbc, x);
-        cross3(rba, x, pa);
-        cross3(rcb, x, pc);
-        double npa = norm3(pa), npc = norm3(pc);
-        for (int k = 0; k < 3; ++k) {
-            pa[k] = pa[k] / npa;
-            pc[k] = pc[k] / npc;
-        }
-        double nba = norm3(rba), nbc = norm3(rbc);
-        double dot = __dadd_rn(__dadd_rn(__dmul_rn(rba[0], rbc[0]), __dmul_rn(rba[1], rbc[1])), __dmul_rn(rba[2], rbc[2]));
-        double cosine = dot / __dmul_rn(nba, nbc);
-        if (cosine > 1.0) cosine = 1.0;
-        else if (cosine < -1.0) cosine = -1.0;
-        double force = __dmul_rn(-d.kangle, __dsub_rn(acos(cosine), d.aHOH));
+        float rcb[3] = {-r2[0], -r2[1], -r2[2]}, x[3], pa[3], pc[3];
+        cross3f(r1, r2, x);
+        cross3f(r1, x, pa);
+        cross3f(rcb, x, pc);
+        float npa = norm3f(pa), npc = norm3f(pc);
+        float nba = norm3f(r1), nbc = norm3f(r2);
+        float cosine = (r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2]) / (nba * nbc);
+        cosine = fminf(1.0f, fmaxf(-1.0f, cosine));
+        float force = -ka * (acosf(cosine) - a0);
+        float sa = force / (npa * nba), sc = force / (npc * nbc);
         double iO = 1.0 / d.mass[o], iH1 = 1.0 / d.mass[h1], iH2 = 1.0 / d.mass[h2];
         for (int k = 0; k < 3; ++k) {
-            double fa = __dmul_rn(pa[k], force) / nba;
-            double fc = __dmul_rn(pc[k], force) / nbc;
-            double fb = -__dadd_rn(fa, fc);
-            s.a_new[3 * o + k] = __dadd_rn(__dadd_rn(s.a_new[3 * o + k], __dmul_rn(iO, fO[k])), fb / d.mass[o]);
-            s.a_new[3 * h1 + k] = __dadd_rn(__dadd_rn(s.a_new[3 * h1 + k], __dmul_rn(iH1, fH1[k])), fa / d.mass[h1]);
-            s.a_new[3 * h2 + k] = __dadd_rn(__dadd_rn(s.a_new[3 * h2 + k], __dmul_rn(iH2, fH2[k])), fc / d.mass[h2]);
+            float fa = pa[k] * sa;
+            float fc = pc[k] * sc;
+            float fb = -(fa + fc);
+            s.a_new[3 * o + k] += (double)(fO[k] + fb) * iO;
+            s.a_new[3 * h1 + k] += (double)(fH1[k] + fa) * iH1;
+            s.a_new[3 * h2 + k] += (double)(fH2[k] + fc) * iH2;
         }
     }
 }
 
 int launch_bonded(nbg_ctx* c, const StateView& s)
 {
-    // FP64-heavy and short: small blocks spread the molecules over every SM
-    k_bonded<<<grid_for(c->n / 3, 32), 32, 0, c->stream>>>(c->d, s);
+    k_bonded<<<grid_for(c->n / 3, 64), 64, 0, c->stream>>>(c->d, s);
     NBG_LAUNCH_CHECK(c, "k_bonded");
     return NBG_OK;
 }

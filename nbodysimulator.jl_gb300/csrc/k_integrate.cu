@@ -8,6 +8,8 @@
 // thermostat terms of thermostats.jl:76-128 evaluated at the start-of-step
 // velocity v. All FP64 arithmetic here uses explicit _rn intrinsics so that
 // no multiply-add is contracted (the reference's Julia arithmetic has none).
+#include <algorithm>
+
 #include "nbg_internal.cuh"
 
 // Split one atom's position into (hi, lo) floats; see nbg_internal.cuh.
@@ -151,14 +153,13 @@ int launch_temperature(nbg_ctx* c, const double* v)
     return NBG_OK;
 }
 
-// Thermostat term of soode_system! for element e of atom i (i < n):
-// Berendsen dv += gamma (T0/T - 1) v (or gamma v when 1/T == Inf),
-// Nose-Hoover dv -= zeta v.
-__device__ __forceinline__ double thermo_term(const Dev& d, int64_t i, double v, double zeta)
+// Thermostat term of soode_system! for element e of atom i (i < n) at
+// temperature T: Berendsen dv += gamma (T0/T - 1) v (or gamma v when
+// 1/T == Inf), Nose-Hoover dv -= zeta v.
+__device__ __forceinline__ double thermo_term_T(const Dev& d, int64_t i, double v, double zeta, double T)
 {
     if (d.therm == NBG_THERMO_BERENDSEN) {
         const RepDev& R = d.reps[d.rep_of[i]];
-        double T = d.red_T[d.rep_of[i]];
         double g = 0.5 / R.tparam;
         if (1.0 / T == INFINITY) return __dmul_rn(g, v);
         return __dmul_rn(__dmul_rn(g, __dsub_rn(R.T0 / T, 1.0)), v);
@@ -167,21 +168,35 @@ __device__ __forceinline__ double thermo_term(const Dev& d, int64_t i, double v,
     return 0.0;
 }
 
+__device__ __forceinline__ double thermo_term(const Dev& d, int64_t i, double v, double zeta)
+{
+    return thermo_term_T(d, i, v, zeta, d.red_T[d.rep_of[i]]);
+}
+
 // v' = v + dt (a/2 + a'/2) with a' = forces + thermostat term at v; stores a'
 // as the next step's a. Also sets the Nose-Hoover rate (thermostats.jl:126).
-__global__ void k_kick(Dev d, StateView s, double dt)
+// With do_T (single system, Berendsen / Nose-Hoover) it also reduces
+// sum m v'^2 over the new velocities: block partials, then the last block
+// to finish adds them in block order and stores T for the next step's
+// thermostat term (every block reads the current T before that).
+__global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int do_T, double* part,
+                                              unsigned* counter)
 {
-    int64_t ncomp = 3 * d.n;
+    const int64_t ncomp = 3 * d.n;
     double zeta = 0.0;
     if (d.therm == NBG_THERMO_NOSEHOOVER) zeta = s.x[3 * d.n];
+    const double T_now = d.red_T[0];
+    double acc = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x) {
         double v = s.v[e];
         double an = s.a_new[e];
         if (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER)
-            an = __dadd_rn(an, thermo_term(d, e / 3, v, zeta));
+            an = __dadd_rn(an, thermo_term_T(d, e / 3, v, zeta, do_T ? T_now : d.red_T[d.rep_of[e / 3]]));
         if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
-        s.v[e] = __dadd_rn(v, __dmul_rn(dt, __dadd_rn(__dmul_rn(0.5, s.a_old[e]), __dmul_rn(0.5, an))));
+        double vn = __dadd_rn(v, __dmul_rn(dt, __dadd_rn(__dmul_rn(0.5, s.a_old[e]), __dmul_rn(0.5, an))));
+        s.v[e] = vn;
         s.a_old[e] = an;
+        if (do_T) acc += d.mass[e / 3] * (vn * vn);
     }
     if (d.therm == NBG_THERMO_NOSEHOOVER && blockIdx.x == 0 && threadIdx.x < 3) {
         int64_t z = 3 * d.n + threadIdx.x;
@@ -190,15 +205,45 @@ __global__ void k_kick(Dev d, StateView s, double dt)
         if (threadIdx.x == 0) {
             const RepDev& R = d.reps[0];
             double it = 1.0 / R.tparam;
-            double T = d.red_T[0];
-            s.v[z] = __dmul_rn(__dmul_rn(it, it), __dsub_rn(T / R.T0, (R.ndf + 1.0) / R.ndf));
+            s.v[z] = __dmul_rn(__dmul_rn(it, it), __dsub_rn(T_now / R.T0, (R.ndf + 1.0) / R.ndf));
         }
+    }
+    if (!do_T) return;
+    __shared__ double sh[256];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = sh[0];
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // fixed-order tree over the block partials
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t += ((volatile double*)part)[b];
+    sh[threadIdx.x] = t;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        d.red_T[0] = sh[0] / (d.kb * d.reps[0].ndf);
+        *counter = 0u;
     }
 }
 
-int launch_kick(nbg_ctx* c, const StateView& s, double dt)
+int launch_kick(nbg_ctx* c, const StateView& s, double dt, bool do_T)
 {
-    k_kick<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->d, s, dt);
+    const int grid = std::min(grid_for(3 * c->n, 256), c->kick_blocks);
+    k_kick<<<grid, 256, 0, c->stream>>>(c->d, s, dt, do_T ? 1 : 0, c->kick_part, c->kick_counter);
     NBG_LAUNCH_CHECK(c, "k_kick");
     return NBG_OK;
 }

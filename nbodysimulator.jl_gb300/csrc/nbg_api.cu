@@ -389,6 +389,9 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     if ((st = dalloc(c, &D.red_partial, (size_t)nrep * D.red_slices))) return st;
     if ((st = dalloc(c, &D.red_T, nrep))) return st;
     if ((st = dalloc(c, &D.red_counter, nrep))) return st;
+    c->kick_blocks = (int)std::min<int64_t>(4096, std::max<int64_t>(1, (3 * n + 255) / 256));
+    if ((st = dalloc(c, &c->kick_part, c->kick_blocks))) return st;
+    if ((st = dalloc(c, &c->kick_counter, 1))) return st;
 
     if (c->path == PATH_LIST) {
         if ((st = dalloc(c, &D.cell_count, D.ncell_total))) return st;
@@ -664,6 +667,7 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
     CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     CK(cudaMemsetAsync(c->ev.a_new, 0, state_bytes(c), c->stream), "dv clear");
     resident_dirty(c);
+    c->T_valid = false;  // the RHS reduces T of its own velocities into red_T
     int st = forces_once(c, c->ev);
     if (st) return st;
     if ((st = launch_rhs_thermostat(c, c->ev))) return st;
@@ -682,6 +686,7 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
     CK(cudaMemcpyAsync(c->st.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     c->state_valid = true;
     c->accel_valid = false;
+    c->T_valid = false;
     c->steps_since_build = -1;
     return NBG_OK;
 }
@@ -760,6 +765,7 @@ static int init_accel(nbg_ctx* c)
     if (!is_em(c)) {
         if ((st = launch_rhs_thermostat(c, c->st))) return st;
         CK(cudaMemcpyAsync(c->st.a_old, c->st.a_new, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "a init");
+        c->T_valid = true;
     }
     c->accel_valid = true;
     return NBG_OK;
@@ -786,9 +792,13 @@ static int step_vv(nbg_ctx* c, double dt, StepRef sr)
     bool force = rebuild_due(c, true);
     if ((st = forces(c, s, force, pos))) return st;
     c->steps_since_build = force ? 0 : c->steps_since_build + 1;
-    if (c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER)
+    const bool thermo_T = c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER;
+    // single systems fold the next step's T into the kick; batches reduce per replica
+    const bool fused_T = thermo_T && c->nrep == 1;
+    if (thermo_T && !(fused_T && c->T_valid))
         if ((st = launch_temperature(c, s.v))) return st;
-    if ((st = launch_kick(c, s, dt))) return st;
+    if ((st = launch_kick(c, s, dt, fused_T))) return st;
+    c->T_valid = fused_T;
     if (c->d.therm == NBG_THERMO_ANDERSEN)
         if ((st = launch_andersen(c, s, dt, sr))) return st;
     return NBG_OK;
@@ -863,6 +873,11 @@ static int capture_graph(nbg_ctx* c, double dt)
         c->graph = nullptr;
     }
     const int64_t G = graph_period(c);
+    if ((c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER) && c->nrep == 1 && !c->T_valid) {
+        int st0 = launch_temperature(c, c->st.v);
+        if (st0) return st0;
+        c->T_valid = true;
+    }
     const int64_t launches0 = c->launches;
     const int64_t ssb0 = c->steps_since_build;
     cudaGraph_t g = nullptr;
@@ -872,6 +887,7 @@ static int capture_graph(nbg_ctx* c, double dt)
     if (st == NBG_OK) st = launch_step_advance(c, G);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->steps_since_build = ssb0;  // capture only recorded the steps
+    c->T_valid = (c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER) && c->nrep == 1;
     if (st != NBG_OK) {
         if (g) cudaGraphDestroy(g);
         return st;
@@ -974,6 +990,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
             CK(cudaMemcpyAsync(c->st.a_old, b.a, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
             c->step = step0;
             c->steps_since_build = -1;
+            c->T_valid = false;
             if ((st = clear_status(c))) { backup_free(c, b); return st; }
             if ((st = launch_pack(c, c->st))) { backup_free(c, b); return st; }
             continue;

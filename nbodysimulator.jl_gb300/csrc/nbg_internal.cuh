@@ -147,6 +147,11 @@ struct nbg_ctx {
     double graph_dt = 0.0;
     bool use_graphs = true;
     bool baoab = false;          // Langevin by BAOAB instead of Euler-Maruyama
+    // temperature folded into the kick (single system, Berendsen / Nose-Hoover)
+    double* kick_part = nullptr;
+    unsigned* kick_counter = nullptr;
+    int kick_blocks = 0;
+    bool T_valid = false;        // red_T holds T of the resident velocities
     std::vector<cudaEvent_t> prof_events;  // start/stop pairs not yet read
     double prof_ms = 0.0;
     int64_t prof_count = 0;
@@ -174,7 +179,7 @@ int launch_force_list(nbg_ctx* c, const StateView& s);
 int launch_bonded(nbg_ctx* c, const StateView& s);
 int launch_drift(nbg_ctx* c, const StateView& s, double dt, StepRef pos);
 int launch_temperature(nbg_ctx* c, const double* v);
-int launch_kick(nbg_ctx* c, const StateView& s, double dt);
+int launch_kick(nbg_ctx* c, const StateView& s, double dt, bool do_T);
 int launch_andersen(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_step_advance(nbg_ctx* c, int64_t by);

@@ -266,6 +266,78 @@ NBG_API int nbg_gravity_accel_noalloc(const double* x, const double* mass, int64
    the roofline denominator of the FP32-bound gravity kernel. */
 NBG_API int nbg_probe_fp32_peak(int device, double* tflops);
 
+/* ------------------------------------------------------------------------
+ * Learned short-range model and r-RESPA (engine extension: the reference has
+ * no learned model and no multiple-time-step integrator, so none of these
+ * replaces a reference interface). One SPC/Fw water system on the
+ * Verlet-list path in a cubic box.
+ *
+ * Model, per species (0 = O, 1 = H), on 64 invariant descriptors of each
+ * atom's environment within 0.6 nm (24 radial Gaussians per neighbour
+ * species and 16 angular invariants): an MLP 64 -> 128 -> 128 -> 1 (tanh)
+ * giving the atom's short-range energy; inference and its backward to the
+ * forces run in BF16 on the tensor cores. Parameters of one species are
+ * NBG_ML_NPARAM floats in this order: W1 [64][128], b1 [128], W2 [128][128],
+ * b2 [128], w3 [128], b3, then the normalisation mean_D [64], sd_D [64],
+ * mean_E, sd_E. Training target: E_i = 1/2 sum_j phi(r_ij) S(r_ij) over atoms
+ * of other molecules, phi = LJ (O-O) + k q_i q_j erfc(4 r / nm) / r (the
+ * real-space part of an Ewald-type split), S = 1 below 0.45 nm with a C2
+ * switch to 0 at 0.6 nm.
+ * ------------------------------------------------------------------------ */
+#define NBG_ML_NPARAM 25091
+#define NBG_ML_NTRAIN 24961 /* leading trainable parameters of a species */
+
+typedef struct nbg_respa_stats {
+    int64_t outer_mts;       /* outer steps integrated by r-RESPA */
+    int64_t outer_fallback;  /* outer steps re-integrated by velocity Verlet (judge over threshold) */
+    int64_t judged;          /* outer steps whose judge value entered the mean */
+    double judge_mean;       /* mean over r-RESPA outer steps of ||F_ml - F_sr|| / ||F_sr|| */
+    double judge_max;
+    double judge_last;       /* largest judge value of the last chunk */
+} nbg_respa_stats;
+
+NBG_API int nbg_ml_param_count(void);
+/* Allocate the model (normalisation mean 0, sd 1; weights 0) and its buffers. */
+NBG_API int nbg_ml_enable(nbg_ctx* ctx);
+NBG_API int nbg_ml_set_params(nbg_ctx* ctx, int32_t species, const float* theta);
+NBG_API int nbg_ml_get_params(nbg_ctx* ctx, int32_t species, float* theta);
+/* Random weights (W1 ~ N(0, (w1_scale/8)^2), W2, w3 ~ N(0, 1/128), biases 0)
+   for both species; the normalisation is kept. Resets the Adam state. */
+NBG_API int nbg_ml_init_params(nbg_ctx* ctx, uint64_t seed, double w1_scale);
+/* At positions u (3n): descriptors [n][64], raw or standardised by the model's mean/sd. */
+NBG_API int nbg_ml_descriptors(nbg_ctx* ctx, const double* u, int32_t standardised, float* desc);
+/* At positions u: learned per-atom energies [n] and forces [3n] (either may be NULL). */
+NBG_API int nbg_ml_eval(nbg_ctx* ctx, const double* u, float* energies, double* forces);
+/* At positions u: exact short-range per-atom energies [n] and forces [3n] (FP32). */
+NBG_API int nbg_ml_labels(nbg_ctx* ctx, const double* u, float* energies, float* forces);
+/* Training set on the device with room for `frames` configurations (empties it). */
+NBG_API int nbg_ml_reserve(nbg_ctx* ctx, int64_t frames);
+/* Append the resident state's raw descriptors and labels; rows[2] = rows per species. */
+NBG_API int nbg_ml_collect(nbg_ctx* ctx, int64_t* rows);
+NBG_API int nbg_ml_rows(nbg_ctx* ctx, int64_t* rows);
+/* Set both species' mean_D, sd_D, mean_E, sd_E from the training set. */
+NBG_API int nbg_ml_normalize(nbg_ctx* ctx);
+/* Adam on the mean squared error of standardised energies over random batches
+   (per species `steps` steps, learning rate lr with a cosine decay over the
+   call). loss[2]: mean loss of the last min(steps, 100) batches. */
+NBG_API int nbg_ml_train(nbg_ctx* ctx, int64_t steps, int32_t batch, double lr, uint64_t seed, double* loss);
+/* Loss and gradient (NBG_ML_NTRAIN floats) of one species' parameters on a
+   batch of standardised inputs x [B][64] and standardised targets y [B]. */
+NBG_API int nbg_ml_batch_gradient(nbg_ctx* ctx, int32_t species, const float* x, const float* y, int32_t B,
+                                  float* grad, double* loss);
+/* Advance the resident state by `outer` r-RESPA steps of inner * dt: the fast
+   force (bonded + learned) every dt, the slow force (exact non-bonded minus
+   learned) every inner * dt (Tuckerman, Berne & Martyna 1992). Every outer
+   step the exact short-range force judges the learned one; a chunk of outer
+   steps whose largest relative RMS error exceeds `threshold` (> 0) is undone
+   and integrated again by velocity Verlet at dt with the exact force.
+   Thermostat: none or Berendsen (applied with the slow kicks). With
+   NBG_RESPA_EXACT_SPLIT the fast force uses the exact short-range force in
+   place of the learned one (the classical split the model stands in for). */
+#define NBG_RESPA_EXACT_SPLIT 1
+NBG_API int nbg_respa_run(nbg_ctx* ctx, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,
+                          nbg_respa_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

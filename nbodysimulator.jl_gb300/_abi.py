@@ -33,6 +33,7 @@ NBG_FLAG_GRAV_PLAIN = 2
 NBG_FLAG_LANGEVIN_BAOAB = 4
 
 _dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
 
 
 class NbgSystemDesc(ctypes.Structure):
@@ -87,6 +88,22 @@ class NbgRunStats(ctypes.Structure):
     ]
 
 
+class NbgRespaStats(ctypes.Structure):
+    _fields_ = [
+        ("outer_mts", ctypes.c_int64),
+        ("outer_fallback", ctypes.c_int64),
+        ("judged", ctypes.c_int64),
+        ("judge_mean", ctypes.c_double),
+        ("judge_max", ctypes.c_double),
+        ("judge_last", ctypes.c_double),
+    ]
+
+
+NBG_ML_NPARAM = 25091
+NBG_ML_NTRAIN = 24961
+NBG_RESPA_EXACT_SPLIT = 1
+
+
 class EngineError(RuntimeError):
     """A libnbg call returned a negative nbg_status."""
 
@@ -122,6 +139,22 @@ SIGNATURES = {
     "nbg_force_kernel_time": (ctypes.c_int, [_vp, _dp, ctypes.POINTER(ctypes.c_int64)]),
     "nbg_probe_fp32_peak": (ctypes.c_int, [ctypes.c_int, _dp]),
     "nbg_gravity_accel_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_double, _vp, _vp]),
+    "nbg_ml_param_count": (ctypes.c_int, []),
+    "nbg_ml_enable": (ctypes.c_int, [_vp]),
+    "nbg_ml_set_params": (ctypes.c_int, [_vp, ctypes.c_int32, _fp]),
+    "nbg_ml_get_params": (ctypes.c_int, [_vp, ctypes.c_int32, _fp]),
+    "nbg_ml_init_params": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_double]),
+    "nbg_ml_descriptors": (ctypes.c_int, [_vp, _dp, ctypes.c_int32, _fp]),
+    "nbg_ml_eval": (ctypes.c_int, [_vp, _dp, _fp, _dp]),
+    "nbg_ml_labels": (ctypes.c_int, [_vp, _dp, _fp, _fp]),
+    "nbg_ml_reserve": (ctypes.c_int, [_vp, ctypes.c_int64]),
+    "nbg_ml_collect": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64)]),
+    "nbg_ml_rows": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64)]),
+    "nbg_ml_normalize": (ctypes.c_int, [_vp]),
+    "nbg_ml_train": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64, _dp]),
+    "nbg_ml_batch_gradient": (ctypes.c_int, [_vp, ctypes.c_int32, _fp, _fp, ctypes.c_int32, _fp, _dp]),
+    "nbg_respa_run": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
+                                     ctypes.c_int32, ctypes.POINTER(NbgRespaStats)]),
 }
 
 _lib = None
@@ -146,6 +179,13 @@ def load_library(path: str = LIB_PATH):
     if path == LIB_PATH:
         _lib = lib
     return lib
+
+
+def as_fptr(arr):
+    """Pointer to a contiguous float32 numpy array (or None)."""
+    if arr is None:
+        return None
+    return arr.ctypes.data_as(_fp)
 
 
 def as_dptr(arr):

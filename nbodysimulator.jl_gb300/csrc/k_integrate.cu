@@ -12,33 +12,6 @@
 
 #include "nbg_internal.cuh"
 
-// Split one atom's position into (hi, lo) floats; see nbg_internal.cuh.
-__device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double* X)
-{
-    const RepDev& R = d.reps[d.rep_of[i]];
-    double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
-    float h[3], l[3];
-    if (d.bc == NBG_BC_CUBIC) {
-        for (int k = 0; k < 3; ++k) {
-            double w = p[k] - R.L * floor(p[k] * R.invL);
-            if (w < 0.0) w += R.L;
-            if (w >= R.L) w -= R.L;
-            double hq = rint(w * (double)R.qscale) * (double)R.qinv;
-            h[k] = (float)hq;
-            l[k] = (float)(w - hq);
-        }
-    } else {
-        for (int k = 0; k < 3; ++k) {
-            h[k] = (float)p[k];
-            l[k] = (float)(p[k] - (double)h[k]);
-        }
-    }
-    float4 hi = d.phi[i];
-    float4 lo = d.plo[i];
-    d.phi[i] = make_float4(h[0], h[1], h[2], hi.w);
-    d.plo[i] = make_float4(l[0], l[1], l[2], lo.w);
-}
-
 __global__ void k_pack(Dev d, const double* X)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x)
@@ -179,7 +152,7 @@ __device__ __forceinline__ double thermo_term(const Dev& d, int64_t i, double v,
 // sum m v'^2 over the new velocities: block partials, then the last block
 // to finish adds them in block order and stores T for the next step's
 // thermostat term (every block reads the current T before that).
-__global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int do_T, double* part,
+__global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int do_T, int thermo, double* part,
                                               unsigned* counter)
 {
     const int64_t ncomp = 3 * d.n;
@@ -190,7 +163,7 @@ __global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x) {
         double v = s.v[e];
         double an = s.a_new[e];
-        if (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER)
+        if (thermo && (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER))
             an = __dadd_rn(an, thermo_term_T(d, e / 3, v, zeta, do_T ? T_now : d.red_T[d.rep_of[e / 3]]));
         if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
         double vn = __dadd_rn(v, __dmul_rn(dt, __dadd_rn(__dmul_rn(0.5, s.a_old[e]), __dmul_rn(0.5, an))));
@@ -198,7 +171,7 @@ __global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int
         s.a_old[e] = an;
         if (do_T) acc += d.mass[e / 3] * (vn * vn);
     }
-    if (d.therm == NBG_THERMO_NOSEHOOVER && blockIdx.x == 0 && threadIdx.x < 3) {
+    if (thermo && d.therm == NBG_THERMO_NOSEHOOVER && blockIdx.x == 0 && threadIdx.x < 3) {
         int64_t z = 3 * d.n + threadIdx.x;
         // dv[:, end] = 0; v[zeta] = tau^-2 (T/T0 - (ndf+1)/ndf)
         s.a_old[z] = 0.0;
@@ -240,10 +213,10 @@ __global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int
     }
 }
 
-int launch_kick(nbg_ctx* c, const StateView& s, double dt, bool do_T)
+int launch_kick(nbg_ctx* c, const StateView& s, double dt, bool do_T, bool thermo)
 {
     const int grid = std::min(grid_for(3 * c->n, 256), c->kick_blocks);
-    k_kick<<<grid, 256, 0, c->stream>>>(c->d, s, dt, do_T ? 1 : 0, c->kick_part, c->kick_counter);
+    k_kick<<<grid, 256, 0, c->stream>>>(c->d, s, dt, do_T ? 1 : 0, thermo ? 1 : 0, c->kick_part, c->kick_counter);
     NBG_LAUNCH_CHECK(c, "k_kick");
     return NBG_OK;
 }

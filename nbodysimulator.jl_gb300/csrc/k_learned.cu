@@ -1,0 +1,1099 @@
+// k_learned.cu - the learned short-range force model of SPC/Fw water and its
+// training (no reference counterpart: an engine feature). The definitions are
+// the ones oracle/learned.py restates in FP64:
+//
+//  descriptor of atom i over atoms j of other molecules with r < ML_RD:
+//    radial   G[s][k] = sum_{j in s} g_k(r) fc(r), Gaussians of width w at
+//             mu_k = ML_R0 + k w (24 per neighbour species s)
+//    angular  p[s][a] = sum psi_a(r) rhat, Q[s][a] = sum psi_a (rhat rhat^T - I/3),
+//             psi_a = fc(r) exp(-r^2 / (2 rho_a^2)), invariants |p|^2, |Q|_F^2
+//    D = [G_O(24), G_H(24), A1_O(4), A1_H(4), A2_O(4), A2_H(4)] (64)
+//  per-species MLP 64 -> 128 -> 128 -> 1 (tanh): E_i = sdE (a2 . w3 + b3) + muE
+//    on the standardised input x = (D - muD) / sdD.
+//  short-range target: E_i = 1/2 sum_j phi(r) S(r), phi = LJ (O-O) +
+//    k q_i q_j erfc(alpha r) / r (the real-space part of an Ewald-type
+//    split), S a C2 smoothstep from 1 at ML_RS to 0 at ML_RD. The screening
+//    keeps the switched region's forces small, so that the remainder (exact
+//    non-bonded force minus this part) varies slowly enough for the outer
+//    step of r-RESPA.
+//
+// Short lists hold, per atom, the long-list atoms within ML_RD + skin split by
+// species (O from the front of the row, H from the back), so the descriptor
+// and force loops run species-uniform. Inference (k_mlp_bf16) runs the MLP
+// forward and its backward to the input on the tensor cores with mma.sync
+// m16n8k16 BF16 tiles (FP32 accumulate): one warp per 16 atoms of one
+// species, weights staged once per block in shared memory (one orientation,
+// ldmatrix / ldmatrix.trans give both), activations kept in registers in the
+// A-fragment layout between layers. Learned forces are scattered to
+// neighbours as 64-bit fixed point (2^-32 units) so the sum does not depend
+// on the order of the atomics. Training runs in FP32 on the CUDA cores.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "nbg_internal.cuh"
+
+#define ML_NK 24
+#define ML_ND 64
+#define ML_NH 128
+#define ML_FQ 4294967296.0f  // fixed-point scale of the learned forces (2^32)
+
+__constant__ float c_rho2inv[4];  // 1 / (2 rho_a^2)
+__constant__ float c_alpha;       // Coulomb screening of the short-range target (1/nm)
+
+struct MLView {
+    // model (per species 0 = O, 1 = H)
+    const float* theta[2];        // FP32 master parameters (layout of oracle/learned.py)
+    const __nv_bfloat16* w1[2];   // W1 [64][128]
+    const __nv_bfloat16* w2[2];   // W2 [128][128]
+    // per atom
+    const int* snbr;              // short list, column-major [k * n + i]
+    const int* scount;            // nO | nH << 16
+    int scap;
+    float* x;                     // descriptor [n][64] (standardised, or raw)
+    float* mom;                   // moments [n][2][4][9]: p (3) and Q (xx, yy, zz, xy, xz, yz)
+    float* dx;                    // dE/dD [n][64]
+    float* e;                     // E_i [n]
+    unsigned long long* fq;       // learned force [3n], fixed point
+    float rd2;                    // RD^2
+    float rs2;                    // (RD + skin)^2 of the short list
+};
+
+static __device__ __forceinline__ int param_off_b1() { return ML_ND * ML_NH; }
+static __device__ __forceinline__ int param_off_w2() { return ML_ND * ML_NH + ML_NH; }
+static __device__ __forceinline__ int param_off_b2() { return ML_ND * ML_NH + ML_NH + ML_NH * ML_NH; }
+static __device__ __forceinline__ int param_off_w3() { return param_off_b2() + ML_NH; }
+static __device__ __forceinline__ int param_off_b3() { return param_off_w3() + ML_NH; }
+static __device__ __forceinline__ int param_off_mu() { return param_off_b3() + 1; }
+static __device__ __forceinline__ int param_off_sd() { return param_off_mu() + ML_ND; }
+static __device__ __forceinline__ int param_off_muE() { return param_off_sd() + ML_ND; }
+
+// fc = (cos(pi r / RD) + 1) / 2 and its derivative
+__device__ __forceinline__ void ml_fc(float r, float& fc, float& dfc)
+{
+    float s, c;
+    __sincosf(r * ((float)M_PI / ML_RD), &s, &c);
+    fc = 0.5f * (c + 1.0f);
+    dfc = -0.5f * ((float)M_PI / ML_RD) * s;
+}
+
+// g_k = scale * exp(-(t - k)^2 / 2) for k = 0..23 (t = (r - R0) / w) by a
+// product recurrence from the middle centre k = 12: upwards
+// g_{k+1} = g_k exp(t - k - 1/2), downwards g_{k-1} = g_k exp(k - t - 1/2),
+// and each ratio shrinks by 1/e per step. Three exponentials instead of 24;
+// for t > -1 every factor that matters stays a normal FP32 number (pairs
+// closer than R0 - w take the direct form).
+__device__ __forceinline__ void ml_gaussians(float t, float scale, float* g)
+{
+    const float d = t - 12.0f;
+    if (d < -13.0f) {
+#pragma unroll
+        for (int k = 0; k < ML_NK; ++k) {
+            const float z = t - (float)k;
+            g[k] = scale * __expf(-0.5f * z * z);
+        }
+        return;
+    }
+    const float einv = 0.36787944117144233f;
+    const float g12 = scale * __expf(-0.5f * d * d);
+    float up = __expf(d - 0.5f), dn = __expf(-d - 0.5f);
+    g[12] = g12;
+    float cur = g12;
+#pragma unroll
+    for (int k = 13; k < ML_NK; ++k) {
+        cur *= up;
+        up *= einv;
+        g[k] = cur;
+    }
+    cur = g12;
+#pragma unroll
+    for (int k = 11; k >= 0; --k) {
+        cur *= dn;
+        dn *= einv;
+        g[k] = cur;
+    }
+}
+
+// ---------------------------------------------------------------------
+// short list: atoms of the long list within RD + skin, O neighbours from the
+// front of the atom's column, H neighbours from the back (warp per atom;
+// column-major so that thread-per-atom readers load a warp's entries in one
+// transaction)
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_short_list(Dev d, MLView m, StepRef pos, int force, int* snbr, int* scount)
+{
+    const int parity = (int)(step_of(pos) & 1);
+    if (!(force || d.rebuild_flag[parity])) return;
+    const int lane = threadIdx.x % 32;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
+    if (i >= d.n) return;
+    const RepDev& R = d.reps[d.rep_of[i]];
+    const float4 hi = d.phi[i], lo = d.plo[i];
+    const int cnt = d.nbr_count[i];
+    const int* nl = d.nbr + i * d.nbr_istride;
+    int* col = snbr + i;  // column-major: entry q at col[q * n]
+    const unsigned below = (1u << lane) - 1u;
+    int nO = 0, nH = 0;
+    for (int k0 = 0; k0 < cnt; k0 += 32) {
+        const int k = k0 + lane;
+        bool take = false;
+        int j = 0;
+        if (k < cnt) {
+            j = nl[(int64_t)k * d.nbr_kstride];
+            float3 dr = split_diff(hi, lo, d.phi[j], d.plo[j], true, R);
+            take = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z < m.rs2;
+        }
+        const bool isO = (j % 3) == 0;
+        const unsigned bo = __ballot_sync(0xffffffffu, take && isO);
+        const unsigned bh = __ballot_sync(0xffffffffu, take && !isO);
+        if (take) {
+            if (isO) {
+                const int p = nO + __popc(bo & below);
+                if (p < m.scap) col[(int64_t)p * d.n] = j;
+            } else {
+                const int p = nH + __popc(bh & below);
+                if (p < m.scap) col[(int64_t)(m.scap - 1 - p) * d.n] = j;
+            }
+        }
+        nO += __popc(bo);
+        nH += __popc(bh);
+    }
+    if (lane == 0) {
+        if (nO + nH > m.scap) {
+            status_set(d.status, ST_SHORT_OVERFLOW);
+            nO = min(nO, m.scap);
+            nH = m.scap - nO;
+        }
+        scount[i] = nO | (nH << 16);
+    }
+}
+
+// Walks entries q0..q1-1 of atom i's short-list column with the next
+// neighbour's index and split position loaded one entry ahead, so that its
+// gathers overlap the current pair's arithmetic.
+struct NbrCursor {
+    const int* col;
+    int64_t stride;
+    int q, q1;
+    int jn;
+    float4 hn, ln;
+    __device__ __forceinline__ void load(const Dev& d)
+    {
+        if (q < q1) {
+            jn = col[(int64_t)q * stride];
+            hn = d.phi[jn];
+            ln = d.plo[jn];
+        }
+    }
+    __device__ __forceinline__ NbrCursor(const Dev& d, const int* c, int64_t n, int a, int b)
+        : col(c), stride(n), q(a), q1(b), jn(0)
+    {
+        load(d);
+    }
+    // current neighbour (index, split position) and advance
+    __device__ __forceinline__ bool next(const Dev& d, int& j, float4& hj, float4& lj)
+    {
+        if (q >= q1) return false;
+        j = jn;
+        hj = hn;
+        lj = ln;
+        ++q;
+        load(d);
+        return true;
+    }
+};
+
+// ---------------------------------------------------------------------
+// descriptors (thread per atom). raw: write D unstandardised.
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_descriptor(Dev d, MLView m, int raw)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const RepDev& R = d.reps[d.rep_of[i]];
+        const float4 hi = d.phi[i], lo = d.plo[i];
+        const int cnt = m.scount[i];
+        const float* th = (i % 3 == 0) ? m.theta[0] : m.theta[1];
+        const float* mu = th + param_off_mu();
+        const float* sd = th + param_off_sd();
+        float* X = m.x + i * ML_ND;
+        float* MO = m.mom + i * 72;
+        for (int s = 0; s < 2; ++s) {
+            const int q0 = s == 0 ? 0 : m.scap - (cnt >> 16);
+            const int q1 = s == 0 ? (cnt & 0xffff) : m.scap;
+            float G[ML_NK];
+            float mo[4][9];
+#pragma unroll
+            for (int k = 0; k < ML_NK; ++k) G[k] = 0.f;
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = 0; c < 9; ++c) mo[a][c] = 0.f;
+            NbrCursor cur(d, m.snbr + i, d.n, q0, q1);
+            int j;
+            float4 hj, lj;
+            while (cur.next(d, j, hj, lj)) {
+                const float3 dr = split_diff(hj, lj, hi, lo, true, R);  // r_j - r_i
+                const float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+                if (!(r2 < m.rd2)) continue;
+                const float ir = rsqrtf(r2), r = r2 * ir;
+                const float ux = dr.x * ir, uy = dr.y * ir, uz = dr.z * ir;
+                float f, df;
+                ml_fc(r, f, df);
+                float gk[ML_NK];
+                ml_gaussians((r - ML_R0) * (1.0f / ML_W), f, gk);
+#pragma unroll
+                for (int k = 0; k < ML_NK; ++k) G[k] += gk[k];
+                const float comp[9] = {ux, uy, uz, ux * ux - (1.0f / 3.0f), uy * uy - (1.0f / 3.0f),
+                                       uz * uz - (1.0f / 3.0f), ux * uy, ux * uz, uy * uz};
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const float psi = f * __expf(-r2 * c_rho2inv[a]);
+#pragma unroll
+                    for (int c = 0; c < 9; ++c) mo[a][c] = fmaf(psi, comp[c], mo[a][c]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < ML_NK; ++k) {
+                const int col = s * ML_NK + k;
+                X[col] = raw ? G[k] : (G[k] - mu[col]) / sd[col];
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float* M = mo[a];
+                const float A1 = M[0] * M[0] + M[1] * M[1] + M[2] * M[2];
+                // |Q|_F^2 of the symmetric matrix (diagonal + 2 x off-diagonal)
+                const float A2 = M[3] * M[3] + M[4] * M[4] + M[5] * M[5] + 2.f * (M[6] * M[6] + M[7] * M[7] + M[8] * M[8]);
+                const int c1 = 48 + 4 * s + a, c2 = 56 + 4 * s + a;
+                X[c1] = raw ? A1 : (A1 - mu[c1]) / sd[c1];
+                X[c2] = raw ? A2 : (A2 - mu[c2]) / sd[c2];
+#pragma unroll
+                for (int c = 0; c < 9; ++c) MO[(s * 4 + a) * 9 + c] = M[c];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// MLP forward + backward to the input, BF16 tensor cores (mma.sync)
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void mma_bf16(float* c, const unsigned* a, const unsigned* b)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void ldsm_x4(unsigned* r, const void* p)
+{
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+__device__ __forceinline__ void ldsm_x4_t(unsigned* r, const void* p)
+{
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+__device__ __forceinline__ float tanh_fast(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ unsigned pack_bf16(float lo, float hi)
+{
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<unsigned*>(&v);
+}
+
+__device__ __forceinline__ unsigned pack_h2(float lo, float hi)
+{
+    __half2 v = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<unsigned*>(&v);
+}
+
+__device__ __forceinline__ float2 unpack_h2(unsigned u)
+{
+    __half2 v = *reinterpret_cast<__half2*>(&u);
+    return __half22float2(v);
+}
+
+#define MLP_WARPS 8
+#define LDW (ML_NH + 8)  // bf16 row stride of the staged weights (272 B: ldmatrix rows spread over banks)
+#define LDX (ML_ND + 8)  // bf16 row stride of a staged input tile (144 B)
+
+struct MlpSmem {
+    __nv_bfloat16 w1[ML_ND * LDW];  // W1 [input k][hidden n]
+    __nv_bfloat16 w2[ML_NH * LDW];  // W2 [hidden k][hidden n]
+    float b1[ML_NH], b2[ML_NH], w3[ML_NH], sdinv[ML_ND];
+    __nv_bfloat16 xs[MLP_WARPS][16 * LDX];
+    unsigned da1[MLP_WARPS][8 * 4 * 32];  // 1 - a1^2 as half2, in each lane's C-fragment order
+};
+
+// atom index of the k-th atom of a species in a water system (O = 3m; H = 3m+1, 3m+2)
+__device__ __forceinline__ int64_t species_atom(int sp, int64_t k) { return sp == 0 ? 3 * k : 3 * (k / 2) + 1 + (k % 2); }
+
+// Fragment layouts (m16n8k16, g = lane / 4, t = lane % 4): A a0..a3 = rows
+// g, g+8 x columns 2t(+1), 2t+8(+1); B b0, b1 = rows 2t(+1), 2t+8(+1) x
+// column g; C c0..c3 = rows g, g+8 x columns 2t(+1). The C tiles of output
+// columns 16u..16u+15 are, packed to BF16, the A fragment of k-tile u of the
+// next product, so activations never leave registers.
+__global__ void __launch_bounds__(MLP_WARPS * 32, 2) k_mlp_bf16(MLView m, int sp, int64_t count)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MlpSmem& S = *reinterpret_cast<MlpSmem*>(smem_raw);
+    const float* th = sp == 0 ? m.theta[0] : m.theta[1];
+    {
+        const uint4* g1 = reinterpret_cast<const uint4*>(sp == 0 ? m.w1[0] : m.w1[1]);
+        const uint4* g2 = reinterpret_cast<const uint4*>(sp == 0 ? m.w2[0] : m.w2[1]);
+        for (int e = threadIdx.x; e < ML_ND * 16; e += blockDim.x)
+            reinterpret_cast<uint4*>(S.w1 + (e >> 4) * LDW)[e & 15] = g1[e];
+        for (int e = threadIdx.x; e < ML_NH * 16; e += blockDim.x)
+            reinterpret_cast<uint4*>(S.w2 + (e >> 4) * LDW)[e & 15] = g2[e];
+        for (int e = threadIdx.x; e < ML_NH; e += blockDim.x) {
+            S.b1[e] = th[param_off_b1() + e];
+            S.b2[e] = th[param_off_b2() + e];
+            S.w3[e] = th[param_off_w3() + e];
+        }
+        for (int e = threadIdx.x; e < ML_ND; e += blockDim.x) S.sdinv[e] = 1.0f / th[param_off_sd() + e];
+    }
+    __syncthreads();
+    const float b3 = th[param_off_b3()];
+    const float muE = th[param_off_muE()], sdE = th[param_off_muE() + 1];
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int g = lane >> 2, t = lane & 3;
+    __nv_bfloat16* xs = S.xs[warp];
+    // per-lane ldmatrix row offsets
+    const int rA = lane & 15, cA = (lane >> 4) * 8;                        // A (and trans-B) tiles
+    const int rB = (lane >> 4) * 8 + (lane & 7), cB = ((lane >> 3) & 1) * 8;  // non-trans B tiles
+    const int64_t ntile = (count + 15) / 16;
+    for (int64_t tile = (int64_t)blockIdx.x * MLP_WARPS + warp; tile < ntile; tile += (int64_t)gridDim.x * MLP_WARPS) {
+        const int64_t k0 = tile * 16;
+        // 16 standardised descriptors to BF16 (rows past count are zero)
+        for (int e = lane; e < 16 * 16; e += 32) {
+            const int r = e >> 4, c4 = e & 15;
+            const int64_t kk = k0 + r;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (kk < count) v = reinterpret_cast<const float4*>(m.x + species_atom(sp, kk) * ML_ND)[c4];
+            uint2 p;
+            p.x = pack_bf16(v.x, v.y);
+            p.y = pack_bf16(v.z, v.w);
+            *reinterpret_cast<uint2*>(xs + r * LDX + 4 * c4) = p;
+        }
+        __syncwarp();
+        unsigned xa[4][4];
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) ldsm_x4(xa[kt], xs + rA * LDX + kt * 16 + cA);
+        // layer 1: a1 = tanh(x W1 + b1), kept as A fragments; 1 - a1^2 as half2
+        // in shared memory (each lane reads back only what it wrote)
+        unsigned a1f[8][4];
+        unsigned* d1h = S.da1[warp];
+#pragma unroll
+        for (int np = 0; np < 8; ++np) {
+            float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt) {
+                unsigned b[4];
+                ldsm_x4_t(b, S.w1 + (kt * 16 + rA) * LDW + np * 16 + cA);
+                mma_bf16(c0, xa[kt], b);
+                mma_bf16(c1, xa[kt], b + 2);
+            }
+            const int col0 = np * 16 + 2 * t, col1 = col0 + 8;
+            float v[8];
+            v[0] = tanh_fast(c0[0] + S.b1[col0]);
+            v[1] = tanh_fast(c0[1] + S.b1[col0 + 1]);
+            v[2] = tanh_fast(c0[2] + S.b1[col0]);
+            v[3] = tanh_fast(c0[3] + S.b1[col0 + 1]);
+            v[4] = tanh_fast(c1[0] + S.b1[col1]);
+            v[5] = tanh_fast(c1[1] + S.b1[col1 + 1]);
+            v[6] = tanh_fast(c1[2] + S.b1[col1]);
+            v[7] = tanh_fast(c1[3] + S.b1[col1 + 1]);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                a1f[np][h] = pack_bf16(v[2 * h], v[2 * h + 1]);
+                d1h[(np * 4 + h) * 32 + lane] = pack_h2(1.f - v[2 * h] * v[2 * h], 1.f - v[2 * h + 1] * v[2 * h + 1]);
+            }
+        }
+        // layer 2: a2 = tanh(a1 W2 + b2); E = sdE (a2.w3 + b3) + muE; g2 = sdE w3 (1 - a2^2)
+        unsigned g2f[8][4];
+        float er0 = 0.f, er1 = 0.f;
+#pragma unroll
+        for (int np = 0; np < 8; ++np) {
+            float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int kt = 0; kt < 8; ++kt) {
+                unsigned b[4];
+                ldsm_x4_t(b, S.w2 + (kt * 16 + rA) * LDW + np * 16 + cA);
+                mma_bf16(c0, a1f[kt], b);
+                mma_bf16(c1, a1f[kt], b + 2);
+            }
+            const int col[2] = {np * 16 + 2 * t, np * 16 + 8 + 2 * t};
+            const float* cc[2] = {c0, c1};
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const int c = col[hh];
+                const float w30 = S.w3[c], w31 = S.w3[c + 1];
+                const float v0 = tanh_fast(cc[hh][0] + S.b2[c]), v1 = tanh_fast(cc[hh][1] + S.b2[c + 1]);
+                const float v2 = tanh_fast(cc[hh][2] + S.b2[c]), v3 = tanh_fast(cc[hh][3] + S.b2[c + 1]);
+                er0 += v0 * w30 + v1 * w31;
+                er1 += v2 * w30 + v3 * w31;
+                g2f[np][2 * hh] = pack_bf16(sdE * w30 * (1.f - v0 * v0), sdE * w31 * (1.f - v1 * v1));
+                g2f[np][2 * hh + 1] = pack_bf16(sdE * w30 * (1.f - v2 * v2), sdE * w31 * (1.f - v3 * v3));
+            }
+        }
+        // energies of rows g and g + 8 (sum over the quad)
+        er0 += __shfl_xor_sync(0xffffffffu, er0, 1);
+        er0 += __shfl_xor_sync(0xffffffffu, er0, 2);
+        er1 += __shfl_xor_sync(0xffffffffu, er1, 1);
+        er1 += __shfl_xor_sync(0xffffffffu, er1, 2);
+        if (t == 0) {
+            if (k0 + g < count) m.e[species_atom(sp, k0 + g)] = sdE * (er0 + b3) + muE;
+            if (k0 + g + 8 < count) m.e[species_atom(sp, k0 + g + 8)] = sdE * (er1 + b3) + muE;
+        }
+        // backward 1: g1 = (g2 W2^T) (1 - a1^2); B(k, n) = W2[n][k]
+        unsigned g1f[8][4];
+#pragma unroll
+        for (int np = 0; np < 8; ++np) {
+            float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int kt = 0; kt < 8; ++kt) {
+                unsigned b[4];
+                ldsm_x4(b, S.w2 + (np * 16 + rB) * LDW + kt * 16 + cB);
+                mma_bf16(c0, g2f[kt], b);
+                mma_bf16(c1, g2f[kt], b + 2);
+            }
+            const float2 d0 = unpack_h2(d1h[(np * 4 + 0) * 32 + lane]), d1 = unpack_h2(d1h[(np * 4 + 1) * 32 + lane]);
+            const float2 d2 = unpack_h2(d1h[(np * 4 + 2) * 32 + lane]), d3 = unpack_h2(d1h[(np * 4 + 3) * 32 + lane]);
+            g1f[np][0] = pack_bf16(c0[0] * d0.x, c0[1] * d0.y);
+            g1f[np][1] = pack_bf16(c0[2] * d1.x, c0[3] * d1.y);
+            g1f[np][2] = pack_bf16(c1[0] * d2.x, c1[1] * d2.y);
+            g1f[np][3] = pack_bf16(c1[2] * d3.x, c1[3] * d3.y);
+        }
+        // backward 2: dE/dD = (g1 W1^T) / sdD; B(k, n) = W1[n][k]
+        const int64_t ag = k0 + g < count ? species_atom(sp, k0 + g) : -1;
+        const int64_t ag8 = k0 + g + 8 < count ? species_atom(sp, k0 + g + 8) : -1;
+#pragma unroll
+        for (int np = 0; np < 4; ++np) {
+            float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int kt = 0; kt < 8; ++kt) {
+                unsigned b[4];
+                ldsm_x4(b, S.w1 + (np * 16 + rB) * LDW + kt * 16 + cB);
+                mma_bf16(c0, g1f[kt], b);
+                mma_bf16(c1, g1f[kt], b + 2);
+            }
+            const int col0 = np * 16 + 2 * t, col1 = col0 + 8;
+            if (ag >= 0) {
+                float* D = m.dx + ag * ML_ND;
+                *reinterpret_cast<float2*>(D + col0) = make_float2(c0[0] * S.sdinv[col0], c0[1] * S.sdinv[col0 + 1]);
+                *reinterpret_cast<float2*>(D + col1) = make_float2(c1[0] * S.sdinv[col1], c1[1] * S.sdinv[col1 + 1]);
+            }
+            if (ag8 >= 0) {
+                float* D = m.dx + ag8 * ML_ND;
+                *reinterpret_cast<float2*>(D + col0) = make_float2(c0[2] * S.sdinv[col0], c0[3] * S.sdinv[col0 + 1]);
+                *reinterpret_cast<float2*>(D + col1) = make_float2(c1[2] * S.sdinv[col1], c1[3] * S.sdinv[col1 + 1]);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------
+// learned forces: F = -dE/dx through the descriptors (thread per atom i,
+// scatter to the neighbours as fixed point)
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void fq_add(unsigned long long* p, float v)
+{
+    atomicAdd(p, (unsigned long long)__float2ll_rn(v * ML_FQ));
+}
+
+__global__ void __launch_bounds__(128) k_ml_force(Dev d, MLView m)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const RepDev& R = d.reps[d.rep_of[i]];
+        const float4 hi = d.phi[i], lo = d.plo[i];
+        const int cnt = m.scount[i];
+        const float* dD = m.dx + i * ML_ND;  // dE/dD (already divided by sdD)
+        const float* MO = m.mom + i * 72;
+        float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
+        for (int s = 0; s < 2; ++s) {
+            const int q0 = s == 0 ? 0 : m.scap - (cnt >> 16);
+            const int q1 = s == 0 ? (cnt & 0xffff) : m.scap;
+            if (q0 >= q1) continue;
+            float cG[ML_NK];
+#pragma unroll
+            for (int k = 0; k < ML_NK; ++k) cG[k] = dD[s * ML_NK + k];
+            float cA1[4], cA2[4], M[4][9];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                cA1[a] = 2.f * dD[48 + 4 * s + a];
+                cA2[a] = 2.f * dD[56 + 4 * s + a];
+#pragma unroll
+                for (int c = 0; c < 9; ++c) M[a][c] = MO[(s * 4 + a) * 9 + c];
+            }
+            NbrCursor cur(d, m.snbr + i, d.n, q0, q1);
+            int j;
+            float4 hj, lj;
+            while (cur.next(d, j, hj, lj)) {
+                const float3 dr = split_diff(hj, lj, hi, lo, true, R);  // r_j - r_i
+                const float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+                if (!(r2 < m.rd2)) continue;
+                const float ir = rsqrtf(r2), r = r2 * ir;
+                const float ux = dr.x * ir, uy = dr.y * ir, uz = dr.z * ir;
+                float f, df;
+                ml_fc(r, f, df);
+                const float tt = (r - ML_R0) * (1.0f / ML_W);
+                // radial: d(g_k fc)/dr = g_k (fc' - fc (t - k) / w)
+                float gk[ML_NK];
+                ml_gaussians(tt, 1.0f, gk);
+                float S0 = 0.f, S1 = 0.f;
+#pragma unroll
+                for (int k = 0; k < ML_NK; ++k) {
+                    const float cg = cG[k] * gk[k];
+                    S0 += cg;
+                    S1 = fmaf(cg, tt - (float)k, S1);
+                }
+                const float dEdr = df * S0 - f * (1.0f / ML_W) * S1;
+                float gx = dEdr * ux, gy = dEdr * uy, gz = dEdr * uz;
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const float e = __expf(-r2 * c_rho2inv[a]);
+                    const float psi = f * e;
+                    const float dpsi = e * (df - 2.f * r * c_rho2inv[a] * f);
+                    const float* Ma = M[a];
+                    // d|p|^2/dr_j = 2 [psi' (p.u) u + psi/r (p - (p.u) u)]
+                    const float pu = Ma[0] * ux + Ma[1] * uy + Ma[2] * uz;
+                    const float s2 = cA1[a] * psi * ir;
+                    const float s1 = cA1[a] * dpsi * pu - s2 * pu;
+                    // d|Q|^2/dr_j = 2 [psi' (uQu) u + psi 2/r (Q u - (uQu) u)]
+                    const float qx = Ma[3] * ux + Ma[6] * uy + Ma[7] * uz;
+                    const float qy = Ma[6] * ux + Ma[4] * uy + Ma[8] * uz;
+                    const float qz = Ma[7] * ux + Ma[8] * uy + Ma[5] * uz;
+                    const float uqu = qx * ux + qy * uy + qz * uz;
+                    const float t2 = 2.f * cA2[a] * psi * ir;
+                    const float t1 = cA2[a] * dpsi * uqu - t2 * uqu;
+                    gx += (s1 + t1) * ux + s2 * Ma[0] + t2 * qx;
+                    gy += (s1 + t1) * uy + s2 * Ma[1] + t2 * qy;
+                    gz += (s1 + t1) * uz + s2 * Ma[2] + t2 * qz;
+                }
+                fq_add(&m.fq[3 * j], -gx);
+                fq_add(&m.fq[3 * j + 1], -gy);
+                fq_add(&m.fq[3 * j + 2], -gz);
+                fi0 += gx;
+                fi1 += gy;
+                fi2 += gz;
+            }
+        }
+        fq_add(&m.fq[3 * i], fi0);
+        fq_add(&m.fq[3 * i + 1], fi1);
+        fq_add(&m.fq[3 * i + 2], fi2);
+    }
+}
+
+// ---------------------------------------------------------------------
+// exact short-range energies and forces (labels and judge), thread per atom
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void smoothstep(float r, float& S, float& dS)
+{
+    float t = (r - ML_RS) * (1.0f / (ML_RD - ML_RS));
+    t = fminf(1.f, fmaxf(0.f, t));
+    const float t2 = t * t, t3 = t2 * t;
+    S = 1.f - 10.f * t3 + 15.f * t3 * t - 6.f * t3 * t2;
+    dS = (-30.f * t2 + 60.f * t3 - 30.f * t3 * t) * (1.0f / (ML_RD - ML_RS));
+}
+
+__global__ void __launch_bounds__(128) k_sr_exact(Dev d, MLView m, float* e_out, float* f_out)
+{
+    const float eps4 = (float)(4.0 * d.lj_eps);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const RepDev& R = d.reps[d.rep_of[i]];
+        const float4 hi = d.phi[i], lo = d.plo[i];
+        const int cnt = m.scount[i];
+        const float kqi = (float)(d.el_k_d * d.charge[i]);
+        const bool oi = (i % 3 == 0);
+        float E = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int s = 0; s < 2; ++s) {
+            const int q0 = s == 0 ? 0 : m.scap - (cnt >> 16);
+            const int q1 = s == 0 ? (cnt & 0xffff) : m.scap;
+            const bool lj_pair = oi && s == 0;  // LJ acts between O atoms only
+            NbrCursor cur(d, m.snbr + i, d.n, q0, q1);
+            int j;
+            float4 hj, lj;
+            while (cur.next(d, j, hj, lj)) {
+                const float3 dr = split_diff(hj, lj, hi, lo, true, R);  // r_j - r_i
+                const float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+                if (!(r2 < m.rd2)) continue;
+                const float ir = rsqrtf(r2), r = r2 * ir;
+                // screened Coulomb k q q erfc(a r) / r and its r-derivative
+                const float kqq = kqi * (float)d.charge[j];
+                const float ec = erfcf(c_alpha * r);
+                float phi = kqq * ec * ir;
+                float dphi = -phi * ir - kqq * ir * (1.1283791670955126f * c_alpha) * __expf(-c_alpha * c_alpha * r2);
+                if (lj_pair) {
+                    const float s2 = d.lj_sig2 * ir * ir, s6 = s2 * s2 * s2;
+                    phi += eps4 * (s6 * s6 - s6);
+                    dphi += eps4 * (-12.f * s6 * s6 + 6.f * s6) * ir;
+                }
+                float S, dS;
+                smoothstep(r, S, dS);
+                E += 0.5f * phi * S;
+                // F_i = d(phi S)/dr (r_j - r_i) / r for the pair energy phi S
+                const float fp = (dphi * S + phi * dS) * ir;
+                fx += fp * dr.x;
+                fy += fp * dr.y;
+                fz += fp * dr.z;
+            }
+        }
+        if (e_out) e_out[i] = E;
+        if (f_out) {
+            f_out[3 * i] = fx;
+            f_out[3 * i + 1] = fy;
+            f_out[3 * i + 2] = fz;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// training (FP32, CUDA cores)
+// ---------------------------------------------------------------------
+// Forward and backward of one batch: thread per sample b. X rows are raw
+// descriptors (standardised here; std != 0 uses them already standardised),
+// y raw labels. Writes x, a1, a2, g1, g2 ([B][128]) and e ([B]: dL/dout);
+// loss into *loss (atomic, FP64).
+__global__ void __launch_bounds__(64) k_train_fb(const float* __restrict__ theta, const float* __restrict__ X,
+                                                 const float* __restrict__ Y, const int* __restrict__ idx, int B,
+                                                 int standardised, float* xs, float* a1, float* a2, float* g1,
+                                                 float* g2, float* eo, double* loss)
+{
+    extern __shared__ float sw[];
+    float* W1 = sw;                  // [64][128]
+    float* W2 = W1 + ML_ND * ML_NH;  // [128][128]
+    for (int e = threadIdx.x; e < ML_ND * ML_NH; e += blockDim.x) W1[e] = theta[e];
+    for (int e = threadIdx.x; e < ML_NH * ML_NH; e += blockDim.x) W2[e] = theta[param_off_w2() + e];
+    __syncthreads();
+    const float* b1 = theta + param_off_b1();
+    const float* b2 = theta + param_off_b2();
+    const float* w3 = theta + param_off_w3();
+    const float b3 = theta[param_off_b3()];
+    const float* mu = theta + param_off_mu();
+    const float* sd = theta + param_off_sd();
+    const float muE = theta[param_off_muE()], sdE = theta[param_off_muE() + 1];
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const int row = idx ? idx[b] : b;
+    const float* D = X + (int64_t)row * ML_ND;
+    float* xb = xs + (int64_t)b * ML_ND;
+    for (int k = 0; k < ML_ND; ++k) xb[k] = standardised ? D[k] : (D[k] - mu[k]) / sd[k];
+    float* A1 = a1 + (int64_t)b * ML_NH;
+    float* A2 = a2 + (int64_t)b * ML_NH;
+    for (int n = 0; n < ML_NH; ++n) {
+        float z = b1[n];
+        for (int k = 0; k < ML_ND; ++k) z = fmaf(xb[k], W1[k * ML_NH + n], z);
+        A1[n] = tanhf(z);
+    }
+    float out = b3;
+    for (int n = 0; n < ML_NH; ++n) {
+        float z = b2[n];
+        for (int k = 0; k < ML_NH; ++k) z = fmaf(A1[k], W2[k * ML_NH + n], z);
+        const float v = tanhf(z);
+        A2[n] = v;
+        out = fmaf(v, w3[n], out);
+    }
+    const float y = standardised ? Y[row] : (Y[row] - muE) / sdE;
+    const float err = out - y;
+    atomicAdd(loss, (double)err * (double)err / (double)B);
+    const float de = 2.f * err / (float)B;
+    eo[b] = de;
+    float* G2 = g2 + (int64_t)b * ML_NH;
+    float* G1 = g1 + (int64_t)b * ML_NH;
+    for (int n = 0; n < ML_NH; ++n) G2[n] = de * w3[n] * (1.f - A2[n] * A2[n]);
+    for (int k = 0; k < ML_NH; ++k) {
+        float s = 0.f;
+        for (int n = 0; n < ML_NH; ++n) s = fmaf(G2[n], W2[k * ML_NH + n], s);
+        G1[k] = s * (1.f - A1[k] * A1[k]);
+    }
+}
+
+// grad[p] for W1 (64x128), b1, W2 (128x128), b2, w3, b3: column sums over the
+// batch in fixed order (thread per parameter)
+__global__ void k_train_grad(int B, const float* __restrict__ xs, const float* __restrict__ a1,
+                             const float* __restrict__ a2, const float* __restrict__ g1, const float* __restrict__ g2,
+                             const float* __restrict__ eo, float* grad)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nW1 = ML_ND * ML_NH, nW2 = ML_NH * ML_NH;
+    if (p >= ML_NTRAIN) return;
+    float s = 0.f;
+    if (p < nW1) {
+        const int k = p / ML_NH, n = p % ML_NH;
+        for (int b = 0; b < B; ++b) s = fmaf(xs[(int64_t)b * ML_ND + k], g1[(int64_t)b * ML_NH + n], s);
+    } else if (p < nW1 + ML_NH) {
+        const int n = p - nW1;
+        for (int b = 0; b < B; ++b) s += g1[(int64_t)b * ML_NH + n];
+    } else if (p < nW1 + ML_NH + nW2) {
+        const int q = p - nW1 - ML_NH, k = q / ML_NH, n = q % ML_NH;
+        for (int b = 0; b < B; ++b) s = fmaf(a1[(int64_t)b * ML_NH + k], g2[(int64_t)b * ML_NH + n], s);
+    } else if (p < nW1 + 2 * ML_NH + nW2) {
+        const int n = p - nW1 - ML_NH - nW2;
+        for (int b = 0; b < B; ++b) s += g2[(int64_t)b * ML_NH + n];
+    } else if (p < nW1 + 3 * ML_NH + nW2) {
+        const int n = p - nW1 - 2 * ML_NH - nW2;
+        for (int b = 0; b < B; ++b) s = fmaf(a2[(int64_t)b * ML_NH + n], eo[b], s);
+    } else {
+        for (int b = 0; b < B; ++b) s += eo[b];
+    }
+    grad[p] = s;
+}
+
+// Adam (Kingma & Ba 2015) on the trainable parameters
+__global__ void k_adam(float* theta, const float* grad, float* m1, float* m2, int count, float lr, float b1, float b2,
+                       float eps, float c1, float c2)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= count) return;
+    const float g = grad[p];
+    const float a = b1 * m1[p] + (1.f - b1) * g;
+    const float v = b2 * m2[p] + (1.f - b2) * g * g;
+    m1[p] = a;
+    m2[p] = v;
+    theta[p] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
+}
+
+// BF16 copies of W1 and W2 for inference
+__global__ void k_ml_pack_bf16(const float* theta, __nv_bfloat16* w1, __nv_bfloat16* w2)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ML_NH * ML_NH; e += gridDim.x * blockDim.x) {
+        if (e < ML_ND * ML_NH) w1[e] = __float2bfloat16_rn(theta[e]);
+        w2[e] = __float2bfloat16_rn(theta[param_off_w2() + e]);
+    }
+}
+
+// copy one species' rows of the raw descriptors and labels into the training set
+__global__ void k_ml_collect(const float* x, const float* e, int64_t n, int sp, float* X, float* Y, int64_t off,
+                             int64_t cap)
+{
+    const int64_t per = sp == 0 ? n / 3 : 2 * (n / 3);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < per; k += (int64_t)gridDim.x * blockDim.x) {
+        if (off + k >= cap) return;
+        const int64_t i = species_atom(sp, k);
+        for (int c = 0; c < ML_ND; ++c) X[(off + k) * ML_ND + c] = x[i * ML_ND + c];
+        Y[off + k] = e[i];
+    }
+}
+
+// mean and standard deviation of each descriptor column and of the labels
+// (one block per column, FP64 sums in fixed order)
+__global__ void k_ml_stats(const float* X, const float* Y, int64_t rows, float* theta)
+{
+    const int col = blockIdx.x;  // 0..63 descriptors, 64 = labels
+    double s = 0.0, s2 = 0.0;
+    for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) {
+        const double v = col < ML_ND ? X[r * ML_ND + col] : Y[r];
+        s += v;
+        s2 += v * v;
+    }
+    __shared__ double a[256], b[256];
+    a[threadIdx.x] = s;
+    b[threadIdx.x] = s2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            a[threadIdx.x] += a[threadIdx.x + w];
+            b[threadIdx.x] += b[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double mean = a[0] / (double)rows;
+        const double var = b[0] / (double)rows - mean * mean;
+        const double sd = sqrt(var > 1e-12 ? var : 1e-12);
+        if (col < ML_ND) {
+            theta[param_off_mu() + col] = (float)mean;
+            theta[param_off_sd() + col] = (float)sd;
+        } else {
+            theta[param_off_muE()] = (float)mean;
+            theta[param_off_muE() + 1] = (float)sd;
+        }
+    }
+}
+
+// random sample indices for a batch (Philox, seed and batch counter)
+__global__ void k_ml_sample(int* idx, int B, int64_t rows, uint64_t seed, uint64_t batch)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const uint4 w = philox(seed, (uint64_t)b, batch, 7u);
+    const uint64_t r = ((uint64_t)w.x << 32) | w.y;
+    idx[b] = (int)(r % (uint64_t)rows);
+}
+
+// a (=, +=, -=) F / m from the fixed-point learned forces (mode 0, 1, -1)
+__global__ void k_ml_accel(const unsigned long long* fq, const double* mass, int64_t n, int mode, double* a)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x) {
+        const double f = (double)(long long)fq[e] * (1.0 / 4294967296.0);
+        const double v = f / mass[e / 3];
+        a[e] = mode == 0 ? v : (mode > 0 ? a[e] + v : a[e] - v);
+    }
+}
+
+// fixed-point forces from FP32 forces (the exact short-range force as the
+// inner force of a classical r-RESPA split)
+__global__ void k_fq_from_f32(const float* f, int64_t n, unsigned long long* fq)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x)
+        fq[e] = (unsigned long long)__float2ll_rn(f[e] * ML_FQ);
+}
+
+// learned forces as FP64 (host export)
+__global__ void k_ml_force_out(const unsigned long long* fq, int64_t n, double* f)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x)
+        f[e] = (double)(long long)fq[e] * (1.0 / 4294967296.0);
+}
+
+// judge sums: |F_ml - F_sr|^2 and |F_sr|^2 into acc[slot][0..1]
+__global__ void k_ml_judge(const unsigned long long* fq, const float* fsr, int64_t n, double* acc, StepRef sr,
+                           int inner, int slots)
+{
+    double s1 = 0.0, s2 = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x) {
+        const double fm = (double)(long long)fq[e] * (1.0 / 4294967296.0);
+        const double dlt = fm - (double)fsr[e];
+        s1 += dlt * dlt;
+        s2 += (double)fsr[e] * (double)fsr[e];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    const int64_t slot = ((step_of(sr) / inner) % slots + slots) % slots;
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(acc + 2 * slot, s1);
+        atomicAdd(acc + 2 * slot + 1, s2);
+    }
+}
+
+// outer r-RESPA kick: v += h (a_slow + Berendsen term at T of v)
+__global__ void k_respa_kick(Dev d, double* v, const double* a, double h, int thermo)
+{
+    const double T = d.red_T[0];
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * d.n; e += (int64_t)gridDim.x * blockDim.x) {
+        double an = a[e];
+        if (thermo && d.therm == NBG_THERMO_BERENDSEN) {
+            const RepDev& R = d.reps[0];
+            const double gm = 0.5 / R.tparam;
+            an += (1.0 / T == INFINITY) ? gm * v[e] : gm * (R.T0 / T - 1.0) * v[e];
+        }
+        if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+        v[e] = v[e] + h * an;
+    }
+}
+
+// ---------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------
+int ml_init_constants()
+{
+    const float rho[4] = {ML_RHO0, ML_RHO1, ML_RHO2, ML_RHO3};
+    float v[4];
+    for (int a = 0; a < 4; ++a) v[a] = 1.0f / (2.0f * rho[a] * rho[a]);
+    if (cudaMemcpyToSymbol(c_rho2inv, v, sizeof(v)) != cudaSuccess) return NBG_ERR_CUDA;
+    const float alpha = ML_ALPHA;
+    return cudaMemcpyToSymbol(c_alpha, &alpha, sizeof(alpha)) == cudaSuccess ? NBG_OK : NBG_ERR_CUDA;
+}
+
+size_t ml_mlp_smem() { return sizeof(MlpSmem); }
+
+static MLView ml_view(nbg_ctx* c)
+{
+    MLView m;
+    for (int s = 0; s < 2; ++s) {
+        m.theta[s] = c->ml_theta[s];
+        m.w1[s] = c->ml_w1[s];
+        m.w2[s] = c->ml_w2[s];
+    }
+    m.snbr = c->ml_snbr;
+    m.scount = c->ml_scnt;
+    m.scap = c->ml_scap;
+    m.x = c->ml_x;
+    m.mom = c->ml_mom;
+    m.dx = c->ml_dx;
+    m.e = c->ml_e;
+    m.fq = c->ml_fq;
+    m.rd2 = ML_RD * ML_RD;
+    const float rs = ML_RD + (float)c->desc.skin;
+    m.rs2 = rs * rs * (1.0f + 1e-5f);
+    return m;
+}
+
+int launch_short_list(nbg_ctx* c, StepRef pos, bool force)
+{
+    MLView m = ml_view(c);
+    k_short_list<<<grid_for(c->n * 32, 256), 256, 0, c->stream>>>(c->d, m, pos, force ? 1 : 0, c->ml_snbr, c->ml_scnt);
+    NBG_LAUNCH_CHECK(c, "k_short_list");
+    return NBG_OK;
+}
+
+int launch_descriptor(nbg_ctx* c, bool raw)
+{
+    k_descriptor<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, ml_view(c), raw ? 1 : 0);
+    NBG_LAUNCH_CHECK(c, "k_descriptor");
+    return NBG_OK;
+}
+
+int launch_mlp(nbg_ctx* c)
+{
+    if (!c->ml_attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
+        if (e != cudaSuccess) return cuda_fail(c, e, "k_mlp_bf16 shared memory");
+        e = cudaFuncSetAttribute(k_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (ML_ND * ML_NH + ML_NH * ML_NH) * (int)sizeof(float));
+        if (e != cudaSuccess) return cuda_fail(c, e, "k_train_fb shared memory");
+        c->ml_attr = true;
+    }
+    const MLView m = ml_view(c);
+    for (int sp = 0; sp < 2; ++sp) {
+        const int64_t count = sp == 0 ? c->n / 3 : 2 * (c->n / 3);
+        const int64_t tiles = (count + 15) / 16;
+        const int grid = (int)std::min<int64_t>((tiles + MLP_WARPS - 1) / MLP_WARPS, (int64_t)c->sms * 2);
+        k_mlp_bf16<<<std::max(grid, 1), MLP_WARPS * 32, sizeof(MlpSmem), c->stream>>>(m, sp, count);
+        NBG_LAUNCH_CHECK(c, "k_mlp_bf16");
+    }
+    return NBG_OK;
+}
+
+int launch_ml_force(nbg_ctx* c)
+{
+    cudaError_t e = cudaMemsetAsync(c->ml_fq, 0, sizeof(unsigned long long) * 3 * c->n, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "ml force clear");
+    k_ml_force<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, ml_view(c));
+    NBG_LAUNCH_CHECK(c, "k_ml_force");
+    return NBG_OK;
+}
+
+int launch_sr_exact(nbg_ctx* c, float* e_out, float* f_out)
+{
+    k_sr_exact<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, ml_view(c), e_out, f_out);
+    NBG_LAUNCH_CHECK(c, "k_sr_exact");
+    return NBG_OK;
+}
+
+int launch_ml_accel(nbg_ctx* c, int mode, double* a)
+{
+    k_ml_accel<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->ml_fq, c->d.mass, c->n, mode, a);
+    NBG_LAUNCH_CHECK(c, "k_ml_accel");
+    return NBG_OK;
+}
+
+int launch_sr_inner(nbg_ctx* c, StepRef pos, bool force_short)
+{
+    int st;
+    if ((st = launch_short_list(c, pos, force_short))) return st;
+    if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
+    k_fq_from_f32<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->ml_fsr, c->n, c->ml_fq);
+    NBG_LAUNCH_CHECK(c, "k_fq_from_f32");
+    return NBG_OK;
+}
+
+int launch_ml_force_out(nbg_ctx* c, double* f)
+{
+    k_ml_force_out<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->ml_fq, c->n, f);
+    NBG_LAUNCH_CHECK(c, "k_ml_force_out");
+    return NBG_OK;
+}
+
+int launch_ml_judge(nbg_ctx* c, StepRef sr, int inner, int slots)
+{
+    k_ml_judge<<<std::min(grid_for(3 * c->n, 256), 1024), 256, 0, c->stream>>>(c->ml_fq, c->ml_fsr, c->n, c->ml_judge,
+                                                                                   sr, inner, slots);
+    NBG_LAUNCH_CHECK(c, "k_ml_judge");
+    return NBG_OK;
+}
+
+int launch_respa_kick(nbg_ctx* c, double* v, const double* a, double h, bool thermo)
+{
+    k_respa_kick<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->d, v, a, h, thermo ? 1 : 0);
+    NBG_LAUNCH_CHECK(c, "k_respa_kick");
+    return NBG_OK;
+}
+
+int launch_ml_pack(nbg_ctx* c, int sp)
+{
+    k_ml_pack_bf16<<<64, 256, 0, c->stream>>>(c->ml_theta[sp], c->ml_w1[sp], c->ml_w2[sp]);
+    NBG_LAUNCH_CHECK(c, "k_ml_pack_bf16");
+    return NBG_OK;
+}
+
+int launch_ml_collect(nbg_ctx* c, int sp, int64_t off)
+{
+    k_ml_collect<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->ml_x, c->ml_esr, c->n, sp, c->ml_X[sp], c->ml_Y[sp],
+                                                            off, c->ml_cap[sp]);
+    NBG_LAUNCH_CHECK(c, "k_ml_collect");
+    return NBG_OK;
+}
+
+int launch_ml_stats(nbg_ctx* c, int sp)
+{
+    k_ml_stats<<<ML_ND + 1, 256, 0, c->stream>>>(c->ml_X[sp], c->ml_Y[sp], c->ml_rows[sp], c->ml_theta[sp]);
+    NBG_LAUNCH_CHECK(c, "k_ml_stats");
+    return NBG_OK;
+}
+
+static int train_fb_grad(nbg_ctx* c, const float* theta, const float* X, const float* Y, const int* idx, int B,
+                         bool standardised, MLTrainScratch& s)
+{
+    const int smem = (ML_ND * ML_NH + ML_NH * ML_NH) * (int)sizeof(float);
+    k_train_fb<<<(B + 63) / 64, 64, smem, c->stream>>>(theta, X, Y, idx, B, standardised ? 1 : 0, s.xs, s.a1, s.a2,
+                                                       s.g1, s.g2, s.eo, s.loss);
+    NBG_LAUNCH_CHECK(c, "k_train_fb");
+    k_train_grad<<<(ML_NTRAIN + 127) / 128, 128, 0, c->stream>>>(B, s.xs, s.a1, s.a2, s.g1, s.g2, s.eo, s.grad);
+    NBG_LAUNCH_CHECK(c, "k_train_grad");
+    return NBG_OK;
+}
+
+int launch_ml_train_step(nbg_ctx* c, int sp, int B, uint64_t seed, uint64_t batch, float lr, int64_t t_adam)
+{
+    MLTrainScratch& s = c->ml_ts;
+    if (!c->ml_attr) {
+        int st = launch_mlp_attrs(c);
+        if (st) return st;
+    }
+    k_ml_sample<<<(B + 255) / 256, 256, 0, c->stream>>>(s.idx, B, c->ml_rows[sp], seed, batch);
+    NBG_LAUNCH_CHECK(c, "k_ml_sample");
+    int st = train_fb_grad(c, c->ml_theta[sp], c->ml_X[sp], c->ml_Y[sp], s.idx, B, false, s);
+    if (st) return st;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)t_adam), c2 = 1.f - powf(b2, (float)t_adam);
+    k_adam<<<(ML_NTRAIN + 255) / 256, 256, 0, c->stream>>>(c->ml_theta[sp], s.grad, s.m1[sp], s.m2[sp], ML_NTRAIN, lr,
+                                                           b1, b2, 1e-8f, c1, c2);
+    NBG_LAUNCH_CHECK(c, "k_adam");
+    return NBG_OK;
+}
+
+int launch_ml_batch_grad(nbg_ctx* c, const float* theta, const float* X, const float* Y, int B)
+{
+    if (!c->ml_attr) {
+        int st = launch_mlp_attrs(c);
+        if (st) return st;
+    }
+    return train_fb_grad(c, theta, X, Y, nullptr, B, true, c->ml_ts);
+}
+
+int launch_mlp_attrs(nbg_ctx* c)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
+    if (e != cudaSuccess) return cuda_fail(c, e, "k_mlp_bf16 shared memory");
+    e = cudaFuncSetAttribute(k_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (ML_ND * ML_NH + ML_NH * ML_NH) * (int)sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(c, e, "k_train_fb shared memory");
+    c->ml_attr = true;
+    return NBG_OK;
+}

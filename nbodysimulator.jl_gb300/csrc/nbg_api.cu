@@ -185,6 +185,8 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     const nbg_system_desc* d0 = &descs[0];
     c->desc = *d0;
     c->desc.mass = c->desc.charge = c->desc.dipole = nullptr;
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (c->sms < 1) c->sms = 1;
     c->nrep = nrep;
     uint32_t pots = d0->kind == NBG_SYSTEM_WATER ? (NBG_POT_LJ | NBG_POT_EL) : d0->potentials;
     int64_t n = 0;
@@ -593,7 +595,8 @@ static int status_error(nbg_ctx* c, unsigned st)
 {
     if (st & ST_NONFINITE) return fail(c, NBG_ERR_NONFINITE, "non-finite acceleration (NaN/Inf state or coincident bodies)");
     if (st & ST_RANGE) return fail(c, NBG_ERR_RANGE, "minimum-image loop exceeded its iteration cap");
-    if (st & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) return fail(c, NBG_ERR_CAPACITY, "list capacity exceeded");
+    if (st & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW))
+        return fail(c, NBG_ERR_CAPACITY, "list capacity exceeded");
     return NBG_OK;
 }
 
@@ -656,7 +659,11 @@ static size_t state_bytes(const nbg_ctx* c) { return sizeof(double) * 3 * (size_
 // The scratch view shares the split positions and the lists with the
 // resident state: the next resident step rebuilds the lists (every step
 // repacks the positions anyway).
-static void resident_dirty(nbg_ctx* c) { c->steps_since_build = -1; }
+static void resident_dirty(nbg_ctx* c)
+{
+    c->steps_since_build = -1;
+    c->respa_valid = false;
+}
 
 extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
 {
@@ -686,6 +693,7 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
     CK(cudaMemcpyAsync(c->st.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     c->state_valid = true;
     c->accel_valid = false;
+    c->respa_valid = false;
     c->T_valid = false;
     c->steps_since_build = -1;
     return NBG_OK;
@@ -927,6 +935,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
     if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
     int st;
+    c->respa_valid = false;  // a_old becomes the velocity-Verlet acceleration
     if ((st = clear_status(c))) return st;
     const bool em = is_em(c);
     if (!em && !c->accel_valid) {
@@ -1125,4 +1134,546 @@ extern "C" int nbg_pair_list(nbg_ctx* c, const double* u, int32_t which, int32_t
     }
     *count = total;
     return NBG_OK;
+}
+
+// ---------------------------------------------------------------------
+// learned short-range model of SPC/Fw water and r-RESPA (engine extension:
+// the reference has neither a learned model nor a multiple-time-step
+// integrator)
+// ---------------------------------------------------------------------
+static int ml_check(nbg_ctx* c)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (!c->ml_on) return fail(c, NBG_ERR_ARG, "learned model not enabled (call nbg_ml_enable)");
+    cudaSetDevice(c->device);
+    return NBG_OK;
+}
+
+static int ml_alloc_short(nbg_ctx* c, int scap)
+{
+    if (scap > 65535) return fail(c, NBG_ERR_CAPACITY, "short-list capacity above 65535");
+    if (c->ml_snbr) dfree(c, c->ml_snbr);
+    c->ml_snbr = nullptr;
+    c->ml_scap = scap;
+    return dalloc(c, &c->ml_snbr, (size_t)scap * c->n);
+}
+
+extern "C" int nbg_ml_param_count(void) { return ML_NPARAM; }
+
+extern "C" int nbg_ml_enable(nbg_ctx* c)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (c->ml_on) return NBG_OK;
+    if (c->d.kind != NBG_SYSTEM_WATER || c->path != PATH_LIST || c->nrep != 1 || c->d.bc != NBG_BC_CUBIC)
+        return fail(c, NBG_ERR_UNSUPPORTED,
+                    "the learned model needs one SPC/Fw water system on the Verlet-list path in a cubic box");
+    cudaSetDevice(c->device);
+    int st;
+    if (ml_init_constants() != NBG_OK) return fail(c, NBG_ERR_CUDA, "learned-model constants");
+    const int64_t n = c->n;
+    for (int s = 0; s < 2; ++s) {
+        if ((st = dalloc(c, &c->ml_theta[s], ML_NPARAM))) return st;
+        if ((st = dalloc(c, &c->ml_w1[s], 64 * 128))) return st;
+        if ((st = dalloc(c, &c->ml_w2[s], 128 * 128))) return st;
+        if ((st = dalloc(c, &c->ml_ts.m1[s], ML_NTRAIN))) return st;
+        if ((st = dalloc(c, &c->ml_ts.m2[s], ML_NTRAIN))) return st;
+    }
+    // unit normalisation until nbg_ml_normalize: sd = 1 (mean 0 from the zeroed allocation)
+    {
+        std::vector<float> th(ML_NPARAM, 0.0f);
+        for (int k = 0; k < 64; ++k) th[ML_NTRAIN + 64 + k] = 1.0f;
+        th[ML_NTRAIN + 129] = 1.0f;
+        for (int s = 0; s < 2; ++s)
+            CK(cudaMemcpyAsync(c->ml_theta[s], th.data(), sizeof(float) * ML_NPARAM, cudaMemcpyHostToDevice, c->stream),
+               "ml params");
+    }
+    const double L = c->desc.box[0];
+    const double rs = 0.6 + c->desc.skin;
+    const double expect = 4.0 / 3.0 * M_PI * rs * rs * rs * (double)n / (L * L * L);
+    const int scap = ((int)std::ceil(1.3 * expect + 32) + 7) / 8 * 8;
+    if ((st = ml_alloc_short(c, scap))) return st;
+    if ((st = dalloc(c, &c->ml_scnt, n))) return st;
+    if ((st = dalloc(c, &c->ml_x, 64 * n))) return st;
+    if ((st = dalloc(c, &c->ml_mom, 72 * n))) return st;
+    if ((st = dalloc(c, &c->ml_dx, 64 * n))) return st;
+    if ((st = dalloc(c, &c->ml_e, n))) return st;
+    if ((st = dalloc(c, &c->ml_fq, 3 * n))) return st;
+    if ((st = dalloc(c, &c->ml_fsr, 3 * n))) return st;
+    if ((st = dalloc(c, &c->ml_esr, n))) return st;
+    if ((st = dalloc(c, &c->ml_a_slow, 3 * c->cols))) return st;
+    c->ml_judge_cap = 64;
+    if ((st = dalloc(c, &c->ml_judge, 2 * c->ml_judge_cap))) return st;
+    if ((st = launch_mlp_attrs(c))) return st;
+    c->ml_on = true;
+    for (int s = 0; s < 2; ++s)
+        if ((st = launch_ml_pack(c, s))) return st;
+    CK(cudaStreamSynchronize(c->stream), "ml enable sync");
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_set_params(nbg_ctx* c, int32_t species, const float* theta)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if ((species != 0 && species != 1) || !theta) return fail(c, NBG_ERR_ARG, "species must be 0 (O) or 1 (H)");
+    CK(cudaMemcpyAsync(c->ml_theta[species], theta, sizeof(float) * ML_NPARAM, cudaMemcpyHostToDevice, c->stream),
+       "ml params upload");
+    if ((st = launch_ml_pack(c, species))) return st;
+    CK(cudaMemsetAsync(c->ml_ts.m1[species], 0, sizeof(float) * ML_NTRAIN, c->stream), "adam reset");
+    CK(cudaMemsetAsync(c->ml_ts.m2[species], 0, sizeof(float) * ML_NTRAIN, c->stream), "adam reset");
+    c->ml_adam_t[species] = 0;
+    c->respa_valid = false;
+    CK(cudaStreamSynchronize(c->stream), "ml params sync");
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_get_params(nbg_ctx* c, int32_t species, float* theta)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if ((species != 0 && species != 1) || !theta) return fail(c, NBG_ERR_ARG, "species must be 0 (O) or 1 (H)");
+    CK(cudaMemcpyAsync(theta, c->ml_theta[species], sizeof(float) * ML_NPARAM, cudaMemcpyDeviceToHost, c->stream),
+       "ml params download");
+    CK(cudaStreamSynchronize(c->stream), "ml params sync");
+    return NBG_OK;
+}
+
+// splitmix64 (Steele, Lea & Flood 2014) and Box-Muller normals for the host-side initialisation
+static uint64_t splitmix64(uint64_t& s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static double host_normal(uint64_t& s)
+{
+    const double u1 = ((splitmix64(s) >> 11) + 1.0) * (1.0 / 9007199254740993.0);
+    const double u2 = (splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2);
+}
+
+extern "C" int nbg_ml_init_params(nbg_ctx* c, uint64_t seed, double w1_scale)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    for (int s = 0; s < 2; ++s) {
+        std::vector<float> th(ML_NPARAM);
+        CK(cudaMemcpyAsync(th.data(), c->ml_theta[s], sizeof(float) * ML_NPARAM, cudaMemcpyDeviceToHost, c->stream),
+           "ml params download");
+        CK(cudaStreamSynchronize(c->stream), "ml params sync");
+        uint64_t r = seed * 2 + (uint64_t)s + 1;
+        int o = 0;
+        for (int k = 0; k < 64 * 128; ++k) th[o++] = (float)(w1_scale * host_normal(r) / 8.0);
+        for (int k = 0; k < 128; ++k) th[o++] = 0.0f;
+        for (int k = 0; k < 128 * 128; ++k) th[o++] = (float)(host_normal(r) / std::sqrt(128.0));
+        for (int k = 0; k < 128; ++k) th[o++] = 0.0f;
+        for (int k = 0; k < 128; ++k) th[o++] = (float)(host_normal(r) / std::sqrt(128.0));
+        th[o++] = 0.0f;
+        if ((st = nbg_ml_set_params(c, s, th.data()))) return st;
+    }
+    return NBG_OK;
+}
+
+// Short list, descriptors and (unless raw) the learned energies and forces
+// of the packed positions of state s. pos: time index of the positions.
+static int ml_forces(nbg_ctx* c, StepRef pos, bool force_short, bool raw)
+{
+    int st;
+    if ((st = launch_short_list(c, pos, force_short))) return st;
+    if ((st = launch_descriptor(c, raw))) return st;
+    if (raw) return NBG_OK;
+    if ((st = launch_mlp(c))) return st;
+    return launch_ml_force(c);
+}
+
+// One-off evaluation at host positions u (scratch view), with capacity
+// retries. what: 0 learned model, 1 raw descriptors only, 2 labels only.
+static int ml_eval_once(nbg_ctx* c, const double* u, int what)
+{
+    CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    resident_dirty(c);
+    c->respa_valid = false;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        int st;
+        if ((st = clear_status(c))) return st;
+        if ((st = launch_pack(c, c->ev))) return st;
+        if ((st = launch_list_build(c, c->ev, true, StepRef{0, nullptr}))) return st;
+        if (what == 2) {
+            if ((st = launch_short_list(c, StepRef{0, nullptr}, true))) return st;
+            if ((st = launch_sr_exact(c, c->ml_esr, c->ml_fsr))) return st;
+        } else if ((st = ml_forces(c, StepRef{0, nullptr}, true, what == 1))) {
+            return st;
+        }
+        unsigned w = 0;
+        if ((st = read_status(c, &w))) return st;
+        if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+        if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW)) {
+            if ((w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && (st = grow_lists(c, w))) return st;
+            if ((w & ST_SHORT_OVERFLOW) && (st = ml_alloc_short(c, c->ml_scap + c->ml_scap / 2 + 32))) return st;
+            continue;
+        }
+        return NBG_OK;
+    }
+    return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
+}
+
+extern "C" int nbg_ml_descriptors(nbg_ctx* c, const double* u, int32_t standardised, float* desc)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (!u || !desc) return fail(c, NBG_ERR_ARG, "null argument");
+    if ((st = ml_eval_once(c, u, standardised ? 0 : 1))) return st;
+    CK(cudaMemcpyAsync(desc, c->ml_x, sizeof(float) * 64 * c->n, cudaMemcpyDeviceToHost, c->stream), "desc download");
+    CK(cudaStreamSynchronize(c->stream), "desc sync");
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_eval(nbg_ctx* c, const double* u, float* energies, double* forces)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (!u) return fail(c, NBG_ERR_ARG, "null positions");
+    if ((st = ml_eval_once(c, u, 0))) return st;
+    if (energies)
+        CK(cudaMemcpyAsync(energies, c->ml_e, sizeof(float) * c->n, cudaMemcpyDeviceToHost, c->stream), "e download");
+    if (forces) {
+        if ((st = launch_ml_force_out(c, c->ev.a_new))) return st;
+        CK(cudaMemcpyAsync(forces, c->ev.a_new, sizeof(double) * 3 * c->n, cudaMemcpyDeviceToHost, c->stream),
+           "f download");
+    }
+    CK(cudaStreamSynchronize(c->stream), "eval sync");
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_labels(nbg_ctx* c, const double* u, float* energies, float* forces)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (!u) return fail(c, NBG_ERR_ARG, "null positions");
+    if ((st = ml_eval_once(c, u, 2))) return st;
+    if (energies)
+        CK(cudaMemcpyAsync(energies, c->ml_esr, sizeof(float) * c->n, cudaMemcpyDeviceToHost, c->stream), "e download");
+    if (forces)
+        CK(cudaMemcpyAsync(forces, c->ml_fsr, sizeof(float) * 3 * c->n, cudaMemcpyDeviceToHost, c->stream),
+           "f download");
+    CK(cudaStreamSynchronize(c->stream), "labels sync");
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_reserve(nbg_ctx* c, int64_t frames)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (frames < 1) return fail(c, NBG_ERR_ARG, "frames must be >= 1");
+    for (int s = 0; s < 2; ++s) {
+        const int64_t cap = frames * (s == 0 ? c->n / 3 : 2 * (c->n / 3));
+        if (c->ml_X[s]) dfree(c, c->ml_X[s]);
+        if (c->ml_Y[s]) dfree(c, c->ml_Y[s]);
+        c->ml_X[s] = nullptr;
+        c->ml_Y[s] = nullptr;
+        if ((st = dalloc(c, &c->ml_X[s], (size_t)cap * 64))) return st;
+        if ((st = dalloc(c, &c->ml_Y[s], (size_t)cap))) return st;
+        c->ml_cap[s] = cap;
+        c->ml_rows[s] = 0;
+    }
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_collect(nbg_ctx* c, int64_t* rows)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
+    if (!c->ml_X[0]) return fail(c, NBG_ERR_ARG, "no training set (call nbg_ml_reserve)");
+    const int64_t per[2] = {c->n / 3, 2 * (c->n / 3)};
+    if (c->ml_rows[0] + per[0] > c->ml_cap[0] || c->ml_rows[1] + per[1] > c->ml_cap[1])
+        return fail(c, NBG_ERR_CAPACITY, "training set full");
+    // evaluate on the resident positions through the scratch path
+    std::vector<double> u(3 * (size_t)c->cols);
+    CK(cudaMemcpyAsync(u.data(), c->st.x, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "u download");
+    CK(cudaStreamSynchronize(c->stream), "collect sync");
+    if ((st = ml_eval_once(c, u.data(), 1))) return st;
+    if ((st = launch_sr_exact(c, c->ml_esr, nullptr))) return st;
+    for (int s = 0; s < 2; ++s) {
+        if ((st = launch_ml_collect(c, s, c->ml_rows[s]))) return st;
+        c->ml_rows[s] += per[s];
+    }
+    CK(cudaStreamSynchronize(c->stream), "collect sync");
+    if (rows) {
+        rows[0] = c->ml_rows[0];
+        rows[1] = c->ml_rows[1];
+    }
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_normalize(nbg_ctx* c)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (c->ml_rows[0] < 2 || c->ml_rows[1] < 2) return fail(c, NBG_ERR_ARG, "training set holds fewer than 2 rows");
+    for (int s = 0; s < 2; ++s)
+        if ((st = launch_ml_stats(c, s))) return st;
+    c->respa_valid = false;
+    CK(cudaStreamSynchronize(c->stream), "normalize sync");
+    return NBG_OK;
+}
+
+static int ml_scratch(nbg_ctx* c, int B)
+{
+    MLTrainScratch& s = c->ml_ts;
+    if (s.B >= B) return NBG_OK;
+    float** bufs[] = {&s.xs, &s.a1, &s.a2, &s.g1, &s.g2, &s.eo, &s.grad};
+    for (float** p : bufs) {
+        if (*p) dfree(c, *p);
+        *p = nullptr;
+    }
+    if (s.idx) dfree(c, s.idx);
+    if (s.loss) dfree(c, s.loss);
+    s.idx = nullptr;
+    s.loss = nullptr;
+    int st;
+    if ((st = dalloc(c, &s.idx, B))) return st;
+    if ((st = dalloc(c, &s.xs, (size_t)B * 64))) return st;
+    if ((st = dalloc(c, &s.a1, (size_t)B * 128))) return st;
+    if ((st = dalloc(c, &s.a2, (size_t)B * 128))) return st;
+    if ((st = dalloc(c, &s.g1, (size_t)B * 128))) return st;
+    if ((st = dalloc(c, &s.g2, (size_t)B * 128))) return st;
+    if ((st = dalloc(c, &s.eo, B))) return st;
+    if ((st = dalloc(c, &s.grad, ML_NTRAIN))) return st;
+    if ((st = dalloc(c, &s.loss, 1))) return st;
+    s.B = B;
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_train(nbg_ctx* c, int64_t steps, int32_t batch, double lr, uint64_t seed, double* loss)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (steps < 0 || batch < 1 || !(lr > 0.0)) return fail(c, NBG_ERR_ARG, "steps >= 0, batch >= 1, lr > 0");
+    if (c->ml_rows[0] < 1 || c->ml_rows[1] < 1) return fail(c, NBG_ERR_ARG, "empty training set");
+    if ((st = ml_scratch(c, batch))) return st;
+    // loss of the last min(steps, 100) batches per species
+    const int64_t tail = std::min<int64_t>(steps, 100);
+    for (int s = 0; s < 2; ++s) {
+        CK(cudaMemsetAsync(c->ml_ts.loss, 0, sizeof(double), c->stream), "loss clear");
+        for (int64_t t = 0; t < steps; ++t) {
+            if (t == steps - tail) CK(cudaMemsetAsync(c->ml_ts.loss, 0, sizeof(double), c->stream), "loss clear");
+            // cosine schedule over this call
+            const double f = 0.5 * (1.0 + std::cos(M_PI * (double)t / (double)steps));
+            c->ml_adam_t[s] += 1;
+            if ((st = launch_ml_train_step(c, s, batch, seed * 2 + (uint64_t)s, (uint64_t)c->ml_adam_t[s],
+                                           (float)(lr * f), c->ml_adam_t[s])))
+                return st;
+        }
+        if ((st = launch_ml_pack(c, s))) return st;
+        double l = 0.0;
+        CK(cudaMemcpyAsync(&l, c->ml_ts.loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "loss read");
+        CK(cudaStreamSynchronize(c->stream), "train sync");
+        if (loss) loss[s] = tail > 0 ? l / (double)tail : 0.0;
+    }
+    c->respa_valid = false;
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_batch_gradient(nbg_ctx* c, int32_t species, const float* x, const float* y, int32_t B,
+                                     float* grad, double* loss)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if ((species != 0 && species != 1) || !x || !y || !grad || B < 1) return fail(c, NBG_ERR_ARG, "bad arguments");
+    if ((st = ml_scratch(c, B))) return st;
+    float *dX = nullptr, *dY = nullptr;
+    CK(cudaMallocAsync((void**)&dX, sizeof(float) * 64 * (size_t)B, c->stream), "batch alloc");
+    CK(cudaMallocAsync((void**)&dY, sizeof(float) * (size_t)B, c->stream), "batch alloc");
+    CK(cudaMemcpyAsync(dX, x, sizeof(float) * 64 * (size_t)B, cudaMemcpyHostToDevice, c->stream), "batch upload");
+    CK(cudaMemcpyAsync(dY, y, sizeof(float) * (size_t)B, cudaMemcpyHostToDevice, c->stream), "batch upload");
+    CK(cudaMemsetAsync(c->ml_ts.loss, 0, sizeof(double), c->stream), "loss clear");
+    st = launch_ml_batch_grad(c, c->ml_theta[species], dX, dY, B);
+    cudaFreeAsync(dX, c->stream);
+    cudaFreeAsync(dY, c->stream);
+    if (st) return st;
+    CK(cudaMemcpyAsync(grad, c->ml_ts.grad, sizeof(float) * ML_NTRAIN, cudaMemcpyDeviceToHost, c->stream),
+       "grad download");
+    double l = 0.0;
+    CK(cudaMemcpyAsync(&l, c->ml_ts.loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "loss read");
+    CK(cudaStreamSynchronize(c->stream), "grad sync");
+    if (loss) *loss = l;
+    return NBG_OK;
+}
+
+extern "C" int nbg_ml_rows(nbg_ctx* c, int64_t* rows)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (!rows) return NBG_ERR_ARG;
+    rows[0] = c->ml_rows[0];
+    rows[1] = c->ml_rows[1];
+    return NBG_OK;
+}
+
+// r-RESPA state of the resident positions: a_old = fast (bonded + learned)
+// and ml_a_slow = slow (exact non-bonded - learned) accelerations.
+static int respa_inner_force(nbg_ctx* c, StepRef pos, bool force_short, bool exact)
+{
+    return exact ? launch_sr_inner(c, pos, force_short) : ml_forces(c, pos, force_short, false);
+}
+
+static int respa_init(nbg_ctx* c, bool exact)
+{
+    int st;
+    const StateView& s = c->st;
+    const StepRef pos{c->step, nullptr};
+    if ((st = launch_pack(c, s))) return st;
+    if ((st = launch_list_build(c, s, true, pos))) return st;
+    c->steps_since_build = 0;
+    if ((st = respa_inner_force(c, pos, true, exact))) return st;
+    if ((st = launch_ml_accel(c, 0, s.a_old))) return st;
+    StateView sb = s;
+    sb.a_new = s.a_old;
+    if ((st = launch_bonded(c, sb))) return st;
+    StateView ss = s;
+    ss.a_new = c->ml_a_slow;
+    if ((st = launch_force_list(c, ss))) return st;
+    if ((st = launch_ml_accel(c, -1, c->ml_a_slow))) return st;
+    c->respa_valid = true;
+    c->respa_exact = exact;
+    c->accel_valid = false;  // a_old no longer holds the velocity-Verlet acceleration
+    c->T_valid = false;
+    return NBG_OK;
+}
+
+// One outer step (Tuckerman, Berne & Martyna 1992): slow half kick, `inner`
+// velocity-Verlet steps of the fast force, the exact force at the new
+// positions (slow force and judge), slow half kick. sr.off: step index of
+// the outer step's start, counted in inner steps.
+static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, bool exact)
+{
+    int st;
+    const StateView& s = c->st;
+    const double H = 0.5 * dt * inner;
+    const bool berendsen = c->d.therm == NBG_THERMO_BERENDSEN;
+    if (berendsen && (st = launch_temperature(c, s.v))) return st;
+    if ((st = launch_respa_kick(c, s.v, c->ml_a_slow, H, true))) return st;
+    for (int m = 0; m < inner; ++m) {
+        const StepRef pos{sr.off + m + 1, sr.base};
+        if ((st = launch_drift(c, s, dt, pos))) return st;
+        const bool force = rebuild_due(c, true);
+        if ((st = launch_list_build(c, s, force, pos))) return st;
+        c->steps_since_build = force ? 0 : c->steps_since_build + 1;
+        if ((st = respa_inner_force(c, pos, force, exact))) return st;
+        if ((st = launch_ml_accel(c, 0, s.a_new))) return st;
+        if ((st = launch_bonded(c, s))) return st;
+        if ((st = launch_kick(c, s, dt, false, false))) return st;
+    }
+    StateView ss = s;
+    ss.a_new = c->ml_a_slow;
+    if ((st = launch_force_list(c, ss))) return st;
+    if ((st = launch_ml_accel(c, -1, c->ml_a_slow))) return st;
+    if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
+    if ((st = launch_ml_judge(c, StepRef{sr.off + inner, sr.base}, inner, c->ml_judge_cap))) return st;
+    if (berendsen && (st = launch_temperature(c, s.v))) return st;
+    return launch_respa_kick(c, s.v, c->ml_a_slow, H, true);
+}
+
+extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,
+                             nbg_respa_stats* out)
+{
+    const bool exact = (flags & NBG_RESPA_EXACT_SPLIT) != 0;
+    int st = ml_check(c);
+    if (st) return st;
+    if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
+    if (!(dt > 0.0) || inner < 1 || outer < 0) return fail(c, NBG_ERR_ARG, "dt > 0, inner >= 1, outer >= 0");
+    if (c->d.therm != NBG_THERMO_NULL && c->d.therm != NBG_THERMO_BERENDSEN)
+        return fail(c, NBG_ERR_UNSUPPORTED, "r-RESPA supports no thermostat or Berendsen");
+    nbg_respa_stats S{};
+    const int64_t chunk = c->ml_judge_cap;
+    Backup b;
+    double* b_slow = nullptr;
+    if ((st = backup_alloc(c, b))) return st;
+    if ((st = dalloc(c, &b_slow, 3 * c->cols))) {
+        backup_free(c, b);
+        return st;
+    }
+    auto done_with = [&](int code) {
+        backup_free(c, b);
+        dfree(c, b_slow);
+        c->accel_valid = false;
+        if (out) *out = S;
+        return code;
+    };
+    if ((st = clear_status(c))) return done_with(st);
+    int64_t done = 0;
+    int retries = 0;
+    std::vector<double> judge(2 * (size_t)chunk);
+    while (done < outer) {
+        const int64_t k = std::min<int64_t>(chunk, outer - done);
+        if ((!c->respa_valid || c->respa_exact != exact) && (st = respa_init(c, exact))) return done_with(st);
+        const int64_t step0 = c->step;
+        const int64_t ssb0 = c->steps_since_build;
+        const size_t sb = state_bytes(c);
+        CK(cudaMemcpyAsync(b.x, c->st.x, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
+        CK(cudaMemcpyAsync(b.v, c->st.v, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
+        CK(cudaMemcpyAsync(b.a, c->st.a_old, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
+        CK(cudaMemcpyAsync(b_slow, c->ml_a_slow, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
+        CK(cudaMemsetAsync(c->ml_judge, 0, sizeof(double) * 2 * chunk, c->stream), "judge clear");
+        for (int64_t o = 0; o < k && st == NBG_OK; ++o) {
+            st = respa_outer(c, dt, inner, StepRef{c->step, nullptr}, exact);
+            c->step += inner;
+        }
+        if (st) return done_with(st);
+        unsigned w = 0;
+        if ((st = read_status(c, &w))) return done_with(st);
+        CK(cudaMemcpyAsync(judge.data(), c->ml_judge, sizeof(double) * 2 * chunk, cudaMemcpyDeviceToHost, c->stream),
+           "judge read");
+        CK(cudaStreamSynchronize(c->stream), "judge sync");
+        auto restore = [&]() -> int {
+            CK(cudaMemcpyAsync(c->st.x, b.x, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
+            CK(cudaMemcpyAsync(c->st.v, b.v, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
+            CK(cudaMemcpyAsync(c->st.a_old, b.a, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
+            CK(cudaMemcpyAsync(c->ml_a_slow, b_slow, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
+            c->step = step0;
+            c->steps_since_build = ssb0;
+            c->T_valid = false;
+            return clear_status(c);
+        };
+        if (w & (ST_NONFINITE | ST_RANGE)) return done_with(status_error(c, w));
+        if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW)) {
+            if (++retries > 6) return done_with(fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough"));
+            if ((w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && (st = grow_lists(c, w))) return done_with(st);
+            if ((w & ST_SHORT_OVERFLOW) && (st = ml_alloc_short(c, c->ml_scap + c->ml_scap / 2 + 32)))
+                return done_with(st);
+            if ((st = restore())) return done_with(st);
+            c->respa_valid = false;  // lists were reallocated: rebuild everything at the chunk start
+            continue;
+        }
+        // the judge: relative RMS error of the learned against the exact short-range force
+        double jmax = 0.0, jsum = 0.0;
+        for (int64_t o = 0; o < k; ++o) {
+            const int64_t slot = ((step0 / inner + o + 1) % chunk + chunk) % chunk;
+            const double num = judge[2 * slot], den = judge[2 * slot + 1];
+            const double r = den > 0.0 ? std::sqrt(num / den) : (num > 0.0 ? INFINITY : 0.0);
+            jmax = std::max(jmax, r);
+            jsum += r;
+        }
+        if (threshold > 0.0 && !(jmax <= threshold)) {
+            // fallback: the chunk again by plain velocity Verlet with the exact force
+            if ((st = restore())) return done_with(st);
+            c->respa_valid = false;
+            c->accel_valid = false;
+            if ((st = advance_impl(c, dt, k * inner))) return done_with(st);
+            S.outer_fallback += k;
+            S.judge_last = jmax;
+        } else {
+            S.outer_mts += k;
+            S.judged += k;
+            S.judge_mean += jsum;
+            S.judge_max = std::max(S.judge_max, jmax);
+            S.judge_last = jmax;
+        }
+        done += k;
+    }
+    if (S.judged > 0) S.judge_mean /= (double)S.judged;
+    return done_with(NBG_OK);
 }

@@ -13,6 +13,7 @@
 //   cell_count/cell_atoms, nbr/nbr_count, xref : cell and Verlet lists.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -27,6 +28,7 @@
 #define ST_NBR_OVERFLOW 2u
 #define ST_NONFINITE 4u
 #define ST_RANGE 8u
+#define ST_SHORT_OVERFLOW 16u  // learned-model short list
 
 // atom flags (plo.w bits)
 #define AF_LJ 1
@@ -106,6 +108,29 @@ struct Dev {
     int grav_plain;
 };
 
+// learned short-range model (k_learned.cu; oracle/learned.py restates it)
+#define ML_RD 0.6f     // descriptor cutoff (nm)
+#define ML_R0 0.07f    // first radial centre
+#define ML_W ((ML_RD - ML_R0) / 23.0f)
+#define ML_RS 0.45f    // start of the short-range switch
+#define ML_ALPHA 4.0f  // Coulomb screening of the short-range target (1/nm)
+#define ML_RHO0 0.1f   // angular envelope widths
+#define ML_RHO1 0.2f
+#define ML_RHO2 0.3f
+#define ML_RHO3 10.0f
+#define ML_NTRAIN (64 * 128 + 128 + 128 * 128 + 128 + 128 + 1)  // trainable parameters per species
+#define ML_NPARAM (ML_NTRAIN + 2 * 64 + 2)                      // plus mean/sd of inputs and label
+
+struct MLTrainScratch {
+    int* idx = nullptr;
+    float *xs = nullptr, *a1 = nullptr, *a2 = nullptr, *g1 = nullptr, *g2 = nullptr, *eo = nullptr;
+    float* grad = nullptr;
+    float* m1[2] = {nullptr, nullptr};  // Adam moments per species
+    float* m2[2] = {nullptr, nullptr};
+    double* loss = nullptr;
+    int B = 0;  // batch capacity of the scratch
+};
+
 struct StateView {
     double* x;
     double* v;
@@ -152,6 +177,29 @@ struct nbg_ctx {
     unsigned* kick_counter = nullptr;
     int kick_blocks = 0;
     bool T_valid = false;        // red_T holds T of the resident velocities
+    int sms = 0;                 // multiprocessors of the device
+    // learned short-range model (water)
+    bool ml_on = false;
+    bool ml_attr = false;        // large shared-memory opt-ins done
+    float* ml_theta[2] = {nullptr, nullptr};
+    __nv_bfloat16* ml_w1[2] = {nullptr, nullptr};
+    __nv_bfloat16* ml_w2[2] = {nullptr, nullptr};
+    int* ml_snbr = nullptr;
+    int* ml_scnt = nullptr;
+    int ml_scap = 0;
+    float *ml_x = nullptr, *ml_mom = nullptr, *ml_dx = nullptr, *ml_e = nullptr;
+    unsigned long long* ml_fq = nullptr;
+    float *ml_fsr = nullptr, *ml_esr = nullptr;
+    float* ml_X[2] = {nullptr, nullptr};
+    float* ml_Y[2] = {nullptr, nullptr};
+    int64_t ml_rows[2] = {0, 0}, ml_cap[2] = {0, 0};
+    MLTrainScratch ml_ts;
+    int64_t ml_adam_t[2] = {0, 0};
+    double* ml_judge = nullptr;  // per outer step: sum |F_ml - F_sr|^2, sum |F_sr|^2
+    int ml_judge_cap = 0;
+    double* ml_a_slow = nullptr;  // r-RESPA slow acceleration (exact non-bonded - learned)
+    bool respa_valid = false;     // a_old holds the fast and ml_a_slow the slow acceleration of st
+    bool respa_exact = false;     // fast force of respa_valid: exact short-range (true) or learned
     std::vector<cudaEvent_t> prof_events;  // start/stop pairs not yet read
     double prof_ms = 0.0;
     int64_t prof_count = 0;
@@ -179,7 +227,7 @@ int launch_force_list(nbg_ctx* c, const StateView& s);
 int launch_bonded(nbg_ctx* c, const StateView& s);
 int launch_drift(nbg_ctx* c, const StateView& s, double dt, StepRef pos);
 int launch_temperature(nbg_ctx* c, const double* v);
-int launch_kick(nbg_ctx* c, const StateView& s, double dt, bool do_T);
+int launch_kick(nbg_ctx* c, const StateView& s, double dt, bool do_T, bool thermo = true);
 int launch_andersen(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_step_advance(nbg_ctx* c, int64_t by);
@@ -190,6 +238,26 @@ int launch_rhs_thermostat(nbg_ctx* c, const StateView& s);
 int gravity_plan_chunks(nbg_ctx* c, int64_t npad);
 int launch_energy(nbg_ctx* c, const StateView& s, double* out_host /*[8]*/);
 int launch_pairs(nbg_ctx* c, const StateView& s, int which, int* out_j, int* out_cnt, int64_t cap_per_atom);
+
+// learned short-range model and r-RESPA (k_learned.cu)
+int ml_init_constants();
+size_t ml_mlp_smem();
+int launch_mlp_attrs(nbg_ctx* c);
+int launch_short_list(nbg_ctx* c, StepRef pos, bool force);
+int launch_descriptor(nbg_ctx* c, bool raw);
+int launch_mlp(nbg_ctx* c);
+int launch_ml_force(nbg_ctx* c);
+int launch_sr_exact(nbg_ctx* c, float* e_out, float* f_out);
+int launch_ml_accel(nbg_ctx* c, int mode, double* a);
+int launch_ml_force_out(nbg_ctx* c, double* f);
+int launch_sr_inner(nbg_ctx* c, StepRef pos, bool force_short);
+int launch_ml_judge(nbg_ctx* c, StepRef sr, int inner, int slots);
+int launch_respa_kick(nbg_ctx* c, double* v, const double* a, double h, bool thermo);
+int launch_ml_pack(nbg_ctx* c, int sp);
+int launch_ml_collect(nbg_ctx* c, int sp, int64_t off);
+int launch_ml_stats(nbg_ctx* c, int sp);
+int launch_ml_train_step(nbg_ctx* c, int sp, int B, uint64_t seed, uint64_t batch, float lr, int64_t t_adam);
+int launch_ml_batch_grad(nbg_ctx* c, const float* theta, const float* X, const float* Y, int B);
 
 // events around the dominant force kernel when profiling is on
 void prof_begin(nbg_ctx* c);
@@ -377,6 +445,33 @@ __device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, in
     o.fy = factor * dr.y;
     o.fz = factor * dr.z;
     return o;
+}
+
+// Split one atom's position into (hi, lo) floats (see the layout note above).
+__device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double* X)
+{
+    const RepDev& R = d.reps[d.rep_of[i]];
+    double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+    float h[3], l[3];
+    if (d.bc == NBG_BC_CUBIC) {
+        for (int k = 0; k < 3; ++k) {
+            double w = p[k] - R.L * floor(p[k] * R.invL);
+            if (w < 0.0) w += R.L;
+            if (w >= R.L) w -= R.L;
+            double hq = rint(w * (double)R.qscale) * (double)R.qinv;
+            h[k] = (float)hq;
+            l[k] = (float)(w - hq);
+        }
+    } else {
+        for (int k = 0; k < 3; ++k) {
+            h[k] = (float)p[k];
+            l[k] = (float)(p[k] - (double)h[k]);
+        }
+    }
+    float4 hi = d.phi[i];
+    float4 lo = d.plo[i];
+    d.phi[i] = make_float4(h[0], h[1], h[2], hi.w);
+    d.plo[i] = make_float4(l[0], l[1], l[2], lo.w);
 }
 
 // TwoSum: s + e = a + b exactly (Knuth).

@@ -135,3 +135,89 @@ class Engine:
     @property
     def kernel_launches(self):
         return int(self.lib.nbg_kernel_launches(self.ctx))
+
+    # ------------------------------------------------------------------
+    # learned short-range model and r-RESPA (SPC/Fw water on the list path)
+    # ------------------------------------------------------------------
+    def ml_enable(self):
+        self._chk(self.lib.nbg_ml_enable(self.ctx))
+
+    def ml_set_params(self, species, theta):
+        theta = np.ascontiguousarray(theta, dtype=np.float32)
+        if theta.size != _abi.NBG_ML_NPARAM:
+            raise ValueError(f"expected {_abi.NBG_ML_NPARAM} parameters, got {theta.size}")
+        self._chk(self.lib.nbg_ml_set_params(self.ctx, int(species), _abi.as_fptr(theta)))
+
+    def ml_get_params(self, species):
+        theta = np.zeros(_abi.NBG_ML_NPARAM, dtype=np.float32)
+        self._chk(self.lib.nbg_ml_get_params(self.ctx, int(species), _abi.as_fptr(theta)))
+        return theta
+
+    def ml_init_params(self, seed=0, w1_scale=0.1):
+        self._chk(self.lib.nbg_ml_init_params(self.ctx, int(seed), float(w1_scale)))
+
+    def ml_descriptors(self, u, standardised=False):
+        u = _f64(u)
+        out = np.zeros((u.shape[0], 64), dtype=np.float32)
+        self._chk(self.lib.nbg_ml_descriptors(self.ctx, _abi.as_dptr(u), 1 if standardised else 0,
+                                              _abi.as_fptr(out)))
+        return out
+
+    def ml_eval(self, u):
+        """Learned per-atom energies (n,) float32 and forces (n, 3) float64."""
+        u = _f64(u)
+        e = np.zeros(u.shape[0], dtype=np.float32)
+        f = np.zeros((u.shape[0], 3))
+        self._chk(self.lib.nbg_ml_eval(self.ctx, _abi.as_dptr(u), _abi.as_fptr(e), _abi.as_dptr(f)))
+        return e, f
+
+    def ml_labels(self, u):
+        """Exact short-range per-atom energies (n,) and forces (n, 3), float32."""
+        u = _f64(u)
+        e = np.zeros(u.shape[0], dtype=np.float32)
+        f = np.zeros((u.shape[0], 3), dtype=np.float32)
+        self._chk(self.lib.nbg_ml_labels(self.ctx, _abi.as_dptr(u), _abi.as_fptr(e), _abi.as_fptr(f)))
+        return e, f
+
+    def ml_reserve(self, frames):
+        self._chk(self.lib.nbg_ml_reserve(self.ctx, int(frames)))
+
+    def ml_collect(self):
+        rows = (ctypes.c_int64 * 2)()
+        self._chk(self.lib.nbg_ml_collect(self.ctx, rows))
+        return int(rows[0]), int(rows[1])
+
+    def ml_rows(self):
+        rows = (ctypes.c_int64 * 2)()
+        self._chk(self.lib.nbg_ml_rows(self.ctx, rows))
+        return int(rows[0]), int(rows[1])
+
+    def ml_normalize(self):
+        self._chk(self.lib.nbg_ml_normalize(self.ctx))
+
+    def ml_train(self, steps, batch=2048, lr=1e-3, seed=0):
+        """Adam steps per species; returns the mean loss of the last batches (O, H)."""
+        loss = np.zeros(2)
+        self._chk(self.lib.nbg_ml_train(self.ctx, int(steps), int(batch), float(lr), int(seed),
+                                        _abi.as_dptr(loss)))
+        return float(loss[0]), float(loss[1])
+
+    def ml_batch_gradient(self, species, x, y):
+        """(loss, gradient of the NBG_ML_NTRAIN trainable parameters) on
+        standardised inputs x (B, 64) and targets y (B,)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(_abi.NBG_ML_NTRAIN, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._chk(self.lib.nbg_ml_batch_gradient(self.ctx, int(species), _abi.as_fptr(x), _abi.as_fptr(y),
+                                                 int(len(y)), _abi.as_fptr(g), ctypes.byref(loss)))
+        return loss.value, g
+
+    def respa_run(self, dt, inner, outer, threshold=0.02, exact_split=False):
+        """Advance the resident state by `outer` r-RESPA steps; returns the
+        stats struct. exact_split: exact short-range force as the fast force."""
+        stats = _abi.NbgRespaStats()
+        flags = _abi.NBG_RESPA_EXACT_SPLIT if exact_split else 0
+        self._chk(self.lib.nbg_respa_run(self.ctx, float(dt), int(inner), int(outer), float(threshold), flags,
+                                         ctypes.byref(stats)))
+        return stats

@@ -18,11 +18,14 @@ has an FP64 counterpart:
     z1 = x W1 + b1, a1 = tanh z1, z2 = a1 W2 + b2, a2 = tanh z2,
     E = sd_E (a2 . w3 + b3) + mu_E
   short-range label: E_i = 1/2 sum_{j, other molecule} phi(r) S(r),
-    phi = LJ (O-O) + k q_i q_j / r, S = 1 below RS, C2 smoothstep to 0 at RD.
+    phi = LJ (O-O) + k q_i q_j erfc(ALPHA r) / r (the real-space part of an
+    Ewald-type split of the Coulomb term), S = 1 below RS, C2 smoothstep to 0
+    at RD.
 """
 import math
 
 import numpy as np
+from scipy.special import erfc
 
 RD = 0.6
 R0 = 0.07
@@ -30,6 +33,7 @@ NK = 24
 W = (RD - R0) / (NK - 1)
 RS = 0.45
 RHO = (0.1, 0.2, 0.3, 10.0)
+ALPHA = 4.0
 NDESC = 64
 NH1 = 128
 NH2 = 128
@@ -186,8 +190,10 @@ def short_range_labels(u, L, q, lj_eps, lj_sigma, k_el):
     for i in range(n):
         j, d, r = neighbours(u, L, i)
         S, dS = smoothstep(r)
-        phi = k_el * q[i] * q[j] / r
-        dphi = -k_el * q[i] * q[j] / (r * r)
+        kqq = k_el * q[i] * q[j]
+        ec = erfc(ALPHA * r)
+        phi = kqq * ec / r
+        dphi = -kqq * ec / (r * r) - kqq * (2.0 * ALPHA / math.sqrt(math.pi)) * np.exp(-(ALPHA * r) ** 2) / r
         if i % 3 == 0:
             o = j % 3 == 0
             sr6 = (lj_sigma / r[o]) ** 6

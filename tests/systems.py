@@ -164,3 +164,19 @@ def state(sim):
 
 def rel_rmse(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def spcfw_water_rf(n_mol, thermo=True, eps_rf=78.5, seed=0, T=300.0):
+    """SPC/Fw water (the benchmark parameters) with reaction-field
+    electrostatics at 0.9 nm (dielectric eps_rf), Berendsen 300 K or no
+    thermostat; the system the learned short-range model is trained on."""
+    pos, vel, L = nbg.workloads.spcfw_water_box(n_mol, seed=seed, T=T)
+    bodies = nbg.workloads.water_molecules(pos, vel)
+    lj = nbg.LennardJonesParameters(0.650299, 0.3165492, 0.9)
+    el = nbg.ElectrostaticParameters(nbg.workloads.K_EL, 0.9, eps_rf)
+    spc = nbg.SPCFwParameters(0.1012, 113.24 * math.pi / 180, nbg.workloads.SPCFW_KB, nbg.workloads.SPCFW_KA)
+    water = nbg.WaterSPCFw(bodies, nbg.workloads.M_H, nbg.workloads.M_O, 0.41, -0.82, lj, el, spc)
+    th = nbg.BerendsenThermostat(T, 0.1) if thermo else nbg.NullThermostat()
+    sim = nbg.NBodySimulation(water, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), th,
+                              kb=nbg.workloads.KB_KJ, skin=0.1, rebuild_every=10)
+    return sim, pos, vel, L

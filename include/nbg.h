@@ -338,6 +338,14 @@ NBG_API int nbg_ml_batch_gradient(nbg_ctx* ctx, int32_t species, const float* x,
 NBG_API int nbg_respa_run(nbg_ctx* ctx, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,
                           nbg_respa_stats* stats);
 
+/* Change a replica's thermostat target temperature (the reference builds a
+   new simulation with another thermostat; this keeps the context). */
+NBG_API int nbg_set_thermostat_target(nbg_ctx* ctx, int32_t replica, double T);
+/* Device time (ms, averaged over `reps` runs on the resident positions) of
+   the learned-force kernels: [0] short list, [1] descriptors, [2] MLP
+   forward and backward (BF16 tensor cores), [3] force scatter. */
+NBG_API int nbg_ml_kernel_times(nbg_ctx* ctx, int32_t reps, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

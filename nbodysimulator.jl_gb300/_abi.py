@@ -155,6 +155,8 @@ SIGNATURES = {
     "nbg_ml_batch_gradient": (ctypes.c_int, [_vp, ctypes.c_int32, _fp, _fp, ctypes.c_int32, _fp, _dp]),
     "nbg_respa_run": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
                                      ctypes.c_int32, ctypes.POINTER(NbgRespaStats)]),
+    "nbg_set_thermostat_target": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_double]),
+    "nbg_ml_kernel_times": (ctypes.c_int, [_vp, ctypes.c_int32, _dp]),
 }
 
 _lib = None

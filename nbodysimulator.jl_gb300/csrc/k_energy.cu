@@ -75,6 +75,65 @@ __global__ void __launch_bounds__(EB) k_energy_pairs(Dev d, const double* X, dou
         for (int k = 0; k < 3; ++k) out[blockIdx.x * 3 + k] = sh[k][0];
 }
 
+// The same LJ and electrostatic sums over the Verlet list (built for X):
+// for each pair inside a cutoff, its term minus the term the reference gives
+// a pair beyond it (LJ at r = R, Coulomb q_i q_j / R); the host adds those
+// constant terms for all pairs analytically. O(N x neighbours) instead of
+// O(N^2); each pair is taken once (j > i) with the same FP64 minimum image.
+__global__ void __launch_bounds__(EB) k_energy_list(Dev d, const double* X, double* out /*[grid][2]*/)
+{
+    const RepDev& R = d.reps[0];
+    double e_lj = 0.0, e_el = 0.0;
+    bool range_err = false;
+    const bool water = d.kind == NBG_SYSTEM_WATER;
+    double s6R = d.lj_sig2_d / d.lj_R2;
+    s6R = __dmul_rn(__dmul_rn(s6R, s6R), s6R);
+    const double ljR = __dsub_rn(__dmul_rn(s6R, s6R), s6R);
+    const double invR = 1.0 / d.el_R;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double* xi = X + 3 * i;
+        const bool lj_i = (d.pots & NBG_POT_LJ) && (!water || i % 3 == 0);
+        const int cnt = d.nbr_count[i];
+        double el_i = 0.0;
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t j = d.nbr[(int64_t)k * d.nbr_kstride + i * d.nbr_istride];
+            if (j <= i) continue;
+            const bool lj = lj_i && (!water || j % 3 == 0);
+            const bool el = (d.pots & NBG_POT_EL) && !el_excluded(d.kind, i, j);
+            if (!(lj || el)) continue;
+            Dist64 q;
+            if (!distance64(xi, X + 3 * j, d.bc, R, q)) {
+                range_err = true;
+                continue;
+            }
+            if (lj && q.r2 < d.lj_R2) {
+                double s6 = d.lj_sig2_d / q.r2;
+                s6 = __dmul_rn(__dmul_rn(s6, s6), s6);
+                e_lj = __dadd_rn(e_lj, __dsub_rn(__dsub_rn(__dmul_rn(s6, s6), s6), ljR));
+            }
+            if (el && q.r2 < d.el_R2) {
+                const double r = sqrt(q.r2);
+                double t = 1.0 / r;
+                if (d.el_krf != 0.0) t = __dadd_rn(t, __dsub_rn(__dmul_rn(d.el_krf, q.r2), d.el_crf - invR));
+                el_i = __dadd_rn(el_i, __dmul_rn(d.charge[j], __dsub_rn(t, invR)));
+            }
+        }
+        if (d.pots & NBG_POT_EL) e_el = __dadd_rn(e_el, __dmul_rn(el_i, d.charge[i]));
+    }
+    if (range_err) status_set(d.status, ST_RANGE);
+    __shared__ double sh[2][EB];
+    sh[0][threadIdx.x] = e_lj;
+    sh[1][threadIdx.x] = e_el;
+    __syncthreads();
+    for (int w = EB / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int k = 0; k < 2; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 2; ++k) out[blockIdx.x * 2 + k] = sh[k][0];
+}
+
 // kinetic sum (v.v) m/2 and m v.v (temperature), bonds and angles
 __global__ void __launch_bounds__(EB) k_energy_local(Dev d, const double* X, const double* V, double* out /*[grid][4]*/)
 {
@@ -127,8 +186,18 @@ int launch_energy(nbg_ctx* c, const StateView& s, double* out_host)
     size_t bytes = sizeof(double) * (3 * (size_t)gp + 4 * (size_t)gl);
     cudaError_t e = cudaMallocAsync((void**)&buf, bytes, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "energy scratch");
-    k_energy_pairs<<<gp, EB, 0, c->stream>>>(c->d, s.x, buf);
-    NBG_LAUNCH_CHECK(c, "k_energy_pairs");
+    const bool list = c->path == PATH_LIST && c->nrep == 1;
+    if (list) {
+        // a list for exactly these positions
+        int st = launch_pack(c, s);
+        if (st) return st;
+        if ((st = launch_list_build(c, s, true, StepRef{0, nullptr}))) return st;
+        k_energy_list<<<gp, EB, 0, c->stream>>>(c->d, s.x, buf);
+        NBG_LAUNCH_CHECK(c, "k_energy_list");
+    } else {
+        k_energy_pairs<<<gp, EB, 0, c->stream>>>(c->d, s.x, buf);
+        NBG_LAUNCH_CHECK(c, "k_energy_pairs");
+    }
     k_energy_local<<<gl, EB, 0, c->stream>>>(c->d, s.x, s.v, buf + 3 * gp);
     NBG_LAUNCH_CHECK(c, "k_energy_local");
     std::vector<double> h(3 * (size_t)gp + 4 * (size_t)gl);
@@ -138,10 +207,22 @@ int launch_energy(nbg_ctx* c, const StateView& s, double* out_host)
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "energy sync");
     double lj = 0, el = 0, g = 0, ke = 0, mv2 = 0, eb = 0, ea = 0;
-    for (int b = 0; b < gp; ++b) {
-        lj += h[3 * b];
-        el += h[3 * b + 1];
-        g += h[3 * b + 2];
+    if (list) {
+        for (int b = 0; b < gp; ++b) {
+            lj += h[2 * b];
+            el += h[2 * b + 1];
+        }
+        // every pair's beyond-cutoff term: LJ(R) per LJ pair, q_i q_j / R per charge pair
+        double s6R = c->d.lj_sig2_d / c->d.lj_R2;
+        s6R = s6R * s6R * s6R;
+        if (c->d.pots & NBG_POT_LJ) lj += (double)c->lj_pairs * (s6R * s6R - s6R);
+        if (c->d.pots & NBG_POT_EL) el += c->el_pair_qq / c->d.el_R;
+    } else {
+        for (int b = 0; b < gp; ++b) {
+            lj += h[3 * b];
+            el += h[3 * b + 1];
+            g += h[3 * b + 2];
+        }
     }
     for (int b = 0; b < gl; ++b) {
         const double* q = h.data() + 3 * gp + 4 * b;

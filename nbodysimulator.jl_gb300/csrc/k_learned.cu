@@ -79,39 +79,77 @@ __device__ __forceinline__ void ml_fc(float r, float& fc, float& dfc)
 // g_k = scale * exp(-(t - k)^2 / 2) for k = 0..23 (t = (r - R0) / w) by a
 // product recurrence from the middle centre k = 12: upwards
 // g_{k+1} = g_k exp(t - k - 1/2), downwards g_{k-1} = g_k exp(k - t - 1/2),
-// and each ratio shrinks by 1/e per step. Three exponentials instead of 24;
-// for t > -1 every factor that matters stays a normal FP32 number (pairs
-// closer than R0 - w take the direct form).
-__device__ __forceinline__ void ml_gaussians(float t, float scale, float* g)
+// each ratio shrinking by 1/e per step. Both chains advance together in
+// FP32x2: returns g_12 and gp[m] = (g_{13+m}, g_{11-m}), m = 0..11 (gp[11].x
+// would be g_24 and is not a centre). Three exponentials instead of 24; for
+// t > -1 every factor that matters stays a normal FP32 number (closer pairs,
+// r < R0 - w, take the direct form).
+__device__ __forceinline__ float ml_gauss_pairs(float t, float scale, float2* gp)
 {
     const float d = t - 12.0f;
     if (d < -13.0f) {
 #pragma unroll
-        for (int k = 0; k < ML_NK; ++k) {
-            const float z = t - (float)k;
-            g[k] = scale * __expf(-0.5f * z * z);
+        for (int m = 0; m < 12; ++m) {
+            const float zu = t - (float)(13 + m), zd = t - (float)(11 - m);
+            gp[m] = make_float2(scale * __expf(-0.5f * zu * zu), scale * __expf(-0.5f * zd * zd));
         }
-        return;
+        return scale * __expf(-0.5f * d * d);
     }
-    const float einv = 0.36787944117144233f;
     const float g12 = scale * __expf(-0.5f * d * d);
-    float up = __expf(d - 0.5f), dn = __expf(-d - 0.5f);
-    g[12] = g12;
-    float cur = g12;
+    float2 cur = make_float2(g12, g12);
+    float2 rat = make_float2(__expf(d - 0.5f), __expf(-d - 0.5f));
+    const float2 einv = make_float2(0.36787944117144233f, 0.36787944117144233f);
 #pragma unroll
-    for (int k = 13; k < ML_NK; ++k) {
-        cur *= up;
-        up *= einv;
-        g[k] = cur;
+    for (int m = 0; m < 12; ++m) {
+        cur = __fmul2_rn(cur, rat);
+        rat = __fmul2_rn(rat, einv);
+        gp[m] = cur;
     }
-    cur = g12;
-#pragma unroll
-    for (int k = 11; k >= 0; --k) {
-        cur *= dn;
-        dn *= einv;
-        g[k] = cur;
-    }
+    return g12;
 }
+
+// Candidates of one species column are gathered four at a time (indices,
+// then split positions, all loads independent) and the pairs inside RD are
+// staged per thread in shared memory, [slot][thread]; the arithmetic then
+// runs over staged pairs only, so that lanes are not idled by rejected
+// candidates and the gathers overlap.
+#define ML_STAGE 24
+#define ML_TPB 128
+
+struct Stager {
+    const int* col;
+    int64_t n;
+    int q, q1;
+    // stage up to ML_STAGE pairs (r_j - r_i, j) into st[.][tid]; returns the count
+    __device__ __forceinline__ int fill(const Dev& d, const RepDev& R, const float4& hi, const float4& lo, float rd2,
+                                       float4 (*st)[ML_TPB], int tid)
+    {
+        int cnt = 0;
+        while (q < q1 && cnt <= ML_STAGE - 4) {
+            int jj[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) jj[u] = (q + u < q1) ? col[(int64_t)(q + u) * n] : -1;
+            float4 hh[4], ll[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (jj[u] >= 0) {
+                    hh[u] = d.phi[jj[u]];
+                    ll[u] = d.plo[jj[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (jj[u] >= 0) {
+                    const float3 dr = split_diff(hh[u], ll[u], hi, lo, true, R);  // r_j - r_i
+                    const float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+                    if (r2 < rd2) st[cnt++][tid] = make_float4(dr.x, dr.y, dr.z, __int_as_float(jj[u]));
+                }
+            }
+            q += 4;
+        }
+        return cnt;
+    }
+};
 
 // ---------------------------------------------------------------------
 // short list: atoms of the long list within RD + skin, O neighbours from the
@@ -205,8 +243,10 @@ struct NbrCursor {
 // ---------------------------------------------------------------------
 // descriptors (thread per atom). raw: write D unstandardised.
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_descriptor(Dev d, MLView m, int raw)
+__global__ void __launch_bounds__(ML_TPB) k_descriptor(Dev d, MLView m, int raw)
 {
+    __shared__ float4 st[ML_STAGE][ML_TPB];
+    const int tid = threadIdx.x;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         const RepDev& R = d.reps[d.rep_of[i]];
         const float4 hi = d.phi[i], lo = d.plo[i];
@@ -217,48 +257,58 @@ __global__ void __launch_bounds__(128) k_descriptor(Dev d, MLView m, int raw)
         float* X = m.x + i * ML_ND;
         float* MO = m.mom + i * 72;
         for (int s = 0; s < 2; ++s) {
-            const int q0 = s == 0 ? 0 : m.scap - (cnt >> 16);
-            const int q1 = s == 0 ? (cnt & 0xffff) : m.scap;
-            float G[ML_NK];
-            float mo[4][9];
+            Stager sg{m.snbr + i, d.n, s == 0 ? 0 : m.scap - (cnt >> 16), s == 0 ? (cnt & 0xffff) : m.scap};
+            float G12 = 0.f;
+            float2 G[12];
+            float2 mo[4][5];  // p (x, y), (z, Qxx), (Qyy, Qzz), (Qxy, Qxz), (Qyz, -)
 #pragma unroll
-            for (int k = 0; k < ML_NK; ++k) G[k] = 0.f;
+            for (int k = 0; k < 12; ++k) G[k] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
-                for (int c = 0; c < 9; ++c) mo[a][c] = 0.f;
-            NbrCursor cur(d, m.snbr + i, d.n, q0, q1);
-            int j;
-            float4 hj, lj;
-            while (cur.next(d, j, hj, lj)) {
-                const float3 dr = split_diff(hj, lj, hi, lo, true, R);  // r_j - r_i
-                const float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
-                if (!(r2 < m.rd2)) continue;
-                const float ir = rsqrtf(r2), r = r2 * ir;
-                const float ux = dr.x * ir, uy = dr.y * ir, uz = dr.z * ir;
-                float f, df;
-                ml_fc(r, f, df);
-                float gk[ML_NK];
-                ml_gaussians((r - ML_R0) * (1.0f / ML_W), f, gk);
+                for (int c = 0; c < 5; ++c) mo[a][c] = make_float2(0.f, 0.f);
+            do {
+                const int nst = sg.fill(d, R, hi, lo, m.rd2, st, tid);
+                for (int c = 0; c < nst; ++c) {
+                    const float4 e = st[c][tid];
+                    const float r2 = e.x * e.x + e.y * e.y + e.z * e.z;
+                    const float ir = rsqrtf(r2), r = r2 * ir;
+                    const float ux = e.x * ir, uy = e.y * ir, uz = e.z * ir;
+                    float f, df;
+                    ml_fc(r, f, df);
+                    float2 gp[12];
+                    G12 += ml_gauss_pairs((r - ML_R0) * (1.0f / ML_W), f, gp);
 #pragma unroll
-                for (int k = 0; k < ML_NK; ++k) G[k] += gk[k];
-                const float comp[9] = {ux, uy, uz, ux * ux - (1.0f / 3.0f), uy * uy - (1.0f / 3.0f),
-                                       uz * uz - (1.0f / 3.0f), ux * uy, ux * uz, uy * uz};
+                    for (int k = 0; k < 12; ++k) G[k] = __fadd2_rn(G[k], gp[k]);
+                    const float2 comp[5] = {make_float2(ux, uy), make_float2(uz, ux * ux - (1.0f / 3.0f)),
+                                            make_float2(uy * uy - (1.0f / 3.0f), uz * uz - (1.0f / 3.0f)),
+                                            make_float2(ux * uy, ux * uz), make_float2(uy * uz, 0.f)};
 #pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    const float psi = f * __expf(-r2 * c_rho2inv[a]);
+                    for (int a = 0; a < 4; ++a) {
+                        const float psi = f * __expf(-r2 * c_rho2inv[a]);
+                        const float2 p2 = make_float2(psi, psi);
 #pragma unroll
-                    for (int c = 0; c < 9; ++c) mo[a][c] = fmaf(psi, comp[c], mo[a][c]);
+                        for (int c = 0; c < 5; ++c) mo[a][c] = __ffma2_rn(p2, comp[c], mo[a][c]);
+                    }
                 }
+            } while (sg.q < sg.q1);
+            // radial: G[k] for k = 13 + m (x) and 11 - m (y)
+            float Gk[ML_NK];
+            Gk[12] = G12;
+#pragma unroll
+            for (int k = 0; k < 12; ++k) {
+                if (k < 11) Gk[13 + k] = G[k].x;
+                Gk[11 - k] = G[k].y;
             }
 #pragma unroll
             for (int k = 0; k < ML_NK; ++k) {
                 const int col = s * ML_NK + k;
-                X[col] = raw ? G[k] : (G[k] - mu[col]) / sd[col];
+                X[col] = raw ? Gk[k] : (Gk[k] - mu[col]) / sd[col];
             }
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
-                const float* M = mo[a];
+                const float M[9] = {mo[a][0].x, mo[a][0].y, mo[a][1].x, mo[a][1].y, mo[a][2].x,
+                                    mo[a][2].y, mo[a][3].x, mo[a][3].y, mo[a][4].x};
                 const float A1 = M[0] * M[0] + M[1] * M[1] + M[2] * M[2];
                 // |Q|_F^2 of the symmetric matrix (diagonal + 2 x off-diagonal)
                 const float A2 = M[3] * M[3] + M[4] * M[4] + M[5] * M[5] + 2.f * (M[6] * M[6] + M[7] * M[7] + M[8] * M[8]);
@@ -345,9 +395,16 @@ __device__ __forceinline__ int64_t species_atom(int sp, int64_t k) { return sp =
 // column g; C c0..c3 = rows g, g+8 x columns 2t(+1). The C tiles of output
 // columns 16u..16u+15 are, packed to BF16, the A fragment of k-tile u of the
 // next product, so activations never leave registers.
-__global__ void __launch_bounds__(MLP_WARPS * 32, 2) k_mlp_bf16(MLView m, int sp, int64_t count)
+// Both species in one launch: blocks [0, blocks_o) take the O atoms, the
+// rest the H atoms (each block stages one species' weights).
+__global__ void __launch_bounds__(MLP_WARPS * 32, 2) k_mlp_bf16(MLView m, int64_t count_o, int64_t count_h,
+                                                                 int blocks_o)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sp = blockIdx.x < (unsigned)blocks_o ? 0 : 1;
+    const int64_t count = sp == 0 ? count_o : count_h;
+    const int64_t blk = sp == 0 ? blockIdx.x : blockIdx.x - blocks_o;
+    const int64_t nblk = sp == 0 ? blocks_o : gridDim.x - blocks_o;
     MlpSmem& S = *reinterpret_cast<MlpSmem*>(smem_raw);
     const float* th = sp == 0 ? m.theta[0] : m.theta[1];
     {
@@ -374,7 +431,7 @@ __global__ void __launch_bounds__(MLP_WARPS * 32, 2) k_mlp_bf16(MLView m, int sp
     const int rA = lane & 15, cA = (lane >> 4) * 8;                        // A (and trans-B) tiles
     const int rB = (lane >> 4) * 8 + (lane & 7), cB = ((lane >> 3) & 1) * 8;  // non-trans B tiles
     const int64_t ntile = (count + 15) / 16;
-    for (int64_t tile = (int64_t)blockIdx.x * MLP_WARPS + warp; tile < ntile; tile += (int64_t)gridDim.x * MLP_WARPS) {
+    for (int64_t tile = blk * MLP_WARPS + warp; tile < ntile; tile += nblk * MLP_WARPS) {
         const int64_t k0 = tile * 16;
         // 16 standardised descriptors to BF16 (rows past count are zero)
         for (int e = lane; e < 16 * 16; e += 32) {
@@ -514,8 +571,10 @@ __device__ __forceinline__ void fq_add(unsigned long long* p, float v)
     atomicAdd(p, (unsigned long long)__float2ll_rn(v * ML_FQ));
 }
 
-__global__ void __launch_bounds__(128) k_ml_force(Dev d, MLView m)
+__global__ void __launch_bounds__(ML_TPB) k_ml_force(Dev d, MLView m)
 {
+    __shared__ float4 st[ML_STAGE][ML_TPB];
+    const int tid = threadIdx.x;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         const RepDev& R = d.reps[d.rep_of[i]];
         const float4 hi = d.phi[i], lo = d.plo[i];
@@ -524,72 +583,88 @@ __global__ void __launch_bounds__(128) k_ml_force(Dev d, MLView m)
         const float* MO = m.mom + i * 72;
         float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
         for (int s = 0; s < 2; ++s) {
-            const int q0 = s == 0 ? 0 : m.scap - (cnt >> 16);
-            const int q1 = s == 0 ? (cnt & 0xffff) : m.scap;
-            if (q0 >= q1) continue;
-            float cG[ML_NK];
+            Stager sg{m.snbr + i, d.n, s == 0 ? 0 : m.scap - (cnt >> 16), s == 0 ? (cnt & 0xffff) : m.scap};
+            if (sg.q >= sg.q1) continue;
+            // coefficients in the pair order of ml_gauss_pairs: c_k and k c_k
+            const float* cg = dD + s * ML_NK;
+            const float c12 = cg[12];
+            float2 cp[12], kp[12];
 #pragma unroll
-            for (int k = 0; k < ML_NK; ++k) cG[k] = dD[s * ML_NK + k];
-            float cA1[4], cA2[4], M[4][9];
+            for (int k = 0; k < 12; ++k) {
+                const float cu = k < 11 ? cg[13 + k] : 0.f, cd = cg[11 - k];
+                cp[k] = make_float2(cu, cd);
+                kp[k] = make_float2((float)(13 + k) * cu, (float)(11 - k) * cd);
+            }
+            float cA1[4], cA2[4], P[4][3], Q[4][6];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 cA1[a] = 2.f * dD[48 + 4 * s + a];
                 cA2[a] = 2.f * dD[56 + 4 * s + a];
 #pragma unroll
-                for (int c = 0; c < 9; ++c) M[a][c] = MO[(s * 4 + a) * 9 + c];
+                for (int c = 0; c < 3; ++c) P[a][c] = MO[(s * 4 + a) * 9 + c];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) Q[a][c] = MO[(s * 4 + a) * 9 + 3 + c];
             }
-            NbrCursor cur(d, m.snbr + i, d.n, q0, q1);
-            int j;
-            float4 hj, lj;
-            while (cur.next(d, j, hj, lj)) {
-                const float3 dr = split_diff(hj, lj, hi, lo, true, R);  // r_j - r_i
-                const float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
-                if (!(r2 < m.rd2)) continue;
-                const float ir = rsqrtf(r2), r = r2 * ir;
-                const float ux = dr.x * ir, uy = dr.y * ir, uz = dr.z * ir;
-                float f, df;
-                ml_fc(r, f, df);
-                const float tt = (r - ML_R0) * (1.0f / ML_W);
-                // radial: d(g_k fc)/dr = g_k (fc' - fc (t - k) / w)
-                float gk[ML_NK];
-                ml_gaussians(tt, 1.0f, gk);
-                float S0 = 0.f, S1 = 0.f;
+            do {
+                const int nst = sg.fill(d, R, hi, lo, m.rd2, st, tid);
+                for (int c = 0; c < nst; ++c) {
+                    const float4 e = st[c][tid];
+                    const int j = __float_as_int(e.w);
+                    const float r2 = e.x * e.x + e.y * e.y + e.z * e.z;
+                    const float ir = rsqrtf(r2), r = r2 * ir;
+                    const float ux = e.x * ir, uy = e.y * ir, uz = e.z * ir;
+                    float f, df;
+                    ml_fc(r, f, df);
+                    const float tt = (r - ML_R0) * (1.0f / ML_W);
+                    // radial: d(g_k fc)/dr = g_k (fc' - fc (t - k) / w); S0 = sum c_k g_k,
+                    // S1 = sum c_k g_k (t - k) = t S0 - sum k c_k g_k
+                    float2 gp[12];
+                    const float g12 = ml_gauss_pairs(tt, 1.0f, gp);
+                    float2 s0 = make_float2(c12 * g12, 0.f), sk = make_float2(12.f * c12 * g12, 0.f);
 #pragma unroll
-                for (int k = 0; k < ML_NK; ++k) {
-                    const float cg = cG[k] * gk[k];
-                    S0 += cg;
-                    S1 = fmaf(cg, tt - (float)k, S1);
-                }
-                const float dEdr = df * S0 - f * (1.0f / ML_W) * S1;
-                float gx = dEdr * ux, gy = dEdr * uy, gz = dEdr * uz;
-#pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    const float e = __expf(-r2 * c_rho2inv[a]);
-                    const float psi = f * e;
-                    const float dpsi = e * (df - 2.f * r * c_rho2inv[a] * f);
-                    const float* Ma = M[a];
-                    // d|p|^2/dr_j = 2 [psi' (p.u) u + psi/r (p - (p.u) u)]
-                    const float pu = Ma[0] * ux + Ma[1] * uy + Ma[2] * uz;
-                    const float s2 = cA1[a] * psi * ir;
-                    const float s1 = cA1[a] * dpsi * pu - s2 * pu;
+                    for (int k = 0; k < 12; ++k) {
+                        s0 = __ffma2_rn(cp[k], gp[k], s0);
+                        sk = __ffma2_rn(kp[k], gp[k], sk);
+                    }
+                    const float S0 = s0.x + s0.y;
+                    const float S1 = tt * S0 - (sk.x + sk.y);
+                    float sr = df * S0 - f * (1.0f / ML_W) * S1;  // coefficient of u
+                    // angular: with psi_a, psi'_a and the moments p_a, Q_a,
+                    // d|p|^2/dr_j = 2 [psi' (p.u) u + psi/r (p - (p.u) u)],
                     // d|Q|^2/dr_j = 2 [psi' (uQu) u + psi 2/r (Q u - (uQu) u)]
-                    const float qx = Ma[3] * ux + Ma[6] * uy + Ma[7] * uz;
-                    const float qy = Ma[6] * ux + Ma[4] * uy + Ma[8] * uz;
-                    const float qz = Ma[7] * ux + Ma[8] * uy + Ma[5] * uz;
-                    const float uqu = qx * ux + qy * uy + qz * uz;
-                    const float t2 = 2.f * cA2[a] * psi * ir;
-                    const float t1 = cA2[a] * dpsi * uqu - t2 * uqu;
-                    gx += (s1 + t1) * ux + s2 * Ma[0] + t2 * qx;
-                    gy += (s1 + t1) * uy + s2 * Ma[1] + t2 * qy;
-                    gz += (s1 + t1) * uz + s2 * Ma[2] + t2 * qz;
+                    const float w6[6] = {ux * ux, uy * uy, uz * uz, 2.f * ux * uy, 2.f * ux * uz, 2.f * uy * uz};
+                    float px = 0.f, py = 0.f, pz = 0.f;  // sum_a s2_a p_a
+                    float W[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // sum_a t2_a Q_a
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const float ea = __expf(-r2 * c_rho2inv[a]);
+                        const float psi = f * ea;
+                        const float dpsi = ea * (df - 2.f * r * c_rho2inv[a] * f);
+                        const float pu = P[a][0] * ux + P[a][1] * uy + P[a][2] * uz;
+                        float uqu = 0.f;
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) uqu = fmaf(Q[a][c], w6[c], uqu);
+                        const float s2 = cA1[a] * psi * ir;
+                        const float t2 = 2.f * cA2[a] * psi * ir;
+                        sr += (cA1[a] * dpsi - s2) * pu + (cA2[a] * dpsi - t2) * uqu;
+                        px = fmaf(s2, P[a][0], px);
+                        py = fmaf(s2, P[a][1], py);
+                        pz = fmaf(s2, P[a][2], pz);
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) W[c] = fmaf(t2, Q[a][c], W[c]);
+                    }
+                    // W u with W = (xx, yy, zz, xy, xz, yz)
+                    const float gx = sr * ux + px + W[0] * ux + W[3] * uy + W[4] * uz;
+                    const float gy = sr * uy + py + W[3] * ux + W[1] * uy + W[5] * uz;
+                    const float gz = sr * uz + pz + W[4] * ux + W[5] * uy + W[2] * uz;
+                    fq_add(&m.fq[3 * j], -gx);
+                    fq_add(&m.fq[3 * j + 1], -gy);
+                    fq_add(&m.fq[3 * j + 2], -gz);
+                    fi0 += gx;
+                    fi1 += gy;
+                    fi2 += gz;
                 }
-                fq_add(&m.fq[3 * j], -gx);
-                fq_add(&m.fq[3 * j + 1], -gy);
-                fq_add(&m.fq[3 * j + 2], -gz);
-                fi0 += gx;
-                fi1 += gy;
-                fi2 += gz;
-            }
+            } while (sg.q < sg.q1);
         }
         fq_add(&m.fq[3 * i], fi0);
         fq_add(&m.fq[3 * i + 1], fi1);
@@ -609,7 +684,7 @@ __device__ __forceinline__ void smoothstep(float r, float& S, float& dS)
     dS = (-30.f * t2 + 60.f * t3 - 30.f * t3 * t) * (1.0f / (ML_RD - ML_RS));
 }
 
-__global__ void __launch_bounds__(128) k_sr_exact(Dev d, MLView m, float* e_out, float* f_out)
+__global__ void __launch_bounds__(ML_TPB) k_sr_exact(Dev d, MLView m, float* e_out, float* f_out)
 {
     const float eps4 = (float)(4.0 * d.lj_eps);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -944,7 +1019,7 @@ int launch_short_list(nbg_ctx* c, StepRef pos, bool force)
 
 int launch_descriptor(nbg_ctx* c, bool raw)
 {
-    k_descriptor<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, ml_view(c), raw ? 1 : 0);
+    k_descriptor<<<grid_for(c->n, ML_TPB), ML_TPB, 0, c->stream>>>(c->d, ml_view(c), raw ? 1 : 0);
     NBG_LAUNCH_CHECK(c, "k_descriptor");
     return NBG_OK;
 }
@@ -960,13 +1035,18 @@ int launch_mlp(nbg_ctx* c)
         c->ml_attr = true;
     }
     const MLView m = ml_view(c);
-    for (int sp = 0; sp < 2; ++sp) {
-        const int64_t count = sp == 0 ? c->n / 3 : 2 * (c->n / 3);
-        const int64_t tiles = (count + 15) / 16;
-        const int grid = (int)std::min<int64_t>((tiles + MLP_WARPS - 1) / MLP_WARPS, (int64_t)c->sms * 2);
-        k_mlp_bf16<<<std::max(grid, 1), MLP_WARPS * 32, sizeof(MlpSmem), c->stream>>>(m, sp, count);
-        NBG_LAUNCH_CHECK(c, "k_mlp_bf16");
+    // two resident blocks per SM, split between the species by their tiles
+    const int64_t count_o = c->n / 3, count_h = 2 * (c->n / 3);
+    const int64_t tiles_o = (count_o + 15) / 16, tiles_h = (count_h + 15) / 16;
+    const int64_t need_o = (tiles_o + MLP_WARPS - 1) / MLP_WARPS, need_h = (tiles_h + MLP_WARPS - 1) / MLP_WARPS;
+    const int64_t slots = (int64_t)c->sms * 2;
+    int64_t bo = need_o, bh = need_h;
+    if (bo + bh > slots) {
+        bo = std::max<int64_t>(1, (slots * tiles_o + (tiles_o + tiles_h) / 2) / (tiles_o + tiles_h));
+        bh = std::max<int64_t>(1, slots - bo);
     }
+    k_mlp_bf16<<<(int)(bo + bh), MLP_WARPS * 32, sizeof(MlpSmem), c->stream>>>(m, count_o, count_h, (int)bo);
+    NBG_LAUNCH_CHECK(c, "k_mlp_bf16");
     return NBG_OK;
 }
 
@@ -974,7 +1054,7 @@ int launch_ml_force(nbg_ctx* c)
 {
     cudaError_t e = cudaMemsetAsync(c->ml_fq, 0, sizeof(unsigned long long) * 3 * c->n, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "ml force clear");
-    k_ml_force<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, ml_view(c));
+    k_ml_force<<<grid_for(c->n, ML_TPB), ML_TPB, 0, c->stream>>>(c->d, ml_view(c));
     NBG_LAUNCH_CHECK(c, "k_ml_force");
     return NBG_OK;
 }

@@ -424,6 +424,26 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         else c->list_lpa = 32;
         if ((st = alloc_lists(c, cell_cap, nbr_cap))) return st;
     }
+    if (c->path == PATH_LIST && nrep == 1) {
+        // constants of the list-based energy (pairs beyond the cutoffs)
+        const bool water = d0->kind == NBG_SYSTEM_WATER;
+        const int64_t nlj = water ? n / 3 : n;
+        c->lj_pairs = (pots & NBG_POT_LJ) ? nlj * (nlj - 1) / 2 : 0;
+        if (pots & NBG_POT_EL) {
+            // sum_{i<j} q_i q_j = ((sum q)^2 - sum q^2) / 2, less the intramolecular pairs of water
+            long double sq = 0.0L, sq2 = 0.0L, excl = 0.0L;
+            for (int64_t i = 0; i < n; ++i) {
+                sq += c->charge_h[i];
+                sq2 += (long double)c->charge_h[i] * c->charge_h[i];
+            }
+            if (water)
+                for (int64_t m = 0; m + 2 < n; m += 3) {
+                    const long double a = c->charge_h[m], b = c->charge_h[m + 1], e = c->charge_h[m + 2];
+                    excl += a * b + a * e + b * e;
+                }
+            c->el_pair_qq = (double)((sq * sq - sq2) / 2.0L - excl);
+        }
+    }
     if (getenv("NBG_NO_GRAPHS")) c->use_graphs = false;  // direct launches, for comparisons
     if (c->path == PATH_GRAVITY) {
         const char* gv = getenv("NBG_GRAVITY_VARIANT");  // kernel-form override for tuning sweeps
@@ -1077,12 +1097,20 @@ extern "C" int nbg_energy(nbg_ctx* c, const double* u, const double* v, nbg_ener
     CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
     CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     int st;
-    if ((st = clear_status(c))) return st;
+    if (c->path == PATH_LIST) resident_dirty(c);  // the list is rebuilt for u
     double h[7];
-    if ((st = launch_energy(c, c->ev, h))) return st;
-    unsigned w = 0;
-    if ((st = read_status(c, &w))) return st;
-    if ((st = status_error(c, w))) return st;
+    for (int attempt = 0;; ++attempt) {
+        if ((st = clear_status(c))) return st;
+        if ((st = launch_energy(c, c->ev, h))) return st;
+        unsigned w = 0;
+        if ((st = read_status(c, &w))) return st;
+        if (attempt < 6 && (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && !(w & (ST_NONFINITE | ST_RANGE))) {
+            if ((st = grow_lists(c, w))) return st;
+            continue;
+        }
+        if ((st = status_error(c, w))) return st;
+        break;
+    }
     out->kinetic = h[0];
     out->lennard_jones = h[1];
     out->electrostatic = h[2];
@@ -1676,4 +1704,53 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
     }
     if (S.judged > 0) S.judge_mean /= (double)S.judged;
     return done_with(NBG_OK);
+}
+
+extern "C" int nbg_set_thermostat_target(nbg_ctx* c, int32_t replica, double T)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (replica < 0 || replica >= c->nrep || !(T >= 0.0) || !std::isfinite(T))
+        return fail(c, NBG_ERR_ARG, "replica in range and a finite T >= 0");
+    cudaSetDevice(c->device);
+    c->reps_h[replica].T0 = T;
+    if (replica == 0) c->desc.thermo_T = T;
+    RepDev* rp = const_cast<RepDev*>(c->d.reps) + replica;
+    CK(cudaMemcpyAsync(rp, &c->reps_h[replica], sizeof(RepDev), cudaMemcpyHostToDevice, c->stream), "replica upload");
+    CK(cudaStreamSynchronize(c->stream), "replica sync");
+    return NBG_OK;  // captured graphs read the replica table at run time
+}
+
+extern "C" int nbg_ml_kernel_times(nbg_ctx* c, int32_t reps, double* ms)
+{
+    int st = ml_check(c);
+    if (st) return st;
+    if (!c->state_valid || reps < 1 || !ms) return fail(c, NBG_ERR_ARG, "resident state, reps >= 1, ms[4]");
+    const StepRef pos{c->step, nullptr};
+    if ((st = launch_pack(c, c->st))) return st;
+    if ((st = launch_list_build(c, c->st, true, pos))) return st;
+    resident_dirty(c);
+    cudaEvent_t ev[5];
+    for (auto& e : ev) CK(cudaEventCreate(&e), "event");
+    double acc[4] = {0, 0, 0, 0};
+    for (int r = 0; r < reps && st == NBG_OK; ++r) {
+        cudaEventRecord(ev[0], c->stream);
+        st = launch_short_list(c, pos, true);
+        cudaEventRecord(ev[1], c->stream);
+        if (!st) st = launch_descriptor(c, false);
+        cudaEventRecord(ev[2], c->stream);
+        if (!st) st = launch_mlp(c);
+        cudaEventRecord(ev[3], c->stream);
+        if (!st) st = launch_ml_force(c);
+        cudaEventRecord(ev[4], c->stream);
+        cudaEventSynchronize(ev[4]);
+        for (int k = 0; k < 4; ++k) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            acc[k] += t;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (st) return st;
+    for (int k = 0; k < 4; ++k) ms[k] = acc[k] / reps;
+    return NBG_OK;
 }

@@ -178,6 +178,10 @@ struct nbg_ctx {
     int kick_blocks = 0;
     bool T_valid = false;        // red_T holds T of the resident velocities
     int sms = 0;                 // multiprocessors of the device
+    // constants of the list-based energy: LJ pairs, and sum of q_i q_j over
+    // all non-excluded pairs (i < j)
+    int64_t lj_pairs = 0;
+    double el_pair_qq = 0.0;
     // learned short-range model (water)
     bool ml_on = false;
     bool ml_attr = false;        // large shared-memory opt-ins done

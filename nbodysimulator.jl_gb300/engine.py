@@ -221,3 +221,12 @@ class Engine:
         self._chk(self.lib.nbg_respa_run(self.ctx, float(dt), int(inner), int(outer), float(threshold), flags,
                                          ctypes.byref(stats)))
         return stats
+
+    def set_thermostat_target(self, T, replica=0):
+        self._chk(self.lib.nbg_set_thermostat_target(self.ctx, int(replica), float(T)))
+
+    def ml_kernel_times(self, reps=10):
+        """Device ms of (short list, descriptors, MLP, force scatter) on the resident positions."""
+        ms = np.zeros(4)
+        self._chk(self.lib.nbg_ml_kernel_times(self.ctx, int(reps), _abi.as_dptr(ms)))
+        return ms

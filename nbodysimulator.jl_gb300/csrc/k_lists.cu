@@ -8,12 +8,17 @@
 //
 // Build, skipped on device unless a rebuild is due (host-forced every
 // rebuild_every steps, or an atom moved more than skin/2):
-//   k_cell_fill  : atom -> cell by its wrapped position, slot by atomicAdd
-//   k_cell_sort  : each cell's atoms sorted by index (deterministic lists),
-//                  counts moved to cell_n and cleared for the next build
-//   k_list_build : 27-cell scan per atom; the list is column-major
-//                  (nbr[k*n + i]) for thread-per-atom force kernels and
-//                  row-major (nbr[i*cap + k]) for lanes-per-atom kernels
+//   k_cell_fill        : atom -> cell by its wrapped position, slot by atomicAdd
+//   k_cell_sort        : each cell's atoms sorted by index (deterministic
+//                        lists), counts moved to cell_n and cleared for the
+//                        next build
+//   k_list_build_cells : one block per cell; the 27 neighbour cells' atoms
+//                        (split-position hi parts moved by the periodic shift
+//                        into the cell's frame) are staged in shared-memory
+//                        tiles in scan order and every atom of the cell tests
+//                        them with broadcast reads. The list is column-major
+//                        (nbr[k*n + i]) for thread-per-atom force kernels and
+//                        row-major (nbr[i*cap + k]) for lanes-per-atom kernels.
 #include "nbg_internal.cuh"
 
 struct ListCtl {
@@ -76,126 +81,116 @@ __global__ void k_cell_sort(Dev d, ListCtl L)
     }
 }
 
-__global__ void k_list_build(Dev d, ListCtl L, const double* X)
-{
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.rebuild_flag[read_parity(L) ^ 1] = 0;
-    if (!need_build(d, L)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.build_count, 1ull);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
-        const RepDev& R = d.reps[d.rep_of[i]];
-        float4 hi = d.phi[i], lo = d.plo[i];
-        int cx = cell_coord(hi.x, R), cy = cell_coord(hi.y, R), cz = cell_coord(hi.z, R);
-        int cnt = 0;
-        const bool water = d.kind == NBG_SYSTEM_WATER;
-        const int o0 = R.nc >= 3 ? -1 : 0, o1 = R.nc >= 3 ? 1 : 0;
-        for (int ox = o0; ox <= o1; ++ox) {
-            int nx = cx + ox;
-            nx += (nx < 0) ? R.nc : 0;
-            nx -= (nx >= R.nc) ? R.nc : 0;
-            for (int oy = o0; oy <= o1; ++oy) {
-                int ny = cy + oy;
-                ny += (ny < 0) ? R.nc : 0;
-                ny -= (ny >= R.nc) ? R.nc : 0;
-                for (int oz = o0; oz <= o1; ++oz) {
-                    int nz = cz + oz;
-                    nz += (nz < 0) ? R.nc : 0;
-                    nz -= (nz >= R.nc) ? R.nc : 0;
-                    int cell = R.cell0 + (nx * R.nc + ny) * R.nc + nz;
-                    int m = d.cell_n[cell];
-                    const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
-                    for (int k = 0; k < m; ++k) {
-                        int j = atoms[k];
-                        if (j == (int)i) continue;
-                        if (water && (j / 3 == (int)(i / 3))) continue;  // intramolecular: never a pair
-                        float4 hj = d.phi[j], lj = d.plo[j];
-                        float3 dr = split_diff(hi, lo, hj, lj, true, R);
-                        float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
-                        if (r2 < R.rl2) {
-                            if (cnt < d.nbr_cap) d.nbr[(int64_t)cnt * d.nbr_kstride + i * d.nbr_istride] = j;
-                            ++cnt;
-                        }
-                    }
-                }
-            }
-        }
-        if (cnt > d.nbr_cap) {
-            status_set(d.status, ST_NBR_OVERFLOW);
-            cnt = d.nbr_cap;
-        }
-        d.nbr_count[i] = cnt;
-        d.xref[3 * i] = X[3 * i];
-        d.xref[3 * i + 1] = X[3 * i + 1];
-        d.xref[3 * i + 2] = X[3 * i + 2];
-    }
-}
+// Candidates of the 27 (or, for a one-cell replica, 1) neighbour cells in
+// scan order (ox, oy, oz from -1 to 1; each cell's atoms by index), TILE at
+// a time. The test r^2 < rl2 on the hi parts is the list's superset test (the
+// force kernels classify every pair exactly); the list order is the scan order.
+#define LB_TILE 1024
 
-// LPA lanes per atom: the group scans the 27 cells in the same order, each
-// chunk of LPA consecutive cell entries tested in parallel; accepted entries
-// keep their scan order through a ballot prefix count, so the row-major list
-// is identical to the one-thread-per-atom list.
-template <int LPA>
-__global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, const double* X)
+__global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, const double* X)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) d.rebuild_flag[read_parity(L) ^ 1] = 0;
     if (!need_build(d, L)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.build_count, 1ull);
-    const int lane = threadIdx.x % LPA;
-    const int gbase = (threadIdx.x % 32) - lane;  // first lane of the group within the warp
-    const unsigned gmask = (LPA == 32) ? 0xffffffffu : (((1u << LPA) - 1u) << gbase);
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPA;
-    if (i >= d.n) return;  // whole groups leave together
-    const RepDev& R = d.reps[d.rep_of[i]];
-    const float4 hi = d.phi[i], lo = d.plo[i];
-    const int cx = cell_coord(hi.x, R), cy = cell_coord(hi.y, R), cz = cell_coord(hi.z, R);
+    __shared__ float4 tile[LB_TILE];
+    __shared__ int nb_cell[27];
+    __shared__ float4 nb_shift[27];
+    __shared__ int nb_pre[28];
     const bool water = d.kind == NBG_SYSTEM_WATER;
-    int cnt = 0;
-    int* out = d.nbr + i * d.nbr_istride;
-    const int o0 = R.nc >= 3 ? -1 : 0, o1 = R.nc >= 3 ? 1 : 0;
-    for (int ox = o0; ox <= o1; ++ox) {
-        int nx = cx + ox;
-        nx += (nx < 0) ? R.nc : 0;
-        nx -= (nx >= R.nc) ? R.nc : 0;
-        for (int oy = o0; oy <= o1; ++oy) {
-            int ny = cy + oy;
-            ny += (ny < 0) ? R.nc : 0;
-            ny -= (ny >= R.nc) ? R.nc : 0;
-            for (int oz = o0; oz <= o1; ++oz) {
-                int nz = cz + oz;
-                nz += (nz < 0) ? R.nc : 0;
-                nz -= (nz >= R.nc) ? R.nc : 0;
-                const int cell = R.cell0 + (nx * R.nc + ny) * R.nc + nz;
-                const int m = d.cell_n[cell];
-                const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
-                for (int k0 = 0; k0 < m; k0 += LPA) {
-                    const int k = k0 + lane;
-                    bool take = false;
-                    int j = 0;
-                    if (k < m) {
-                        j = atoms[k];
-                        if (j != (int)i && !(water && (j / 3 == (int)(i / 3)))) {
-                            float3 dr = split_diff(hi, lo, d.phi[j], d.plo[j], true, R);
-                            float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
-                            take = r2 < R.rl2;
+    for (int cell = blockIdx.x; cell < d.ncell_total; cell += gridDim.x) {
+        int cnt = d.cell_n[cell];
+        if (cnt > d.cell_cap) cnt = d.cell_cap;
+        if (cnt == 0) continue;
+        const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
+        const RepDev& R = d.reps[d.rep_of[atoms[0]]];
+        const int nc = R.nc;
+        const int lc = cell - R.cell0;
+        const int cx = lc / (nc * nc), cy = (lc / nc) % nc, cz = lc % nc;
+        const bool one = nc < 3;  // one cell holds the replica: minimum image per pair
+        const int nnb = one ? 1 : 27;
+        __syncthreads();  // previous cell's use of the shared tables is over
+        if (threadIdx.x < nnb) {
+            int ox = 0, oy = 0, oz = 0;
+            if (!one) {
+                ox = threadIdx.x / 9 - 1;
+                oy = (threadIdx.x / 3) % 3 - 1;
+                oz = threadIdx.x % 3 - 1;
+            }
+            int nx = cx + ox, ny = cy + oy, nz = cz + oz;
+            float sx = 0.f, sy = 0.f, sz = 0.f;
+            if (nx < 0) { nx += nc; sx = -R.Lh; }
+            if (nx >= nc) { nx -= nc; sx = R.Lh; }
+            if (ny < 0) { ny += nc; sy = -R.Lh; }
+            if (ny >= nc) { ny -= nc; sy = R.Lh; }
+            if (nz < 0) { nz += nc; sz = -R.Lh; }
+            if (nz >= nc) { nz -= nc; sz = R.Lh; }
+            nb_cell[threadIdx.x] = R.cell0 + (nx * nc + ny) * nc + nz;
+            nb_shift[threadIdx.x] = make_float4(sx, sy, sz, 0.f);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int q = 0; q < nnb; ++q) {
+                nb_pre[q] = acc;
+                acc += min(d.cell_n[nb_cell[q]], d.cell_cap);
+            }
+            nb_pre[nnb] = acc;
+        }
+        __syncthreads();
+        const int total = nb_pre[nnb];
+        for (int a0 = 0; a0 < cnt; a0 += blockDim.x) {
+            const int a = a0 + threadIdx.x;
+            const bool active = a < cnt;
+            const int i = active ? atoms[a] : -1;
+            float4 hi = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (active) hi = d.phi[i];
+            const int mol0 = water && active ? 3 * (i / 3) : -8;  // first atom of i's molecule
+            int lcnt = 0;
+            for (int t0 = 0; t0 < total; t0 += LB_TILE) {
+                const int tn = min(LB_TILE, total - t0);
+                __syncthreads();  // the previous tile is consumed
+                for (int k = threadIdx.x; k < tn; k += blockDim.x) {
+                    const int g = t0 + k;
+                    int q = 0;
+                    while (q + 1 < nnb && nb_pre[q + 1] <= g) ++q;
+                    const int j = d.cell_atoms[(int64_t)nb_cell[q] * d.cell_cap + (g - nb_pre[q])];
+                    const float4 hj = d.phi[j];
+                    const float4 sh = nb_shift[q];
+                    tile[k] = make_float4(hj.x + sh.x, hj.y + sh.y, hj.z + sh.z, __int_as_float(j));
+                }
+                __syncthreads();
+                if (active) {
+                    for (int k = 0; k < tn; ++k) {
+                        const float4 c = tile[k];
+                        float dx = c.x - hi.x, dy = c.y - hi.y, dz = c.z - hi.z;
+                        if (one) {
+                            // s = rint(d / L) by the 1.5 * 2^23 trick (|d / L| <= 1)
+                            const float magic = 12582912.0f;
+                            dx = __fmaf_rn(-__fsub_rn(__fmaf_rn(dx, R.invLf, magic), magic), R.Lh, dx);
+                            dy = __fmaf_rn(-__fsub_rn(__fmaf_rn(dy, R.invLf, magic), magic), R.Lh, dy);
+                            dz = __fmaf_rn(-__fsub_rn(__fmaf_rn(dz, R.invLf, magic), magic), R.Lh, dz);
+                        }
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const int j = __float_as_int(c.w);
+                        if (r2 < R.rl2 && j != i && (unsigned)(j - mol0) >= 3u) {
+                            if (lcnt < d.nbr_cap) d.nbr[(int64_t)lcnt * d.nbr_kstride + (int64_t)i * d.nbr_istride] = j;
+                            ++lcnt;
                         }
                     }
-                    const unsigned bal = __ballot_sync(gmask, take);
-                    if (take) {
-                        const int pos = cnt + __popc(bal & gmask & ((1u << (gbase + lane)) - 1u));
-                        if (pos < d.nbr_cap) out[pos] = j;
-                    }
-                    cnt += __popc(bal & gmask);
                 }
+            }
+            if (active) {
+                if (lcnt > d.nbr_cap) {
+                    status_set(d.status, ST_NBR_OVERFLOW);
+                    lcnt = d.nbr_cap;
+                }
+                d.nbr_count[i] = lcnt;
+                d.xref[3 * i] = X[3 * i];
+                d.xref[3 * i + 1] = X[3 * i + 1];
+                d.xref[3 * i + 2] = X[3 * i + 2];
             }
         }
     }
-    if (lane == 0) {
-        if (cnt > d.nbr_cap) {
-            status_set(d.status, ST_NBR_OVERFLOW);
-            cnt = d.nbr_cap;
-        }
-        d.nbr_count[i] = cnt;
-    }
-    if (lane < 3) d.xref[3 * i + lane] = X[3 * i + lane];
 }
 
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos)
@@ -207,17 +202,11 @@ int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos)
     int gs = cells < 65536 ? cells : 65536;
     k_cell_sort<<<gs, 128, sizeof(int) * c->d.cell_cap, c->stream>>>(c->d, L);
     NBG_LAUNCH_CHECK(c, "k_cell_sort");
-    const int lpa = c->list_lpa;
-    if (lpa <= 1) {
-        k_list_build<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, L, s.x);
-    } else {
-        const int per_block = 256 / lpa;
-        const int grid = (int)((c->n + per_block - 1) / per_block);
-        if (lpa == 4) k_list_build_lanes<4><<<grid, 256, 0, c->stream>>>(c->d, L, s.x);
-        else if (lpa == 8) k_list_build_lanes<8><<<grid, 256, 0, c->stream>>>(c->d, L, s.x);
-        else if (lpa == 16) k_list_build_lanes<16><<<grid, 256, 0, c->stream>>>(c->d, L, s.x);
-        else k_list_build_lanes<32><<<grid, 256, 0, c->stream>>>(c->d, L, s.x);
-    }
+    // a block per cell, sized to the mean occupancy (cells above it take a second pass)
+    const double occ = (double)c->n / std::max(c->d.ncell_total, 1);
+    int bs = 32 * (int)std::ceil(1.15 * occ / 32.0);
+    bs = std::min(256, std::max(32, bs));
+    k_list_build_cells<<<c->d.ncell_total, bs, 0, c->stream>>>(c->d, L, s.x);
     NBG_LAUNCH_CHECK(c, "k_list_build");
     return NBG_OK;
 }

@@ -10,7 +10,11 @@
 //                    Per pair: FP32 differences of hi/lo split positions (exact
 //                    to ~2^-24 of |r_ij|, or plain FP32 positions when PLAIN),
 //                    one rsqrt, partial sums per tile folded into a compensated
-//                    (TwoSum) pair.
+//                    (TwoSum) pair. With tile boxes (bodies sorted along a
+//                    Morton curve each evaluation), a tile pair whose boxes are
+//                    apart by at least an eighth of their largest coordinate
+//                    uses the plain difference: its error, 2^-24 of the
+//                    coordinates, is then below 2^-21 of |r_ij|.
 //  k_allpairs        every other potential on small / unbounded systems, all
 //                    pairs through shared-memory tiles, same pair code as the
 //                    list kernel plus gravity and the magnetic dipole term.
@@ -19,6 +23,8 @@
 //  k_bonded          SPC/Fw harmonic bonds and H-O-H angles, one thread per
 //                    molecule (basic_potentials.jl:367-433), FP32 terms from
 //                    FP64 intramolecular differences.
+#include <cub/device/device_radix_sort.cuh>
+
 #include "nbg_internal.cuh"
 
 #define GB 128         // gravity block size = j-tile size
@@ -136,7 +142,8 @@ __device__ __forceinline__ void grav_tile(const float4* sh_hi, const float4* sh_
 // basic_potentials.jl:318-324), the j == i term skipped (:318).
 template <bool PLAIN, int TI, bool PACKED>
 __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
-                                                int64_t n, int64_t npad, int jchunks, double* __restrict__ part)
+                                                int64_t n, int64_t npad, int jchunks, double* __restrict__ part,
+                                                const float4* __restrict__ box)
 {
     static_assert(TI == 1 || TI == 2 || TI == 4, "TI");
     static_assert(!PACKED || TI >= 2, "packed needs pairs");
@@ -161,16 +168,43 @@ __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, 
     Acc2 ax[TI], ay[TI], az[TI];
 #pragma unroll
     for (int k = 0; k < TI; ++k) ax[k] = ay[k] = az[k] = Acc2{0.f, 0.f};
+    // box of this block's bodies (the union of its TI tiles' boxes)
+    float bx0 = 0.f, by0 = 0.f, bz0 = 0.f, bx1 = 0.f, by1 = 0.f, bz1 = 0.f, bm = 0.f;
+    if (!PLAIN && box) {
+        bx0 = by0 = bz0 = INFINITY;
+        bx1 = by1 = bz1 = -INFINITY;
+#pragma unroll
+        for (int k = 0; k < TI; ++k) {
+            const int64_t ti = ib0 / GB + k;
+            const float4 lo4 = box[2 * ti], hi4 = box[2 * ti + 1];
+            bx0 = fminf(bx0, lo4.x); by0 = fminf(by0, lo4.y); bz0 = fminf(bz0, lo4.z);
+            bx1 = fmaxf(bx1, hi4.x); by1 = fmaxf(by1, hi4.y); bz1 = fmaxf(bz1, hi4.z);
+            bm = fmaxf(bm, lo4.w);
+        }
+    }
     for (int64_t t = t0; t < t1; ++t) {
         const int64_t j0 = t * GB;
+        // far tile pair: the boxes' gap g with 64 g^2 >= (largest coordinate)^2
+        bool far = false;
+        if (!PLAIN && box) {
+            const float4 lo4 = box[2 * t], hi4 = box[2 * t + 1];
+            const float gx = fmaxf(0.f, fmaxf(bx0 - hi4.x, lo4.x - bx1));
+            const float gy = fmaxf(0.f, fmaxf(by0 - hi4.y, lo4.y - by1));
+            const float gz = fmaxf(0.f, fmaxf(bz0 - hi4.z, lo4.z - bz1));
+            const float g2 = gx * gx + gy * gy + gz * gz;
+            const float mm = fmaxf(bm, lo4.w);
+            far = g2 > 0.f && 64.f * g2 >= mm * mm;
+        }
         __syncthreads();
         sh_hi[threadIdx.x] = phi[j0 + threadIdx.x];
-        if (!PLAIN) sh_lo[threadIdx.x] = plo[j0 + threadIdx.x];
+        if (!PLAIN && !far) sh_lo[threadIdx.x] = plo[j0 + threadIdx.x];
         __syncthreads();
         float px[TI], py[TI], pz[TI];
 #pragma unroll
         for (int k = 0; k < TI; ++k) px[k] = py[k] = pz[k] = 0.f;
-        if ((j0 < ib0 + TI * GB) && (j0 + GB > ib0))
+        if (!PLAIN && far)
+            grav_tile<true, TI, PACKED, false>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
+        else if ((j0 < ib0 + TI * GB) && (j0 + GB > ib0))
             grav_tile<PLAIN, TI, PACKED, true>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
         else
             grav_tile<PLAIN, TI, PACKED, false>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
@@ -192,7 +226,7 @@ __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, 
     }
 }
 
-typedef void (*grav_kernel_t)(const float4*, const float4*, int64_t, int64_t, int, double*);
+typedef void (*grav_kernel_t)(const float4*, const float4*, int64_t, int64_t, int, double*, const float4*);
 
 // Kernel variants: bodies per thread (TI) x packed FP32x2; index
 // 0: TI=2 scalar, 1: TI=2 packed, 2: TI=4 scalar, 3: TI=4 packed, 4: TI=1 scalar.
@@ -208,16 +242,95 @@ static grav_kernel_t grav_variant(bool plain, int v)
 }
 static int grav_ti(int v) { return v == 2 || v == 3 ? 4 : (v == 4 ? 1 : 2); }
 
-// a_i = -G sum_chunks partial_i (fixed chunk order)
+// a_i = -G sum_chunks partial_i (fixed chunk order); with a permutation the
+// partials are in sorted order and body perm[s] receives slot s
 __global__ void k_gravity_reduce(const double* __restrict__ part, int64_t n, int jchunks, double G,
-                                 double* __restrict__ A, unsigned* status)
+                                 double* __restrict__ A, unsigned* status, const int* __restrict__ perm)
 {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x) {
         double s = 0.0;
         for (int c = 0; c < jchunks; ++c) s += part[(int64_t)c * 3 * n + e];
         double a = -G * s;
         if (!isfinite(a)) status_set(status, ST_NONFINITE);
-        A[e] = a;
+        const int64_t slot = e / 3;
+        A[perm ? 3 * (int64_t)perm[slot] + (e - 3 * slot) : e] = a;
+    }
+}
+
+// Morton order of the bodies: 10 bits per dimension of the position in
+// [-S, S]^3 (clamped), interleaved (x in the top bit of each triple).
+__device__ __forceinline__ unsigned spread3(unsigned v)
+{
+    v &= 1023u;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void k_grav_keys(const double* __restrict__ X, int64_t n, double inv2S, unsigned* keys, int* vals)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        unsigned q[3];
+        for (int k = 0; k < 3; ++k) {
+            double t = (X[3 * i + k] * inv2S + 0.5) * 1024.0;
+            t = t < 0.0 ? 0.0 : (t > 1023.0 ? 1023.0 : t);
+            q[k] = isfinite(t) ? (unsigned)t : 0u;
+        }
+        keys[i] = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
+        vals[i] = (int)i;
+    }
+}
+
+// split positions and masses in sorted order (slot s holds body perm[s])
+__global__ void k_grav_pack_sorted(const double* __restrict__ X, const double* __restrict__ mass,
+                                   const int* __restrict__ perm, int64_t n, float4* phi, float4* plo)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = perm[s];
+        float h[3], l[3];
+        for (int k = 0; k < 3; ++k) {
+            const double p = X[3 * i + k];
+            h[k] = (float)p;
+            l[k] = (float)(p - (double)h[k]);
+        }
+        phi[s] = make_float4(h[0], h[1], h[2], (float)mass[i]);
+        plo[s] = make_float4(l[0], l[1], l[2], 0.f);
+    }
+}
+
+// per 128-body tile: box min (x, y, z, largest |coordinate|) and max (x, y, z, 0)
+// over the real bodies (an empty tile gets an inverted box)
+__global__ void __launch_bounds__(GB) k_grav_boxes(const float4* __restrict__ phi, int64_t n, float4* box)
+{
+    const int64_t s = blockIdx.x * (int64_t)GB + threadIdx.x;
+    float v[7];
+    if (s < n) {
+        const float4 h = phi[s];
+        v[0] = h.x; v[1] = h.y; v[2] = h.z;
+        v[3] = -h.x; v[4] = -h.y; v[5] = -h.z;
+        v[6] = fmaxf(fabsf(h.x), fmaxf(fabsf(h.y), fabsf(h.z)));
+    } else {
+        for (int k = 0; k < 6; ++k) v[k] = INFINITY;
+        v[6] = 0.f;
+    }
+    // min of v[0..5] (max as min of negatives), max of v[6]
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int k = 0; k < 6; ++k) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+        v[6] = fmaxf(v[6], __shfl_xor_sync(0xffffffffu, v[6], o));
+    }
+    __shared__ float red[GB / 32][7];
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 7; ++k) red[threadIdx.x / 32][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < GB / 32; ++w) {
+            for (int k = 0; k < 6; ++k) v[k] = fminf(v[k], red[w][k]);
+            v[6] = fmaxf(v[6], red[w][6]);
+        }
+        box[2 * blockIdx.x] = make_float4(v[0], v[1], v[2], v[6]);
+        box[2 * blockIdx.x + 1] = make_float4(-v[3], -v[4], -v[5], 0.f);
     }
 }
 
@@ -254,14 +367,50 @@ int launch_gravity(nbg_ctx* c, const StateView& s)
 {
     int64_t units = (c->npad / (grav_ti(c->grav_variant) * GB)) * c->grav_chunks;
     grav_kernel_t kern = grav_variant(c->d.grav_plain, c->grav_variant);
+    const int* perm = nullptr;
+    if (c->grav_sort) {
+        // Morton sort (every 8th evaluation: the bodies move little in
+        // between), sorted split positions, tile boxes
+        if (!c->grav_perm_valid || c->grav_evals % 8 == 0) {
+            const double S = c->grav_scale > 0.0 ? c->grav_scale : 1.0;
+            k_grav_keys<<<grid_for(c->n, 256), 256, 0, c->stream>>>(s.x, c->n, 0.5 / S, c->grav_keys[0],
+                                                                     c->grav_vals[0]);
+            NBG_LAUNCH_CHECK(c, "k_grav_keys");
+            size_t bytes = c->grav_sort_bytes;
+            cudaError_t e = cub::DeviceRadixSort::SortPairs(c->grav_sort_tmp, bytes, c->grav_keys[0], c->grav_keys[1],
+                                                            c->grav_vals[0], c->grav_vals[1], (int)c->n, 0, 30,
+                                                            c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "gravity Morton sort");
+            c->launches += 4;  // the sort's own passes
+            c->grav_perm_valid = true;
+        }
+        ++c->grav_evals;
+        perm = c->grav_vals[1];
+        k_grav_pack_sorted<<<grid_for(c->n, 256), 256, 0, c->stream>>>(s.x, c->d.mass, perm, c->n, c->d.phi,
+                                                                          c->d.plo);
+        NBG_LAUNCH_CHECK(c, "k_grav_pack_sorted");
+        k_grav_boxes<<<(unsigned)(c->npad / GB), GB, 0, c->stream>>>(c->d.phi, c->n, c->grav_box);
+        NBG_LAUNCH_CHECK(c, "k_grav_boxes");
+    }
     prof_begin(c);
-    kern<<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks, c->grav_part);
+    kern<<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks, c->grav_part,
+                                                c->grav_sort ? c->grav_box : nullptr);
     prof_end(c);
     NBG_LAUNCH_CHECK(c, "k_gravity");
     k_gravity_reduce<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->grav_part, c->n, c->grav_chunks, c->d.G,
-                                                                      s.a_new, c->d.status);
+                                                                      s.a_new, c->d.status, perm);
     NBG_LAUNCH_CHECK(c, "k_gravity_reduce");
     return NBG_OK;
+}
+
+// scratch of the Morton sort (keys, values and cub's temporary storage) and
+// the tile boxes
+size_t gravity_sort_bytes(int64_t n)
+{
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (unsigned*)nullptr, (unsigned*)nullptr, (int*)nullptr,
+                                    (int*)nullptr, (int)n, 0, 30);
+    return bytes;
 }
 
 int gravity_plan_chunks(nbg_ctx* c, int64_t npad) { return plan_gravity(c, npad); }
@@ -584,9 +733,9 @@ cudaError_t gravity_raw_launch(const float4* phi, const float4* plo, int64_t n, 
                                double* part, double G, double* a, unsigned* status, cudaStream_t stream)
 {
     int64_t units = (npad / (2 * GB)) * jchunks;
-    k_gravity<false, 2, true><<<(unsigned)units, GB, 0, stream>>>(phi, plo, n, npad, jchunks, part);
+    k_gravity<false, 2, true><<<(unsigned)units, GB, 0, stream>>>(phi, plo, n, npad, jchunks, part, nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_gravity_reduce<<<grid_for(3 * n, 256), 256, 0, stream>>>(part, n, jchunks, G, a, status);
+    k_gravity_reduce<<<grid_for(3 * n, 256), 256, 0, stream>>>(part, n, jchunks, G, a, status, nullptr);
     return cudaGetLastError();
 }

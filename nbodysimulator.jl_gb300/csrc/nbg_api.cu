@@ -450,6 +450,18 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         if (gv) c->grav_variant = atoi(gv);
         c->grav_chunks = gravity_plan_chunks(c, c->npad);
         if ((st = dalloc(c, &c->grav_part, (size_t)c->grav_chunks * 3 * n))) return st;
+        if (!c->d.grav_plain && !getenv("NBG_GRAVITY_NO_SORT")) {
+            c->grav_sort = true;
+            for (int k = 0; k < 2; ++k) {
+                if ((st = dalloc(c, &c->grav_keys[k], n))) return st;
+                if ((st = dalloc(c, &c->grav_vals[k], n))) return st;
+            }
+            c->grav_sort_bytes = gravity_sort_bytes(n);
+            unsigned char* tmp = nullptr;
+            if ((st = dalloc(c, &tmp, c->grav_sort_bytes))) return st;
+            c->grav_sort_tmp = tmp;
+            if ((st = dalloc(c, &c->grav_box, 2 * (c->npad / 128)))) return st;
+        }
     }
     return NBG_OK;
 }
@@ -685,12 +697,24 @@ static void resident_dirty(nbg_ctx* c)
     c->respa_valid = false;
 }
 
+// half-width of the Morton cube of the gravity sort from host positions
+static void grav_scale_from(nbg_ctx* c, const double* u)
+{
+    if (!c->grav_sort) return;
+    c->grav_perm_valid = false;  // new positions: sort at the next evaluation
+    double m = 0.0;
+    for (int64_t e = 0; e < 3 * c->n; ++e)
+        if (std::isfinite(u[e])) m = std::max(m, std::fabs(u[e]));
+    c->grav_scale = m > 0.0 ? m * 1.0001 : 1.0;
+}
+
 extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
 {
     (void)t;
     if (!c || !dv || !v || !u) return NBG_ERR_ARG;
     cudaSetDevice(c->device);
     CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    grav_scale_from(c, u);
     CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     CK(cudaMemsetAsync(c->ev.a_new, 0, state_bytes(c), c->stream), "dv clear");
     resident_dirty(c);
@@ -710,6 +734,7 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
     if (!c || !u || !v) return NBG_ERR_ARG;
     cudaSetDevice(c->device);
     CK(cudaMemcpyAsync(c->st.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    grav_scale_from(c, u);
     CK(cudaMemcpyAsync(c->st.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     c->state_valid = true;
     c->accel_valid = false;

@@ -163,6 +163,17 @@ struct nbg_ctx {
     int grav_variant = 1;     // k_gravity form (bodies per thread, packed FP32x2)
     int list_lpa = 0;         // lanes per atom of k_force_list (1 = thread per atom)
     double* grav_part = nullptr;
+    // compensated gravity: bodies re-sorted along a Morton curve every
+    // evaluation; far tile pairs take the plain FP32 difference
+    bool grav_sort = false;
+    double grav_scale = 0.0;          // half-width of the Morton cube (largest |coordinate| seen)
+    unsigned* grav_keys[2] = {nullptr, nullptr};
+    int* grav_vals[2] = {nullptr, nullptr};  // [1] = the permutation (slot -> body)
+    void* grav_sort_tmp = nullptr;
+    size_t grav_sort_bytes = 0;
+    float4* grav_box = nullptr;       // 2 per 128-body tile
+    int64_t grav_evals = 0;           // gravity evaluations issued (the sort runs on every 8th)
+    bool grav_perm_valid = false;     // the permutation belongs to the positions being evaluated
     // profiling of the dominant force kernel
     bool profiling = false;
     // captured step graphs (velocity Verlet / Euler-Maruyama)
@@ -240,6 +251,7 @@ int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt);
 int launch_set_step(nbg_ctx* c, int64_t value);
 int launch_rhs_thermostat(nbg_ctx* c, const StateView& s);
 int gravity_plan_chunks(nbg_ctx* c, int64_t npad);
+size_t gravity_sort_bytes(int64_t n);
 int launch_energy(nbg_ctx* c, const StateView& s, double* out_host /*[8]*/);
 int launch_pairs(nbg_ctx* c, const StateView& s, int which, int* out_j, int* out_cnt, int64_t cap_per_atom);
 

@@ -11,10 +11,10 @@
 //                    to ~2^-24 of |r_ij|, or plain FP32 positions when PLAIN),
 //                    one rsqrt, partial sums per tile folded into a compensated
 //                    (TwoSum) pair. With tile boxes (bodies sorted along a
-//                    Morton curve each evaluation), a tile pair whose boxes are
-//                    apart by at least an eighth of their largest coordinate
-//                    uses the plain difference: its error, 2^-24 of the
-//                    coordinates, is then below 2^-21 of |r_ij|.
+//                    Morton curve), a tile pair whose boxes or radial shells
+//                    are apart by at least 1/16 of their largest |r| uses the
+//                    plain difference: its error, 2^-24 of the coordinates,
+//                    is then below 2^-19 of |r_ij|.
 //  k_allpairs        every other potential on small / unbounded systems, all
 //                    pairs through shared-memory tiles, same pair code as the
 //                    list kernel plus gravity and the magnetic dipole term.
@@ -168,34 +168,45 @@ __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, 
     Acc2 ax[TI], ay[TI], az[TI];
 #pragma unroll
     for (int k = 0; k < TI; ++k) ax[k] = ay[k] = az[k] = Acc2{0.f, 0.f};
-    // box of this block's bodies (the union of its TI tiles' boxes)
-    float bx0 = 0.f, by0 = 0.f, bz0 = 0.f, bx1 = 0.f, by1 = 0.f, bz1 = 0.f, bm = 0.f;
+    // box and radial shell of this block's bodies (the union of its TI tiles')
+    float bx0 = 0.f, by0 = 0.f, bz0 = 0.f, bx1 = 0.f, by1 = 0.f, bz1 = 0.f, br1 = 0.f, br0 = 0.f;
     if (!PLAIN && box) {
-        bx0 = by0 = bz0 = INFINITY;
-        bx1 = by1 = bz1 = -INFINITY;
+        bx0 = by0 = bz0 = br0 = INFINITY;
+        bx1 = by1 = bz1 = br1 = -INFINITY;
 #pragma unroll
         for (int k = 0; k < TI; ++k) {
             const int64_t ti = ib0 / GB + k;
             const float4 lo4 = box[2 * ti], hi4 = box[2 * ti + 1];
             bx0 = fminf(bx0, lo4.x); by0 = fminf(by0, lo4.y); bz0 = fminf(bz0, lo4.z);
             bx1 = fmaxf(bx1, hi4.x); by1 = fmaxf(by1, hi4.y); bz1 = fmaxf(bz1, hi4.z);
-            bm = fmaxf(bm, lo4.w);
+            br1 = fmaxf(br1, lo4.w);
+            br0 = fminf(br0, hi4.w);
         }
     }
+    __shared__ unsigned char far_s[GB];  // far flags of the next GB tiles of the chunk
     for (int64_t t = t0; t < t1; ++t) {
         const int64_t j0 = t * GB;
-        // far tile pair: the boxes' gap g with 64 g^2 >= (largest coordinate)^2
-        bool far = false;
-        if (!PLAIN && box) {
-            const float4 lo4 = box[2 * t], hi4 = box[2 * t + 1];
-            const float gx = fmaxf(0.f, fmaxf(bx0 - hi4.x, lo4.x - bx1));
-            const float gy = fmaxf(0.f, fmaxf(by0 - hi4.y, lo4.y - by1));
-            const float gz = fmaxf(0.f, fmaxf(bz0 - hi4.z, lo4.z - bz1));
-            const float g2 = gx * gx + gy * gy + gz * gz;
-            const float mm = fmaxf(bm, lo4.w);
-            far = g2 > 0.f && 64.f * g2 >= mm * mm;
+        // far tile pair: a lower bound g of |r_ij| (the boxes' gap, or the
+        // radial shells' gap) with 16 g >= the largest |r| of both tiles;
+        // flags for GB tiles at a time, one tile per thread
+        if (!PLAIN && box && (t - t0) % GB == 0) {
+            __syncthreads();
+            const int64_t tt = t + threadIdx.x;
+            bool f = false;
+            if (tt < t1) {
+                const float4 lo4 = box[2 * tt], hi4 = box[2 * tt + 1];
+                const float gx = fmaxf(0.f, fmaxf(bx0 - hi4.x, lo4.x - bx1));
+                const float gy = fmaxf(0.f, fmaxf(by0 - hi4.y, lo4.y - by1));
+                const float gz = fmaxf(0.f, fmaxf(bz0 - hi4.z, lo4.z - bz1));
+                const float gr = fmaxf(0.f, fmaxf(br0 - lo4.w, hi4.w - br1));
+                const float g2 = fmaxf(gx * gx + gy * gy + gz * gz, gr * gr);
+                const float mm = fmaxf(br1, lo4.w);
+                f = g2 > 0.f && 256.f * g2 >= mm * mm;
+            }
+            far_s[threadIdx.x] = f ? 1 : 0;
         }
         __syncthreads();
+        const bool far = !PLAIN && box && far_s[(t - t0) % GB];
         sh_hi[threadIdx.x] = phi[j0 + threadIdx.x];
         if (!PLAIN && !far) sh_lo[threadIdx.x] = plo[j0 + threadIdx.x];
         __syncthreads();
@@ -257,26 +268,30 @@ __global__ void k_gravity_reduce(const double* __restrict__ part, int64_t n, int
     }
 }
 
-// Morton order of the bodies: 10 bits per dimension of the position in
-// [-S, S]^3 (clamped), interleaved (x in the top bit of each triple).
-__device__ __forceinline__ unsigned spread3(unsigned v)
+// Morton order of the bodies: 21 bits per dimension of the position in
+// [-S, S]^3 (clamped), interleaved (x in the top bit of each triple). The
+// fine grid keeps a concentrated core ordered when a few bodies lie far out.
+__device__ __forceinline__ unsigned long long spread3(unsigned long long v)
 {
-    v &= 1023u;
-    v = (v | (v << 16)) & 0x030000FFu;
-    v = (v | (v << 8)) & 0x0300F00Fu;
-    v = (v | (v << 4)) & 0x030C30C3u;
-    v = (v | (v << 2)) & 0x09249249u;
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
     return v;
 }
 
-__global__ void k_grav_keys(const double* __restrict__ X, int64_t n, double inv2S, unsigned* keys, int* vals)
+__global__ void k_grav_keys(const double* __restrict__ X, int64_t n, double inv2S, unsigned long long* keys,
+                            int* vals)
 {
+    const double cells = 2097152.0;  // 2^21
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        unsigned q[3];
+        unsigned long long q[3];
         for (int k = 0; k < 3; ++k) {
-            double t = (X[3 * i + k] * inv2S + 0.5) * 1024.0;
-            t = t < 0.0 ? 0.0 : (t > 1023.0 ? 1023.0 : t);
-            q[k] = isfinite(t) ? (unsigned)t : 0u;
+            double t = (X[3 * i + k] * inv2S + 0.5) * cells;
+            t = t < 0.0 ? 0.0 : (t > cells - 1.0 ? cells - 1.0 : t);
+            q[k] = isfinite(t) ? (unsigned long long)t : 0ull;
         }
         keys[i] = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
         vals[i] = (int)i;
@@ -300,37 +315,32 @@ __global__ void k_grav_pack_sorted(const double* __restrict__ X, const double* _
     }
 }
 
-// per 128-body tile: box min (x, y, z, largest |coordinate|) and max (x, y, z, 0)
-// over the real bodies (an empty tile gets an inverted box)
+// per 128-body tile over its real bodies: box min (x, y, z, largest |r|) and
+// box max (x, y, z, smallest |r|) (an empty tile gets an inverted box)
 __global__ void __launch_bounds__(GB) k_grav_boxes(const float4* __restrict__ phi, int64_t n, float4* box)
 {
     const int64_t s = blockIdx.x * (int64_t)GB + threadIdx.x;
-    float v[7];
+    float v[8];  // minima of x, y, z, -x, -y, -z, |r|, -|r|
     if (s < n) {
         const float4 h = phi[s];
+        const float r = sqrtf(h.x * h.x + h.y * h.y + h.z * h.z);
         v[0] = h.x; v[1] = h.y; v[2] = h.z;
         v[3] = -h.x; v[4] = -h.y; v[5] = -h.z;
-        v[6] = fmaxf(fabsf(h.x), fmaxf(fabsf(h.y), fabsf(h.z)));
+        v[6] = r; v[7] = -r;
     } else {
-        for (int k = 0; k < 6; ++k) v[k] = INFINITY;
-        v[6] = 0.f;
+        for (int k = 0; k < 8; ++k) v[k] = INFINITY;
     }
-    // min of v[0..5] (max as min of negatives), max of v[6]
-    for (int o = 16; o > 0; o >>= 1) {
-        for (int k = 0; k < 6; ++k) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
-        v[6] = fmaxf(v[6], __shfl_xor_sync(0xffffffffu, v[6], o));
-    }
-    __shared__ float red[GB / 32][7];
+    for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 8; ++k) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    __shared__ float red[GB / 32][8];
     if ((threadIdx.x & 31) == 0)
-        for (int k = 0; k < 7; ++k) red[threadIdx.x / 32][k] = v[k];
+        for (int k = 0; k < 8; ++k) red[threadIdx.x / 32][k] = v[k];
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < GB / 32; ++w) {
-            for (int k = 0; k < 6; ++k) v[k] = fminf(v[k], red[w][k]);
-            v[6] = fmaxf(v[6], red[w][6]);
-        }
-        box[2 * blockIdx.x] = make_float4(v[0], v[1], v[2], v[6]);
-        box[2 * blockIdx.x + 1] = make_float4(-v[3], -v[4], -v[5], 0.f);
+        for (int w = 1; w < GB / 32; ++w)
+            for (int k = 0; k < 8; ++k) v[k] = fminf(v[k], red[w][k]);
+        box[2 * blockIdx.x] = make_float4(v[0], v[1], v[2], -v[7]);
+        box[2 * blockIdx.x + 1] = make_float4(-v[3], -v[4], -v[5], v[6]);
     }
 }
 
@@ -378,10 +388,10 @@ int launch_gravity(nbg_ctx* c, const StateView& s)
             NBG_LAUNCH_CHECK(c, "k_grav_keys");
             size_t bytes = c->grav_sort_bytes;
             cudaError_t e = cub::DeviceRadixSort::SortPairs(c->grav_sort_tmp, bytes, c->grav_keys[0], c->grav_keys[1],
-                                                            c->grav_vals[0], c->grav_vals[1], (int)c->n, 0, 30,
+                                                            c->grav_vals[0], c->grav_vals[1], (int)c->n, 0, 63,
                                                             c->stream);
             if (e != cudaSuccess) return cuda_fail(c, e, "gravity Morton sort");
-            c->launches += 4;  // the sort's own passes
+            c->launches += 8;  // the sort's own passes
             c->grav_perm_valid = true;
         }
         ++c->grav_evals;
@@ -408,8 +418,8 @@ int launch_gravity(nbg_ctx* c, const StateView& s)
 size_t gravity_sort_bytes(int64_t n)
 {
     size_t bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (unsigned*)nullptr, (unsigned*)nullptr, (int*)nullptr,
-                                    (int*)nullptr, (int)n, 0, 30);
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                    (int*)nullptr, (int*)nullptr, (int)n, 0, 63);
     return bytes;
 }
 

@@ -167,7 +167,7 @@ struct nbg_ctx {
     // evaluation; far tile pairs take the plain FP32 difference
     bool grav_sort = false;
     double grav_scale = 0.0;          // half-width of the Morton cube (largest |coordinate| seen)
-    unsigned* grav_keys[2] = {nullptr, nullptr};
+    unsigned long long* grav_keys[2] = {nullptr, nullptr};
     int* grav_vals[2] = {nullptr, nullptr};  // [1] = the permutation (slot -> body)
     void* grav_sort_tmp = nullptr;
     size_t grav_sort_bytes = 0;

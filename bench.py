@@ -333,8 +333,8 @@ def run_mts(args, rank, world):
     eng.ml_init_params(seed=0, w1_scale=0.1)
     torch.cuda.synchronize()
     t_train = time.perf_counter()
-    loss1 = eng.ml_train(4000, batch=2048, lr=1e-3, seed=1)
-    loss2 = eng.ml_train(4000, batch=2048, lr=3e-4, seed=2)
+    loss1 = eng.ml_train(args.train_steps, batch=2048, lr=1e-3, seed=1)
+    loss2 = eng.ml_train(args.train_steps, batch=2048, lr=3e-4, seed=2)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t_train
     eng.advance(dt, 1000)  # back at 300 K; a state none of the frames saw
@@ -353,10 +353,12 @@ def run_mts(args, rank, world):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         l0 = eng.kernel_launches
+        torch.cuda.nvtx.range_push("timed")
         e0.record(stream)
         res = fn(None)
         e1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         return e0.elapsed_time(e1), eng.kernel_launches - l0, res
 
     sampler = ClockSampler(device)
@@ -405,7 +407,7 @@ def run_mts(args, rank, world):
                        "dt_outer_fs": dt * inner * 1e3, "electrostatics": "reaction field eps_rf 78.5, 0.9 nm",
                        "thermostat": "Berendsen 300 K tau 0.1 ps", "l2": "no flush (state L2-resident across steps)",
                        "training": {"frames": frames_per_T * len(temps), "temperatures_K": list(temps),
-                                    "atom_environments": list(rows), "adam_steps_per_species": 8000, "batch": 2048,
+                                    "atom_environments": list(rows), "adam_steps_per_species": 2 * args.train_steps, "batch": 2048,
                                     "final_loss_std_units": list(loss2), "train_s": t_train}},
             "plain_ns_per_day": ns_plain, "exact_split_ns_per_day": ns_ex,
             "speedup_vs_plain": ns_ml / ns_plain, "exact_split_speedup_vs_plain": ns_ex / ns_plain,
@@ -418,7 +420,8 @@ def run_mts(args, rank, world):
             "ml_kernel_ms": {"short_list": ml_ms[0], "descriptors": ml_ms[1], "mlp_bf16": ml_ms[2],
                              "force_scatter": ml_ms[3]},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None, "traffic": None, "kernel": "k_mlp_bf16",
+                         "frac": achieved / peak if peak else None,
+                         "traffic": profile_traffic(f"k_mlp_bf16:{w['name']}"), "kernel": "k_mlp_bf16",
                          "kernel_ms": ml_ms[2], "peak_source": "measured" if peak else None},
             "e2e": {"value": n * K / e2e_s, "unit": "atom-steps/s", "h2d_bytes_per_step": 2 * uh.nbytes / K,
                     "d2h_bytes_per_step": 2 * uh.nbytes / K,
@@ -450,6 +453,8 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="gravity body count (smaller profiling captures)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--grav-plain", action="store_true", help="gravity with plain FP32 positions")
+    ap.add_argument("--train-steps", type=int, default=4000,
+                    help="mts: Adam steps per species in each of the two training phases")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.steps is None:
@@ -510,6 +515,7 @@ def main():
     sampler = ClockSampler(device)
     launches0 = eng.kernel_launches
     step_ms = []
+    torch.cuda.nvtx.range_push("timed")  # ncu --nvtx --nvtx-include timed/ captures this region
     if not flush_steps:
         # all K steps back to back (the step loop replays captured CUDA graphs)
         flush.fill_(0.0)
@@ -530,6 +536,7 @@ def main():
             e1.record(stream)
             torch.cuda.synchronize()
             step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.nvtx.range_pop()
     launches = eng.kernel_launches - launches0
     clocks = sampler.stop()
     # the dominant force kernel's launch time: a separate pass with CUDA events

@@ -339,8 +339,8 @@ __global__ void k_baoab_drift(Dev d, StateView s, double dt, StepRef sr)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         const RepDev& R = d.reps[d.rep_of[i]];
         const int64_t li = i - R.atom0;
-        const double c1 = exp(-R.tparam * dt);
-        const double sd = sqrt(1.0 - c1 * c1) * sqrt(d.kb * R.T0 / d.mass[i]);
+        const double c1 = R.bc1;                              // exp(-gamma dt), set by the host for this dt
+        const double sd = __dmul_rn(R.bsd, d.rsqrt_mass[i]);  // sqrt(1 - c1^2) sqrt(kb T0 / m)
         float z[3];
         philox_normals3<float>(R.seed, (uint64_t)li, (uint64_t)step, z);
         for (int k = 0; k < 3; ++k) {

@@ -341,6 +341,14 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     if ((st = dalloc(c, &dp, n))) return st;
     D.inv_mass = dp;
     CK(cudaMemcpy(dp, im.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "inv_mass upload");
+    {
+        std::vector<double> rs(n);
+        for (int64_t i = 0; i < n; ++i) rs[i] = std::sqrt(im[i]);
+        double* rp = nullptr;
+        if ((st = dalloc(c, &rp, n))) return st;
+        D.rsqrt_mass = rp;
+        CK(cudaMemcpy(rp, rs.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "rsqrt_mass upload");
+    }
     if ((st = dalloc(c, &dp, n))) return st;
     D.charge = dp;
     CK(cudaMemcpy(dp, c->charge_h.data(), sizeof(double) * n, cudaMemcpyHostToDevice), "charge upload");
@@ -981,6 +989,22 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
     if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
     int st;
     c->respa_valid = false;  // a_old becomes the velocity-Verlet acceleration
+    if (c->baoab && c->baoab_dt != dt) {
+        // per-replica BAOAB coefficients for this dt (host FP64, uploaded before any capture)
+        for (int r = 0; r < c->nrep; ++r) {
+            RepDev& R = c->reps_h[r];
+            R.bc1 = std::exp(-R.tparam * dt);
+            R.bsd = std::sqrt(1.0 - R.bc1 * R.bc1) * std::sqrt(c->d.kb * R.T0);
+        }
+        CK(cudaMemcpyAsync(const_cast<RepDev*>(c->d.reps), c->reps_h.data(), sizeof(RepDev) * c->nrep,
+                           cudaMemcpyHostToDevice, c->stream), "replica upload");
+        CK(cudaStreamSynchronize(c->stream), "replica sync");
+        c->baoab_dt = dt;
+        if (c->graph) {
+            cudaGraphExecDestroy(c->graph);
+            c->graph = nullptr;
+        }
+    }
     if ((st = clear_status(c))) return st;
     const bool em = is_em(c);
     if (!em && !c->accel_valid) {
@@ -1739,6 +1763,7 @@ extern "C" int nbg_set_thermostat_target(nbg_ctx* c, int32_t replica, double T)
     cudaSetDevice(c->device);
     c->reps_h[replica].T0 = T;
     if (replica == 0) c->desc.thermo_T = T;
+    c->baoab_dt = -1.0;  // BAOAB noise amplitude follows T0
     RepDev* rp = const_cast<RepDev*>(c->d.reps) + replica;
     CK(cudaMemcpyAsync(rp, &c->reps_h[replica], sizeof(RepDev), cudaMemcpyHostToDevice, c->stream), "replica upload");
     CK(cudaStreamSynchronize(c->stream), "replica sync");

@@ -54,6 +54,7 @@ struct RepDev {
     int cell0;          // first cell of the replica
     double cell_inv;    // nc / L
     double T0, tparam;  // thermostat target and tau / nu / gamma
+    double bc1, bsd;    // BAOAB: exp(-gamma dt) and sqrt(1 - c1^2) sqrt(kb T0) for the current dt
     double sigma;       // Langevin noise amplitude (potential systems)
     double sigma_num;   // sqrt(2 gamma kb T) (water)
     double ndf;         // 3N - Nc
@@ -77,6 +78,7 @@ struct Dev {
     // per atom
     const double* mass;
     const double* inv_mass;
+    const double* rsqrt_mass;     // 1 / sqrt(m)
     const double* charge;
     const double* dipole;
     const int* rep_of;
@@ -183,6 +185,7 @@ struct nbg_ctx {
     double graph_dt = 0.0;
     bool use_graphs = true;
     bool baoab = false;          // Langevin by BAOAB instead of Euler-Maruyama
+    double baoab_dt = -1.0;      // dt of the BAOAB coefficients in the replica table
     // temperature folded into the kick (single system, Berendsen / Nose-Hoover)
     double* kick_part = nullptr;
     unsigned* kick_counter = nullptr;

@@ -709,7 +709,8 @@ static void resident_dirty(nbg_ctx* c)
 static void grav_scale_from(nbg_ctx* c, const double* u)
 {
     if (!c->grav_sort) return;
-    c->grav_perm_valid = false;  // new positions: sort at the next evaluation
+    // any permutation gives the same forces; the next sort (every 8th
+    // evaluation) follows the new positions
     double m = 0.0;
     for (int64_t e = 0; e < 3 * c->n; ++e)
         if (std::isfinite(u[e])) m = std::max(m, std::fabs(u[e]));

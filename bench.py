@@ -283,6 +283,17 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(value, dist, device):
+    """The largest of every rank's `value` (the job's time is its slowest
+    rank's); `value` itself without a process group."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def mts_sim(nbg, n_mol, thermo=True, T=300.0, seed=0):
     """SPC/Fw water (benchmark parameters), reaction field (eps_rf 78.5) at 0.9 nm."""
     pos, vel, L = nbg.workloads.spcfw_water_box(n_mol, seed=seed, T=T)
@@ -545,12 +556,9 @@ def main():
     eng.advance(dt, min(args.steps, 20 if args.workload == "gravity" else 200))
     kern_ms, kern_n = eng.force_kernel_time()
     eng.set_profiling(False)
-    total_ms = float(sum(step_ms))
-    t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{device}")
+    total_ms = max_over_ranks(float(sum(step_ms)), dist, f"cuda:{device}")
     if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dist.barrier()
-    total_ms = float(t.item())
     value = n * args.steps * world / (total_ms / 1e3)
 
     # end-to-end: the drop-in right-hand side on pinned host buffers, with the

@@ -49,7 +49,7 @@ __global__ void k_drift_pack(Dev d, StateView s, double dt, double dtsq, int che
             double dy = s.x[3 * i + 1] - d.xref[3 * i + 1];
             double dz = s.x[3 * i + 2] - d.xref[3 * i + 2];
             double d2 = dx * dx + dy * dy + dz * dz;
-            if (!(d2 <= d.skin_half2)) d.rebuild_flag[parity] = 1;
+            if (!(d2 <= d.skin_half2)) d.rebuild_flag[parity * d.nrep + d.rep_of[i]] = 1;
         }
     }
 }
@@ -65,7 +65,7 @@ __global__ void k_pack_disp(Dev d, const double* X, int check_disp, StepRef pos)
             double dy = X[3 * i + 1] - d.xref[3 * i + 1];
             double dz = X[3 * i + 2] - d.xref[3 * i + 2];
             double d2 = dx * dx + dy * dy + dz * dz;
-            if (!(d2 <= d.skin_half2)) d.rebuild_flag[parity] = 1;
+            if (!(d2 <= d.skin_half2)) d.rebuild_flag[parity * d.nrep + d.rep_of[i]] = 1;
         }
     }
 }
@@ -356,7 +356,7 @@ __global__ void k_baoab_drift(Dev d, StateView s, double dt, StepRef sr)
             double dx = s.x[3 * i] - d.xref[3 * i];
             double dy = s.x[3 * i + 1] - d.xref[3 * i + 1];
             double dz = s.x[3 * i + 2] - d.xref[3 * i + 2];
-            if (!(dx * dx + dy * dy + dz * dz <= d.skin_half2)) d.rebuild_flag[parity] = 1;
+            if (!(dx * dx + dy * dy + dz * dz <= d.skin_half2)) d.rebuild_flag[parity * d.nrep + d.rep_of[i]] = 1;
         }
     }
 }

@@ -160,10 +160,10 @@ struct Stager {
 __global__ void __launch_bounds__(256) k_short_list(Dev d, MLView m, StepRef pos, int force, int* snbr, int* scount)
 {
     const int parity = (int)(step_of(pos) & 1);
-    if (!(force || d.rebuild_flag[parity])) return;
     const int lane = threadIdx.x % 32;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
     if (i >= d.n) return;
+    if (!(force || d.rebuild_flag[parity * d.nrep + d.rep_of[i]])) return;
     const RepDev& R = d.reps[d.rep_of[i]];
     const float4 hi = d.phi[i], lo = d.plo[i];
     const int cnt = d.nbr_count[i];

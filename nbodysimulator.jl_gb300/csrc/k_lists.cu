@@ -30,9 +30,12 @@ struct ListCtl {
 
 __device__ __forceinline__ int read_parity(const ListCtl& L) { return (int)(step_of(L.pos) & 1); }
 
-__device__ __forceinline__ bool need_build(const Dev& d, const ListCtl& L)
+// Replica r's list is rebuilt when the host forces it or one of its atoms
+// moved more than skin/2 (flags per replica, so one fast atom in a batch
+// rebuilds only its own replica).
+__device__ __forceinline__ bool need_build(const Dev& d, const ListCtl& L, int rep)
 {
-    return L.force || d.rebuild_flag[read_parity(L)] != 0;
+    return L.force || d.rebuild_flag[read_parity(L) * d.nrep + rep] != 0;
 }
 
 __device__ __forceinline__ int cell_coord(float h, const RepDev& R)
@@ -45,8 +48,13 @@ __device__ __forceinline__ int cell_coord(float h, const RepDev& R)
 
 __global__ void k_cell_fill(Dev d, ListCtl L)
 {
-    if (!need_build(d, L)) return;
+    // the other parity's flags start clean for the next drift (nothing of
+    // this build reads them)
+    const int other = (read_parity(L) ^ 1) * d.nrep;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.nrep; r += gridDim.x * blockDim.x)
+        d.rebuild_flag[other + r] = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!need_build(d, L, d.rep_of[i])) continue;
         const RepDev& R = d.reps[d.rep_of[i]];
         float4 h = d.phi[i];
         int cx = cell_coord(h.x, R), cy = cell_coord(h.y, R), cz = cell_coord(h.z, R);
@@ -60,9 +68,11 @@ __global__ void k_cell_fill(Dev d, ListCtl L)
 // One block per cell: rank sort of the (distinct) atom indices.
 __global__ void k_cell_sort(Dev d, ListCtl L)
 {
-    if (!need_build(d, L)) return;
     extern __shared__ int sh[];
     for (int cell = blockIdx.x; cell < d.ncell_total; cell += gridDim.x) {
+        const int rep = d.cell_rep[cell];
+        if (!need_build(d, L, rep)) continue;
+        if (threadIdx.x == 0 && cell == d.reps[rep].cell0) atomicAdd(d.build_count, 1ull);  // one per replica
         int cnt = d.cell_count[cell];
         if (cnt > d.cell_cap) cnt = d.cell_cap;
         int* src = d.cell_atoms + (int64_t)cell * d.cell_cap;
@@ -88,10 +98,8 @@ __global__ void k_cell_sort(Dev d, ListCtl L)
 // 27 cells in the same order as the block-per-cell build.
 __global__ void k_list_build(Dev d, ListCtl L, const double* X)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.rebuild_flag[read_parity(L) ^ 1] = 0;
-    if (!need_build(d, L)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.build_count, 1ull);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!need_build(d, L, d.rep_of[i])) continue;
         const RepDev& R = d.reps[d.rep_of[i]];
         float4 hi = d.phi[i], lo = d.plo[i];
         int cx = cell_coord(hi.x, R), cy = cell_coord(hi.y, R), cz = cell_coord(hi.z, R);
@@ -146,14 +154,12 @@ __global__ void k_list_build(Dev d, ListCtl L, const double* X)
 template <int LPA>
 __global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, const double* X)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.rebuild_flag[read_parity(L) ^ 1] = 0;
-    if (!need_build(d, L)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.build_count, 1ull);
     const int lane = threadIdx.x % LPA;
     const int gbase = (threadIdx.x % 32) - lane;  // first lane of the group within the warp
     const unsigned gmask = (LPA == 32) ? 0xffffffffu : (((1u << LPA) - 1u) << gbase);
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LPA;
     if (i >= d.n) return;  // whole groups leave together
+    if (!need_build(d, L, d.rep_of[i])) return;
     const RepDev& R = d.reps[d.rep_of[i]];
     const float4 hi = d.phi[i], lo = d.plo[i];
     const int cx = cell_coord(hi.x, R), cy = cell_coord(hi.y, R), cz = cell_coord(hi.z, R);
@@ -216,20 +222,19 @@ __global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, cons
 
 __global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, const double* X)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.rebuild_flag[read_parity(L) ^ 1] = 0;
-    if (!need_build(d, L)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.build_count, 1ull);
     __shared__ float4 tile[LB_TILE];
     __shared__ int nb_cell[27];
     __shared__ float4 nb_shift[27];
     __shared__ int nb_pre[28];
     const bool water = d.kind == NBG_SYSTEM_WATER;
     for (int cell = blockIdx.x; cell < d.ncell_total; cell += gridDim.x) {
+        const int rep = d.cell_rep[cell];
+        if (!need_build(d, L, rep)) continue;
         int cnt = d.cell_n[cell];
         if (cnt > d.cell_cap) cnt = d.cell_cap;
         if (cnt == 0) continue;
         const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
-        const RepDev& R = d.reps[d.rep_of[atoms[0]]];
+        const RepDev& R = d.reps[rep];
         const int nc = R.nc;
         const int lc = cell - R.cell0;
         const int cx = lc / (nc * nc), cy = (lc / nc) % nc, cz = lc % nc;

@@ -322,6 +322,18 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     D.ncell_total = cell0;
 
     int st;
+    {
+        std::vector<int> cr((size_t)std::max(cell0, 1), 0);
+        for (int r = 0; r < nrep; ++r) {
+            const RepDev& R = c->reps_h[r];
+            if (c->path != PATH_LIST) break;
+            for (int k = 0; k < R.nc * R.nc * R.nc; ++k) cr[(size_t)R.cell0 + k] = r;
+        }
+        int* cp = nullptr;
+        if ((st = dalloc(c, &cp, cr.size()))) return st;
+        CK(cudaMemcpy(cp, cr.data(), sizeof(int) * cr.size(), cudaMemcpyHostToDevice), "cell_rep upload");
+        D.cell_rep = cp;
+    }
     // state
     StateView* views[2] = {&c->st, &c->ev};
     for (StateView* sv : views) {
@@ -391,7 +403,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     }
 
     if ((st = dalloc(c, &D.status, 4))) return st;
-    if ((st = dalloc(c, &D.rebuild_flag, 2))) return st;
+    if ((st = dalloc(c, &D.rebuild_flag, 2 * (size_t)nrep))) return st;
     if ((st = dalloc(c, &D.build_count, 1))) return st;
     if ((st = dalloc(c, &D.step_dev, 1))) return st;
     // slices of 256 atoms per replica (the last block adds them in order)

@@ -97,7 +97,8 @@ struct Dev {
     int64_t nbr_kstride;  // n (column-major, thread per atom) or 1 (row-major, lanes per atom)
     int64_t nbr_istride;  // 1 or nbr_cap
     double* xref;
-    int* rebuild_flag;          // [2], indexed by the parity of the position time index
+    int* rebuild_flag;          // [2][nrep]: per replica, by the parity of the position time index
+    const int* cell_rep;        // replica of each cell
     unsigned long long* build_count;
     unsigned* status;
     int64_t* step_dev;          // step counter read by graph-captured kernels

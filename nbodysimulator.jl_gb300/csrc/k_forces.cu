@@ -548,9 +548,23 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
         float px = 0.f, py = 0.f, pz = 0.f;
         bool range_err = false;
         const int* nl = d.nbr + i * d.nbr_istride;
+        // the next neighbour's index and split position are loaded one entry
+        // ahead, so that their gathers overlap this pair's arithmetic
+        int jn = 0;
+        float4 hn = make_float4(0.f, 0.f, 0.f, 0.f), ln = hn;
+        if (cnt > 0) {
+            jn = __ldg(nl);
+            hn = __ldg(&d.phi[jn]);
+            ln = __ldg(&d.plo[jn]);
+        }
         for (int k = 0; k < cnt; ++k) {
-            int j = __ldg(nl + (int64_t)k * d.nbr_kstride);
-            float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
+            const int j = jn;
+            const float4 hj = hn, lj = ln;
+            if (k + 1 < cnt) {
+                jn = __ldg(nl + (int64_t)(k + 1) * d.nbr_kstride);
+                hn = __ldg(&d.phi[jn]);
+                ln = __ldg(&d.plo[jn]);
+            }
             PairOut o = pair_cutoff(d, R, i, j, hi_i, lo_i, hj, lj, kqi, s.x);
             range_err |= o.range_err;
             px += o.fx;

@@ -652,6 +652,30 @@ def main():
             eng.compute_forces()
             a_gpu = eng.get_accel()[:ns]
             line["force_rel_rmse"] = float(np.linalg.norm(a_gpu - a_ref) / np.linalg.norm(a_ref))
+            if args.workload == "gravity" and not args.grav_plain:
+                # the same steps with plain FP32 position differences everywhere
+                dp = wl.descs[0]
+                dp.flags |= nbg._abi.NBG_FLAG_GRAV_PLAIN
+                ep = nbg.Engine([dp], device)
+                ep.set_stream(stream.cuda_stream)
+                ep.set_state(u0, v0)
+                ep.advance(dt, args.warmup)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                ep.advance(dt, args.steps)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms_plain = e0.elapsed_time(e1) / args.steps
+                ep.set_state(u_end, v_end)
+                ep.compute_forces()
+                a_plain = ep.get_accel()[:ns]
+                line["plain_fp32_positions"] = {
+                    "value": n / (ms_plain / 1e3), "unit": "atom-steps/s", "ms_per_step": ms_plain,
+                    "l2": "no flush (steps back to back)",
+                    "force_rel_rmse": float(np.linalg.norm(a_plain - a_ref) / np.linalg.norm(a_ref))}
+                ep.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -105,7 +105,7 @@ __global__ void k_list_build(Dev d, ListCtl L, const double* X)
         int cx = cell_coord(hi.x, R), cy = cell_coord(hi.y, R), cz = cell_coord(hi.z, R);
         int cnt = 0;
         const bool water = d.kind == NBG_SYSTEM_WATER;
-        const int o0 = R.nc >= 3 ? -1 : 0, o1 = R.nc >= 3 ? 1 : 0;
+        const int o0 = -R.ns, o1 = R.ns;
         for (int ox = o0; ox <= o1; ++ox) {
             int nx = cx + ox;
             nx += (nx < 0) ? R.nc : 0;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, cons
     const bool water = d.kind == NBG_SYSTEM_WATER;
     int cnt = 0;
     int* out = d.nbr + i * d.nbr_istride;
-    const int o0 = R.nc >= 3 ? -1 : 0, o1 = R.nc >= 3 ? 1 : 0;
+    const int o0 = -R.ns, o1 = R.ns;
     for (int ox = o0; ox <= o1; ++ox) {
         int nx = cx + ox;
         nx += (nx < 0) ? R.nc : 0;
@@ -214,18 +214,18 @@ __global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, cons
     if (lane < 3) d.xref[3 * i + lane] = X[3 * i + lane];
 }
 
-// Candidates of the 27 (or, for a one-cell replica, 1) neighbour cells in
-// scan order (ox, oy, oz from -1 to 1; each cell's atoms by index), TILE at
-// a time. The test r^2 < rl2 on the hi parts is the list's superset test (the
+// Candidates of the stencil's cells (125 or 27, or for a one-cell replica 1)
+// in scan order (ox, oy, oz from -ns to ns; each cell's atoms by index), TILE
+// at a time. The test r^2 < rl2 on the hi parts is the list's superset test (the
 // force kernels classify every pair exactly); the list order is the scan order.
 #define LB_TILE 1024
 
 __global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, const double* X)
 {
     __shared__ float4 tile[LB_TILE];
-    __shared__ int nb_cell[27];
-    __shared__ float4 nb_shift[27];
-    __shared__ int nb_pre[28];
+    __shared__ int nb_cell[125];
+    __shared__ float4 nb_shift[125];
+    __shared__ int nb_pre[126];
     const bool water = d.kind == NBG_SYSTEM_WATER;
     for (int cell = blockIdx.x; cell < d.ncell_total; cell += gridDim.x) {
         const int rep = d.cell_rep[cell];
@@ -238,16 +238,12 @@ __global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, cons
         const int nc = R.nc;
         const int lc = cell - R.cell0;
         const int cx = lc / (nc * nc), cy = (lc / nc) % nc, cz = lc % nc;
-        const bool one = nc < 3;  // one cell holds the replica: minimum image per pair
-        const int nnb = one ? 1 : 27;
+        const bool one = R.ns == 0;  // one cell holds the replica: minimum image per pair
+        const int w = 2 * R.ns + 1;  // stencil width (1, 3 or 5)
+        const int nnb = w * w * w;
         __syncthreads();  // previous cell's use of the shared tables is over
-        if (threadIdx.x < nnb) {
-            int ox = 0, oy = 0, oz = 0;
-            if (!one) {
-                ox = threadIdx.x / 9 - 1;
-                oy = (threadIdx.x / 3) % 3 - 1;
-                oz = threadIdx.x % 3 - 1;
-            }
+        for (int q = threadIdx.x; q < nnb; q += blockDim.x) {
+            const int ox = q / (w * w) - R.ns, oy = (q / w) % w - R.ns, oz = q % w - R.ns;
             int nx = cx + ox, ny = cy + oy, nz = cz + oz;
             float sx = 0.f, sy = 0.f, sz = 0.f;
             if (nx < 0) { nx += nc; sx = -R.Lh; }
@@ -256,15 +252,18 @@ __global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, cons
             if (ny >= nc) { ny -= nc; sy = R.Lh; }
             if (nz < 0) { nz += nc; sz = -R.Lh; }
             if (nz >= nc) { nz -= nc; sz = R.Lh; }
-            nb_cell[threadIdx.x] = R.cell0 + (nx * nc + ny) * nc + nz;
-            nb_shift[threadIdx.x] = make_float4(sx, sy, sz, 0.f);
+            const int cq = R.cell0 + (nx * nc + ny) * nc + nz;
+            nb_cell[q] = cq;
+            nb_shift[q] = make_float4(sx, sy, sz, 0.f);
+            nb_pre[q + 1] = min(d.cell_n[cq], d.cell_cap);  // counts, summed below
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             int acc = 0;
             for (int q = 0; q < nnb; ++q) {
+                const int cq = nb_pre[q + 1];
                 nb_pre[q] = acc;
-                acc += min(d.cell_n[nb_cell[q]], d.cell_cap);
+                acc += cq;
             }
             nb_pre[nnb] = acc;
         }
@@ -283,8 +282,14 @@ __global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, cons
                 __syncthreads();  // the previous tile is consumed
                 for (int k = threadIdx.x; k < tn; k += blockDim.x) {
                     const int g = t0 + k;
-                    int q = 0;
-                    while (q + 1 < nnb && nb_pre[q + 1] <= g) ++q;
+                    // the stencil cell holding entry g: the last q with nb_pre[q] <= g
+                    int lo_q = 0, hi_q = nnb - 1;
+                    while (lo_q < hi_q) {
+                        const int mid = (lo_q + hi_q + 1) >> 1;
+                        if (nb_pre[mid] <= g) lo_q = mid;
+                        else hi_q = mid - 1;
+                    }
+                    const int q = lo_q;
                     const int j = d.cell_atoms[(int64_t)nb_cell[q] * d.cell_cap + (g - nb_pre[q])];
                     const float4 hj = d.phi[j];
                     const float4 sh = nb_shift[q];

@@ -51,6 +51,7 @@ struct RepDev {
     float el_lo, el_hi;
     float rl2;          // Verlet-list radius^2 (inflated)
     int nc;             // cells per dimension
+    int ns;             // cell stencil half-width: cells >= rl / ns (0: one cell holds the replica)
     int cell0;          // first cell of the replica
     double cell_inv;    // nc / L
     double T0, tparam;  // thermostat target and tau / nu / gamma

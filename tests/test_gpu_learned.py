@@ -226,3 +226,54 @@ def test_respa_judge_falls_back_to_velocity_verlet(water, trained):
     ua, va = eng.get_state()
     assert np.abs(ua - ub).max() < 1e-6
     assert np.abs(va - vb).max() < 1e-4
+
+
+def test_learned_api_errors(gpu):
+    """The learned model refuses systems it does not model, and the r-RESPA
+    entry point refuses bad arguments and unsupported thermostats."""
+    import systems as S
+    nbg = S.nbg
+    # a Lennard-Jones liquid: not water
+    sim = S.lj_liquid(1000, seed=2)
+    eng = sim.engine()
+    with pytest.raises(nbg.EngineError) as e:
+        eng.ml_enable()
+    assert e.value.status == -6  # NBG_ERR_UNSUPPORTED
+    # calls before nbg_ml_enable
+    sim, pos, vel, L = systems.spcfw_water_rf(1000)
+    eng = sim.engine()
+    with pytest.raises(nbg.EngineError):
+        eng.ml_eval(pos)
+    eng.ml_enable()
+    with pytest.raises(nbg.EngineError):
+        eng.ml_set_params(2, np.zeros(nbg._abi.NBG_ML_NPARAM, dtype=np.float32))
+    with pytest.raises(nbg.EngineError):  # no resident state yet
+        eng.respa_run(DT, 4, 1)
+    eng.set_state(pos, vel)
+    with pytest.raises(nbg.EngineError):
+        eng.respa_run(-DT, 4, 1)
+    with pytest.raises(nbg.EngineError):
+        eng.respa_run(DT, 0, 1)
+    with pytest.raises(nbg.EngineError):  # empty training set
+        eng.ml_train(10)
+    # Andersen is not supported by r-RESPA
+    simA, pos, vel, L = systems.spcfw_water_rf(1000)
+    simA.thermostat = nbg.AndersenThermostat(300.0, 10.0)
+    engA = simA.engine()
+    engA.ml_enable()
+    engA.set_state(pos, vel)
+    with pytest.raises(nbg.EngineError) as e:
+        engA.respa_run(DT, 4, 1)
+    assert e.value.status == -6
+
+
+def test_thermostat_target_moves_temperature(water):
+    """nbg_set_thermostat_target: a Berendsen run re-targeted to 320 K heats up."""
+    sim, pos, vel, L = systems.spcfw_water_rf(1000)
+    eng = sim.engine()
+    eng.set_state(water["u"], water["v"])
+    eng.set_thermostat_target(320.0)
+    eng.advance(DT, 3000)
+    u, v = eng.get_state()
+    T = eng.energy(u, v)["temperature"]
+    assert 305.0 < T < 335.0, T

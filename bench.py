@@ -350,6 +350,7 @@ def run_mts(args, rank, world):
     t_train = time.perf_counter() - t_train
     eng.advance(dt, 1000)  # back at 300 K; a state none of the frames saw
     u0, v0 = eng.get_state()
+    tuned = eng.autotune(5)  # lanes per atom of the exact non-bonded force
     _, f_ml = eng.ml_eval(u0)
     _, f_sr = eng.ml_labels(u0)
     f_sr = f_sr.astype(np.float64)
@@ -417,6 +418,7 @@ def run_mts(args, rank, world):
             "config": {"workload": w["name"], "N": n, "dt_inner_fs": dt * 1e3, "inner_steps": inner,
                        "dt_outer_fs": dt * inner * 1e3, "electrostatics": "reaction field eps_rf 78.5, 0.9 nm",
                        "thermostat": "Berendsen 300 K tau 0.1 ps", "l2": "no flush (state L2-resident across steps)",
+                       "lanes_per_atom": tuned[0], "autotune_force_ms": tuned[1],
                        "training": {"frames": frames_per_T * len(temps), "temperatures_K": list(temps),
                                     "atom_environments": list(rows), "adam_steps_per_species": 2 * args.train_steps, "batch": 2048,
                                     "final_loss_std_units": list(loss2), "train_s": t_train}},
@@ -516,6 +518,10 @@ def main():
 
     eng.set_state(u0, v0)
     e_start = None if batch else eng.energy(u0, v0)
+    tuned = None
+    if args.workload in ("lj", "water", "ensemble"):
+        # the list force kernel's lanes per atom, timed on this state (untimed here)
+        tuned = eng.autotune(5)
     eng.advance(dt, args.warmup)
     torch.cuda.synchronize()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
@@ -615,6 +621,9 @@ def main():
               "parallelism": "replicas only" if world > 1 else "single GPU"}
     if args.workload == "gravity":
         config["gravity_precision"] = "plain FP32 positions" if args.grav_plain else "hi/lo split positions (compensated)"
+    if tuned is not None:
+        config["lanes_per_atom"] = tuned[0]
+        config["autotune_force_ms"] = tuned[1]
     if batch:
         config.update(integrator="BAOAB Langevin (gamma=1)", replicas=len(wl.sizes),
                       atoms_min=int(min(wl.sizes)), atoms_max=int(max(wl.sizes)))

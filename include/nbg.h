@@ -338,6 +338,13 @@ NBG_API int nbg_ml_batch_gradient(nbg_ctx* ctx, int32_t species, const float* x,
 NBG_API int nbg_respa_run(nbg_ctx* ctx, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,
                           nbg_respa_stats* stats);
 
+/* Autotuner of the Verlet-list force kernel: times every lanes-per-atom form
+   (index 0: a thread per atom; 1..4: 4, 8, 16, 32 lanes per atom) over `reps`
+   launches on the resident positions, writes the times (ms, may be NULL) to
+   ms[5] and keeps the fastest form for the context (*lpa: 1, 4, 8, 16 or 32).
+   Results do not depend on the choice beyond FP32 summation order. */
+NBG_API int nbg_autotune(nbg_ctx* ctx, int32_t reps, int32_t* lpa, double* ms);
+
 /* Change a replica's thermostat target temperature (the reference builds a
    new simulation with another thermostat; this keeps the context). */
 NBG_API int nbg_set_thermostat_target(nbg_ctx* ctx, int32_t replica, double T);

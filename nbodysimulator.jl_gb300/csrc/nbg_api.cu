@@ -159,6 +159,18 @@ static int choose_path(const nbg_system_desc* descs, int nrep)
     return -1;
 }
 
+// Verlet-list layout of the force kernel's lanes per atom
+static void set_list_layout(nbg_ctx* c)
+{
+    if (c->list_lpa <= 1) {  // column-major for thread per atom
+        c->d.nbr_kstride = c->n;
+        c->d.nbr_istride = 1;
+    } else {                 // row-major for lanes per atom
+        c->d.nbr_kstride = 1;
+        c->d.nbr_istride = c->d.nbr_cap;
+    }
+}
+
 static int alloc_lists(nbg_ctx* c, int cell_cap, int nbr_cap)
 {
     int st;
@@ -170,13 +182,7 @@ static int alloc_lists(nbg_ctx* c, int cell_cap, int nbr_cap)
     if ((st = dalloc(c, &c->d.nbr, (size_t)c->n * nbr_cap))) return st;
     c->d.cell_cap = cell_cap;
     c->d.nbr_cap = nbr_cap;
-    if (c->list_lpa <= 1) {  // column-major for thread per atom
-        c->d.nbr_kstride = c->n;
-        c->d.nbr_istride = 1;
-    } else {                 // row-major for lanes per atom
-        c->d.nbr_kstride = 1;
-        c->d.nbr_istride = nbr_cap;
-    }
+    set_list_layout(c);
     return NBG_OK;
 }
 
@@ -1832,4 +1838,64 @@ extern "C" int nbg_ml_kernel_times(nbg_ctx* c, int32_t reps, double* ms)
     if (st) return st;
     for (int k = 0; k < 4; ++k) ms[k] = acc[k] / reps;
     return NBG_OK;
+}
+
+// Autotuner of the Verlet-list force kernel: on the resident positions, time
+// every lanes-per-atom form (a thread per atom with a column-major list, or
+// 4 / 8 / 16 / 32 lanes per atom with a row-major list) over `reps` launches
+// and keep the fastest for this context.
+extern "C" int nbg_autotune(nbg_ctx* c, int32_t reps, int32_t* lpa_out, double* ms_out)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (c->path != PATH_LIST) return fail(c, NBG_ERR_UNSUPPORTED, "autotuning applies to the Verlet-list path");
+    if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
+    cudaSetDevice(c->device);
+    if (reps < 1) reps = 1;
+    const int cands[5] = {1, 4, 8, 16, 32};
+    const int keep = c->list_lpa;
+    int best = keep;
+    double best_ms = INFINITY;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    int st = NBG_OK;
+    for (int k = 0; k < 5 && st == NBG_OK; ++k) {
+        c->list_lpa = cands[k];
+        set_list_layout(c);
+        if ((st = clear_status(c))) break;
+        if ((st = launch_pack(c, c->st))) break;
+        if ((st = launch_list_build(c, c->st, true, StepRef{c->step, nullptr}))) break;
+        if ((st = launch_force_list(c, c->st))) break;  // warm-up
+        cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < reps && st == NBG_OK; ++r) st = launch_force_list(c, c->st);
+        cudaEventRecord(e1, c->stream);
+        if (st) break;
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            st = cuda_fail(c, e, "autotune sync");
+            break;
+        }
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        unsigned w = 0;
+        if ((st = read_status(c, &w))) break;
+        if ((st = status_error(c, w))) break;
+        const double ms = (double)t / reps;
+        if (ms_out) ms_out[k] = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cands[k];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->list_lpa = st == NBG_OK ? best : keep;
+    set_list_layout(c);
+    resident_dirty(c);  // the next step rebuilds the list in the chosen layout
+    if (c->graph) {     // captured launches hold the previous form
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    if (lpa_out) *lpa_out = c->list_lpa;
+    return st;
 }

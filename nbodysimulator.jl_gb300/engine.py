@@ -230,3 +230,11 @@ class Engine:
         ms = np.zeros(4)
         self._chk(self.lib.nbg_ml_kernel_times(self.ctx, int(reps), _abi.as_dptr(ms)))
         return ms
+
+    def autotune(self, reps=5):
+        """Time the list force kernel in every lanes-per-atom form on the resident
+        state and keep the fastest; returns (lanes per atom, {form: ms})."""
+        lpa = ctypes.c_int32()
+        ms = np.zeros(5)
+        self._chk(self.lib.nbg_autotune(self.ctx, int(reps), ctypes.byref(lpa), _abi.as_dptr(ms)))
+        return lpa.value, dict(zip(("thread", "4", "8", "16", "32"), ms.tolist()))

@@ -119,7 +119,7 @@ def algorithmic_work(workload, n, eng):
         return 20.0 * n * (n - 1), "TFLOP/s", "fp32"
     # list kernels: per atom 32 B split position + 24 B acceleration write + 4 B
     # per list entry + 32 B per neighbour gather (counted once per atom in HBM terms)
-    nbr = 73.6 if workload == "lj" else 419.0
+    nbr = 419.0 if workload == "water" else 73.6  # water: 1.0 nm list; LJ liquids (single and ensemble): 2.8 sigma
     return n * (32 + 24 + 4 * nbr), "GB/s", "hbm"
 
 

@@ -49,7 +49,7 @@ __device__ __forceinline__ int cell_coord(float h, const RepDev& R)
 __global__ void k_cell_fill(Dev d, ListCtl L)
 {
     // the other parity's flags start clean for the next drift (nothing of
-    // this build reads them)
+    // this rebuild reads them)
     const int other = (read_parity(L) ^ 1) * d.nrep;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.nrep; r += gridDim.x * blockDim.x)
         d.rebuild_flag[other + r] = 0;

@@ -1,6 +1,6 @@
 """Build the FP64 oracle (test infrastructure) into oracle/_build/liboracle.so.
 
-The oracle is the checker for the CUDA engine; only tests, the smoke check and
+The oracle is test infrastructure for the CUDA engine; only tests, the smoke check and
 the benchmark's CPU-baseline leg load it. Usage: python oracle/build.py
 """
 import os

@@ -1,6 +1,6 @@
 """FP64 numpy restatement of the learned force model (test infrastructure).
 
-TEST INFRASTRUCTURE ONLY: the checker for the engine's learned-model kernels
+TEST INFRASTRUCTURE ONLY: the oracle of the engine's learned-model kernels
 (descriptors, per-species MLP, forces by the chain rule, training gradients).
 The reference has no learned model; this file restates this project's model
 definition (the same constants as the CUDA engine) so that every GPU quantity

@@ -1,7 +1,7 @@
 /*
  * oracle.c - FP64 CPU restatement of NBodySimulator.jl's hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker for the CUDA engine
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle the CUDA engine is tested against
  * (libnbg.so): only the tests, the smoke check and the benchmark's CPU-baseline
  * leg load it. It is never part of the product path.
  *

@@ -1,6 +1,6 @@
 """ctypes wrapper of the FP64 oracle (oracle.c).
 
-TEST INFRASTRUCTURE ONLY: the checker for the CUDA engine. Only tests/, the
+TEST INFRASTRUCTURE ONLY: the oracle the CUDA engine is tested against. Only tests/, the
 smoke check and bench.py's CPU-baseline leg may import this module. It takes
 the same nbg_system_desc the engine takes (built by the package's
 system_descriptor), so both sides see identical inputs.

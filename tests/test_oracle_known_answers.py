@@ -1,6 +1,6 @@
 """The FP64 oracle against the known answers of the reference's own tests
 (NBodySimulator.jl test/*.jl). These pin the oracle before it is used as
-the checker of the GPU engine. CPU only."""
+the oracle of the GPU engine. CPU only."""
 import math
 
 import numpy as np

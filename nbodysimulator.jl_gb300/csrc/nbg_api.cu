@@ -1683,8 +1683,11 @@ static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, bool exact)
     ss.a_new = c->ml_a_slow;
     if ((st = launch_force_list(c, ss))) return st;
     if ((st = launch_ml_accel(c, -1, c->ml_a_slow))) return st;
-    if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
-    if ((st = launch_ml_judge(c, StepRef{sr.off + inner, sr.base}, inner, c->ml_judge_cap))) return st;
+    if (!exact) {
+        // the judge: the learned against the exact short-range force at these positions
+        if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
+        if ((st = launch_ml_judge(c, StepRef{sr.off + inner, sr.base}, inner, c->ml_judge_cap))) return st;
+    }
     if (berendsen && (st = launch_temperature(c, s.v))) return st;
     return launch_respa_kick(c, s.v, c->ml_a_slow, H, true);
 }

@@ -684,7 +684,7 @@ __device__ __forceinline__ void smoothstep(float r, float& S, float& dS)
     dS = (-30.f * t2 + 60.f * t3 - 30.f * t3 * t) * (1.0f / (ML_RD - ML_RS));
 }
 
-__global__ void __launch_bounds__(ML_TPB) k_sr_exact(Dev d, MLView m, float* e_out, float* f_out)
+__global__ void __launch_bounds__(ML_TPB) k_sr_exact(Dev d, MLView m, float* e_out, float* f_out, double* a_out)
 {
     const float eps4 = (float)(4.0 * d.lj_eps);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -731,6 +731,12 @@ __global__ void __launch_bounds__(ML_TPB) k_sr_exact(Dev d, MLView m, float* e_o
             f_out[3 * i] = fx;
             f_out[3 * i + 1] = fy;
             f_out[3 * i + 2] = fz;
+        }
+        if (a_out) {
+            const double im = d.inv_mass[i];
+            a_out[3 * i] = (double)fx * im;
+            a_out[3 * i + 1] = (double)fy * im;
+            a_out[3 * i + 2] = (double)fz * im;
         }
     }
 }
@@ -919,14 +925,6 @@ __global__ void k_ml_accel(const unsigned long long* fq, const double* mass, int
     }
 }
 
-// fixed-point forces from FP32 forces (the exact short-range force as the
-// inner force of a classical r-RESPA split)
-__global__ void k_fq_from_f32(const float* f, int64_t n, unsigned long long* fq)
-{
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x)
-        fq[e] = (unsigned long long)__float2ll_rn(f[e] * ML_FQ);
-}
-
 // learned forces as FP64 (host export)
 __global__ void k_ml_force_out(const unsigned long long* fq, int64_t n, double* f)
 {
@@ -956,19 +954,56 @@ __global__ void k_ml_judge(const unsigned long long* fq, const float* fsr, int64
     }
 }
 
-// outer r-RESPA kick: v += h (a_slow + Berendsen term at T of v)
-__global__ void k_respa_kick(Dev d, double* v, const double* a, double h, int thermo)
+// outer r-RESPA kick: v += h (a_slow + Berendsen term at T of v), T read
+// from red_T (the temperature of v, reduced by the kick that produced v).
+// With Berendsen it also reduces sum m v'^2 of its output into red_T (block
+// partials; the last block to finish adds them in block order).
+__global__ void __launch_bounds__(256) k_respa_kick(Dev d, double* v, const double* a, double h, double* part,
+                                                    unsigned* counter)
 {
+    const bool berendsen = d.therm == NBG_THERMO_BERENDSEN;
     const double T = d.red_T[0];
+    double acc = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * d.n; e += (int64_t)gridDim.x * blockDim.x) {
         double an = a[e];
-        if (thermo && d.therm == NBG_THERMO_BERENDSEN) {
+        if (berendsen) {
             const RepDev& R = d.reps[0];
             const double gm = 0.5 / R.tparam;
             an += (1.0 / T == INFINITY) ? gm * v[e] : gm * (R.T0 / T - 1.0) * v[e];
         }
         if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
-        v[e] = v[e] + h * an;
+        const double vn = v[e] + h * an;
+        v[e] = vn;
+        if (berendsen) acc += d.mass[e / 3] * (vn * vn);
+    }
+    if (!berendsen) return;
+    __shared__ double sh[256];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = sh[0];
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t += ((volatile double*)part)[b];
+    sh[threadIdx.x] = t;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        d.red_T[0] = sh[0] / (d.kb * d.reps[0].ndf);
+        *counter = 0u;
     }
 }
 
@@ -1059,9 +1094,9 @@ int launch_ml_force(nbg_ctx* c)
     return NBG_OK;
 }
 
-int launch_sr_exact(nbg_ctx* c, float* e_out, float* f_out)
+int launch_sr_exact(nbg_ctx* c, float* e_out, float* f_out, double* a_out)
 {
-    k_sr_exact<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, ml_view(c), e_out, f_out);
+    k_sr_exact<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, ml_view(c), e_out, f_out, a_out);
     NBG_LAUNCH_CHECK(c, "k_sr_exact");
     return NBG_OK;
 }
@@ -1073,13 +1108,26 @@ int launch_ml_accel(nbg_ctx* c, int mode, double* a)
     return NBG_OK;
 }
 
-int launch_sr_inner(nbg_ctx* c, StepRef pos, bool force_short)
+int launch_sr_inner(nbg_ctx* c, StepRef pos, bool force_short, double* a_out)
 {
     int st;
     if ((st = launch_short_list(c, pos, force_short))) return st;
-    if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
-    k_fq_from_f32<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->ml_fsr, c->n, c->ml_fq);
-    NBG_LAUNCH_CHECK(c, "k_fq_from_f32");
+    return launch_sr_exact(c, nullptr, c->ml_fsr, a_out);
+}
+
+// a (=, +=, -=) F / m from FP32 forces (the exact short-range force)
+__global__ void k_accel_from_f32(const float* f, const double* inv_mass, int64_t n, int mode, double* a)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * n; e += (int64_t)gridDim.x * blockDim.x) {
+        const double v = (double)f[e] * inv_mass[e / 3];
+        a[e] = mode == 0 ? v : (mode > 0 ? a[e] + v : a[e] - v);
+    }
+}
+
+int launch_sr_accel(nbg_ctx* c, int mode, double* a)
+{
+    k_accel_from_f32<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->ml_fsr, c->d.inv_mass, c->n, mode, a);
+    NBG_LAUNCH_CHECK(c, "k_accel_from_f32");
     return NBG_OK;
 }
 
@@ -1098,9 +1146,10 @@ int launch_ml_judge(nbg_ctx* c, StepRef sr, int inner, int slots)
     return NBG_OK;
 }
 
-int launch_respa_kick(nbg_ctx* c, double* v, const double* a, double h, bool thermo)
+int launch_respa_kick(nbg_ctx* c, double* v, const double* a, double h)
 {
-    k_respa_kick<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->d, v, a, h, thermo ? 1 : 0);
+    const int grid = std::min(grid_for(3 * c->n, 256), c->kick_blocks);
+    k_respa_kick<<<grid, 256, 0, c->stream>>>(c->d, v, a, h, c->kick_part, c->kick_counter);
     NBG_LAUNCH_CHECK(c, "k_respa_kick");
     return NBG_OK;
 }

@@ -1627,9 +1627,20 @@ extern "C" int nbg_ml_rows(nbg_ctx* c, int64_t* rows)
 
 // r-RESPA state of the resident positions: a_old = fast (bonded + learned)
 // and ml_a_slow = slow (exact non-bonded - learned) accelerations.
-static int respa_inner_force(nbg_ctx* c, StepRef pos, bool force_short, bool exact)
+// The fast non-bonded acceleration into a: learned (fixed-point forces, then
+// converted) or exact short-range (written directly).
+static int respa_inner_force(nbg_ctx* c, StepRef pos, bool force_short, bool exact, double* a)
 {
-    return exact ? launch_sr_inner(c, pos, force_short) : ml_forces(c, pos, force_short, false);
+    if (exact) return launch_sr_inner(c, pos, force_short, a);
+    int st = ml_forces(c, pos, force_short, false);
+    if (st) return st;
+    return launch_ml_accel(c, 0, a);
+}
+
+// a -= the fast non-bonded acceleration of the last respa_inner_force
+static int respa_sub_fast(nbg_ctx* c, bool exact, double* a)
+{
+    return exact ? launch_sr_accel(c, -1, a) : launch_ml_accel(c, -1, a);
 }
 
 static int respa_init(nbg_ctx* c, bool exact)
@@ -1640,15 +1651,15 @@ static int respa_init(nbg_ctx* c, bool exact)
     if ((st = launch_pack(c, s))) return st;
     if ((st = launch_list_build(c, s, true, pos))) return st;
     c->steps_since_build = 0;
-    if ((st = respa_inner_force(c, pos, true, exact))) return st;
-    if ((st = launch_ml_accel(c, 0, s.a_old))) return st;
+    if ((st = respa_inner_force(c, pos, true, exact, s.a_old))) return st;
     StateView sb = s;
     sb.a_new = s.a_old;
     if ((st = launch_bonded(c, sb))) return st;
     StateView ss = s;
     ss.a_new = c->ml_a_slow;
     if ((st = launch_force_list(c, ss))) return st;
-    if ((st = launch_ml_accel(c, -1, c->ml_a_slow))) return st;
+    if ((st = respa_sub_fast(c, exact, c->ml_a_slow))) return st;
+    if (c->d.therm == NBG_THERMO_BERENDSEN && (st = launch_temperature(c, s.v))) return st;  // T for the first kick
     c->respa_valid = true;
     c->respa_exact = exact;
     c->accel_valid = false;  // a_old no longer holds the velocity-Verlet acceleration
@@ -1665,31 +1676,29 @@ static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, bool exact)
     int st;
     const StateView& s = c->st;
     const double H = 0.5 * dt * inner;
+    // Berendsen: every kick reduces the temperature of its output for the next one
     const bool berendsen = c->d.therm == NBG_THERMO_BERENDSEN;
-    if (berendsen && (st = launch_temperature(c, s.v))) return st;
-    if ((st = launch_respa_kick(c, s.v, c->ml_a_slow, H, true))) return st;
+    if ((st = launch_respa_kick(c, s.v, c->ml_a_slow, H))) return st;
     for (int m = 0; m < inner; ++m) {
         const StepRef pos{sr.off + m + 1, sr.base};
         if ((st = launch_drift(c, s, dt, pos))) return st;
         const bool force = rebuild_due(c, true);
         if ((st = launch_list_build(c, s, force, pos))) return st;
         c->steps_since_build = force ? 0 : c->steps_since_build + 1;
-        if ((st = respa_inner_force(c, pos, force, exact))) return st;
-        if ((st = launch_ml_accel(c, 0, s.a_new))) return st;
+        if ((st = respa_inner_force(c, pos, force, exact, s.a_new))) return st;
         if ((st = launch_bonded(c, s))) return st;
-        if ((st = launch_kick(c, s, dt, false, false))) return st;
+        if ((st = launch_kick(c, s, dt, berendsen, false))) return st;
     }
     StateView ss = s;
     ss.a_new = c->ml_a_slow;
     if ((st = launch_force_list(c, ss))) return st;
-    if ((st = launch_ml_accel(c, -1, c->ml_a_slow))) return st;
+    if ((st = respa_sub_fast(c, exact, c->ml_a_slow))) return st;
     if (!exact) {
         // the judge: the learned against the exact short-range force at these positions
         if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
         if ((st = launch_ml_judge(c, StepRef{sr.off + inner, sr.base}, inner, c->ml_judge_cap))) return st;
     }
-    if (berendsen && (st = launch_temperature(c, s.v))) return st;
-    return launch_respa_kick(c, s.v, c->ml_a_slow, H, true);
+    return launch_respa_kick(c, s.v, c->ml_a_slow, H);
 }
 
 extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,

@@ -268,12 +268,13 @@ int launch_short_list(nbg_ctx* c, StepRef pos, bool force);
 int launch_descriptor(nbg_ctx* c, bool raw);
 int launch_mlp(nbg_ctx* c);
 int launch_ml_force(nbg_ctx* c);
-int launch_sr_exact(nbg_ctx* c, float* e_out, float* f_out);
+int launch_sr_exact(nbg_ctx* c, float* e_out, float* f_out, double* a_out = nullptr);
 int launch_ml_accel(nbg_ctx* c, int mode, double* a);
 int launch_ml_force_out(nbg_ctx* c, double* f);
-int launch_sr_inner(nbg_ctx* c, StepRef pos, bool force_short);
+int launch_sr_inner(nbg_ctx* c, StepRef pos, bool force_short, double* a_out);
+int launch_sr_accel(nbg_ctx* c, int mode, double* a);
 int launch_ml_judge(nbg_ctx* c, StepRef sr, int inner, int slots);
-int launch_respa_kick(nbg_ctx* c, double* v, const double* a, double h, bool thermo);
+int launch_respa_kick(nbg_ctx* c, double* v, const double* a, double h);
 int launch_ml_pack(nbg_ctx* c, int sp);
 int launch_ml_collect(nbg_ctx* c, int sp, int64_t off);
 int launch_ml_stats(nbg_ctx* c, int sp);

@@ -282,10 +282,26 @@ __device__ __forceinline__ unsigned long long spread3(unsigned long long v)
     return v;
 }
 
-__global__ void k_grav_keys(const double* __restrict__ X, int64_t n, double inv2S, unsigned long long* keys,
-                            int* vals)
+// Largest |coordinate| of the finite positions, rounded up to FP32, as the
+// bits of a non-negative float (which order like unsigned integers): the
+// half-width of the Morton cube. *ext must be 0 before the launch.
+__global__ void k_grav_extent(const double* __restrict__ X, int64_t m, unsigned* ext)
+{
+    float v = 0.f;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const double a = fabs(X[e]);
+        if (isfinite(a)) v = fmaxf(v, __double2float_ru(a));
+    }
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(ext, __float_as_uint(v));
+}
+
+__global__ void k_grav_keys(const double* __restrict__ X, int64_t n, const unsigned* __restrict__ ext,
+                            unsigned long long* keys, int* vals)
 {
     const double cells = 2097152.0;  // 2^21
+    const double S = (double)__uint_as_float(*ext) * 1.0001;
+    const double inv2S = S > 0.0 && isfinite(S) ? 0.5 / S : 0.5;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         unsigned long long q[3];
         for (int k = 0; k < 3; ++k) {
@@ -382,8 +398,11 @@ int launch_gravity(nbg_ctx* c, const StateView& s)
         // Morton sort (every 8th evaluation: the bodies move little in
         // between), sorted split positions, tile boxes
         if (!c->grav_perm_valid || c->grav_evals % 8 == 0) {
-            const double S = c->grav_scale > 0.0 ? c->grav_scale : 1.0;
-            k_grav_keys<<<grid_for(c->n, 256), 256, 0, c->stream>>>(s.x, c->n, 0.5 / S, c->grav_keys[0],
+            cudaError_t me = cudaMemsetAsync(c->grav_extent, 0, sizeof(unsigned), c->stream);
+            if (me != cudaSuccess) return cuda_fail(c, me, "gravity extent clear");
+            k_grav_extent<<<2 * c->sms, 256, 0, c->stream>>>(s.x, 3 * c->n, c->grav_extent);
+            NBG_LAUNCH_CHECK(c, "k_grav_extent");
+            k_grav_keys<<<grid_for(c->n, 256), 256, 0, c->stream>>>(s.x, c->n, c->grav_extent, c->grav_keys[0],
                                                                      c->grav_vals[0]);
             NBG_LAUNCH_CHECK(c, "k_grav_keys");
             size_t bytes = c->grav_sort_bytes;

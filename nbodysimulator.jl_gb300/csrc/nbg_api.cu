@@ -503,6 +503,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
             if ((st = dalloc(c, &tmp, c->grav_sort_bytes))) return st;
             c->grav_sort_tmp = tmp;
             if ((st = dalloc(c, &c->grav_box, 2 * (c->npad / 128)))) return st;
+            if ((st = dalloc(c, &c->grav_extent, 1))) return st;
         }
     }
     return NBG_OK;
@@ -739,37 +740,42 @@ static void resident_dirty(nbg_ctx* c)
     c->respa_valid = false;
 }
 
-// half-width of the Morton cube of the gravity sort from host positions
-static void grav_scale_from(nbg_ctx* c, const double* u)
-{
-    if (!c->grav_sort) return;
-    // any permutation gives the same forces; the next sort (every 8th
-    // evaluation) follows the new positions
-    double m = 0.0;
-    for (int64_t e = 0; e < 3 * c->n; ++e)
-        if (std::isfinite(u[e])) m = std::max(m, std::fabs(u[e]));
-    c->grav_scale = m > 0.0 ? m * 1.0001 : 1.0;
-}
-
 extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
 {
     (void)t;
     if (!c || !dv || !v || !u) return NBG_ERR_ARG;
     cudaSetDevice(c->device);
     CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
-    grav_scale_from(c, u);
-    CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
-    CK(cudaMemsetAsync(c->ev.a_new, 0, state_bytes(c), c->stream), "dv clear");
+    // only the Berendsen and Nose-Hoover terms of the right-hand side read v
+    if (c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER)
+        CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     resident_dirty(c);
     c->T_valid = false;  // the RHS reduces T of its own velocities into red_T
-    int st = forces_once(c, c->ev);
-    if (st) return st;
-    if ((st = launch_rhs_thermostat(c, c->ev))) return st;
-    CK(cudaMemcpyAsync(dv, c->ev.a_new, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "dv download");
-    if (c->d.therm == NBG_THERMO_NOSEHOOVER)
-        CK(cudaMemcpyAsync(v + 3 * c->n, c->ev.v + 3 * c->n, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "v download");
-    CK(cudaStreamSynchronize(c->stream), "accel sync");
-    return NBG_OK;
+    // the whole evaluation, the download and the status word in one stream
+    // pass with one synchronisation; a list overflow grows the lists and
+    // evaluates again
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        int st;
+        if ((st = clear_status(c))) return st;
+        CK(cudaMemsetAsync(c->ev.a_new, 0, state_bytes(c), c->stream), "dv clear");
+        // the sorted gravity path packs its own (permuted) split positions
+        if (!(c->path == PATH_GRAVITY && c->grav_sort) && (st = launch_pack(c, c->ev))) return st;
+        if ((st = forces(c, c->ev, true, StepRef{0, nullptr}))) return st;
+        if ((st = launch_rhs_thermostat(c, c->ev))) return st;
+        CK(cudaMemcpyAsync(dv, c->ev.a_new, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "dv download");
+        if (c->d.therm == NBG_THERMO_NOSEHOOVER)
+            CK(cudaMemcpyAsync(v + 3 * c->n, c->ev.v + 3 * c->n, sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+               "v download");
+        unsigned w = 0;
+        if ((st = read_status(c, &w))) return st;
+        if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+        if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
+            if ((st = grow_lists(c, w))) return st;
+            continue;
+        }
+        return status_error(c, w);
+    }
+    return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
 }
 
 extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
@@ -777,7 +783,6 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
     if (!c || !u || !v) return NBG_ERR_ARG;
     cudaSetDevice(c->device);
     CK(cudaMemcpyAsync(c->st.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
-    grav_scale_from(c, u);
     CK(cudaMemcpyAsync(c->st.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     c->state_valid = true;
     c->accel_valid = false;

@@ -167,10 +167,10 @@ struct nbg_ctx {
     int grav_variant = 1;     // k_gravity form (bodies per thread, packed FP32x2)
     int list_lpa = 0;         // lanes per atom of k_force_list (1 = thread per atom)
     double* grav_part = nullptr;
-    // compensated gravity: bodies re-sorted along a Morton curve every
+    // compensated gravity: bodies re-sorted along a Morton curve every 8th
     // evaluation; far tile pairs take the plain FP32 difference
     bool grav_sort = false;
-    double grav_scale = 0.0;          // half-width of the Morton cube (largest |coordinate| seen)
+    unsigned* grav_extent = nullptr;  // half-width of the Morton cube (FP32 bits), found on the device
     unsigned long long* grav_keys[2] = {nullptr, nullptr};
     int* grav_vals[2] = {nullptr, nullptr};  // [1] = the permutation (slot -> body)
     void* grav_sort_tmp = nullptr;

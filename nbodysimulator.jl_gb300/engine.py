@@ -54,11 +54,19 @@ class Engine:
         except Exception:
             pass
 
-    def accel(self, v, u, t=0.0):
-        """soode_system!(dv, v, u, p, t); returns dv. With Nose-Hoover the
-        thermostat rate is written into v[-1, 0] as in the reference."""
+    def accel(self, v, u, t=0.0, out=None):
+        """soode_system!(dv, v, u, p, t); returns dv (written into `out` when
+        given: a C-contiguous float64 array of u's shape, e.g. pinned). With
+        Nose-Hoover the thermostat rate is written into v[-1, 0] as in the
+        reference."""
         u = _f64(u)
-        dv = np.zeros_like(u)
+        if out is None:
+            dv = np.zeros_like(u)
+        else:
+            if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous
+                    and out.shape == u.shape):
+                raise TypeError("out must be a C-contiguous float64 array of u's shape")
+            dv = out
         if not (isinstance(v, np.ndarray) and v.dtype == np.float64 and v.flags.c_contiguous):
             raise TypeError("v must be a C-contiguous float64 array (it may be written)")
         self._chk(self.lib.nbg_accel(self.ctx, _abi.as_dptr(dv), _abi.as_dptr(v), _abi.as_dptr(u), float(t)))

@@ -47,7 +47,7 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
 // basic_potentials.jl:318-324), the j == i term skipped (:318).
 // Accumulate one j-tile (sh_hi / sh_lo) into the per-body partials.
 // DIAG: the tile holds some of this thread's own bodies (j == i skipped).
-template <bool PLAIN, int TI, bool PACKED, bool DIAG>
+template <bool PLAIN, int TI, bool PACKED, bool DIAG, bool UNIFORM>
 __device__ __forceinline__ void grav_tile(const float4* sh_hi, const float4* sh_lo, int64_t j0, const int64_t* ii,
                                           const float* hx, const float* hy, const float* hz, const float* lx,
                                           const float* ly, const float* lz, float* px, float* py, float* pz)
@@ -118,7 +118,8 @@ __device__ __forceinline__ void grav_tile(const float4* sh_hi, const float4* sh_
                 if (j0 + jj == ii[2 * q]) ri.x = 0.0f;
                 if (j0 + jj == ii[2 * q + 1]) ri.y = 0.0f;
             }
-            float2 sc = __fmul2_rn(__fmul2_rn(jm, ri), __fmul2_rn(ri, ri));
+            // equal masses: m_j leaves the sum (the reduction multiplies by G m)
+            float2 sc = UNIFORM ? __fmul2_rn(ri, __fmul2_rn(ri, ri)) : __fmul2_rn(__fmul2_rn(jm, ri), __fmul2_rn(ri, ri));
             px2[q] = __ffma2_rn(sc, dx, px2[q]);
             py2[q] = __ffma2_rn(sc, dy, py2[q]);
             pz2[q] = __ffma2_rn(sc, dz, pz2[q]);
@@ -140,13 +141,15 @@ __device__ __forceinline__ void grav_tile(const float4* sh_hi, const float4* sh_
 // issued FP32 instructions; both forms round every element identically.
 // Per pair: p += m_j (r_i - r_j) |r_i - r_j|^-3 (gravitational_acceleration!,
 // basic_potentials.jl:318-324), the j == i term skipped (:318).
-template <bool PLAIN, int TI, bool PACKED>
-__global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
+// UNIFORM: every body has the same mass, which the reduction applies.
+template <bool PLAIN, int TI, bool PACKED, bool UNIFORM>
+__global__ void __launch_bounds__(GB, TI == 2 ? 8 : 1) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
                                                 int64_t n, int64_t npad, int jchunks, double* __restrict__ part,
-                                                const float4* __restrict__ box)
+                                                const float4* __restrict__ box, float far2)
 {
     static_assert(TI == 1 || TI == 2 || TI == 4, "TI");
     static_assert(!PACKED || TI >= 2, "packed needs pairs");
+    static_assert(PACKED || !UNIFORM, "the uniform-mass form is packed");
     __shared__ float4 sh_hi[GB];
     __shared__ float4 sh_lo[PLAIN ? 1 : GB];
     const int64_t ntile = npad / GB;
@@ -155,11 +158,15 @@ __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, 
     const int64_t t0 = (int64_t)jc * ntile / jchunks;
     const int64_t t1 = (int64_t)(jc + 1) * ntile / jchunks;
     const int64_t ib0 = iblock * (TI * GB);
+    // thread t owns bodies ib0 + TI t .. + TI - 1: a warp's bodies lie in one
+    // of the block's TI 128-body tiles (its i-tile `it`), so the far test of a
+    // tile pair is uniform over the warp
+    const int it = (int)((threadIdx.x * TI) / GB);
     float hx[TI], hy[TI], hz[TI], lx[TI], ly[TI], lz[TI];
     int64_t ii[TI];
 #pragma unroll
     for (int k = 0; k < TI; ++k) {
-        ii[k] = ib0 + threadIdx.x + k * GB;
+        ii[k] = ib0 + (int64_t)threadIdx.x * TI + k;
         float4 h = phi[ii[k]];
         hx[k] = h.x; hy[k] = h.y; hz[k] = h.z;
         float4 l = PLAIN ? make_float4(0.f, 0.f, 0.f, 0.f) : plo[ii[k]];
@@ -168,57 +175,52 @@ __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, 
     Acc2 ax[TI], ay[TI], az[TI];
 #pragma unroll
     for (int k = 0; k < TI; ++k) ax[k] = ay[k] = az[k] = Acc2{0.f, 0.f};
-    // box and radial shell of this block's bodies (the union of its TI tiles')
-    float bx0 = 0.f, by0 = 0.f, bz0 = 0.f, bx1 = 0.f, by1 = 0.f, bz1 = 0.f, br1 = 0.f, br0 = 0.f;
-    if (!PLAIN && box) {
-        bx0 = by0 = bz0 = br0 = INFINITY;
-        bx1 = by1 = bz1 = br1 = -INFINITY;
-#pragma unroll
-        for (int k = 0; k < TI; ++k) {
-            const int64_t ti = ib0 / GB + k;
-            const float4 lo4 = box[2 * ti], hi4 = box[2 * ti + 1];
-            bx0 = fminf(bx0, lo4.x); by0 = fminf(by0, lo4.y); bz0 = fminf(bz0, lo4.z);
-            bx1 = fmaxf(bx1, hi4.x); by1 = fmaxf(by1, hi4.y); bz1 = fmaxf(bz1, hi4.z);
-            br1 = fmaxf(br1, lo4.w);
-            br0 = fminf(br0, hi4.w);
-        }
-    }
-    __shared__ unsigned char far_s[GB];  // far flags of the next GB tiles of the chunk
+    // boxes and radial shells of the block's TI i-tiles
+    __shared__ float4 ibox_s[2 * TI];
+    if (!PLAIN && box && threadIdx.x < 2 * TI) ibox_s[threadIdx.x] = box[2 * (ib0 / GB) + threadIdx.x];
+    constexpr unsigned ALL_FAR = (1u << TI) - 1u;
+    __shared__ unsigned char far_s[GB];  // per j-tile of the next GB: bit k = far from i-tile k
     for (int64_t t = t0; t < t1; ++t) {
         const int64_t j0 = t * GB;
         // far tile pair: a lower bound g of |r_ij| (the boxes' gap, or the
-        // radial shells' gap) with 16 g >= the largest |r| of both tiles;
-        // flags for GB tiles at a time, one tile per thread
+        // radial shells' gap) with F g >= the largest |r| of both tiles
+        // (far2 = F^2; F = 16 by default);
+        // flags for GB j-tiles at a time, one j-tile per thread
         if (!PLAIN && box && (t - t0) % GB == 0) {
             __syncthreads();
             const int64_t tt = t + threadIdx.x;
-            bool f = false;
+            unsigned f = 0;
             if (tt < t1) {
                 const float4 lo4 = box[2 * tt], hi4 = box[2 * tt + 1];
-                const float gx = fmaxf(0.f, fmaxf(bx0 - hi4.x, lo4.x - bx1));
-                const float gy = fmaxf(0.f, fmaxf(by0 - hi4.y, lo4.y - by1));
-                const float gz = fmaxf(0.f, fmaxf(bz0 - hi4.z, lo4.z - bz1));
-                const float gr = fmaxf(0.f, fmaxf(br0 - lo4.w, hi4.w - br1));
-                const float g2 = fmaxf(gx * gx + gy * gy + gz * gz, gr * gr);
-                const float mm = fmaxf(br1, lo4.w);
-                f = g2 > 0.f && 256.f * g2 >= mm * mm;
+#pragma unroll
+                for (int k = 0; k < TI; ++k) {
+                    const float4 a = ibox_s[2 * k], b = ibox_s[2 * k + 1];  // (min x,y,z, max|r|), (max x,y,z, min|r|)
+                    const float gx = fmaxf(0.f, fmaxf(a.x - hi4.x, lo4.x - b.x));
+                    const float gy = fmaxf(0.f, fmaxf(a.y - hi4.y, lo4.y - b.y));
+                    const float gz = fmaxf(0.f, fmaxf(a.z - hi4.z, lo4.z - b.z));
+                    const float gr = fmaxf(0.f, fmaxf(b.w - lo4.w, hi4.w - a.w));
+                    const float g2 = fmaxf(gx * gx + gy * gy + gz * gz, gr * gr);
+                    const float mm = fmaxf(a.w, lo4.w);
+                    if (g2 > 0.f && far2 * g2 >= mm * mm) f |= 1u << k;
+                }
             }
-            far_s[threadIdx.x] = f ? 1 : 0;
+            far_s[threadIdx.x] = (unsigned char)f;
         }
         __syncthreads();
-        const bool far = !PLAIN && box && far_s[(t - t0) % GB];
+        const unsigned fl = (!PLAIN && box) ? far_s[(t - t0) % GB] : 0u;
+        const bool far = (fl >> it) & 1u;
         sh_hi[threadIdx.x] = phi[j0 + threadIdx.x];
-        if (!PLAIN && !far) sh_lo[threadIdx.x] = plo[j0 + threadIdx.x];
+        if (!PLAIN && fl != ALL_FAR) sh_lo[threadIdx.x] = plo[j0 + threadIdx.x];
         __syncthreads();
         float px[TI], py[TI], pz[TI];
 #pragma unroll
         for (int k = 0; k < TI; ++k) px[k] = py[k] = pz[k] = 0.f;
         if (!PLAIN && far)
-            grav_tile<true, TI, PACKED, false>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
+            grav_tile<true, TI, PACKED, false, UNIFORM>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
         else if ((j0 < ib0 + TI * GB) && (j0 + GB > ib0))
-            grav_tile<PLAIN, TI, PACKED, true>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
+            grav_tile<PLAIN, TI, PACKED, true, UNIFORM>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
         else
-            grav_tile<PLAIN, TI, PACKED, false>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
+            grav_tile<PLAIN, TI, PACKED, false, UNIFORM>(sh_hi, sh_lo, j0, ii, hx, hy, hz, lx, ly, lz, px, py, pz);
 #pragma unroll
         for (int k = 0; k < TI; ++k) {
             ax[k].add(px[k]);
@@ -237,20 +239,26 @@ __global__ void __launch_bounds__(GB) k_gravity(const float4* __restrict__ phi, 
     }
 }
 
-typedef void (*grav_kernel_t)(const float4*, const float4*, int64_t, int64_t, int, double*, const float4*);
+typedef void (*grav_kernel_t)(const float4*, const float4*, int64_t, int64_t, int, double*, const float4*, float);
 
 // Kernel variants: bodies per thread (TI) x packed FP32x2; index
 // 0: TI=2 scalar, 1: TI=2 packed, 2: TI=4 scalar, 3: TI=4 packed, 4: TI=1 scalar.
-static grav_kernel_t grav_variant(bool plain, int v)
+// uniform (equal masses) selects the packed forms without m_j in the loop.
+static grav_kernel_t grav_variant(bool plain, int v, bool uniform)
 {
     switch (v) {
-    case 0: return plain ? k_gravity<true, 2, false> : k_gravity<false, 2, false>;
-    case 2: return plain ? k_gravity<true, 4, false> : k_gravity<false, 4, false>;
-    case 3: return plain ? k_gravity<true, 4, true> : k_gravity<false, 4, true>;
-    case 4: return plain ? k_gravity<true, 1, false> : k_gravity<false, 1, false>;
-    default: return plain ? k_gravity<true, 2, true> : k_gravity<false, 2, true>;
+    case 0: return plain ? k_gravity<true, 2, false, false> : k_gravity<false, 2, false, false>;
+    case 2: return plain ? k_gravity<true, 4, false, false> : k_gravity<false, 4, false, false>;
+    case 3:
+        if (uniform) return plain ? k_gravity<true, 4, true, true> : k_gravity<false, 4, true, true>;
+        return plain ? k_gravity<true, 4, true, false> : k_gravity<false, 4, true, false>;
+    case 4: return plain ? k_gravity<true, 1, false, false> : k_gravity<false, 1, false, false>;
+    default:
+        if (uniform) return plain ? k_gravity<true, 2, true, true> : k_gravity<false, 2, true, true>;
+        return plain ? k_gravity<true, 2, true, false> : k_gravity<false, 2, true, false>;
     }
 }
+static bool grav_variant_packed(int v) { return v == 1 || v == 3 || v < 0 || v > 4; }
 static int grav_ti(int v) { return v == 2 || v == 3 ? 4 : (v == 4 ? 1 : 2); }
 
 // a_i = -G sum_chunks partial_i (fixed chunk order); with a permutation the
@@ -366,7 +374,8 @@ static int plan_gravity(nbg_ctx* c, int64_t npad)
 {
     int dev = c->device, sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, grav_variant(c->d.grav_plain, c->grav_variant), GB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, grav_variant(c->d.grav_plain, c->grav_variant, c->grav_uniform),
+                                                  GB, 0);
     if (sms < 1) sms = 1;
     if (occ < 1) occ = 1;
     const double slots = (double)sms * occ;
@@ -392,7 +401,8 @@ static int plan_gravity(nbg_ctx* c, int64_t npad)
 int launch_gravity(nbg_ctx* c, const StateView& s)
 {
     int64_t units = (c->npad / (grav_ti(c->grav_variant) * GB)) * c->grav_chunks;
-    grav_kernel_t kern = grav_variant(c->d.grav_plain, c->grav_variant);
+    const bool uniform = c->grav_uniform && grav_variant_packed(c->grav_variant);
+    grav_kernel_t kern = grav_variant(c->d.grav_plain, c->grav_variant, uniform);
     const int* perm = nullptr;
     if (c->grav_sort) {
         // Morton sort (every 8th evaluation: the bodies move little in
@@ -423,10 +433,11 @@ int launch_gravity(nbg_ctx* c, const StateView& s)
     }
     prof_begin(c);
     kern<<<(unsigned)units, GB, 0, c->stream>>>(c->d.phi, c->d.plo, c->n, c->npad, c->grav_chunks, c->grav_part,
-                                                c->grav_sort ? c->grav_box : nullptr);
+                                                c->grav_sort ? c->grav_box : nullptr, c->grav_far2);
     prof_end(c);
     NBG_LAUNCH_CHECK(c, "k_gravity");
-    k_gravity_reduce<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->grav_part, c->n, c->grav_chunks, c->d.G,
+    k_gravity_reduce<<<grid_for(3 * c->n, 256), 256, 0, c->stream>>>(c->grav_part, c->n, c->grav_chunks,
+                                                                      uniform ? c->d.G * c->grav_m0 : c->d.G,
                                                                       s.a_new, c->d.status, perm);
     NBG_LAUNCH_CHECK(c, "k_gravity_reduce");
     return NBG_OK;
@@ -753,7 +764,7 @@ int gravity_raw_chunks(int device, int64_t npad, int max_chunks)
 {
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<false, 2, true>, GB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gravity<false, 2, true, false>, GB, 0);
     if (sms < 1) sms = 1;
     if (occ < 1) occ = 1;
     const double slots = (double)sms * occ;
@@ -776,7 +787,7 @@ cudaError_t gravity_raw_launch(const float4* phi, const float4* plo, int64_t n, 
                                double* part, double G, double* a, unsigned* status, cudaStream_t stream)
 {
     int64_t units = (npad / (2 * GB)) * jchunks;
-    k_gravity<false, 2, true><<<(unsigned)units, GB, 0, stream>>>(phi, plo, n, npad, jchunks, part, nullptr);
+    k_gravity<false, 2, true, false><<<(unsigned)units, GB, 0, stream>>>(phi, plo, n, npad, jchunks, part, nullptr, 0.f);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_gravity_reduce<<<grid_for(3 * n, 256), 256, 0, stream>>>(part, n, jchunks, G, a, status, nullptr);

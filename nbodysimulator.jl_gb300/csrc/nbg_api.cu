@@ -490,6 +490,13 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     if (c->path == PATH_GRAVITY) {
         const char* gv = getenv("NBG_GRAVITY_VARIANT");  // kernel-form override for tuning sweeps
         if (gv) c->grav_variant = atoi(gv);
+        const char* gf = getenv("NBG_GRAVITY_FAR_FACTOR");  // far-criterion override for accuracy sweeps
+        if (gf && atof(gf) > 0.0) c->grav_far2 = (float)(atof(gf) * atof(gf));
+        // equal masses (the Plummer workloads): the mass leaves the pair loop
+        // (NBG_GRAVITY_MASSES keeps m_j in the loop, for comparisons)
+        c->grav_m0 = c->mass_h[0];
+        c->grav_uniform = std::isfinite(c->grav_m0) && c->grav_m0 > 0.0 && !getenv("NBG_GRAVITY_MASSES");
+        for (int64_t i = 1; i < n && c->grav_uniform; ++i) c->grav_uniform = c->mass_h[i] == c->grav_m0;
         c->grav_chunks = gravity_plan_chunks(c, c->npad);
         if ((st = dalloc(c, &c->grav_part, (size_t)c->grav_chunks * 3 * n))) return st;
         if (!c->d.grav_plain && !getenv("NBG_GRAVITY_NO_SORT")) {

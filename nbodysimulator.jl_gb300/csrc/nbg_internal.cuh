@@ -165,6 +165,9 @@ struct nbg_ctx {
     int64_t npad = 0;
     int grav_chunks = 1;
     int grav_variant = 1;     // k_gravity form (bodies per thread, packed FP32x2)
+    bool grav_uniform = false;  // every body has mass grav_m0: the reduction applies G m
+    float grav_far2 = 256.f;    // a tile pair is far when (F g)^2 >= max|r|^2, F = 16
+    double grav_m0 = 0.0;
     int list_lpa = 0;         // lanes per atom of k_force_list (1 = thread per atom)
     double* grav_part = nullptr;
     // compensated gravity: bodies re-sorted along a Morton curve every 8th

@@ -138,8 +138,12 @@ def lj_liquid(n=1000, seed=1, rho=0.8, T=1.0, jitter=0.0, skin=0.3, R=2.5, therm
     return nbg.NBodySimulation(system, (0.0, 1.0), *args, kb=1.0, skin=skin, flags=flags)
 
 
-def plummer(n, seed=3, flags=0):
+def plummer(n, seed=3, flags=0, mass_spread=0.0):
+    """Seeded Plummer sphere; mass_spread > 0 scales each mass by a seeded
+    factor in [1 - spread, 1 + spread] (unequal masses)."""
     pos, vel, m = nbg.workloads.plummer_sphere(n, seed=seed)
+    if mass_spread:
+        m = m * np.random.default_rng(seed + 1).uniform(1.0 - mass_spread, 1.0 + mass_spread, n)
     bodies = [nbg.MassBody(pos[i], vel[i], m[i]) for i in range(n)]
     return nbg.NBodySimulation(nbg.GravitationalSystem(bodies, 1.0), (0.0, 1.0), flags=flags)
 

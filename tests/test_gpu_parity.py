@@ -43,6 +43,18 @@ def test_gravity_forces(gpu, oracle, flags):
     assert np.abs((m[:, None] * ag).sum(axis=0)).max() <= 1e-6 * np.abs(m[:, None] * ag).sum()
 
 
+@pytest.mark.parametrize("flags", [0, nbg._abi.NBG_FLAG_GRAV_PLAIN])
+def test_gravity_forces_unequal_masses(gpu, oracle, flags):
+    """Unequal masses keep m_j inside the pair loop (equal masses apply G m
+    once, in the reduction): both forms against the oracle."""
+    sim = S.plummer(2500, seed=9, flags=flags, mass_spread=0.5)
+    eng, desc, keep, u, v, ag, ar = _accel_pair(gpu, oracle, sim)
+    err = S.rel_rmse(ag, ar)
+    assert err <= (FORCE_TOL if not flags else 1e-3), err
+    m = np.asarray(keep[0])
+    assert np.abs((m[:, None] * ag).sum(axis=0)).max() <= 1e-6 * np.abs(m[:, None] * ag).sum()
+
+
 def test_gravity_tile_edges(gpu, oracle):
     """N not a multiple of the 256-body tile: padding bodies contribute nothing."""
     for n in (3, 257, 511, 1000):

@@ -12,13 +12,14 @@
 //   k_cell_sort        : each cell's atoms sorted by index (deterministic
 //                        lists), counts moved to cell_n and cleared for the
 //                        next build
-//   k_list_build_cells : (at least two cells per SM) one block per cell; the 27 neighbour cells' atoms
-//                        (split-position hi parts moved by the periodic shift
-//                        into the cell's frame) are staged in shared-memory
-//                        tiles in scan order and every atom of the cell tests
-//                        them with broadcast reads. The list is column-major
-//                        (nbr[k*n + i]) for thread-per-atom force kernels and
-//                        row-major (nbr[i*cap + k]) for lanes-per-atom kernels.
+//   k_list_build_warps : (at least two cells per SM) one warp per 32 atoms of a cell; the
+//                        stencil cells' atoms (split-position hi parts moved
+//                        by the periodic shift into the cell's frame) pass
+//                        through a per-warp buffer in scan order and every
+//                        atom of the cell tests them with broadcast reads. The
+//                        list is column-major (nbr[k*n + i]) for
+//                        thread-per-atom force kernels and row-major
+//                        (nbr[i*cap + k]) for lanes-per-atom kernels.
 //   k_list_build(_lanes): (fewer cells) a thread or a group of lanes per atom
 //                        scanning its 27 cells with gathers of the split positions.
 #include "nbg_internal.cuh"
@@ -94,8 +95,8 @@ __global__ void k_cell_sort(Dev d, ListCtl L)
 }
 
 // Per-atom builds, for systems with too few cells to fill the GPU one
-// block per cell: the thread (or group of LPA lanes) of an atom scans its
-// 27 cells in the same order as the block-per-cell build.
+// warp per cell: the thread (or group of LPA lanes) of an atom scans its
+// 27 cells in the same order as the warp-per-cell build.
 __global__ void k_list_build(Dev d, ListCtl L, const double* X)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -214,26 +215,61 @@ __global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, cons
     if (lane < 3) d.xref[3 * i + lane] = X[3 * i + lane];
 }
 
-// Candidates of the stencil's cells (125 or 27, or for a one-cell replica 1)
-// in scan order (ox, oy, oz from -ns to ns; each cell's atoms by index), TILE
-// at a time. The test r^2 < rl2 on the hi parts is the list's superset test (the
-// force kernels classify every pair exactly); the list order is the scan order.
-#define LB_TILE 1024
+// Warp per (cell, chunk of 32 of its atoms): lane l holds atom l of the
+// chunk. The stencil's cells (125 or 27, or for a one-cell replica 1)
+// pass their atoms through a per-warp buffer of 32 candidates (split-position
+// hi parts moved by the periodic shift into the cell's frame, index in w) read
+// back by broadcast; the next chunk's index and position gathers are issued
+// before the current chunk's tests. The test r^2 < rl2 on the hi parts is the
+// list's superset test (the force kernels classify every pair exactly). The
+// candidates come in the stencil order of the per-atom builders (cell q =
+// ((ox+ns) w + oy+ns) w + oz+ns, then slot order), so the lists are the same.
+#define LW_WARPS 4
+#define LW_NB 125
 
-__global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, const double* X)
+template <bool ONE, bool WATER>
+__device__ __forceinline__ int lw_test(const float4* cand, int bn, const float4& hi, int i, int mol0, float rl2,
+                                       const RepDev& R, int* row, int64_t kstride, int cap, int lcnt)
 {
-    __shared__ float4 tile[LB_TILE];
-    __shared__ int nb_cell[125];
-    __shared__ float4 nb_shift[125];
-    __shared__ int nb_pre[126];
+#pragma unroll 4
+    for (int k = 0; k < bn; ++k) {
+        const float4 c = cand[k];
+        float dx = c.x - hi.x, dy = c.y - hi.y, dz = c.z - hi.z;
+        if (ONE) {
+            // s = rint(d / L) by the 1.5 * 2^23 trick (|d / L| <= 1)
+            const float magic = 12582912.0f;
+            dx = __fmaf_rn(-__fsub_rn(__fmaf_rn(dx, R.invLf, magic), magic), R.Lh, dx);
+            dy = __fmaf_rn(-__fsub_rn(__fmaf_rn(dy, R.invLf, magic), magic), R.Lh, dy);
+            dz = __fmaf_rn(-__fsub_rn(__fmaf_rn(dz, R.invLf, magic), magic), R.Lh, dz);
+        }
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const int j = __float_as_int(c.w);
+        if (r2 < rl2 && j != i && (!WATER || (unsigned)(j - mol0) >= 3u)) {
+            if (lcnt < cap) row[(int64_t)lcnt * kstride] = j;
+            ++lcnt;
+        }
+    }
+    return lcnt;
+}
+
+__global__ void __launch_bounds__(LW_WARPS * 32) k_list_build_warps(Dev d, ListCtl L, const double* X, int chunks)
+{
+    __shared__ int nb_code[LW_WARPS][LW_NB];  // stencil cell | (shift + 1) per axis in bits 24-29
+    __shared__ int nb_cnt[LW_WARPS][LW_NB];
+    __shared__ float4 cand[LW_WARPS][32];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool water = d.kind == NBG_SYSTEM_WATER;
-    for (int cell = blockIdx.x; cell < d.ncell_total; cell += gridDim.x) {
+    // work item: (cell, c), c < chunks; it takes the cell's atoms from 32 c
+    // in strides of 32 chunks, so that cells holding many atoms spread over
+    // several warps
+    const int64_t items = (int64_t)d.ncell_total * chunks;
+    for (int64_t it = blockIdx.x * (int64_t)LW_WARPS + wid; it < items; it += (int64_t)gridDim.x * LW_WARPS) {
+        const int cell = (int)(it / chunks);
+        const int c0 = (int)(it % chunks) * 32;
         const int rep = d.cell_rep[cell];
         if (!need_build(d, L, rep)) continue;
-        int cnt = d.cell_n[cell];
-        if (cnt > d.cell_cap) cnt = d.cell_cap;
-        if (cnt == 0) continue;
-        const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
+        const int cnt = min(d.cell_n[cell], d.cell_cap);
+        if (c0 >= cnt) continue;
         const RepDev& R = d.reps[rep];
         const int nc = R.nc;
         const int lc = cell - R.cell0;
@@ -241,80 +277,82 @@ __global__ void __launch_bounds__(256) k_list_build_cells(Dev d, ListCtl L, cons
         const bool one = R.ns == 0;  // one cell holds the replica: minimum image per pair
         const int w = 2 * R.ns + 1;  // stencil width (1, 3 or 5)
         const int nnb = w * w * w;
-        __syncthreads();  // previous cell's use of the shared tables is over
-        for (int q = threadIdx.x; q < nnb; q += blockDim.x) {
+        __syncwarp();  // the previous cell's tables are consumed
+        for (int q = lane; q < nnb; q += 32) {
             const int ox = q / (w * w) - R.ns, oy = (q / w) % w - R.ns, oz = q % w - R.ns;
             int nx = cx + ox, ny = cy + oy, nz = cz + oz;
-            float sx = 0.f, sy = 0.f, sz = 0.f;
-            if (nx < 0) { nx += nc; sx = -R.Lh; }
-            if (nx >= nc) { nx -= nc; sx = R.Lh; }
-            if (ny < 0) { ny += nc; sy = -R.Lh; }
-            if (ny >= nc) { ny -= nc; sy = R.Lh; }
-            if (nz < 0) { nz += nc; sz = -R.Lh; }
-            if (nz >= nc) { nz -= nc; sz = R.Lh; }
+            int sx = 1, sy = 1, sz = 1;
+            if (nx < 0) { nx += nc; sx = 0; }
+            if (nx >= nc) { nx -= nc; sx = 2; }
+            if (ny < 0) { ny += nc; sy = 0; }
+            if (ny >= nc) { ny -= nc; sy = 2; }
+            if (nz < 0) { nz += nc; sz = 0; }
+            if (nz >= nc) { nz -= nc; sz = 2; }
             const int cq = R.cell0 + (nx * nc + ny) * nc + nz;
-            nb_cell[q] = cq;
-            nb_shift[q] = make_float4(sx, sy, sz, 0.f);
-            nb_pre[q + 1] = min(d.cell_n[cq], d.cell_cap);  // counts, summed below
+            nb_code[wid][q] = cq | (sx << 24) | (sy << 26) | (sz << 28);
+            nb_cnt[wid][q] = min(d.cell_n[cq], d.cell_cap);
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int q = 0; q < nnb; ++q) {
-                const int cq = nb_pre[q + 1];
-                nb_pre[q] = acc;
-                acc += cq;
-            }
-            nb_pre[nnb] = acc;
-        }
-        __syncthreads();
-        const int total = nb_pre[nnb];
-        for (int a0 = 0; a0 < cnt; a0 += blockDim.x) {
-            const int a = a0 + threadIdx.x;
+        __syncwarp();
+        const float Lh = R.Lh, rl2 = R.rl2;
+        const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
+        for (int a0 = c0; a0 < cnt; a0 += 32 * chunks) {
+            const int a = a0 + lane;
             const bool active = a < cnt;
             const int i = active ? atoms[a] : -1;
-            float4 hi = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (active) hi = d.phi[i];
+            const float4 hi = active ? d.phi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
             const int mol0 = water && active ? 3 * (i / 3) : -8;  // first atom of i's molecule
+            int* row = d.nbr + (int64_t)(active ? i : 0) * d.nbr_istride;
             int lcnt = 0;
-            for (int t0 = 0; t0 < total; t0 += LB_TILE) {
-                const int tn = min(LB_TILE, total - t0);
-                __syncthreads();  // the previous tile is consumed
-                for (int k = threadIdx.x; k < tn; k += blockDim.x) {
-                    const int g = t0 + k;
-                    // the stencil cell holding entry g: the last q with nb_pre[q] <= g
-                    int lo_q = 0, hi_q = nnb - 1;
-                    while (lo_q < hi_q) {
-                        const int mid = (lo_q + hi_q + 1) >> 1;
-                        if (nb_pre[mid] <= g) lo_q = mid;
-                        else hi_q = mid - 1;
-                    }
-                    const int q = lo_q;
-                    const int j = d.cell_atoms[(int64_t)nb_cell[q] * d.cell_cap + (g - nb_pre[q])];
-                    const float4 hj = d.phi[j];
-                    const float4 sh = nb_shift[q];
-                    tile[k] = make_float4(hj.x + sh.x, hj.y + sh.y, hj.z + sh.z, __int_as_float(j));
+            // chunk (q, b0): atoms b0 .. b0 + 31 of stencil cell q
+            int q = 0;
+            while (q < nnb && nb_cnt[wid][q] == 0) ++q;
+            int b0 = 0;
+            int jn = -1;
+            float4 hn = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (q < nnb) {
+                const int cq = nb_code[wid][q] & 0xffffff;
+                if (lane < nb_cnt[wid][q]) {
+                    jn = d.cell_atoms[(int64_t)cq * d.cell_cap + lane];
+                    hn = d.phi[jn];
                 }
-                __syncthreads();
+            }
+            while (q < nnb) {
+                const int code = nb_code[wid][q];
+                const int cn = nb_cnt[wid][q];
+                const int bn = min(32, cn - b0);
+                const int j = jn;
+                const float4 hj = hn;
+                // the next chunk's gathers go out before this chunk's tests
+                int q2 = q, b2 = b0 + 32;
+                if (b2 >= cn) {
+                    b2 = 0;
+                    ++q2;
+                    while (q2 < nnb && nb_cnt[wid][q2] == 0) ++q2;
+                }
+                if (q2 < nnb) {
+                    const int cq2 = nb_code[wid][q2] & 0xffffff;
+                    jn = -1;
+                    if (b2 + lane < nb_cnt[wid][q2]) {
+                        jn = d.cell_atoms[(int64_t)cq2 * d.cell_cap + b2 + lane];
+                        hn = d.phi[jn];
+                    }
+                }
+                const float sx = (float)(((code >> 24) & 3) - 1) * Lh;
+                const float sy = (float)(((code >> 26) & 3) - 1) * Lh;
+                const float sz = (float)(((code >> 28) & 3) - 1) * Lh;
+                if (lane < bn) cand[wid][lane] = make_float4(hj.x + sx, hj.y + sy, hj.z + sz, __int_as_float(j));
+                __syncwarp();
                 if (active) {
-                    for (int k = 0; k < tn; ++k) {
-                        const float4 c = tile[k];
-                        float dx = c.x - hi.x, dy = c.y - hi.y, dz = c.z - hi.z;
-                        if (one) {
-                            // s = rint(d / L) by the 1.5 * 2^23 trick (|d / L| <= 1)
-                            const float magic = 12582912.0f;
-                            dx = __fmaf_rn(-__fsub_rn(__fmaf_rn(dx, R.invLf, magic), magic), R.Lh, dx);
-                            dy = __fmaf_rn(-__fsub_rn(__fmaf_rn(dy, R.invLf, magic), magic), R.Lh, dy);
-                            dz = __fmaf_rn(-__fsub_rn(__fmaf_rn(dz, R.invLf, magic), magic), R.Lh, dz);
-                        }
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        const int j = __float_as_int(c.w);
-                        if (r2 < R.rl2 && j != i && (unsigned)(j - mol0) >= 3u) {
-                            if (lcnt < d.nbr_cap) d.nbr[(int64_t)lcnt * d.nbr_kstride + (int64_t)i * d.nbr_istride] = j;
-                            ++lcnt;
-                        }
-                    }
+                    if (one)
+                        lcnt = water ? lw_test<true, true>(cand[wid], bn, hi, i, mol0, rl2, R, row, d.nbr_kstride, d.nbr_cap, lcnt)
+                                     : lw_test<true, false>(cand[wid], bn, hi, i, mol0, rl2, R, row, d.nbr_kstride, d.nbr_cap, lcnt);
+                    else
+                        lcnt = water ? lw_test<false, true>(cand[wid], bn, hi, i, mol0, rl2, R, row, d.nbr_kstride, d.nbr_cap, lcnt)
+                                     : lw_test<false, false>(cand[wid], bn, hi, i, mol0, rl2, R, row, d.nbr_kstride, d.nbr_cap, lcnt);
                 }
+                __syncwarp();
+                q = q2;
+                b0 = b2;
             }
             if (active) {
                 if (lcnt > d.nbr_cap) {
@@ -340,11 +378,12 @@ int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos)
     k_cell_sort<<<gs, 128, sizeof(int) * c->d.cell_cap, c->stream>>>(c->d, L);
     NBG_LAUNCH_CHECK(c, "k_cell_sort");
     if (c->d.ncell_total >= 2 * c->sms) {
-        // a block per cell, sized to the mean occupancy (cells above it take a second pass)
+        // warps per cell from the mean occupancy (with margin); fuller cells loop
         const double occ = (double)c->n / std::max(c->d.ncell_total, 1);
-        int bs = 32 * (int)std::ceil(1.15 * occ / 32.0);
-        bs = std::min(256, std::max(32, bs));
-        k_list_build_cells<<<c->d.ncell_total, bs, 0, c->stream>>>(c->d, L, s.x);
+        const int chunks = std::max(1, std::min((c->d.cell_cap + 31) / 32, (int)std::ceil(1.5 * occ / 32.0)));
+        const int64_t items = (int64_t)c->d.ncell_total * chunks;
+        const int64_t blocks = std::min<int64_t>((items + LW_WARPS - 1) / LW_WARPS, 1 << 20);
+        k_list_build_warps<<<(unsigned)blocks, LW_WARPS * 32, 0, c->stream>>>(c->d, L, s.x, chunks);
     } else {
         const int lpa = c->list_lpa;
         if (lpa <= 1) {

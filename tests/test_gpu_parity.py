@@ -336,3 +336,28 @@ def test_batch_nve_matches_single_contexts(gpu):
         u1, v1, _, _, _ = single.run(us[r], vs[r], 0.005, 10, 0, save_trajectory=False)
         assert np.abs(ug[off:off + n] - u1).max() <= 1e-7 * descs[r].box[0]
         off += n
+
+
+def test_batch_many_cells_matches_oracle(gpu, oracle):
+    """A batch with at least two cells per SM, which the warp-per-cell list
+    builder serves (a single-cell replica among them): accelerations per
+    replica against the oracle, and 40 velocity-Verlet steps (list rebuilds
+    by displacement included) against separate contexts, whose fewer cells
+    take the per-atom builders with the same candidate order."""
+    import torch
+    sizes = [256, 4000, 3000, 2000, 1200]
+    descs, keep, us, vs = _ensemble(nbg, sizes, lambda r: None)
+    cells = sum(max(int(d.box[0] // (d.lj_cutoff + d.skin)), 1) ** 3 if d.box[0] >= 3 * (d.lj_cutoff + d.skin) else 1
+                for d in descs)
+    assert cells >= 2 * torch.cuda.get_device_properties(0).multi_processor_count, cells
+    eng = nbg.Engine(descs, 0)
+    U, V = np.concatenate(us), np.concatenate(vs)
+    ab = eng.accel(V.copy(), U)
+    ug, vg, _, _, _ = eng.run(U, V, 0.005, 40, 0, save_trajectory=False)
+    off = 0
+    for r, n in enumerate(sizes):
+        ao, _ = oracle.accel(descs[r], vs[r], us[r])
+        assert S.rel_rmse(ab[off:off + n], ao) <= FORCE_TOL, r
+        u1, v1, _, _, _ = nbg.Engine(descs[r], 0).run(us[r], vs[r], 0.005, 40, 0, save_trajectory=False)
+        assert np.abs(ug[off:off + n] - u1).max() <= 1e-7 * descs[r].box[0], r
+        off += n

@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(AT) k_allpairs(Dev d, StateView s)
     }
     if (range_err) status_set(d.status, ST_RANGE);
     if (!active) return;
-    double im = 1.0 / d.mass[i];
+    const double im = d.inv_mass[i];
     double a[3] = {fx.value() * im, fy.value() * im, fz.value() * im};
     if (d.pots & NBG_POT_GRAV) {
         a[0] += -d.G * gx.value();
@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
         }
         fx.add(px); fy.add(py); fz.add(pz);
         if (range_err) status_set(d.status, ST_RANGE);
-        double im = 1.0 / d.mass[i];
+        const double im = d.inv_mass[i];
         double a0 = fx.value() * im, a1 = fy.value() * im, a2 = fz.value() * im;
         if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
         s.a_new[3 * i] = a0;
@@ -616,10 +616,22 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
     }
 }
 
+// (h, e) += the partner lane's (h, e), h by TwoSum with its error into e
+__device__ __forceinline__ void lane_join(float& h, float& e, int o, int width)
+{
+    const float h2 = __shfl_xor_sync(0xffffffffu, h, o, width);
+    const float e2 = __shfl_xor_sync(0xffffffffu, e, o, width);
+    float sum, err;
+    two_sum(h, h2, sum, err);
+    h = sum;
+    e = __fadd_rn(__fadd_rn(e, e2), err);
+}
+
 // LPA lanes per atom over a row-major list: the group reads its atom's
 // entries coalesced, each lane keeps an FP32 partial of every LPA-th entry,
-// and the partials are joined by an xor butterfly of shuffles in FP64 (a
-// fixed order: deterministic). For small systems, where one atom per thread
+// and the partials are joined by a compensated FP32 xor butterfly of shuffles
+// (a fixed order: deterministic); one FP64 multiply by 1/m per component
+// gives the acceleration. For small systems, where one atom per thread
 // leaves the GPU waiting on memory latency.
 template <int LPA>
 __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
@@ -646,17 +658,20 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
         py += o.fy;
         pz += o.fz;
     }
-    double vx = px, vy = py, vz = pz;
+    // join the lanes' partials: compensated FP32 butterfly (TwoSum; every
+    // lane ends with the same value, whatever the order of its operands)
+    float ex = 0.f, ey = 0.f, ez = 0.f;
 #pragma unroll
     for (int o = LPA / 2; o > 0; o >>= 1) {
-        vx += __shfl_xor_sync(0xffffffffu, vx, o, LPA);
-        vy += __shfl_xor_sync(0xffffffffu, vy, o, LPA);
-        vz += __shfl_xor_sync(0xffffffffu, vz, o, LPA);
+        lane_join(px, ex, o, LPA);
+        lane_join(py, ey, o, LPA);
+        lane_join(pz, ez, o, LPA);
     }
     if (range_err) status_set(d.status, ST_RANGE);
     if (active && lane == 0) {
-        double im = 1.0 / d.mass[i];
-        double a0 = vx * im, a1 = vy * im, a2 = vz * im;
+        const double im = d.inv_mass[i];
+        const double a0 = ((double)px + (double)ex) * im, a1 = ((double)py + (double)ey) * im,
+                     a2 = ((double)pz + (double)ez) * im;
         if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
         s.a_new[3 * i] = a0;
         s.a_new[3 * i + 1] = a1;
@@ -737,7 +752,7 @@ __global__ void k_bonded(Dev d, StateView s)
         cosine = fminf(1.0f, fmaxf(-1.0f, cosine));
         float force = -ka * (acosf(cosine) - a0);
         float sa = force / (npa * nba), sc = force / (npc * nbc);
-        double iO = 1.0 / d.mass[o], iH1 = 1.0 / d.mass[h1], iH2 = 1.0 / d.mass[h2];
+        const double iO = d.inv_mass[o], iH1 = d.inv_mass[h1], iH2 = d.inv_mass[h2];
         for (int k = 0; k < 3; ++k) {
             float fa = pa[k] * sa;
             float fc = pc[k] * sc;

@@ -343,12 +343,14 @@ __global__ void k_baoab_drift(Dev d, StateView s, double dt, StepRef sr)
         const double sd = __dmul_rn(R.bsd, d.rsqrt_mass[i]);  // sqrt(1 - c1^2) sqrt(kb T0 / m)
         float z[3];
         philox_normals3<float>(R.seed, (uint64_t)li, (uint64_t)step, z);
+        // fused multiply-adds: FP64 issues slowly on this GPU, and BAOAB has
+        // no reference arithmetic to follow operation by operation
         for (int k = 0; k < 3; ++k) {
             const int64_t e = 3 * i + k;
-            double vh = __dadd_rn(s.v[e], __dmul_rn(hdt, s.a_old[e]));
-            double x = __dadd_rn(s.x[e], __dmul_rn(hdt, vh));
-            double vo = __dadd_rn(__dmul_rn(c1, vh), __dmul_rn(sd, (double)z[k]));
-            s.x[e] = __dadd_rn(x, __dmul_rn(hdt, vo));
+            const double vh = fma(hdt, s.a_old[e], s.v[e]);
+            const double x = fma(hdt, vh, s.x[e]);
+            const double vo = fma(c1, vh, sd * (double)z[k]);
+            s.x[e] = fma(hdt, vo, x);
             s.v[e] = vo;
         }
         pack_atom(d, i, s.x);

@@ -235,12 +235,25 @@ NBG_API int nbg_pair_list(nbg_ctx* ctx, const double* u, int32_t which, int32_t*
 /*
  * Profiling support (no reference counterpart). With profiling on, CUDA
  * events bracket every launch of the context's dominant force kernel
- * (gravity all-pairs, Verlet-list pair forces or the all-pairs kernel);
+ * (gravity all-pairs, Verlet-list pair forces or the all-pairs kernel; for a
+ * context on the cluster step loop, the whole multi-step cluster launch);
  * nbg_force_kernel_time returns their summed duration and count since the
  * last reset and resets them.
  */
 NBG_API int nbg_set_profiling(nbg_ctx* ctx, int on);
 NBG_API int nbg_force_kernel_time(nbg_ctx* ctx, double* total_ms, int64_t* launches);
+
+/*
+ * Small systems (no reference counterpart): one potential system under cubic
+ * boundaries without thermostat, up to 2048 atoms, runs velocity Verlet as one
+ * persistent launch per chunk of steps over a thread-block cluster (the
+ * positions shared in distributed shared memory, one cluster barrier per
+ * step) instead of a CUDA graph of kernels. Returns 1 and the cluster's CTAs
+ * and lanes per atom when the context uses it, 0 otherwise (either pointer
+ * may be NULL). The environment variable NBG_NO_CLUSTER, read at creation,
+ * keeps such a system on the graph step loop.
+ */
+NBG_API int nbg_cluster_shape(nbg_ctx* ctx, int32_t* ctas, int32_t* lanes);
 
 /*
  * All-pairs gravity accelerations that allocate no device memory. It has no

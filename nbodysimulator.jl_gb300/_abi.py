@@ -158,6 +158,7 @@ SIGNATURES = {
     "nbg_set_thermostat_target": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_double]),
     "nbg_ml_kernel_times": (ctypes.c_int, [_vp, ctypes.c_int32, _dp]),
     "nbg_autotune": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp]),
+    "nbg_cluster_shape": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
 }
 
 _lib = None

@@ -1,0 +1,330 @@
+// k_cluster.cu - velocity Verlet for small systems (up to 2048 atoms) as one
+// persistent launch over a thread-block cluster.
+//
+// A step of a small system is a handful of microsecond kernels, so launches,
+// not arithmetic, set its pace. Here the cluster's CTAs (up to 16 SMs) run
+// many steps in one launch:
+//   - CTA r owns atoms [r per, (r+1) per); its threads drift them (FP64, the
+//     reference's velocity-Verlet arithmetic), split the new positions and
+//     push them into every CTA's shared memory (distributed shared memory),
+//     in the buffer of the step's parity;
+//   - one cluster barrier per step (release/acquire) publishes them; with two
+//     parity buffers, a CTA writing step s+1 can never overwrite what another
+//     CTA still reads of step s;
+//   - each CTA keeps the Verlet lists of its own atoms in shared memory,
+//     rebuilt from the shared positions (all atoms scanned, the FP32 superset
+//     test of the list builders) when any atom moved more than skin/2 since
+//     the last build, every rebuild_every steps, and at the first step of a
+//     launch;
+//   - LPA lanes per atom evaluate the pairs (pair_cutoff: the exact pair set;
+//     the ambiguous ones read FP64 positions, which the drift also writes to
+//     a global copy of the step's parity, through L2), join their partials
+//     (compensated FP32) and the group's first lane kicks the velocity.
+// Every thread of every CTA passes the same cluster barriers (no early exit).
+#include <cooperative_groups.h>
+
+#include "nbg_internal.cuh"
+
+namespace cg = cooperative_groups;
+
+#define CL_THREADS 1024
+#define CL_MAX 16
+
+// (h, e) += the partner lane's (h, e), h by TwoSum with its error into e
+__device__ __forceinline__ void cl_join(float& h, float& e, int o, int width)
+{
+    const float h2 = __shfl_xor_sync(0xffffffffu, h, o, width);
+    const float e2 = __shfl_xor_sync(0xffffffffu, e, o, width);
+    float sum, err;
+    two_sum(h, h2, sum, err);
+    h = sum;
+    e = __fadd_rn(__fadd_rn(e, e2), err);
+}
+
+// Shared memory (dynamic): split positions [parity][hi, lo][n] (float4), the
+// own atoms' positions at the last list build [per][3] (double), their lists
+// [per][cap], counts [per] (int) and force partials [per][6] (float: h, e per
+// component).
+template <int LPA>
+__global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s, double* xb, double dt, int nsteps,
+                                                              int rebuild_every, int per, int cap)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int C = (int)cl.num_blocks();
+    const int n = (int)d.n;
+    extern __shared__ float4 cl_pos[];
+    double* xref_s = reinterpret_cast<double*>(cl_pos + 4 * (size_t)n);
+    int* lst = reinterpret_cast<int*>(xref_s + 3 * (size_t)per);
+    int* cnt = lst + (size_t)per * cap;
+    float* fsum = reinterpret_cast<float*>(cnt + per);
+    __shared__ unsigned flag[2];  // rebuild requests of the step of each parity
+    __shared__ int build_s;
+    const RepDev& R = d.reps[0];
+    const int tid = threadIdx.x;
+    const int a0 = rank * per;
+    const int na = max(0, min(n - a0, per));
+    const int g = tid / LPA, lane = tid % LPA;  // lane group g <-> own atom a0 + g
+    const unsigned gshift = (unsigned)((tid & 31) / LPA * LPA);
+    const unsigned gmask = (LPA == 32 ? 0xffffffffu : ((1u << LPA) - 1u));
+    const double dtsq = dt * dt;
+    const float magic = 12582912.0f;  // 1.5 * 2^23: rint by addition
+
+    // own atom k = tid keeps its state in the registers of thread k for the
+    // whole launch
+    const int ko = tid;
+    const bool owner = tid < na;
+    const int io = owner ? a0 + ko : 0;
+    double x[3], v[3], a[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        x[k] = owner ? s.x[3 * io + k] : 0.0;
+        v[k] = owner ? s.v[3 * io + k] : 0.0;
+        a[k] = owner ? s.a_old[3 * io + k] : 0.0;
+    }
+    const double im_o = owner ? d.inv_mass[io] : 0.0;
+
+    // the static w parts (charge, atom flags) of every atom in both parities
+    for (int j = tid; j < n; j += CL_THREADS) {
+        const float wh = d.phi[j].w, wl = d.plo[j].w;
+        for (int p = 0; p < 2; ++p) {
+            cl_pos[(2 * p) * (size_t)n + j].w = wh;
+            cl_pos[(2 * p + 1) * (size_t)n + j].w = wl;
+        }
+    }
+    if (tid < 2) flag[tid] = 0u;
+    // every CTA of the cluster is running (and initialised) before any
+    // remote shared-memory access
+    cl.sync();
+
+    int since = 0;
+    for (int st = 0; st <= nsteps; ++st) {
+        // kick of the previous step with the forces its groups left in fsum
+        if (owner && st > 0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double an = ((double)fsum[6 * ko + 2 * k] + (double)fsum[6 * ko + 2 * k + 1]) * im_o;
+                if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+                v[k] = kick1(v[k], a[k], an, dt);
+                a[k] = an;
+            }
+        }
+        if (st == nsteps) break;  // uniform: every thread leaves after the last kick
+        const int par = st & 1;
+        float4* ph = cl_pos + (2 * par) * (size_t)n;
+        float4* pl = ph + n;
+        double* X = xb + (size_t)par * 3 * n;  // FP64 positions of this step
+        // drift, split and displacement check of the own atoms
+        bool moved = false;
+        if (owner) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                x[k] = drift1(x[k], v[k], a[k], dt, dtsq);
+                X[3 * io + k] = x[k];
+            }
+            float h[3], l[3];
+            split_position(d, R, x, h, l);
+            ph[io] = make_float4(h[0], h[1], h[2], ph[io].w);
+            pl[io] = make_float4(l[0], l[1], l[2], pl[io].w);
+            // (step 0 rebuilds regardless: xref_s is set there)
+            const double* xr = xref_s + 3 * ko;
+            const double dx = x[0] - xr[0], dy = x[1] - xr[1], dz = x[2] - xr[2];
+            moved = st > 0 && !(dx * dx + dy * dy + dz * dz <= d.skin_half2);
+        }
+        const int any_moved = __syncthreads_or(moved ? 1 : 0);
+        // push the own atoms' split positions to the other CTAs: (atom, rank) items
+        for (int w = tid; w < na * C; w += CL_THREADS) {
+            const int k = w / C, r = w % C;
+            if (r == rank) continue;
+            const int i = a0 + k;
+            float4* rh = cl.map_shared_rank(ph, r);
+            float4* rl = cl.map_shared_rank(pl, r);
+            rh[i] = ph[i];
+            rl[i] = pl[i];
+        }
+        if (any_moved && tid < C) *cl.map_shared_rank(&flag[par], tid) = 1u;
+        // arrive (release) / wait (acquire) at cluster scope: the pushed
+        // positions and the FP64 copies X are visible past it
+        cl.sync();
+        if (tid == 0) {
+            build_s = (st == 0 || flag[par] != 0u || (rebuild_every > 0 && since >= rebuild_every)) ? 1 : 0;
+            // the next writes to flag[par] come at step st + 2, after the
+            // barrier of step st + 1, which this CTA passes only later
+            flag[par] = 0u;
+        }
+        __syncthreads();
+        if (build_s) {
+            // lists of the own atoms: group g scans every atom j (lane-strided),
+            // entries in j order (ballot-compacted)
+            const bool active = g < na;
+            const int i = active ? a0 + g : 0;
+            const float4 hi = ph[i];
+            int c0 = 0;
+            for (int jb = 0; jb < n; jb += LPA) {
+                const int j = jb + lane;
+                bool take = false;
+                if (active && j < n && j != i) {
+                    const float4 hj = ph[j];
+                    float dx = hj.x - hi.x, dy = hj.y - hi.y, dz = hj.z - hi.z;
+                    dx = __fmaf_rn(-__fsub_rn(__fmaf_rn(dx, R.invLf, magic), magic), R.Lh, dx);
+                    dy = __fmaf_rn(-__fsub_rn(__fmaf_rn(dy, R.invLf, magic), magic), R.Lh, dy);
+                    dz = __fmaf_rn(-__fsub_rn(__fmaf_rn(dz, R.invLf, magic), magic), R.Lh, dz);
+                    take = dx * dx + dy * dy + dz * dz < R.rl2;
+                }
+                const unsigned m = (__ballot_sync(0xffffffffu, take) >> gshift) & gmask;
+                if (take) {
+                    const int q = c0 + __popc(m & ((1u << lane) - 1u));
+                    if (q < cap) lst[g * cap + q] = j;
+                }
+                c0 += __popc(m);
+            }
+            if (active && lane == 0) {
+                if (c0 > cap) {
+                    status_set(d.status, ST_NBR_OVERFLOW);
+                    c0 = cap;
+                }
+                cnt[g] = c0;
+            }
+            if (owner) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) xref_s[3 * ko + k] = x[k];
+            }
+            since = 0;
+            __syncthreads();
+        }
+        ++since;
+        // forces of the own atoms: FP32 partials joined over the group, left
+        // in fsum for the owner's kick
+        {
+            const bool active = g < na;
+            const int i = active ? a0 + g : 0;
+            const float4 hi_i = ph[i], lo_i = pl[i];
+            const float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[i]) : 0.0f;
+            const int c = active ? cnt[g] : 0;
+            float px = 0.f, py = 0.f, pz = 0.f;
+            bool range_err = false;
+            for (int k = lane; k < c; k += LPA) {
+                const int j = lst[g * cap + k];
+                const PairOut o = pair_cutoff<true>(d, R, i, j, hi_i, lo_i, ph[j], pl[j], kqi, X);
+                range_err |= o.range_err;
+                px += o.fx;
+                py += o.fy;
+                pz += o.fz;
+            }
+            float ex = 0.f, ey = 0.f, ez = 0.f;
+#pragma unroll
+            for (int o = LPA / 2; o > 0; o >>= 1) {
+                cl_join(px, ex, o, LPA);
+                cl_join(py, ey, o, LPA);
+                cl_join(pz, ez, o, LPA);
+            }
+            if (range_err) status_set(d.status, ST_RANGE);
+            if (active && lane == 0) {
+                float* f = fsum + 6 * g;
+                f[0] = px; f[1] = ex; f[2] = py; f[3] = ey; f[4] = pz; f[5] = ez;
+            }
+        }
+        // the next kick and drift touch only this CTA's own atoms: a block
+        // barrier, no cluster barrier
+        __syncthreads();
+    }
+    if (owner) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            s.x[3 * io + k] = x[k];
+            s.v[3 * io + k] = v[k];
+            s.a_old[3 * io + k] = a[k];
+            d.xref[3 * io + k] = xref_s[3 * ko + k];
+        }
+    }
+}
+
+typedef void (*cluster_kernel_t)(Dev, StateView, double*, double, int, int, int, int);
+
+static cluster_kernel_t cluster_kernel(int lpa)
+{
+    switch (lpa) {
+    case 4: return k_cluster_vv<4>;
+    case 8: return k_cluster_vv<8>;
+    case 16: return k_cluster_vv<16>;
+    default: return k_cluster_vv<32>;
+    }
+}
+
+// Plan the cluster path for the current list capacity: cluster size (16 where
+// the device allows it, else the portable 8), atoms per CTA, lanes per atom
+// and shared-memory bytes. Returns false when the system does not qualify
+// (one replica of a potential system under cubic boundaries, no
+// thermostat, small enough for the shared-memory copies).
+bool cluster_plan(nbg_ctx* c)
+{
+    c->cluster_ok = false;
+    if (c->cluster_disabled || c->path != PATH_LIST || c->nrep != 1 || c->d.kind != NBG_SYSTEM_POTENTIAL ||
+        c->d.bc != NBG_BC_CUBIC || c->d.therm != NBG_THERMO_NULL || c->baoab || c->n < 64 || c->n > 2048)
+        return false;
+    const int n = (int)c->n, cap = c->d.nbr_cap;
+    for (int C = CL_MAX; C >= 8; C /= 2) {
+        const int per = (n + C - 1) / C;
+        if (per > 128) continue;  // owner threads: 4 warps x 32 lanes
+        int lpa = 32;
+        while (lpa > 4 && per * lpa > CL_THREADS) lpa /= 2;
+        if (per * lpa > CL_THREADS) continue;
+        const size_t bytes = sizeof(float4) * 4 * (size_t)n + sizeof(double) * 3 * (size_t)per +
+                             sizeof(int) * ((size_t)per * cap + per) + sizeof(float) * 6 * (size_t)per;
+        if (bytes > 200 * 1024) continue;
+        cluster_kernel_t k = cluster_kernel(lpa);
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess ||
+            (C > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(C);
+        cfg.blockDim = dim3(CL_THREADS);
+        cfg.dynamicSmemBytes = bytes;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)k, &cfg) != cudaSuccess || clusters < 1) {
+            cudaGetLastError();
+            continue;
+        }
+        c->cluster_ok = true;
+        c->cluster_size = C;
+        c->cluster_per = per;
+        c->cluster_lpa = lpa;
+        c->cluster_bytes = bytes;
+        c->cluster_cap = cap;
+        return true;
+    }
+    return false;
+}
+
+int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every)
+{
+    cluster_kernel_t k = cluster_kernel(c->cluster_lpa);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = c->cluster_size;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(c->cluster_size);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = c->cluster_bytes;
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    prof_begin(c);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k, c->d, s, c->cluster_x, dt, (int)nsteps, rebuild_every,
+                                       c->cluster_per, c->cluster_cap);
+    prof_end(c);
+    if (e != cudaSuccess) return cuda_fail(c, e, "k_cluster_vv launch");
+    NBG_LAUNCH_CHECK(c, "k_cluster_vv");
+    return NBG_OK;
+}

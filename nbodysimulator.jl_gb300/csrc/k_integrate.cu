@@ -29,11 +29,6 @@ int launch_pack(nbg_ctx* c, const StateView& s)
 // position, then the Verlet-list displacement check (moved more than skin/2
 // since the last build: flag a rebuild). One thread per atom; the thread after
 // the last atom moves the Nose-Hoover column (zeta += dt v_zeta, a = 0).
-__device__ __forceinline__ double drift1(double u, double v, double a, double dt, double dtsq)
-{
-    return __dadd_rn(__dadd_rn(u, __dmul_rn(dt, v)), __dmul_rn(dtsq, __dmul_rn(0.5, a)));
-}
-
 __global__ void k_drift_pack(Dev d, StateView s, double dt, double dtsq, int check_disp, StepRef pos)
 {
     const int parity = (int)(step_of(pos) & 1);
@@ -166,7 +161,7 @@ __global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int
         if (thermo && (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER))
             an = __dadd_rn(an, thermo_term_T(d, e / 3, v, zeta, do_T ? T_now : d.red_T[d.rep_of[e / 3]]));
         if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
-        double vn = __dadd_rn(v, __dmul_rn(dt, __dadd_rn(__dmul_rn(0.5, s.a_old[e]), __dmul_rn(0.5, an))));
+        double vn = kick1(v, s.a_old[e], an, dt);
         s.v[e] = vn;
         s.a_old[e] = an;
         if (do_T) acc += d.mass[e / 3] * (vn * vn);

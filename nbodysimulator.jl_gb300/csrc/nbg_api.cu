@@ -40,6 +40,8 @@ static int fail(nbg_ctx* c, int code, const std::string& msg)
         if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
     } while (0)
 
+static int plan_cluster(nbg_ctx* c);
+
 template <typename T>
 static int dalloc(nbg_ctx* c, T** p, size_t count)
 {
@@ -487,6 +489,8 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         }
     }
     if (getenv("NBG_NO_GRAPHS")) c->use_graphs = false;  // direct launches, for comparisons
+    if (getenv("NBG_NO_CLUSTER")) c->cluster_disabled = true;  // the graph step loop for small systems too
+    if ((st = plan_cluster(c))) return st;
     if (c->path == PATH_GRAVITY) {
         const char* gv = getenv("NBG_GRAVITY_VARIANT");  // kernel-form override for tuning sweeps
         if (gv) c->grav_variant = atoi(gv);
@@ -513,6 +517,15 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
             if ((st = dalloc(c, &c->grav_extent, 1))) return st;
         }
     }
+    return NBG_OK;
+}
+
+// The persistent cluster step loop for small systems (k_cluster.cu), if the
+// system qualifies at the current list capacity; its FP64 position copies.
+static int plan_cluster(nbg_ctx* c)
+{
+    if (!cluster_plan(c)) return NBG_OK;
+    if (!c->cluster_x) return dalloc(c, &c->cluster_x, 6 * (size_t)c->n);
     return NBG_OK;
 }
 
@@ -570,6 +583,14 @@ extern "C" int nbg_force_kernel_time(nbg_ctx* c, double* total_ms, int64_t* laun
     c->prof_ms = 0.0;
     c->prof_count = 0;
     return NBG_OK;
+}
+
+extern "C" int nbg_cluster_shape(nbg_ctx* c, int32_t* ctas, int32_t* lanes)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (ctas) *ctas = c->cluster_ok ? c->cluster_size : 0;
+    if (lanes) *lanes = c->cluster_ok ? c->cluster_lpa : 0;
+    return c->cluster_ok ? 1 : 0;
 }
 
 static void release(nbg_ctx* c)
@@ -713,7 +734,9 @@ static int grow_lists(nbg_ctx* c, unsigned st)
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;
     }
-    return alloc_lists(c, cell_cap, nbr_cap);
+    int rc = alloc_lists(c, cell_cap, nbr_cap);
+    if (rc) return rc;
+    return plan_cluster(c);  // the lists' shared-memory share grew
 }
 
 // Evaluate forces on a one-off state (scratch view), retrying on overflow.
@@ -1078,6 +1101,15 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
         int64_t s = 0;
         bool counter_set = false;
         while (s < k) {
+            if (c->cluster_ok) {
+                // the whole chunk in one persistent cluster launch (its lists
+                // live in shared memory: the global ones are rebuilt later)
+                if ((st = launch_cluster_vv(c, c->st, dt, k - s, c->desc.rebuild_every))) break;
+                c->step += k - s;
+                c->steps_since_build = -1;
+                s = k;
+                continue;
+            }
             if (graphs && graph_aligned(c) && k - s >= graph_period(c)) {
                 if (!c->graph || c->graph_dt != dt) {
                     if ((st = capture_graph(c, dt))) break;

@@ -165,6 +165,12 @@ struct nbg_ctx {
     int64_t npad = 0;
     int grav_chunks = 1;
     int grav_variant = 1;     // k_gravity form (bodies per thread, packed FP32x2)
+    // small systems: velocity Verlet in one persistent cluster launch (k_cluster.cu)
+    bool cluster_disabled = false;
+    bool cluster_ok = false;
+    int cluster_size = 0, cluster_per = 0, cluster_lpa = 0, cluster_cap = 0;
+    size_t cluster_bytes = 0;
+    double* cluster_x = nullptr;  // FP64 positions of the two step parities [2][3n]
     bool grav_uniform = false;  // every body has mass grav_m0: the reduction applies G m
     float grav_far2 = 256.f;    // a tile pair is far when (F g)^2 >= max|r|^2, F = 16
     double grav_m0 = 0.0;
@@ -244,6 +250,8 @@ struct StepRef {
 
 int launch_pack(nbg_ctx* c, const StateView& s);
 int launch_gravity(nbg_ctx* c, const StateView& s);
+bool cluster_plan(nbg_ctx* c);
+int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every);
 int launch_allpairs(nbg_ctx* c, const StateView& s);
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
 int launch_force_list(nbg_ctx* c, const StateView& s);
@@ -351,11 +359,14 @@ __device__ __forceinline__ bool wrap_periodic64(double& x, double lo, double hi)
     return true;
 }
 
+// CG: load the positions through L2 (__ldcg), for kernels whose other blocks
+// wrote them earlier in the same launch.
+template <bool CG = false>
 __device__ __forceinline__ bool distance64(const double* xi, const double* xj, int bc, const RepDev& R, Dist64& o)
 {
-    double x = __dsub_rn(xi[0], xj[0]);
-    double y = __dsub_rn(xi[1], xj[1]);
-    double z = __dsub_rn(xi[2], xj[2]);
+    double x = __dsub_rn(CG ? __ldcg(xi) : xi[0], CG ? __ldcg(xj) : xj[0]);
+    double y = __dsub_rn(CG ? __ldcg(xi + 1) : xi[1], CG ? __ldcg(xj + 1) : xj[1]);
+    double z = __dsub_rn(CG ? __ldcg(xi + 2) : xi[2], CG ? __ldcg(xj + 2) : xj[2]);
     bool ok = true;
     if (bc == NBG_BC_CUBIC) {
         double size = R.L;
@@ -419,6 +430,7 @@ struct PairOut {
 // near the half-box image ambiguity) are decided by the reference's FP64
 // arithmetic on the unwrapped positions, so the pair set equals the
 // reference's bit for bit.
+template <bool CG = false>
 __device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, int64_t i, int64_t j,
                                                const float4& hi_i, const float4& lo_i, const float4& hi_j,
                                                const float4& lo_j, float kqi, const double* X)
@@ -443,7 +455,7 @@ __device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, in
     }
     if (amb || d.bc == NBG_BC_PERIODIC) {
         Dist64 q;
-        bool ok = distance64(X + 3 * i, X + 3 * j, d.bc, R, q);
+        bool ok = distance64<CG>(X + 3 * i, X + 3 * j, d.bc, R, q);
         if (!ok) {
             o.range_err = true;
             o.lj_in = o.el_in = 0;
@@ -472,12 +484,9 @@ __device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, in
     return o;
 }
 
-// Split one atom's position into (hi, lo) floats (see the layout note above).
-__device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double* X)
+// Split a position into (hi, lo) floats (see the layout note above).
+__device__ __forceinline__ void split_position(const Dev& d, const RepDev& R, const double* p, float* h, float* l)
 {
-    const RepDev& R = d.reps[d.rep_of[i]];
-    double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
-    float h[3], l[3];
     if (d.bc == NBG_BC_CUBIC) {
         for (int k = 0; k < 3; ++k) {
             double w = p[k] - R.L * floor(p[k] * R.invL);
@@ -493,10 +502,31 @@ __device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double*
             l[k] = (float)(p[k] - (double)h[k]);
         }
     }
+}
+
+__device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double* X)
+{
+    const RepDev& R = d.reps[d.rep_of[i]];
+    const double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+    float h[3], l[3];
+    split_position(d, R, p, h, l);
     float4 hi = d.phi[i];
     float4 lo = d.plo[i];
     d.phi[i] = make_float4(h[0], h[1], h[2], hi.w);
     d.plo[i] = make_float4(l[0], l[1], l[2], lo.w);
+}
+
+// Velocity-Verlet drift of one component, u' = u + dt v + dt^2 (a/2), with
+// no contracted multiply-add (the reference's arithmetic).
+__device__ __forceinline__ double drift1(double u, double v, double a, double dt, double dtsq)
+{
+    return __dadd_rn(__dadd_rn(u, __dmul_rn(dt, v)), __dmul_rn(dtsq, __dmul_rn(0.5, a)));
+}
+
+// Velocity-Verlet kick of one component, v' = v + dt (a/2 + a'/2).
+__device__ __forceinline__ double kick1(double v, double a, double an, double dt)
+{
+    return __dadd_rn(v, __dmul_rn(dt, __dadd_rn(__dmul_rn(0.5, a), __dmul_rn(0.5, an))));
 }
 
 // TwoSum: s + e = a + b exactly (Knuth).

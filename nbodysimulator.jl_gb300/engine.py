@@ -133,6 +133,15 @@ class Engine:
     def set_profiling(self, on=True):
         self._chk(self.lib.nbg_set_profiling(self.ctx, 1 if on else 0))
 
+    def cluster_shape(self):
+        """(CTAs, lanes per atom) of the persistent cluster step loop, or None
+        when the context runs the graph step loop."""
+        ctas, lanes = ctypes.c_int32(), ctypes.c_int32()
+        used = self.lib.nbg_cluster_shape(self.ctx, ctypes.byref(ctas), ctypes.byref(lanes))
+        if used < 0:
+            self._chk(used)
+        return (ctas.value, lanes.value) if used == 1 else None
+
     def force_kernel_time(self):
         """(summed ms, launches) of the dominant force kernel since the last call."""
         ms = ctypes.c_double()

@@ -361,3 +361,52 @@ def test_batch_many_cells_matches_oracle(gpu, oracle):
         u1, v1, _, _, _ = nbg.Engine(descs[r], 0).run(us[r], vs[r], 0.005, 40, 0, save_trajectory=False)
         assert np.abs(ug[off:off + n] - u1).max() <= 1e-7 * descs[r].box[0], r
         off += n
+
+
+def _engine_without_cluster(desc):
+    """An engine on the graph step loop (NBG_NO_CLUSTER is read at creation)."""
+    import os
+    os.environ["NBG_NO_CLUSTER"] = "1"
+    try:
+        return nbg.Engine(desc, 0)
+    finally:
+        del os.environ["NBG_NO_CLUSTER"]
+
+
+@pytest.mark.parametrize("n", [1000, 512])
+def test_cluster_step_loop(gpu, oracle, n):
+    """Small NVE systems run velocity Verlet as one persistent cluster launch
+    per chunk (positions in distributed shared memory, lists per CTA):
+    - 20 steps against the oracle, within 1e-8 of the box or 3x the graph
+      step loop's own deviation on the same system;
+    - 60 steps in launches of 20 (trajectory frames; lists rebuilt in each)
+      against the graph step loop on the same system. The lists hold the same
+      pairs in another order, so the two differ by FP32 summation order;
+    - 600 steps conserve energy as well as the graph loop does. (Trajectories
+      that long are not compared: a truncated LJ force jumps at the cutoff,
+      so rounding-level differences move pair crossings by a step and grow
+      fast.)"""
+    sim = S.lj_liquid(n, seed=12, jitter=0.1)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    L = desc.box[0]
+    eng = nbg.Engine(desc, 0)
+    assert eng.cluster_shape() is not None
+    ref = _engine_without_cluster(desc)
+    assert ref.cluster_shape() is None
+    ug, vg, _, _, _ = eng.run(u, v, 0.005, 20, 0, save_trajectory=False)
+    ur, vr, _, _, _ = ref.run(u, v, 0.005, 20, 0, save_trajectory=False)
+    uo, vo = oracle.run(desc, u, v, 0.005, 20)
+    err, err_ref = np.abs(ug - uo).max(), np.abs(ur - uo).max()
+    assert err <= max(1e-8 * L, 3.0 * err_ref), (err, err_ref)
+    assert np.abs(vg - vo).max() <= max(1e-6 * np.abs(vo).max(), 3.0 * np.abs(vr - vo).max())
+    ug, vg, tug, _, _ = eng.run(u, v, 0.005, 60, 20)
+    ur, vr, tur, _, _ = ref.run(u, v, 0.005, 60, 20)
+    assert np.abs(tug - tur).max() <= 1e-7 * L
+    assert np.abs(vg - vr).max() <= 1e-5 * np.abs(vr).max()
+    ug, vg, _, _, _ = eng.run(u, v, 0.005, 600, 0, save_trajectory=False)
+    ur, vr, _, _, _ = ref.run(u, v, 0.005, 600, 0, save_trajectory=False)
+    e0 = eng.energy(u, v)["total"]
+    d_cl = abs(eng.energy(ug, vg)["total"] - e0)
+    d_ref = abs(ref.energy(ur, vr)["total"] - e0)
+    assert d_cl <= 3.0 * d_ref + 1e-5 * abs(e0), (d_cl, d_ref)

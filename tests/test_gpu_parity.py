@@ -410,3 +410,28 @@ def test_cluster_step_loop(gpu, oracle, n):
     d_cl = abs(eng.energy(ug, vg)["total"] - e0)
     d_ref = abs(ref.energy(ur, vr)["total"] - e0)
     assert d_cl <= 3.0 * d_ref + 1e-5 * abs(e0), (d_cl, d_ref)
+
+
+def test_cluster_step_loop_list_regrowth(gpu, oracle):
+    """A compressed region overflows the cluster path's list capacity: the
+    chunk is undone, the lists grow (the cluster plan follows the new
+    capacity) and the chunk runs again, matching the oracle as closely as the
+    graph step loop does."""
+    pos, vel, L = nbg.workloads.lj_argon_lattice(1000, seed=8, jitter=0.05)
+    sel = slice(0, 300)
+    ctr = pos[sel].mean(axis=0)
+    pos[sel] = ctr + 0.8 * (pos[sel] - ctr)  # density ~1.6 there: ~150 neighbours
+    bodies = [nbg.MassBody(pos[i], vel[i], 1.0) for i in range(len(pos))]
+    system = nbg.PotentialNBodySystem(bodies, {"lennard_jones": nbg.LennardJonesParameters(1.0, 1.0, 2.5)})
+    sim = nbg.NBodySimulation(system, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), kb=1.0, skin=0.3)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    eng = nbg.Engine(desc, 0)
+    assert eng.cluster_shape() is not None
+    ref = _engine_without_cluster(desc)
+    ug, vg, _, _, _ = eng.run(u, v, 0.002, 20, 0, save_trajectory=False)
+    ur, vr, _, _, _ = ref.run(u, v, 0.002, 20, 0, save_trajectory=False)
+    uo, vo = oracle.run(desc, u, v, 0.002, 20)
+    err, err_ref = np.abs(ug - uo).max(), np.abs(ur - uo).max()
+    assert err <= max(1e-8 * L, 3.0 * err_ref), (err, err_ref)
+    assert eng.cluster_shape() is not None  # still on the cluster path, with the larger lists

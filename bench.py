@@ -19,9 +19,13 @@ value    : device-timed steps on the resident state (CUDA events on the
            engine's stream, L2 flushed between timed steps).
 e2e      : the same steps through the reference-facing drop-in, nbg_accel
            on pinned host buffers (the SciML velocity-Verlet loop calling the
-           GPU right-hand side): every step uploads u and v and reads back dv.
+           GPU right-hand side, its update done in place on the host threads):
+           every step uploads u (and v where the thermostat reads it) and
+           reads back dv.
 roofline : the dominant force kernel's algorithmic FLOP/s (20 flop per pair)
-           or bytes against the measured peak.
+           or bytes against the measured peak; for the LJ workload, which
+           runs as persistent cluster launches of many steps, the whole step
+           loop's time per step.
 cpu_baseline : the FP64 oracle (a restatement of the reference's O(N^2)
            per-atom loops) on a bounded sample of the same step, host cores.
 With --gpus N > 1 (torchrun) every rank runs its own replica: replicas only,

@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     __shared__ unsigned flag[2];  // rebuild requests of the step of each parity
     __shared__ int build_s;
     const RepDev& R = d.reps[0];
+    const PairK K(R);
     const int tid = threadIdx.x;
     const int a0 = rank * per;
     const int na = max(0, min(n - a0, per));
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             bool range_err = false;
             for (int k = lane; k < c; k += LPA) {
                 const int j = lst[g * cap + k];
-                const PairOut o = pair_cutoff<true>(d, R, i, j, hi_i, lo_i, ph[j], pl[j], kqi, X);
+                const PairOut o = pair_cutoff<true>(d, R, K, i, j, hi_i, lo_i, ph[j], pl[j], kqi, X);
                 range_err |= o.range_err;
                 px += o.fx;
                 py += o.fy;

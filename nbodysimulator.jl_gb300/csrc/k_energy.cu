@@ -253,7 +253,7 @@ __global__ void k_pairs(Dev d, StateView s, int which, int use_list, int* out_j,
         for (int64_t k = use_list ? 0 : R.atom0; k < m; ++k) {
             int64_t j = use_list ? d.nbr[k * d.nbr_kstride + i * d.nbr_istride] : k;
             if (j == i) continue;
-            PairOut o = pair_cutoff(d, R, i, j, hi, lo, d.phi[j], d.plo[j], 0.0f, s.x);
+            PairOut o = pair_cutoff(d, R, PairK(R), i, j, hi, lo, d.phi[j], d.plo[j], 0.0f, s.x);
             if (o.range_err) status_set(d.status, ST_RANGE);
             bool in = which == NBG_POT_LJ ? o.lj_in : o.el_in;
             if (in) {

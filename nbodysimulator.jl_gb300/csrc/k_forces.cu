@@ -470,6 +470,7 @@ __global__ void __launch_bounds__(AT) k_allpairs(Dev d, StateView s)
     const bool active = i < d.n;
     const int64_t ii = active ? i : 0;
     const RepDev& R = d.reps[0];
+    const PairK K(R);
     float4 hi_i = d.phi[ii], lo_i = d.plo[ii];
     float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[ii]) : 0.0f;
     float3 mi = make_float3(0.f, 0.f, 0.f);
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(AT) k_allpairs(Dev d, StateView s)
             if (jg == ii) continue;
             float4 hj = sh_hi[k], lj = sh_lo[k];
             if (cutpots) {
-                PairOut o = pair_cutoff(d, R, ii, jg, hi_i, lo_i, hj, lj, kqi, s.x);
+                PairOut o = pair_cutoff(d, R, K, ii, jg, hi_i, lo_i, hj, lj, kqi, s.x);
                 range_err |= o.range_err;
                 px += o.fx;
                 py += o.fy;
@@ -571,6 +572,7 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         const RepDev& R = d.reps[d.rep_of[i]];
+        const PairK K(R);
         const float4 hi_i = d.phi[i], lo_i = d.plo[i];
         const float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[i]) : 0.0f;
         const int cnt = d.nbr_count[i];
@@ -595,7 +597,7 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
                 hn = __ldg(&d.phi[jn]);
                 ln = __ldg(&d.plo[jn]);
             }
-            PairOut o = pair_cutoff(d, R, i, j, hi_i, lo_i, hj, lj, kqi, s.x);
+            PairOut o = pair_cutoff(d, R, K, i, j, hi_i, lo_i, hj, lj, kqi, s.x);
             range_err |= o.range_err;
             px += o.fx;
             py += o.fy;
@@ -643,6 +645,7 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
     const bool active = i < d.n;
     const int64_t ia = active ? i : 0;
     const RepDev& R = d.reps[d.rep_of[ia]];
+    const PairK K(R);
     const float4 hi_i = d.phi[ia], lo_i = d.plo[ia];
     const float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[ia]) : 0.0f;
     const int cnt = active ? d.nbr_count[ia] : 0;
@@ -652,7 +655,7 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
     for (int k = lane; k < cnt; k += LPA) {
         int j = __ldg(nl + k);
         float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
-        PairOut o = pair_cutoff(d, R, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
+        PairOut o = pair_cutoff(d, R, K, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
         range_err |= o.range_err;
         px += o.fx;
         py += o.fy;

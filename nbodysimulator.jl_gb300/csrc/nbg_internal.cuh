@@ -383,10 +383,23 @@ __device__ __forceinline__ bool distance64(const double* xi, const double* xj, i
     return ok;
 }
 
+// The FP32 constants of a replica's pair test, copied into registers before
+// a pair loop (read through a reference to the replica table they would be
+// loaded again for every pair).
+struct PairK {
+    float invLf, Lh, Ll, lj_lo, lj_hi, el_lo, el_hi;
+    __device__ __forceinline__ explicit PairK(const RepDev& R)
+        : invLf(R.invLf), Lh(R.Lh), Ll(R.Ll), lj_lo(R.lj_lo), lj_hi(R.lj_hi), el_lo(R.el_lo), el_hi(R.el_hi)
+    {
+    }
+};
+
 // FP32 difference of two split positions; under cubic boundaries the hi
 // parts are exact multiples of the grid and the image shift is exact.
+// R: a RepDev or a PairK (invLf, Lh, Ll).
+template <class P>
 __device__ __forceinline__ float3 split_diff(const float4& hi_i, const float4& lo_i, const float4& hi_j,
-                                             const float4& lo_j, bool cubic, const RepDev& R)
+                                             const float4& lo_j, bool cubic, const P& R)
 {
     float dxh = __fsub_rn(hi_i.x, hi_j.x);
     float dyh = __fsub_rn(hi_i.y, hi_j.y);
@@ -431,7 +444,7 @@ struct PairOut {
 // arithmetic on the unwrapped positions, so the pair set equals the
 // reference's bit for bit.
 template <bool CG = false>
-__device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, int64_t i, int64_t j,
+__device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, const PairK& K, int64_t i, int64_t j,
                                                const float4& hi_i, const float4& lo_i, const float4& hi_j,
                                                const float4& lo_j, float kqi, const double* X)
 {
@@ -440,18 +453,18 @@ __device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, in
     o.lj_in = o.el_in = 0;
     o.range_err = false;
     const bool cubic = d.bc == NBG_BC_CUBIC;
-    float3 dr = split_diff(hi_i, lo_i, hi_j, lo_j, cubic, R);
+    float3 dr = split_diff(hi_i, lo_i, hi_j, lo_j, cubic, K);
     float r2 = __fmaf_rn(dr.x, dr.x, __fmaf_rn(dr.y, dr.y, __fmul_rn(dr.z, dr.z)));
     const bool lj_pair = (d.pots & NBG_POT_LJ) && ((__float_as_int(lo_i.w) & __float_as_int(lo_j.w) & AF_LJ) != 0);
     const bool el_pair = (d.pots & NBG_POT_EL) && !el_excluded(d.kind, i, j);
     bool amb = false;
     if (lj_pair) {
-        if (r2 < R.lj_lo) o.lj_in = 1;
-        else if (r2 < R.lj_hi) amb = true;
+        if (r2 < K.lj_lo) o.lj_in = 1;
+        else if (r2 < K.lj_hi) amb = true;
     }
     if (el_pair) {
-        if (r2 < R.el_lo) o.el_in = 1;
-        else if (r2 < R.el_hi) amb = true;
+        if (r2 < K.el_lo) o.el_in = 1;
+        else if (r2 < K.el_hi) amb = true;
     }
     if (amb || d.bc == NBG_BC_PERIODIC) {
         Dist64 q;

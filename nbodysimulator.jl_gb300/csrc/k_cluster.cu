@@ -5,12 +5,15 @@
 // not arithmetic, set its pace. Here the cluster's CTAs (up to 16 SMs) run
 // many steps in one launch:
 //   - CTA r owns atoms [r per, (r+1) per); its threads drift them (FP64, the
-//     reference's velocity-Verlet arithmetic), split the new positions and
-//     push them into every CTA's shared memory (distributed shared memory),
-//     in the buffer of the step's parity;
-//   - one cluster barrier per step (release/acquire) publishes them; with two
-//     parity buffers, a CTA writing step s+1 can never overwrite what another
-//     CTA still reads of step s;
+//     reference's velocity-Verlet arithmetic) and split the new positions
+//     into its shared memory, in the buffer of the step's parity; one thread
+//     sends the contiguous range to every other CTA's same buffer as two bulk
+//     asynchronous copies (cp.async.bulk, distributed shared memory), which
+//     complete as transaction bytes on the receiver's mbarrier of that parity;
+//   - one cluster barrier per step (release/acquire) orders the rebuild flags
+//     and the FP64 copies, then every CTA waits (bounded) for its mbarrier;
+//     with two parity buffers, a copy of step s+2 can only start after the
+//     barrier of step s+1, when every CTA is done reading step s;
 //   - each CTA keeps the Verlet lists of its own atoms in shared memory,
 //     rebuilt from the shared positions (all atoms scanned, the FP32 superset
 //     test of the list builders) when any atom moved more than skin/2 since
@@ -18,8 +21,10 @@
 //     launch;
 //   - LPA lanes per atom evaluate the pairs (pair_cutoff: the exact pair set;
 //     the ambiguous ones read FP64 positions, which the drift also writes to
-//     a global copy of the step's parity, through L2), join their partials
-//     (compensated FP32) and the group's first lane kicks the velocity.
+//     a global copy of the step's parity, through L2) and join their
+//     partials (compensated FP32) into shared memory; the atom's owner thread,
+//     which keeps its x, v, a in registers for the whole launch, kicks the
+//     velocity at the start of the next step.
 // Every thread of every CTA passes the same cluster barriers (no early exit).
 #include <cooperative_groups.h>
 
@@ -29,6 +34,52 @@ namespace cg = cooperative_groups;
 
 #define CL_THREADS 1024
 #define CL_MAX 16
+
+// mbarrier and bulk-copy helpers (shared-memory addresses as 32-bit
+// shared-window offsets; remote ones from mapa)
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned cluster_addr(unsigned a, int rank)
+{
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned a, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned a, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned a, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bytes (a multiple of 16, 16-byte aligned ends) of this CTA's shared memory
+// to another CTA's, completing as transaction bytes on that CTA's mbarrier
+__device__ __forceinline__ void bulk_copy_to_peer(unsigned dst_cluster, unsigned src, unsigned bytes,
+                                                  unsigned mbar_cluster)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst_cluster),
+        "r"(src), "r"(bytes), "r"(mbar_cluster)
+        : "memory");
+}
+
+#define CL_WAIT_TRIES (1u << 16)
 
 // (h, e) += the partner lane's (h, e), h by TwoSum with its error into e
 __device__ __forceinline__ void cl_join(float& h, float& e, int o, int width)
@@ -60,6 +111,8 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     float* fsum = reinterpret_cast<float*>(cnt + per);
     __shared__ unsigned flag[2];  // rebuild requests of the step of each parity
     __shared__ int build_s;
+    __shared__ __align__(8) unsigned long long mbar[2];  // other CTAs' positions of each parity arrived
+    __shared__ int wait_failed;
     const RepDev& R = d.reps[0];
     const PairK K(R);
     const int tid = threadIdx.x;
@@ -94,6 +147,12 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
         }
     }
     if (tid < 2) flag[tid] = 0u;
+    if (tid == 0) {
+        wait_failed = 0;
+        mbar_init(smem_addr(&mbar[0]), 1);
+        mbar_init(smem_addr(&mbar[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     // every CTA of the cluster is running (and initialised) before any
     // remote shared-memory access
     cl.sync();
@@ -132,21 +191,45 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             const double dx = x[0] - xr[0], dy = x[1] - xr[1], dz = x[2] - xr[2];
             moved = st > 0 && !(dx * dx + dy * dy + dz * dz <= d.skin_half2);
         }
+        // the owners' generic writes become visible to the bulk-copy engine
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const int any_moved = __syncthreads_or(moved ? 1 : 0);
-        // push the own atoms' split positions to the other CTAs: (atom, rank) items
-        for (int w = tid; w < na * C; w += CL_THREADS) {
-            const int k = w / C, r = w % C;
-            if (r == rank) continue;
-            const int i = a0 + k;
-            float4* rh = cl.map_shared_rank(ph, r);
-            float4* rl = cl.map_shared_rank(pl, r);
-            rh[i] = ph[i];
-            rl[i] = pl[i];
+        // the own atoms' split positions (contiguous hi and lo ranges) go to
+        // every other CTA as two bulk copies each, completing on its mbarrier
+        // of this parity; this CTA expects the other (n - na) atoms' 32 bytes
+        if (tid == 0) {
+            const unsigned mb = smem_addr(&mbar[par]);
+            mbar_arrive_expect_tx(mb, (unsigned)(n - na) * 32u);
+            if (na > 0) {
+                const unsigned sh = smem_addr(ph + a0), sl = smem_addr(pl + a0), bytes = (unsigned)na * 16u;
+                for (int r = 0; r < C; ++r) {
+                    if (r == rank) continue;
+                    const unsigned rmb = cluster_addr(mb, r);
+                    bulk_copy_to_peer(cluster_addr(sh, r), sh, bytes, rmb);
+                    bulk_copy_to_peer(cluster_addr(sl, r), sl, bytes, rmb);
+                }
+            }
         }
         if (any_moved && tid < C) *cl.map_shared_rank(&flag[par], tid) = 1u;
-        // arrive (release) / wait (acquire) at cluster scope: the pushed
-        // positions and the FP64 copies X are visible past it
+        // arrive (release) / wait (acquire) at cluster scope: the rebuild
+        // flags and the FP64 copies X are visible past it
         cl.sync();
+        // the other CTAs' positions of this step: the k-th use of mbar[par]
+        // completes phase k (bounded wait; after a timeout the launch stops
+        // waiting and reports ST_TIMEOUT)
+        {
+            const unsigned mb = smem_addr(&mbar[par]), phase = (unsigned)((st >> 1) & 1);
+            if (!wait_failed) {
+                unsigned tries = 0;
+                while (!mbar_try_wait(mb, phase)) {
+                    if (++tries >= CL_WAIT_TRIES) {
+                        wait_failed = 1;
+                        status_set(d.status, ST_TIMEOUT);
+                        break;
+                    }
+                }
+            }
+        }
         if (tid == 0) {
             build_s = (st == 0 || flag[par] != 0u || (rebuild_every > 0 && since >= rebuild_every)) ? 1 : 0;
             // the next writes to flag[par] come at step st + 2, after the
@@ -229,6 +312,9 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
         // barrier, no cluster barrier
         __syncthreads();
     }
+    // every CTA has waited for all copies into its shared memory, so after
+    // this barrier no copy reads a CTA's shared memory any more: all may exit
+    cl.sync();
     if (owner) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {

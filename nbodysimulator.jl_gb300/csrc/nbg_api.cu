@@ -698,6 +698,7 @@ static int status_error(nbg_ctx* c, unsigned st)
 {
     if (st & ST_NONFINITE) return fail(c, NBG_ERR_NONFINITE, "non-finite acceleration (NaN/Inf state or coincident bodies)");
     if (st & ST_RANGE) return fail(c, NBG_ERR_RANGE, "minimum-image loop exceeded its iteration cap");
+    if (st & ST_TIMEOUT) return fail(c, NBG_ERR_TIMEOUT, "a device-side wait for data from other blocks ran out");
     if (st & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW))
         return fail(c, NBG_ERR_CAPACITY, "list capacity exceeded");
     return NBG_OK;
@@ -1132,7 +1133,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
         }
         unsigned w = 0;
         if ((st = read_status(c, &w))) { backup_free(c, b); return st; }
-        if (w & (ST_NONFINITE | ST_RANGE)) {
+        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) {
             backup_free(c, b);
             return status_error(c, w);
         }

@@ -29,6 +29,7 @@
 #define ST_NONFINITE 4u
 #define ST_RANGE 8u
 #define ST_SHORT_OVERFLOW 16u  // learned-model short list
+#define ST_TIMEOUT 32u         // a bounded wait in a kernel ran out
 
 // atom flags (plo.w bits)
 #define AF_LJ 1

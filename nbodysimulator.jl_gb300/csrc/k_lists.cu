@@ -8,7 +8,9 @@
 //
 // Build, skipped on device unless a rebuild is due (host-forced every
 // rebuild_every steps, or an atom moved more than skin/2):
-//   k_cell_fill        : atom -> cell by its wrapped position, slot by atomicAdd
+//   k_cell_fill        : atom -> cell by its wrapped position (the image taken
+//                        at the build is kept for the packing until the
+//                        next), slot by atomicAdd
 //   k_cell_sort        : each cell's atoms sorted by index (deterministic
 //                        lists), counts moved to cell_n and cleared for the
 //                        next build
@@ -47,7 +49,11 @@ __device__ __forceinline__ int cell_coord(float h, const RepDev& R)
     return c;
 }
 
-__global__ void k_cell_fill(Dev d, ListCtl L)
+// At a build the atom's periodic image is taken afresh (the wrap into
+// [0, L)), stored in d.img and its split position packed with it; until the
+// next build the drift packs with that image, so that a replica's lists and
+// positions keep one frame.
+__global__ void k_cell_fill(Dev d, ListCtl L, const double* X)
 {
     // the other parity's flags start clean for the next drift (nothing of
     // this rebuild reads them)
@@ -57,6 +63,23 @@ __global__ void k_cell_fill(Dev d, ListCtl L)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         if (!need_build(d, L, d.rep_of[i])) continue;
         const RepDev& R = d.reps[d.rep_of[i]];
+        if (d.img && d.bc == NBG_BC_CUBIC) {
+            double im[3];
+            for (int k = 0; k < 3; ++k) {
+                const double p = X[3 * i + k];
+                double m = floor(p * R.invL);
+                const double w = fma(-R.L, m, p);
+                if (w < 0.0) m -= 1.0;
+                else if (w >= R.L) m += 1.0;
+                im[k] = m;
+                d.img[3 * i + k] = m;
+            }
+            const double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+            float hh[3], ll[3];
+            split_position_image(R, p, im, hh, ll);
+            d.phi[i] = make_float4(hh[0], hh[1], hh[2], d.phi[i].w);
+            d.plo[i] = make_float4(ll[0], ll[1], ll[2], d.plo[i].w);
+        }
         float4 h = d.phi[i];
         int cx = cell_coord(h.x, R), cy = cell_coord(h.y, R), cz = cell_coord(h.z, R);
         int cell = R.cell0 + (cx * R.nc + cy) * R.nc + cz;
@@ -371,7 +394,7 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_list_build_warps(Dev d, ListC
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos)
 {
     ListCtl L{pos, force ? 1 : 0};
-    k_cell_fill<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, L);
+    k_cell_fill<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, L, s.x);
     NBG_LAUNCH_CHECK(c, "k_cell_fill");
     int cells = c->d.ncell_total;
     int gs = cells < 65536 ? cells : 65536;

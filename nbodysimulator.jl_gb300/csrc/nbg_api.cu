@@ -444,6 +444,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         if ((st = dalloc(c, &D.cell_n, D.ncell_total))) return st;
         if ((st = dalloc(c, &D.nbr_count, n))) return st;
         if ((st = dalloc(c, &D.xref, 3 * n))) return st;
+        if (d0->bc == NBG_BC_CUBIC && (st = dalloc(c, &D.img, 3 * n))) return st;
         int cell_cap = ((2 * max_cell_occ + 16 + 7) / 8) * 8;
         int nbr_cap = ((int)std::ceil(1.3 * max_nbr + 32) + 7) / 8 * 8;
         // lanes per atom of the list force kernel: a group of lanes per atom

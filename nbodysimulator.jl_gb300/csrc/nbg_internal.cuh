@@ -99,6 +99,7 @@ struct Dev {
     int64_t nbr_kstride;  // n (column-major, thread per atom) or 1 (row-major, lanes per atom)
     int64_t nbr_istride;  // 1 or nbr_cap
     double* xref;
+    double* img;                // list path, cubic: per atom the periodic image index fixed at its replica's last list build
     int* rebuild_flag;          // [2][nrep]: per replica, by the parity of the position time index
     const int* cell_rep;        // replica of each cell
     unsigned long long* build_count;
@@ -518,12 +519,27 @@ __device__ __forceinline__ void split_position(const Dev& d, const RepDev& R, co
     }
 }
 
+// Split of a position shifted by a given periodic image, w = p - L img:
+// between list builds (img fixed at the build) w stays within skin/2 of the
+// box, well inside the exact range of the hi grid (|w| < 4 L).
+__device__ __forceinline__ void split_position_image(const RepDev& R, const double* p, const double* img, float* h,
+                                                     float* l)
+{
+    for (int k = 0; k < 3; ++k) {
+        const double w = fma(-R.L, img[k], p[k]);
+        const double hq = rint(w * (double)R.qscale) * (double)R.qinv;
+        h[k] = (float)hq;
+        l[k] = (float)(w - hq);
+    }
+}
+
 __device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double* X)
 {
     const RepDev& R = d.reps[d.rep_of[i]];
     const double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
     float h[3], l[3];
-    split_position(d, R, p, h, l);
+    if (d.img && d.bc == NBG_BC_CUBIC) split_position_image(R, p, d.img + 3 * i, h, l);
+    else split_position(d, R, p, h, l);
     float4 hi = d.phi[i];
     float4 lo = d.plo[i];
     d.phi[i] = make_float4(h[0], h[1], h[2], hi.w);

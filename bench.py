@@ -656,7 +656,12 @@ def main():
         drift_key = "gravity" if args.workload == "gravity" else "potential"
         E0 = e_start["kinetic"] + e_start[drift_key]
         E1 = e_end["kinetic"] + e_end[drift_key]
-        line["energy_drift_rel"] = (E1 - E0) / abs(E0) if E0 else None
+        if args.workload == "water":
+            # Berendsen at 300 K from a jittered lattice: the thermostat removes
+            # the energy the melting lattice releases, so energy is not conserved
+            line["energy_change_rel_thermostatted"] = (E1 - E0) / abs(E0) if E0 else None
+        else:
+            line["energy_drift_rel"] = (E1 - E0) / abs(E0) if E0 else None
         if args.workload != "gravity":
             line["temperature_start"] = e_start["temperature"]
             line["temperature_end"] = e_end["temperature"]

@@ -1740,7 +1740,7 @@ static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, bool exact)
     if ((st = launch_force_list(c, ss))) return st;
     if ((st = respa_sub_fast(c, exact, c->ml_a_slow))) return st;
     if (!exact) {
-        // the judge: the learned against the exact short-range force at these positions
+        // r-RESPA error check: the learned against the exact short-range force at these positions
         if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
         if ((st = launch_ml_judge(c, StepRef{sr.off + inner, sr.base}, inner, c->ml_judge_cap))) return st;
     }
@@ -1818,7 +1818,7 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
             c->respa_valid = false;  // lists were reallocated: rebuild everything at the chunk start
             continue;
         }
-        // the judge: relative RMS error of the learned against the exact short-range force
+        // r-RESPA error check: relative RMS error of the learned against the exact short-range force
         double jmax = 0.0, jsum = 0.0;
         for (int64_t o = 0; o < k; ++o) {
             const int64_t slot = ((step0 / inner + o + 1) % chunk + chunk) % chunk;

@@ -169,8 +169,8 @@ def _zero_output(theta):
 def test_respa_ablation(water, trained):
     """Same start, NVE, 2 fs outer step (4 x 0.5 fs): the trained network
     keeps the energy close to velocity Verlet's; the split without it (fast
-    force = bonded only) drifts far more. The judge measures the learned
-    force against the exact short-range force every outer step."""
+    force = bonded only) drifts far more. The r-RESPA error check measures
+    the learned force against the exact short-range force every outer step."""
     thO, thH, _, held = trained
     eng = _nve(water)
     u, v = held

@@ -645,7 +645,6 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
     const bool active = i < d.n;
     const int64_t ia = active ? i : 0;
     const RepDev& R = d.reps[d.rep_of[ia]];
-    const PairK K(R);
     const float4 hi_i = d.phi[ia], lo_i = d.plo[ia];
     const float kqi = (d.pots & NBG_POT_EL) ? (float)(d.el_k_d * d.charge[ia]) : 0.0f;
     const int cnt = active ? d.nbr_count[ia] : 0;
@@ -655,7 +654,7 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
     for (int k = lane; k < cnt; k += LPA) {
         int j = __ldg(nl + k);
         float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
-        PairOut o = pair_cutoff(d, R, K, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
+        PairOut o = pair_cutoff(d, R, R, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
         range_err |= o.range_err;
         px += o.fx;
         py += o.fy;

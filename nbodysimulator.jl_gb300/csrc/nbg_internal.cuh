@@ -445,8 +445,10 @@ struct PairOut {
 // near the half-box image ambiguity) are decided by the reference's FP64
 // arithmetic on the unwrapped positions, so the pair set equals the
 // reference's bit for bit.
-template <bool CG = false>
-__device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, const PairK& K, int64_t i, int64_t j,
+// K: the FP32 pair constants, a PairK in registers or the RepDev itself
+// (fewer registers; the lanes-per-atom kernel keeps more warps resident so)
+template <bool CG = false, class KT = PairK>
+__device__ __forceinline__ PairOut pair_cutoff(const Dev& d, const RepDev& R, const KT& K, int64_t i, int64_t j,
                                                const float4& hi_i, const float4& lo_i, const float4& hi_j,
                                                const float4& lo_j, float kqi, const double* X)
 {

@@ -651,15 +651,21 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
     float px = 0.f, py = 0.f, pz = 0.f;
     bool range_err = false;
     const int* nl = d.nbr + ia * d.nbr_istride;
-    for (int k = lane; k < cnt; k += LPA) {
-        int j = __ldg(nl + k);
-        float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
-        PairOut o = pair_cutoff(d, R, R, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
-        range_err |= o.range_err;
-        px += o.fx;
-        py += o.fy;
-        pz += o.fz;
-    }
+    // the pair constants in registers pay off for the short lists of 4-lane
+    // groups (LJ ensembles); longer lists keep fewer registers (more warps)
+    auto pair_loop = [&](const auto& K) {
+        for (int k = lane; k < cnt; k += LPA) {
+            int j = __ldg(nl + k);
+            float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
+            PairOut o = pair_cutoff(d, R, K, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
+            range_err |= o.range_err;
+            px += o.fx;
+            py += o.fy;
+            pz += o.fz;
+        }
+    };
+    if constexpr (LPA <= 4) pair_loop(PairK(R));
+    else pair_loop(R);
     // join the lanes' partials: compensated FP32 butterfly (TwoSum; every
     // lane ends with the same value, whatever the order of its operands)
     float ex = 0.f, ey = 0.f, ez = 0.f;

@@ -449,7 +449,8 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         int nbr_cap = ((int)std::ceil(1.3 * max_nbr + 32) + 7) / 8 * 8;
         // lanes per atom of the list force kernel: a group of lanes per atom
         // until the GPU holds ~64 resident lanes per SM-thread slot, then one
-        // thread per atom (column-major list)
+        // thread per atom (column-major list); and at least one lane per 32
+        // list entries (long water lists, as the autotuner finds)
         const char* lv = getenv("NBG_LIST_LPA");  // override for tuning sweeps
         if (lv) {
             c->list_lpa = atoi(lv);
@@ -459,6 +460,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
             double threads_wanted = (double)std::max(sms, 1) * 2048.0;
             int lpa = 1;
             while (lpa < 32 && (double)n * lpa < threads_wanted && lpa * 4 <= max_nbr) lpa *= 2;
+            while (lpa < 32 && lpa * 32 < max_nbr) lpa *= 2;
             c->list_lpa = lpa;
         }
         // supported group sizes: 1 (thread per atom), 4, 8, 16, 32

@@ -154,11 +154,24 @@ __global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int
     double zeta = 0.0;
     if (d.therm == NBG_THERMO_NOSEHOOVER) zeta = s.x[3 * d.n];
     const double T_now = d.red_T[0];
+    // Berendsen on a single system: the factor g (T0/T - 1) is the same for
+    // every component, so its three FP64 divisions run once per thread (the
+    // same operations as thermo_term_T, so the same bits)
+    const bool hoist = thermo && d.therm == NBG_THERMO_BERENDSEN && d.nrep == 1;
+    double bfac = 0.0;
+    if (hoist) {
+        const RepDev& R0 = d.reps[0];
+        const double T = do_T ? T_now : d.red_T[0];
+        const double g = 0.5 / R0.tparam;
+        bfac = (1.0 / T == INFINITY) ? g : __dmul_rn(g, __dsub_rn(R0.T0 / T, 1.0));
+    }
     double acc = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x) {
         double v = s.v[e];
         double an = s.a_new[e];
-        if (thermo && (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER))
+        if (hoist)
+            an = __dadd_rn(an, __dmul_rn(bfac, v));
+        else if (thermo && (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER))
             an = __dadd_rn(an, thermo_term_T(d, e / 3, v, zeta, do_T ? T_now : d.red_T[d.rep_of[e / 3]]));
         if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
         double vn = kick1(v, s.a_old[e], an, dt);
@@ -222,8 +235,17 @@ __global__ void k_rhs_thermostat(Dev d, StateView s)
 {
     int64_t ncomp = 3 * d.n;
     double zeta = d.therm == NBG_THERMO_NOSEHOOVER ? s.x[3 * d.n] : 0.0;
+    // Berendsen on a single system: one factor for every component (as in k_kick)
+    const bool hoist = d.therm == NBG_THERMO_BERENDSEN && d.nrep == 1;
+    double bfac = 0.0;
+    if (hoist) {
+        const RepDev& R0 = d.reps[0];
+        const double T = d.red_T[0];
+        const double g = 0.5 / R0.tparam;
+        bfac = (1.0 / T == INFINITY) ? g : __dmul_rn(g, __dsub_rn(R0.T0 / T, 1.0));
+    }
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x)
-        s.a_new[e] = __dadd_rn(s.a_new[e], thermo_term(d, e / 3, s.v[e], zeta));
+        s.a_new[e] = __dadd_rn(s.a_new[e], hoist ? __dmul_rn(bfac, s.v[e]) : thermo_term(d, e / 3, s.v[e], zeta));
 }
 
 __global__ void k_rhs_nh_column(Dev d, StateView s)

@@ -963,14 +963,17 @@ __global__ void __launch_bounds__(256) k_respa_kick(Dev d, double* v, const doub
 {
     const bool berendsen = d.therm == NBG_THERMO_BERENDSEN;
     const double T = d.red_T[0];
+    // the Berendsen factor once per thread (its FP64 divisions are slow here)
+    double fac = 0.0;
+    if (berendsen) {
+        const RepDev& R = d.reps[0];
+        const double gm = 0.5 / R.tparam;
+        fac = (1.0 / T == INFINITY) ? gm : gm * (R.T0 / T - 1.0);
+    }
     double acc = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * d.n; e += (int64_t)gridDim.x * blockDim.x) {
         double an = a[e];
-        if (berendsen) {
-            const RepDev& R = d.reps[0];
-            const double gm = 0.5 / R.tparam;
-            an += (1.0 / T == INFINITY) ? gm * v[e] : gm * (R.T0 / T - 1.0) * v[e];
-        }
+        if (berendsen) an += fac * v[e];
         if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
         const double vn = v[e] + h * an;
         v[e] = vn;

@@ -17,8 +17,9 @@
 //   - each CTA keeps the Verlet lists of its own atoms in shared memory,
 //     rebuilt from the shared positions (all atoms scanned, the FP32 superset
 //     test of the list builders) when any atom moved more than skin/2 since
-//     the last build, every rebuild_every steps, and at the first step of a
-//     launch;
+//     the last build and every rebuild_every steps; a launch stores them (and
+//     the steps since the build) at its end and the next one starts from them
+//     unless the host invalidated them (a new state), else it builds first;
 //   - LPA lanes per atom evaluate the pairs (pair_cutoff: the exact pair set;
 //     the ambiguous ones read FP64 positions, which the drift also writes to
 //     a global copy of the step's parity, through L2) and join their
@@ -98,7 +99,8 @@ __device__ __forceinline__ void cl_join(float& h, float& e, int o, int width)
 // component).
 template <int LPA>
 __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s, double* xb, double dt, int nsteps,
-                                                              int rebuild_every, int per, int cap)
+                                                              int rebuild_every, int per, int cap, int* lst_g,
+                                                              int* cnt_g, double* xref_g, int* since_g, int reuse)
 {
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
@@ -146,6 +148,15 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             cl_pos[(2 * p + 1) * (size_t)n + j].w = wl;
         }
     }
+    int since = 0;
+    if (reuse) {
+        // the lists, their reference positions and the steps since their
+        // build, as the previous launch left them
+        for (int t = tid; t < na * cap; t += CL_THREADS) lst[t] = lst_g[(size_t)rank * per * cap + t];
+        for (int t = tid; t < na; t += CL_THREADS) cnt[t] = cnt_g[(size_t)rank * per + t];
+        for (int t = tid; t < 3 * na; t += CL_THREADS) xref_s[t] = xref_g[3 * (size_t)a0 + t];
+        since = *since_g;
+    }
     if (tid < 2) flag[tid] = 0u;
     if (tid == 0) {
         wait_failed = 0;
@@ -157,7 +168,6 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     // remote shared-memory access
     cl.sync();
 
-    int since = 0;
     for (int st = 0; st <= nsteps; ++st) {
         // kick of the previous step with the forces its groups left in fsum
         if (owner && st > 0) {
@@ -186,10 +196,11 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             split_position(d, R, x, h, l);
             ph[io] = make_float4(h[0], h[1], h[2], ph[io].w);
             pl[io] = make_float4(l[0], l[1], l[2], pl[io].w);
-            // (step 0 rebuilds regardless: xref_s is set there)
+            // (a launch that does not reuse lists builds at step 0, which
+            // sets xref_s)
             const double* xr = xref_s + 3 * ko;
             const double dx = x[0] - xr[0], dy = x[1] - xr[1], dz = x[2] - xr[2];
-            moved = st > 0 && !(dx * dx + dy * dy + dz * dz <= d.skin_half2);
+            moved = (st > 0 || reuse) && !(dx * dx + dy * dy + dz * dz <= d.skin_half2);
         }
         // the owners' generic writes become visible to the bulk-copy engine
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -231,7 +242,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             }
         }
         if (tid == 0) {
-            build_s = (st == 0 || flag[par] != 0u || (rebuild_every > 0 && since >= rebuild_every)) ? 1 : 0;
+            build_s = ((st == 0 && !reuse) || flag[par] != 0u || (rebuild_every > 0 && since >= rebuild_every)) ? 1 : 0;
             // the next writes to flag[par] come at step st + 2, after the
             // barrier of step st + 1, which this CTA passes only later
             flag[par] = 0u;
@@ -324,9 +335,15 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             d.xref[3 * io + k] = xref_s[3 * ko + k];
         }
     }
+    // the lists for the next launch (with their own reference positions:
+    // d.xref also serves the global lists, which other calls rebuild)
+    for (int t = tid; t < 3 * na; t += CL_THREADS) xref_g[3 * (size_t)a0 + t] = xref_s[t];
+    for (int t = tid; t < na * cap; t += CL_THREADS) lst_g[(size_t)rank * per * cap + t] = lst[t];
+    for (int t = tid; t < na; t += CL_THREADS) cnt_g[(size_t)rank * per + t] = cnt[t];
+    if (rank == 0 && tid == 0) *since_g = since;
 }
 
-typedef void (*cluster_kernel_t)(Dev, StateView, double*, double, int, int, int, int);
+typedef void (*cluster_kernel_t)(Dev, StateView, double*, double, int, int, int, int, int*, int*, double*, int*, int);
 
 static cluster_kernel_t cluster_kernel(int lpa)
 {
@@ -409,7 +426,8 @@ int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps,
     cfg.numAttrs = 1;
     prof_begin(c);
     cudaError_t e = cudaLaunchKernelEx(&cfg, k, c->d, s, c->cluster_x, dt, (int)nsteps, rebuild_every,
-                                       c->cluster_per, c->cluster_cap);
+                                       c->cluster_per, c->cluster_cap, c->cluster_lists, c->cluster_cnt,
+                                       c->cluster_xref, c->cluster_since, c->cluster_lists_valid ? 1 : 0);
     prof_end(c);
     if (e != cudaSuccess) return cuda_fail(c, e, "k_cluster_vv launch");
     NBG_LAUNCH_CHECK(c, "k_cluster_vv");

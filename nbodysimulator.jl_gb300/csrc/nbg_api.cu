@@ -527,8 +527,19 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
 // system qualifies at the current list capacity; its FP64 position copies.
 static int plan_cluster(nbg_ctx* c)
 {
+    c->cluster_lists_valid = false;
     if (!cluster_plan(c)) return NBG_OK;
-    if (!c->cluster_x) return dalloc(c, &c->cluster_x, 6 * (size_t)c->n);
+    int st;
+    if (!c->cluster_x && (st = dalloc(c, &c->cluster_x, 6 * (size_t)c->n))) return st;
+    if (c->cluster_lists) dfree(c, c->cluster_lists);
+    if (c->cluster_cnt) dfree(c, c->cluster_cnt);
+    c->cluster_lists = nullptr;
+    c->cluster_cnt = nullptr;
+    const size_t slots = (size_t)c->cluster_size * c->cluster_per;
+    if ((st = dalloc(c, &c->cluster_lists, slots * c->cluster_cap))) return st;
+    if ((st = dalloc(c, &c->cluster_cnt, slots))) return st;
+    if (!c->cluster_since && (st = dalloc(c, &c->cluster_since, 1))) return st;
+    if (!c->cluster_xref && (st = dalloc(c, &c->cluster_xref, 3 * (size_t)c->n))) return st;
     return NBG_OK;
 }
 
@@ -772,6 +783,7 @@ static void resident_dirty(nbg_ctx* c)
 {
     c->steps_since_build = -1;
     c->respa_valid = false;
+    c->cluster_lists_valid = false;
 }
 
 extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
@@ -823,6 +835,7 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
     c->respa_valid = false;
     c->T_valid = false;
     c->steps_since_build = -1;
+    c->cluster_lists_valid = false;
     return NBG_OK;
 }
 
@@ -1109,11 +1122,13 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
                 // the whole chunk in one persistent cluster launch (its lists
                 // live in shared memory: the global ones are rebuilt later)
                 if ((st = launch_cluster_vv(c, c->st, dt, k - s, c->desc.rebuild_every))) break;
+                c->cluster_lists_valid = true;
                 c->step += k - s;
                 c->steps_since_build = -1;
                 s = k;
                 continue;
             }
+            c->cluster_lists_valid = false;  // the graph or direct steps below move the state
             if (graphs && graph_aligned(c) && k - s >= graph_period(c)) {
                 if (!c->graph || c->graph_dt != dt) {
                     if ((st = capture_graph(c, dt))) break;
@@ -1151,6 +1166,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
             CK(cudaMemcpyAsync(c->st.a_old, b.a, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
             c->step = step0;
             c->steps_since_build = -1;
+            c->cluster_lists_valid = false;
             c->T_valid = false;
             if ((st = clear_status(c))) { backup_free(c, b); return st; }
             if ((st = launch_pack(c, c->st))) { backup_free(c, b); return st; }

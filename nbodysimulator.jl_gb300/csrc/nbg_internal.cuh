@@ -173,6 +173,13 @@ struct nbg_ctx {
     int cluster_size = 0, cluster_per = 0, cluster_lpa = 0, cluster_cap = 0;
     size_t cluster_bytes = 0;
     double* cluster_x = nullptr;  // FP64 positions of the two step parities [2][3n]
+    // the lists a cluster launch leaves for the next ([CTA][per][cap], counts,
+    // steps since the build); valid only while nothing else changed the state
+    int* cluster_lists = nullptr;
+    int* cluster_cnt = nullptr;
+    double* cluster_xref = nullptr;  // [3n] positions at the cluster lists' build
+    int* cluster_since = nullptr;
+    bool cluster_lists_valid = false;
     bool grav_uniform = false;  // every body has mass grav_m0: the reduction applies G m
     float grav_far2 = 256.f;    // a tile pair is far when (F g)^2 >= max|r|^2, F = 16
     double grav_m0 = 0.0;

@@ -7,7 +7,7 @@ velocity Verlet with dt = 1e-3. A step is one velocity-Verlet step of all
 bodies (one all-pairs force evaluation). Metric: atom-steps/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-                  [--workload gravity|lj|water|ensemble|mts]
+                  [--workload gravity|lj|water|ensemble|mts|rdf]
 
 --workload mts (learned multiple-time-step water): 32,768 SPC/Fw molecules,
 reaction field at 0.9 nm; the learned short-range model is trained on the GPU
@@ -26,6 +26,10 @@ roofline : the dominant force kernel's algorithmic FLOP/s (20 flop per pair)
            or bytes against the measured peak; for the LJ workload, which
            runs as persistent cluster launches of many steps, the whole step
            loop's time per step.
+--workload rdf: the radial distribution function's pair histogram
+(nbg_rdf_histogram, 1000 bins) over 512 frames of the 12,288-atom water box,
+its 4096 oxygens (4.3e9 pair distances per step); metric pairs/s.
+
 cpu_baseline : the FP64 oracle (a restatement of the reference's O(N^2)
            per-atom loops) on a bounded sample of the same step, host cores.
 With --gpus N > 1 (torchrun) every rank runs its own replica: replicas only,
@@ -54,7 +58,9 @@ WORKLOADS = {
     "water": dict(name="spcfw-water-12288", n=12288, dt=0.0005, steps=2000),
     "ensemble": dict(name="lj-langevin-ensemble-256", n=None, dt=0.005, steps=5000),
     "mts": dict(name="spcfw-water-98304-learned-respa", n=98304, dt=0.0005, steps=400),
+    "rdf": dict(name="rdf-water-oxygens-4096x512", n=12288, dt=None, steps=20, frames=512, maxbin=1000),
 }
+RDF_FLOP_PER_PAIR = 40.0  # the FP32 screen of one pair (FMA = 2)
 
 
 class Workload:
@@ -239,6 +245,33 @@ def cpu_baseline(oracle, wl, target_s=8.0):
             "value_1thread": one, "sample_1thread": f"{m} atoms on 1 thread"}
 
 
+def rdf_frames(nbg, n_atoms, nframes, seed=0, step_nm=0.01):
+    """A trajectory of the SPC/Fw water box (n_atoms / 3 molecules at
+    0.997 g/cm^3): frame 0 is the seeded lattice, later frames add a Gaussian
+    random walk of step_nm per coordinate and frame (unwrapped positions).
+    Returns (frames (nframes, n_atoms, 3), oxygen columns, L)."""
+    pos, _, L = nbg.workloads.spcfw_water_box(n_atoms // 3, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    frames = np.empty((nframes,) + pos.shape)
+    frames[0] = pos
+    for f in range(1, nframes):
+        frames[f] = frames[f - 1] + rng.normal(scale=step_nm, size=pos.shape)
+    return frames, np.arange(0, pos.shape[0], 3, dtype=np.int32), L
+
+
+def rdf_cpu_rate(oracle, frames, idx, L, maxbin, target_s):
+    """The oracle's histogram on whole frames until target_s has passed:
+    (pairs/s, frames done, seconds)."""
+    npairs = len(idx) * (len(idx) - 1) // 2
+    done, t0 = 0, time.perf_counter()
+    while True:
+        oracle.rdf_histogram(frames[done % len(frames)][None], idx, L, maxbin)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= target_s:
+            return done * npairs / el, done, el
+
+
 def run_reference(args, rank):
     """--impl reference: the oracle's restatement of the reference's O(N^2)
     per-atom loops on the host cores, each step a bounded sample of the
@@ -248,6 +281,33 @@ def run_reference(args, rank):
     nbg = G.load_package()
     oracle = G.load_oracle()
     w = WORKLOADS[args.workload]
+    if args.workload == "rdf":
+        # each step: the reference rdf's pair loops over `ref_frames` whole frames
+        frames, idx, L = rdf_frames(nbg, w["n"], w["frames"])
+        cores = os.cpu_count() or 1
+        oracle.set_threads(cores)
+        npairs = len(idx) * (len(idx) - 1) // 2
+        k = args.ref_frames
+        for s in range(args.warmup):
+            oracle.rdf_histogram(frames[s % len(frames)][None], idx, L, w["maxbin"])
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            f0 = (s * k) % len(frames)
+            oracle.rdf_histogram(frames[f0:f0 + k], idx, L, w["maxbin"])
+        el = time.perf_counter() - t0
+        val = args.steps * k * npairs / el
+        sample = (f"{k} whole frame(s) per step ({len(idx)} oxygens, {npairs} pairs each) of the "
+                  f"{w['frames']}-frame trajectory: the FP64 restatement of the reference rdf's loops")
+        line = {"metric": "rdf pairs/s", "value": val, "unit": "pairs/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded lattice + random walk)", "impl": "reference",
+                "config": {"workload": w["name"], "atoms": w["n"], "participants": len(idx),
+                           "frames": w["frames"], "maxbin": w["maxbin"], "sample_frames_per_step": k},
+                "cpu_baseline": {"value": val, "unit": "pairs/s", "cores": cores, "kind": "port", "sample": sample},
+                "e2e": {"value": val, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     wl = Workload(nbg, args.workload, n=args.n)
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
@@ -457,6 +517,108 @@ def run_mts(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_rdf(args, rank, world):
+    """The radial distribution function's pair histogram over a trajectory:
+    one step = nbg_rdf_histogram over all frames (every replica its own)."""
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = local
+    nbg = G.load_package()
+    lib = nbg.load_library()
+    w = WORKLOADS["rdf"]
+    maxbin = w["maxbin"]
+    frames, idx, L = rdf_frames(nbg, w["n"], w["frames"], seed=rank)
+    npairs = w["frames"] * (len(idx) * (len(idx) - 1) // 2)
+    hist = lambda fr, out: nbg._abi.rdf_histogram(fr, idx, L, maxbin, device, out=out)
+    fd = torch.from_numpy(frames).to(f"cuda:{device}")
+    out = torch.zeros(maxbin, dtype=torch.float64, device=f"cuda:{device}")
+    pk = ctypes.c_double()
+    peak = pk.value if lib.nbg_probe_fp32_peak(device, ctypes.byref(pk)) == 0 else None
+    for _ in range(args.warmup):
+        hist(fd, out)
+    ref_hist = out.cpu().numpy().copy()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    stream = torch.cuda.current_stream()  # the legacy default stream, where the library launches
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(device)
+    step_ms, pair_ms, pack_ms = [], [], []
+    torch.cuda.nvtx.range_push("timed")
+    for s in range(args.steps):
+        flush.fill_(float(s))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        hist(fd, out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        km = nbg._abi.rdf_kernel_times()
+        pack_ms.append(km[0])
+        pair_ms.append(km[1])
+    torch.cuda.nvtx.range_pop()
+    clocks = sampler.stop()
+    total_ms = max_over_ranks(float(sum(step_ms)), dist, f"cuda:{device}")
+    value = npairs * args.steps * world / (total_ms / 1e3)
+    deterministic = bool(np.array_equal(out.cpu().numpy(), ref_hist))
+
+    e2e = None
+    if not args.no_e2e:
+        # the public call on host buffers: frames uploaded, histogram read back, every step
+        fh = torch.from_numpy(frames).pin_memory()
+        hh = torch.zeros(maxbin, dtype=torch.float64).pin_memory()
+        fhn, hhn = fh.numpy(), hh.numpy()
+        hist(fhn, hhn)
+        e2e_steps = max(3, min(args.steps, 20))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            hist(fhn, hhn)
+        e2e_s = time.perf_counter() - t0
+        deterministic = deterministic and bool(np.array_equal(hhn, ref_hist))
+        e2e = {"value": npairs * e2e_steps * world / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": fhn.nbytes,
+               "d2h_bytes_per_step": hhn.nbytes + 8,
+               "path": "nbg_rdf_histogram on pinned host frames (all columns uploaded, histogram and status read back)",
+               "steps": e2e_steps}
+
+    pairs_kernel_ms = statistics.mean(pair_ms)
+    achieved = npairs * RDF_FLOP_PER_PAIR / (pairs_kernel_ms / 1e3) / 1e12
+    line = {"metric": "rdf pairs/s", "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 screen, f64 (the reference's arithmetic) for pairs near a bin edge; integer counts",
+            "data": "synthetic (seeded water lattice + Gaussian random walk, unwrapped)",
+            "config": {"workload": w["name"], "atoms": w["n"], "participants": len(idx), "frames": w["frames"],
+                       "maxbin": maxbin, "L_nm": L, "l2": "512 MB buffer written between timed steps (L2 flushed)",
+                       "parallelism": "replicas only" if world > 1 else "single GPU"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None,
+                         "traffic": profile_traffic(f"k_rdf_pairs:{w['name']}"), "kernel": "k_rdf_pairs",
+                         "kernel_ms": pairs_kernel_ms, "kernel_launches": args.steps,
+                         "flop_per_pair": RDF_FLOP_PER_PAIR,
+                         "peak_source": "FP32 FMA probe measured in this run (nbg_probe_fp32_peak)"},
+            "split_kernel_ms": statistics.mean(pack_ms), "e2e": e2e, "gpu_launches": 3 * args.steps,
+            "clocks": clocks, "histogram_repeatable": deterministic}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        oracle = G.load_oracle()
+        cores = os.cpu_count() or 1
+        oracle.set_threads(cores)
+        # parity on two frames, then the oracle's rate on whole frames
+        pick = [0, w["frames"] - 1]
+        gsub = nbg._abi.rdf_histogram(frames[pick], idx, L, maxbin, device)
+        line["parity_two_frames_exact"] = bool(np.array_equal(gsub, oracle.rdf_histogram(frames[pick], idx, L,
+                                                                                          maxbin)))
+        rate, done, el = rdf_cpu_rate(oracle, frames, idx, L, maxbin, 10.0)
+        line["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                "sample": f"{done} whole frames ({len(idx)} oxygens each) in {el:.1f} s: the FP64 "
+                                          "restatement of the reference rdf's loops"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -467,6 +629,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-flush", action="store_true", help="time all steps back to back (no L2 flush)")
     ap.add_argument("--ref-sample", type=int, default=2048)
+    ap.add_argument("--ref-frames", type=int, default=16, help="rdf: whole frames per reference step")
     ap.add_argument("--n", type=int, default=None, help="gravity body count (smaller profiling captures)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--grav-plain", action="store_true", help="gravity with plain FP32 positions")
@@ -493,8 +656,8 @@ def main():
     import torch
     if dist is not None:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    if args.workload == "mts":
-        run_mts(args, rank, world)
+    if args.workload in ("mts", "rdf"):
+        (run_mts if args.workload == "mts" else run_rdf)(args, rank, world)
         if dist is not None:
             dist.destroy_process_group()
         return

@@ -366,6 +366,24 @@ NBG_API int nbg_set_thermostat_target(nbg_ctx* ctx, int32_t replica, double T);
    forward and backward (BF16 tensor cores), [3] force scatter. */
 NBG_API int nbg_ml_kernel_times(nbg_ctx* ctx, int32_t reps, double* ms);
 
+/* Pair histogram of the radial distribution function (replaces the loops of
+   rdf, nbody_simulation_result.jl:664-709; the normalisation to g(r) stays
+   with the caller). frames: nframes x ncols x 3 positions (the reference's
+   3 x N columns per saved time), idx: the nidx participant columns (host
+   memory; the reference's LJ participants), cubic boundaries of side L.
+   For every frame and every unordered pair of participants with minimum-image
+   distance r, r^2 < (L/2)^2 and bin = ceil(r / (L / maxbin)) in 2..maxbin,
+   hist[bin - 1] += 2: the reference's counts exactly (FP32 screening, FP64
+   arithmetic of the reference for every pair near a bin edge). frames and
+   hist may be host or device memory of `device`; 1 <= maxbin <= 16384.
+   NBG_ERR_NONFINITE for a non-finite coordinate, NBG_ERR_RANGE for one more
+   than 16384 boxes out. Context-free; calls are serialised. */
+NBG_API int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t ncols, const int32_t* idx,
+                              int64_t nidx, double L, int32_t maxbin, int device, double* hist);
+/* Device time (ms, CUDA events on the launching stream) of the last
+   nbg_rdf_histogram call's kernels: [0] position split, [1] pair histogram. */
+NBG_API int nbg_rdf_kernel_times(double* ms);
+
 #ifdef __cplusplus
 }
 #endif

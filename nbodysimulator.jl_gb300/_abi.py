@@ -6,6 +6,8 @@ fails to load, every entry point raises instead of falling back to the CPU.
 import ctypes
 import os
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libnbg.so")
 
@@ -159,6 +161,9 @@ SIGNATURES = {
     "nbg_ml_kernel_times": (ctypes.c_int, [_vp, ctypes.c_int32, _dp]),
     "nbg_autotune": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp]),
     "nbg_cluster_shape": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "nbg_rdf_histogram": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.c_int64, ctypes.c_double, ctypes.c_int32, ctypes.c_int, _vp]),
+    "nbg_rdf_kernel_times": (ctypes.c_int, [_dp]),
 }
 
 _lib = None
@@ -197,3 +202,33 @@ def as_dptr(arr):
     if arr is None:
         return None
     return arr.ctypes.data_as(_dp)
+
+
+def rdf_histogram(frames, idx, L, maxbin=1000, device=0, out=None):
+    """nbg_rdf_histogram: the reference rdf's pair counts (hist[bin] += 2 per
+    pair) over frames of shape (nframes, ncols, 3) for the columns idx.
+    frames and out may be numpy arrays or CUDA tensors (data_ptr())."""
+    lib = load_library()
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    if hasattr(frames, "data_ptr"):
+        nframes, ncols = int(frames.shape[0]), int(frames.shape[1])
+        fptr = frames.data_ptr()
+    else:
+        frames = np.ascontiguousarray(frames, dtype=np.float64)
+        nframes, ncols = frames.shape[0], frames.shape[1]
+        fptr = frames.ctypes.data
+    if out is None:
+        out = np.zeros(maxbin)
+    optr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+    st = lib.nbg_rdf_histogram(fptr, nframes, ncols, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(idx),
+                               float(L), int(maxbin), int(device), optr)
+    if st != NBG_OK:
+        raise EngineError(st, "nbg_rdf_histogram")
+    return out
+
+
+def rdf_kernel_times():
+    """(split ms, pair-histogram ms) of the last rdf_histogram call."""
+    ms = (ctypes.c_double * 2)()
+    load_library().nbg_rdf_kernel_times(ms)
+    return ms[0], ms[1]

@@ -1,0 +1,583 @@
+// k_rdf.cu - the radial distribution function's pair histogram
+// (rdf, nbody_simulation_result.jl:664-709) over a trajectory of frames.
+//
+// The reference visits every unordered pair of the LJ participants in every
+// saved frame, takes the minimum-image distance under cubic boundaries
+// (get_interparticle_distance, boundary_conditions.jl:138-165), and adds 2 to
+// bin ceil(r / dr), dr = L / maxbin, when r^2 < (L/2)^2 and 1 < bin <= maxbin.
+// The counts are integers, so parity is bit-exact:
+//
+//   k_rdf_pack    one thread per (frame, participant): wraps the position
+//                 into the box and splits it into an FP32 hi part on the grid
+//                 2^-k (k = 22 - ceil(log2 L)) and an FP32 lo remainder, and
+//                 keeps the unwrapped FP64 position contiguous per frame;
+//   k_rdf_pairs   a grid-stride loop over (frame, tile pair) items of
+//                 TILE x TILE participants, one i per thread, the j tile in
+//                 shared memory as structure-of-arrays float4 groups, two j
+//                 per packed FP32x2 instruction. The split difference gives
+//                 q = r / dr to ~6 ulp. A pair whose q lies within
+//                 RDF_MARGIN * q of an integer, or whose r^2 lies within
+//                 RDF_MARGIN of (L/2)^2, is undecided: a bit in a per-thread
+//                 mask over 32 j, queued in shared memory once per 32 j, and
+//                 decided by the whole block with the reference's FP64
+//                 arithmetic on the unwrapped positions (the loop minimum
+//                 image, r^2, then bin > b <=> r^2 >= thresh[b], a table the
+//                 host builds with IEEE sqrt and division: the reference's
+//                 ceil(sqrt(r^2) / dr) exactly). All other pairs are counted
+//                 in a per-block shared histogram by predicated atomics:
+//                 weight 2 for an off-diagonal tile pair (each unordered pair
+//                 once), weight 1 on a diagonal tile, which runs the full
+//                 square (each unordered pair twice; a self pair has r = 0,
+//                 bin 0). A participant with a coordinate beyond
+//                 RDF_FAR_BOXES boxes has a NaN hi part, so all its pairs take
+//                 the FP64 path: there the rounding of the reference's long
+//                 wrap loops can exceed the band;
+//   k_rdf_finish  hist[b] = counts[b].
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "nbg_internal.cuh"
+
+#define RDF_CHUNK 32  // j per undecided-pair mask
+#define RDF_QCAP 1024
+#define RDF_MAXBIN 16384
+// half-width of the band around a bin edge (relative to q) and around
+// (L/2)^2 (relative to r^2) in which the FP32 estimate is not trusted; its
+// error is below 6 ulp = 3.6e-7
+#define RDF_MARGIN 2e-6f
+// |coordinate| / L from which a participant's pairs are all decided in FP64.
+// Below it the reference's rounding (the difference and up to 2 * 64 wrap
+// steps, each within half an ulp of 128 L) stays under 3e-12 L, far inside the
+// band (2e-6 dr >= 1.2e-10 L for maxbin <= RDF_MAXBIN).
+#define RDF_FAR_BOXES 64.0
+// blocks flush their int32 counts after this many items (<= 2^17 counts each)
+#define RDF_FLUSH_ITEMS 8192
+// q^2 offset of a padding j (beyond any q^2 band)
+#define RDF_PAD 1e30f
+
+struct RdfArgs {
+    const float4* hi;        // [nframes][npad] wrapped hi parts (x, y, z, 0)
+    const float4* lo;        // [nframes][npad] lo remainders
+    const double4_32a* raw;  // [nframes][npad] the unwrapped positions (x, y, z, 0)
+    const double* thresh;    // [maxbin + 1]: bin > b <=> r^2 >= thresh[b]
+    int64_t nidx, npad;
+    int64_t tiles, tile_pairs, items;
+    double L, radius, half2;  // FP64 constants of the reference's formula
+    float invLf, Lh, Ll;      // FP32 image shift (hi grid split of L)
+    float inv_dr, inv_dr2;    // maxbin / L and its square
+    float hq2_lo, hq2_hi;     // (maxbin / 2)^2 band for the half-box test
+    int maxbin;
+    unsigned long long* counts;  // [maxbin] the reference's hist
+    unsigned* status;
+};
+
+struct RdfPackArgs {
+    const double* frames;
+    const int32_t* idx;
+    float4* hi;
+    float4* lo;
+    double4_32a* raw;
+    int64_t ncols, nidx, npad, nframes;
+    double L, invL, qscale, qinv, far, limit;
+    unsigned* status;
+};
+
+__global__ void __launch_bounds__(256) k_rdf_pack(RdfPackArgs a)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= a.nframes * a.npad) return;
+    const int64_t f = t / a.npad, s = t - f * a.npad;
+    float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+    double4_32a r = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+    if (s < a.nidx) {
+        const double* p = a.frames + (f * a.ncols + a.idx[s]) * 3;
+        r = make_double4_32a(p[0], p[1], p[2], 0.0);
+        unsigned st = 0u;
+        bool far = false;
+        for (int k = 0; k < 3; ++k) {
+            const double x = p[k];
+            if (!isfinite(x)) {
+                st |= ST_NONFINITE;
+                continue;
+            }
+            // coordinates beyond `limit` would take the reference's
+            // minimum-image loops more than MINIMAGE_MAX_ITERS passes
+            if (fabs(x) > a.limit) {
+                st |= ST_RANGE;
+                continue;
+            }
+            far = far || fabs(x) >= a.far;
+            double w = fma(-a.L, floor(x * a.invL), x);
+            if (w < 0.0) w += a.L;
+            if (w >= a.L) w -= a.L;
+            const double hq = rint(w * a.qscale) * a.qinv;
+            h[k] = (float)hq;
+            l[k] = (float)(w - hq);
+        }
+        if (st) atomicOr(a.status, st);
+        if (far || st) h[0] = __int_as_float(0x7fc00000);  // NaN: every pair of this one in FP64
+    }
+    a.hi[t] = make_float4(h[0], h[1], h[2], 0.f);
+    a.lo[t] = make_float4(l[0], l[1], l[2], 0.f);
+    a.raw[t] = r;
+}
+
+// 1 / sqrt(x) by the approximate hardware instruction, subnormals flushed
+// (q^2 below 2^-126 is a self or coincident pair: bin 0 either way)
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// The reference's arithmetic for one ordered pair: FP64 difference of the
+// unwrapped positions, the minimum-image loops, r2 = (x^2 + y^2) + z^2, then
+// bin = ceil(sqrt(r2) / dr) as the place of r2 among the thresholds.
+// Returns the 1-based bin to count, or 0.
+__device__ __forceinline__ int rdf_bin64(const RdfArgs& a, int64_t f, int64_t i, int64_t j)
+{
+    const double4_32a pi = a.raw[f * a.npad + i], pj = a.raw[f * a.npad + j];
+    double x = __dsub_rn(pi.x, pj.x);
+    double y = __dsub_rn(pi.y, pj.y);
+    double z = __dsub_rn(pi.z, pj.z);
+    if (!(wrap_cubic64(x, a.L, a.radius) && wrap_cubic64(y, a.L, a.radius) && wrap_cubic64(z, a.L, a.radius))) {
+        atomicOr(a.status, ST_RANGE);
+        return 0;
+    }
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+    if (!(r2 < a.half2)) return 0;
+    int b = (int)ceilf(sqrtf((float)r2) * a.inv_dr);  // an estimate; the thresholds decide
+    b = min(max(b, 1), a.maxbin);
+    const double t0 = a.thresh[b - 1], t1 = a.thresh[b];
+    if (!(r2 >= t0 && r2 < t1)) {                       // the estimate was off by a bin or more
+        while (b > 0 && r2 < a.thresh[b - 1]) --b;      // now bin >= b
+        while (b <= a.maxbin && r2 >= a.thresh[b]) ++b; // now bin <= b
+    }
+    return (b > 1 && b <= a.maxbin) ? b : 0;
+}
+
+// TILE participants per tile (threads per block), UNROLL groups of 4 j in
+// flight, MINB blocks per SM for the register budget
+template <int TILE, int UNROLL, int MINB>
+__global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
+{
+    extern __shared__ unsigned rdf_hist[];  // [maxbin]
+    // the j tile: hi x, y, z, lo x, y, z, q^2 offset (0, or RDF_PAD past nidx)
+    __shared__ __align__(16) float sj[7][TILE];
+    __shared__ unsigned queue[RDF_QCAP];  // (i in tile) << 16 | (j in tile)
+    __shared__ int qn;
+    const int t = threadIdx.x;
+    for (int b = t; b < a.maxbin; b += TILE) rdf_hist[b] = 0u;
+    const float magic = 12582912.0f;  // 1.5 * 2^23: x + magic rounds x to an integer
+    const int magic_bits = __float_as_int(magic);
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 mg = make_float2(magic, magic), mmg = make_float2(-magic, -magic);
+    const float2 invL = make_float2(a.invLf, a.invLf);
+    const float2 mLh = make_float2(-a.Lh, -a.Lh), mLl = make_float2(-a.Ll, -a.Ll);
+    const float2 c2 = make_float2(a.inv_dr2, a.inv_dr2);
+    const float2 marg = make_float2(RDF_MARGIN, RDF_MARGIN);
+    int since_flush = 0;
+    for (int64_t item = blockIdx.x; item < a.items; item += gridDim.x) {
+        const int64_t f = item / a.tile_pairs;
+        const int64_t p = item - f * a.tile_pairs;
+        // tile pair {ti, tj}, tj = ti + s (mod tiles): every unordered pair once
+        const int64_t s = p / a.tiles;
+        const int64_t ti = p - s * a.tiles;
+        int64_t tj = ti + s;
+        if (tj >= a.tiles) tj -= a.tiles;
+        __syncthreads();  // the previous item's tile and queue are consumed
+        const int64_t jb = tj * TILE;
+        {
+            const float4 h = a.hi[f * a.npad + jb + t], l = a.lo[f * a.npad + jb + t];
+            sj[0][t] = h.x;
+            sj[1][t] = h.y;
+            sj[2][t] = h.z;
+            sj[3][t] = l.x;
+            sj[4][t] = l.y;
+            sj[5][t] = l.z;
+            sj[6][t] = (jb + t < a.nidx) ? 0.f : RDF_PAD;
+        }
+        if (t == 0) qn = 0;
+        __syncthreads();
+        const unsigned w = (s == 0) ? 1u : 2u;
+        const int64_t i = ti * TILE + t;
+        if (i < a.nidx) {
+            const float4 hi = a.hi[f * a.npad + i], li = a.lo[f * a.npad + i];
+            const float2 hx = make_float2(hi.x, hi.x), hy = make_float2(hi.y, hi.y), hz = make_float2(hi.z, hi.z);
+            const float2 lx = make_float2(li.x, li.x), ly = make_float2(li.y, li.y), lz = make_float2(li.z, li.z);
+            for (int c = 0; c < TILE; c += RDF_CHUNK) {
+                unsigned amb = 0u;
+#pragma unroll UNROLL
+                for (int g = 0; g < RDF_CHUNK; g += 4) {
+                    float4 J[7];
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) J[k] = *reinterpret_cast<const float4*>(&sj[k][c + g]);
+#pragma unroll
+                    for (int half = 0; half < 2; ++half) {
+                        float2 v[7];
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) v[k] = half ? make_float2(J[k].z, J[k].w) : make_float2(J[k].x, J[k].y);
+                        // hi and lo differences, the image shift s = rint(dh / L) on both
+                        float2 dxh = __ffma2_rn(v[0], m1, hx), dyh = __ffma2_rn(v[1], m1, hy);
+                        float2 dzh = __ffma2_rn(v[2], m1, hz);
+                        const float2 dxl = __ffma2_rn(v[3], m1, lx), dyl = __ffma2_rn(v[4], m1, ly);
+                        const float2 dzl = __ffma2_rn(v[5], m1, lz);
+                        const float2 sx = __fadd2_rn(__ffma2_rn(dxh, invL, mg), mmg);
+                        const float2 sy = __fadd2_rn(__ffma2_rn(dyh, invL, mg), mmg);
+                        const float2 sz = __fadd2_rn(__ffma2_rn(dzh, invL, mg), mmg);
+                        const float2 dx = __fadd2_rn(__ffma2_rn(sx, mLh, dxh), __ffma2_rn(sx, mLl, dxl));
+                        const float2 dy = __fadd2_rn(__ffma2_rn(sy, mLh, dyh), __ffma2_rn(sy, mLl, dyl));
+                        const float2 dz = __fadd2_rn(__ffma2_rn(sz, mLh, dzh), __ffma2_rn(sz, mLl, dzl));
+                        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                        const float2 q2 = __ffma2_rn(r2, c2, v[6]);  // (r / dr)^2, or past the band for padding
+                        // q = sqrt(q2); q2 = 0 (a self pair) gives NaN, which no test below passes
+                        const float2 q = __fmul2_rn(q2, make_float2(rsqrt_ftz(q2.x), rsqrt_ftz(q2.y)));
+                        const float2 tq = __fadd2_rn(q, mg);
+                        const float2 dq = __ffma2_rn(__fadd2_rn(tq, mmg), m1, q);  // q - nearest integer
+                        const float2 mq = __fmul2_rn(q, marg);
+#pragma unroll
+                        for (int e = 0; e < 2; ++e) {
+                            const float Q2 = e ? q2.y : q2.x, Q = e ? q.y : q.x;
+                            const float T = e ? tq.y : tq.x, D = e ? dq.y : dq.x, M = e ? mq.y : mq.x;
+                            const bool inside = Q2 <= a.hq2_lo;   // NaN (a far participant): false
+                            const bool beyond = Q2 >= a.hq2_hi;
+                            const bool near = fabsf(D) < M;       // at q < 0.5, |D| = q: never
+                            if (!beyond && (!inside || near)) amb |= 1u << (g + 2 * half + e);
+                            // bin - 1 = ceil(q) - 1 = nearest - (q below it)
+                            if (inside && !near && Q > 1.0f)
+                                atomicAdd(&rdf_hist[(__float_as_int(T) - magic_bits) - (int)(__float_as_uint(D) >> 31)],
+                                          w);
+                        }
+                    }
+                }
+                if (amb) {  // this chunk's undecided pairs, for the block's FP64 pass
+                    int slot = atomicAdd(&qn, __popc(amb));
+                    while (amb) {
+                        const int b = __ffs(amb) - 1;
+                        amb &= amb - 1u;
+                        if (slot < RDF_QCAP) {
+                            queue[slot] = ((unsigned)t << 16) | (unsigned)(c + b);
+                        } else if (jb + c + b < a.nidx) {
+                            const int bin = rdf_bin64(a, f, i, jb + c + b);
+                            if (bin) atomicAdd(&rdf_hist[bin - 1], w);
+                        }
+                        ++slot;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // the queued pairs of this item, decided in FP64 by the whole block
+        const int nq = min(qn, RDF_QCAP);
+        for (int e = t; e < nq; e += TILE) {
+            const unsigned pr = queue[e];
+            const int64_t j = jb + (pr & 0xffffu);
+            if (j < a.nidx) {
+                const int bin = rdf_bin64(a, f, ti * TILE + (pr >> 16), j);
+                if (bin) atomicAdd(&rdf_hist[bin - 1], w);
+            }
+        }
+        if (++since_flush == RDF_FLUSH_ITEMS) {
+            since_flush = 0;
+            __syncthreads();
+            for (int b = t; b < a.maxbin; b += TILE) {
+                const unsigned c = rdf_hist[b];
+                if (c) {
+                    atomicAdd(a.counts + b, (unsigned long long)c);
+                    rdf_hist[b] = 0u;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int b = t; b < a.maxbin; b += TILE) {
+        const unsigned c = rdf_hist[b];
+        if (c) atomicAdd(a.counts + b, (unsigned long long)c);
+    }
+}
+
+__global__ void k_rdf_finish(const unsigned long long* counts, int maxbin, double* hist)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < maxbin) hist[b] = (double)counts[b];
+}
+
+// The instantiated forms of k_rdf_pairs; NBG_RDF_FORM=<index> picks one
+// (default 0).
+struct RdfForm {
+    void (*kernel)(RdfArgs);
+    int tile, unroll, minb;
+};
+const RdfForm kRdfForms[] = {
+    {k_rdf_pairs<256, 8, 2>, 256, 8, 2}, {k_rdf_pairs<256, 4, 3>, 256, 4, 3}, {k_rdf_pairs<256, 2, 4>, 256, 2, 4},
+    {k_rdf_pairs<128, 8, 4>, 128, 8, 4}, {k_rdf_pairs<128, 4, 6>, 128, 4, 6}, {k_rdf_pairs<128, 2, 8>, 128, 2, 8},
+};
+const int kRdfFormCount = (int)(sizeof(kRdfForms) / sizeof(kRdfForms[0]));
+
+namespace {
+
+// Scratch of the histogram, kept across calls on the same device and grown
+// on demand; one call at a time.
+struct RdfScratch {
+    int device = -1;
+    double* frames = nullptr;
+    size_t frames_cap = 0;
+    double4_32a* packed = nullptr;  // N float4 hi, N float4 lo, N double4 raw (2 N double4_32a)
+    size_t packed_cap = 0;
+    int32_t* idx = nullptr;
+    size_t idx_cap = 0;
+    std::vector<int32_t> idx_host;  // what idx holds
+    unsigned long long* counts = nullptr;
+    double* hist = nullptr;
+    double* thresh = nullptr;  // [RDF_MAXBIN + 1]
+    double thresh_L = 0.0;     // the box and bin count thresh was built for
+    int thresh_maxbin = 0;
+    unsigned* status = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // pack start/end, pairs start/end
+    double last_ms[2] = {0.0, 0.0};                             // the last call's pack, pairs
+    int sms = 0;
+    int form = 0;        // index into kRdfForms
+    int occ_maxbin = 0;  // the histogram size pair_blocks was sized for
+    int pair_blocks = 0;
+};
+
+std::mutex g_rdf_mutex;
+RdfScratch g_rdf;
+
+void rdf_release(RdfScratch& s)
+{
+    for (cudaEvent_t& e : s.ev)
+        if (e) cudaEventDestroy(e);
+    cudaFree(s.frames);
+    cudaFree(s.packed);
+    cudaFree(s.idx);
+    cudaFree(s.counts);
+    cudaFree(s.hist);
+    cudaFree(s.thresh);
+    cudaFree(s.status);
+    s = RdfScratch();
+}
+
+template <class T>
+bool grow(T*& p, size_t& cap, size_t n)
+{
+    if (n <= cap) return true;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return false;
+    cap = n;
+    return true;
+}
+
+// The smallest r^2 >= 0 whose bin ceil(sqrt(r^2) / dr) exceeds b, with the
+// reference's IEEE double sqrt and division (nbody_simulation_result.jl:683):
+// bin > b <=> sqrt(r2) / dr > b, monotone in r2, found by bisection over the
+// ordered bit patterns of the non-negative doubles.
+double rdf_threshold(double dr, int b)
+{
+    uint64_t lo = 0, hi = 0x7ff0000000000000ull;  // 0 (false) and +inf (true)
+    while (hi - lo > 1) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        double x;
+        std::memcpy(&x, &mid, sizeof x);
+        if (std::sqrt(x) / dr > (double)b)
+            hi = mid;
+        else
+            lo = mid;
+    }
+    double x;
+    std::memcpy(&x, &hi, sizeof x);
+    return x;
+}
+
+bool is_device_pointer(const void* p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t ncols, const int32_t* idx,
+                                 int64_t nidx, double L, int32_t maxbin, int device, double* hist)
+{
+    if (!hist || nframes < 0 || ncols < 0 || nidx < 0 || !(L > 0.0) || !std::isfinite(L) || maxbin < 1 ||
+        maxbin > RDF_MAXBIN || nidx > (int64_t)1 << 30)
+        return NBG_ERR_ARG;
+    if (nframes > 0 && nidx > 0 && !frames) return NBG_ERR_ARG;
+    if (nidx > 0 && !idx) return NBG_ERR_ARG;
+    for (int64_t a = 0; a < nidx; ++a)
+        if (idx[a] < 0 || idx[a] >= ncols) return NBG_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_rdf_mutex);
+    if (cudaSetDevice(device) != cudaSuccess) return NBG_ERR_CUDA;
+    RdfScratch& S = g_rdf;
+    if (S.device != device) {
+        if (S.device >= 0) {
+            int cur = device;
+            cudaSetDevice(S.device);
+            rdf_release(S);
+            cudaSetDevice(cur);
+        }
+        S.device = device;
+        if (cudaMalloc(&S.counts, RDF_MAXBIN * sizeof(unsigned long long)) != cudaSuccess ||
+            cudaMalloc(&S.hist, RDF_MAXBIN * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&S.thresh, (RDF_MAXBIN + 1) * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&S.status, sizeof(unsigned)) != cudaSuccess) {
+            rdf_release(S);
+            return NBG_ERR_NOMEM;
+        }
+        for (cudaEvent_t& e : S.ev)
+            if (cudaEventCreate(&e) != cudaSuccess) {
+                rdf_release(S);
+                return NBG_ERR_CUDA;
+            }
+        cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, device);
+        for (const RdfForm& fm : kRdfForms)
+            cudaFuncSetAttribute(fm.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 RDF_MAXBIN * (int)sizeof(unsigned));
+        const char* env = std::getenv("NBG_RDF_FORM");
+        S.form = env ? std::atoi(env) : 0;
+        if (S.form < 0 || S.form >= kRdfFormCount) S.form = 0;
+    }
+    const RdfForm& form = kRdfForms[S.form];
+    if (S.occ_maxbin != maxbin) {
+        // a grid of all the blocks that fit at once with this histogram size
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, form.kernel, form.tile, maxbin * sizeof(unsigned));
+        S.pair_blocks = S.sms * std::max(per_sm, 1);
+        S.occ_maxbin = maxbin;
+    }
+    cudaStream_t st = 0;
+    const bool dev_out = is_device_pointer(hist);
+    double* hist_d = dev_out ? hist : S.hist;
+    cudaMemsetAsync(S.counts, 0, maxbin * sizeof(unsigned long long), st);
+    cudaMemsetAsync(S.status, 0, sizeof(unsigned), st);
+    const int64_t tiles = (nidx + form.tile - 1) / form.tile;
+    const int64_t npad = tiles * form.tile;
+    if (nframes > 0 && nidx > 0) {
+        const double* frames_d = frames;
+        if (!is_device_pointer(frames)) {
+            const size_t n = (size_t)nframes * (size_t)ncols * 3;
+            if (!grow(S.frames, S.frames_cap, n)) return NBG_ERR_NOMEM;
+            if (cudaMemcpyAsync(S.frames, frames, n * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
+                return NBG_ERR_CUDA;
+            frames_d = S.frames;
+        }
+        const size_t nslots = (size_t)nframes * (size_t)npad;
+        if (!grow(S.packed, S.packed_cap, 2 * nslots)) return NBG_ERR_NOMEM;
+        if (S.idx_host.size() != (size_t)nidx ||
+            std::memcmp(S.idx_host.data(), idx, (size_t)nidx * sizeof(int32_t)) != 0) {
+            if (!grow(S.idx, S.idx_cap, (size_t)nidx)) return NBG_ERR_NOMEM;
+            S.idx_host.assign(idx, idx + nidx);
+            if (cudaMemcpyAsync(S.idx, S.idx_host.data(), (size_t)nidx * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                st) != cudaSuccess)
+                return NBG_ERR_CUDA;
+        }
+        // the hi grid of the wrapped positions, as for the force kernels
+        const int e = (int)std::ceil(std::log2(L));
+        const int k = 22 - e;
+        const double Lh = std::rint(L * std::ldexp(1.0, k)) * std::ldexp(1.0, -k);
+        RdfPackArgs pa;
+        pa.frames = frames_d;
+        pa.idx = S.idx;
+        pa.hi = reinterpret_cast<float4*>(S.packed);
+        pa.lo = pa.hi + nslots;
+        pa.raw = S.packed + nslots;
+        pa.ncols = ncols;
+        pa.nidx = nidx;
+        pa.npad = npad;
+        pa.nframes = nframes;
+        pa.L = L;
+        pa.invL = 1.0 / L;
+        pa.qscale = std::ldexp(1.0, k);
+        pa.qinv = std::ldexp(1.0, -k);
+        pa.far = RDF_FAR_BOXES * L;
+        pa.limit = 0.25 * MINIMAGE_MAX_ITERS * L;
+        pa.status = S.status;
+        const int64_t pack_threads = nframes * npad;
+        cudaEventRecord(S.ev[0], st);
+        k_rdf_pack<<<(unsigned)((pack_threads + 255) / 256), 256, 0, st>>>(pa);
+        cudaEventRecord(S.ev[1], st);
+        // invalid coordinates end the call here (their pairs would all take
+        // the FP64 path)
+        unsigned pst = 0;
+        if (cudaMemcpyAsync(&pst, S.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return NBG_ERR_CUDA;
+        if (pst & ST_NONFINITE) return NBG_ERR_NONFINITE;
+        if (pst & ST_RANGE) return NBG_ERR_RANGE;
+
+        RdfArgs a;
+        a.hi = pa.hi;
+        a.lo = pa.lo;
+        a.raw = pa.raw;
+        a.nidx = nidx;
+        a.npad = npad;
+        a.tiles = tiles;
+        a.tile_pairs = tiles * (tiles + 1) / 2;
+        a.items = nframes * a.tile_pairs;
+        if (S.thresh_L != L || S.thresh_maxbin != maxbin) {
+            const double dr = L / maxbin;  // pbc.L / maxbin
+            std::vector<double> th(maxbin + 1);
+            for (int b = 0; b <= maxbin; ++b) th[b] = rdf_threshold(dr, b);
+            if (cudaMemcpy(S.thresh, th.data(), th.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+                return NBG_ERR_CUDA;
+            S.thresh_L = L;
+            S.thresh_maxbin = maxbin;
+        }
+        a.thresh = S.thresh;
+        a.L = L;
+        a.radius = 0.5 * L;
+        a.inv_dr = (float)(maxbin / L);
+        a.half2 = (0.5 * L) * (0.5 * L);
+        a.invLf = (float)(1.0 / L);
+        a.Lh = (float)Lh;
+        a.Ll = (float)(L - Lh);
+        const double qmax = 0.5 * maxbin;  // q = r / dr at r = L / 2
+        a.inv_dr2 = (float)((maxbin / L) * (maxbin / L));
+        a.hq2_lo = (float)(qmax * qmax * (1.0 - RDF_MARGIN));
+        a.hq2_hi = (float)(qmax * qmax * (1.0 + RDF_MARGIN));
+        a.maxbin = maxbin;
+        a.counts = S.counts;
+        a.status = S.status;
+        const int64_t blocks = std::min<int64_t>(a.items, S.pair_blocks);
+        cudaEventRecord(S.ev[2], st);
+        form.kernel<<<(unsigned)blocks, form.tile, maxbin * sizeof(unsigned), st>>>(a);
+        cudaEventRecord(S.ev[3], st);
+    }
+    k_rdf_finish<<<(maxbin + 255) / 256, 256, 0, st>>>(S.counts, maxbin, hist_d);
+    if (!dev_out &&
+        cudaMemcpyAsync(hist, hist_d, maxbin * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return NBG_ERR_CUDA;
+    unsigned status = 0;
+    if (cudaMemcpyAsync(&status, S.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return NBG_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return NBG_ERR_CUDA;
+    S.last_ms[0] = S.last_ms[1] = 0.0;
+    if (nframes > 0 && nidx > 0) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, S.ev[0], S.ev[1]) == cudaSuccess) S.last_ms[0] = ms;
+        if (cudaEventElapsedTime(&ms, S.ev[2], S.ev[3]) == cudaSuccess) S.last_ms[1] = ms;
+    }
+    if (status & ST_NONFINITE) return NBG_ERR_NONFINITE;
+    if (status & ST_RANGE) return NBG_ERR_RANGE;
+    return NBG_OK;
+}
+
+extern "C" int nbg_rdf_kernel_times(double* ms)
+{
+    if (!ms) return NBG_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_rdf_mutex);
+    ms[0] = g_rdf.last_ms[0];
+    ms[1] = g_rdf.last_ms[1];
+    return NBG_OK;
+}

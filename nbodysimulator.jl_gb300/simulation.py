@@ -449,26 +449,18 @@ def msd(sr):
     return ts, (d * d).sum(axis=2).mean(axis=1)
 
 
-def rdf(sr):
-    """Radial distribution function with 1000 bins under cubic boundaries
-    (nbody_simulation_result.jl:664-709); host-side post-processing."""
+def rdf(sr, maxbin=1000):
+    """Radial distribution function under cubic boundaries
+    (nbody_simulation_result.jl:664-709): the pair histogram of every saved
+    frame on the GPU (nbg_rdf_histogram), then the reference's normalisation
+    by the ideal-gas shell counts. Returns (bin centres, g(r))."""
     sysm = sr.simulation.system
     L = sr.simulation.boundary_conditions.L
     idx = np.arange(0, 3 * len(sysm.bodies), 3) if isinstance(sysm, WaterSPCFw) else np.arange(len(sysm.bodies))
-    maxbin = 1000
     dr = L / maxbin
-    hist = np.zeros(maxbin)
+    frames = np.ascontiguousarray(np.stack([np.asarray(u, dtype=np.float64) for u in sr.solution.u]))
+    hist = _abi.rdf_histogram(frames, idx, L, maxbin)
     n = len(idx)
-    for k in range(len(sr.solution.t)):
-        cc = sr.solution.u[k][idx]
-        for a in range(n - 1):
-            dx = cc[a] - cc[a + 1:]
-            dx = dx - L * np.round(dx / L)
-            r2 = (dx * dx).sum(axis=1)
-            r = np.sqrt(r2[r2 < (0.5 * L) ** 2])
-            b = np.ceil(r / dr).astype(int)
-            b = b[(b > 1) & (b <= maxbin)]
-            np.add.at(hist, b - 1, 2)
     c = 4 / 3 * math.pi * n / L ** 3
     rl = np.arange(maxbin) * dr
     nideal = c * ((rl + dr) ** 3 - rl ** 3)

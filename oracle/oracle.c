@@ -92,6 +92,50 @@ static pairdist distance(const double* ri, const double* rj, const nbg_system_de
     return p;
 }
 
+/* rdf's histogram (nbody_simulation_result.jl:664-709): in every frame, each
+   unordered pair of the atoms idx[] (the reference's LJ participants) under
+   cubic boundaries of side L, r from get_interparticle_distance, counted
+   twice in bin = ceil(r / dr), dr = L / maxbin, when r^2 < (L/2)^2 and
+   1 < bin <= maxbin. frames: nframes x (3 x ncols), the reference's layout.
+   Threads split the pair rows and add integer-valued histograms, so the
+   result does not depend on the thread count. */
+void oracle_rdf_histogram(const double* frames, int64_t nframes, int64_t ncols, const int32_t* idx, int64_t nidx,
+                          double L, int32_t maxbin, double* hist)
+{
+    nbg_system_desc d;
+    memset(&d, 0, sizeof d);
+    d.bc = NBG_BC_CUBIC;
+    d.box[0] = L;
+    const double dr = L / maxbin;
+    const double half = 0.5 * L;
+    const double half2 = half * half; /* (0.5 * pbc.L)^2 */
+    for (int32_t b = 0; b < maxbin; ++b) hist[b] = 0.0;
+    int nt = g_threads;
+    double* part = (double*)calloc((size_t)nt * maxbin, sizeof(double));
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 16)
+    for (int64_t a = 0; a < nidx; ++a) {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        double* h = part + (size_t)t * maxbin;
+        for (int64_t f = 0; f < nframes; ++f) {
+            const double* cc = frames + f * 3 * ncols;
+            const double* ri = cc + 3 * (int64_t)idx[a];
+            for (int64_t b = a + 1; b < nidx; ++b) {
+                pairdist p = distance(ri, cc + 3 * (int64_t)idx[b], &d);
+                if (p.r2 < half2) {
+                    const double bin = ceil(p.r / dr);
+                    if (bin > 1 && bin <= maxbin) h[(int64_t)bin - 1] += 2.0;
+                }
+            }
+        }
+    }
+    for (int t = 0; t < nt; ++t)
+        for (int32_t b = 0; b < maxbin; ++b) hist[b] += part[(size_t)t * maxbin + b];
+    free(part);
+}
+
 static int is_water(const nbg_system_desc* d) { return d->kind == NBG_SYSTEM_WATER; }
 static int64_t nh_cols(const nbg_system_desc* d) { return d->n + (d->thermostat == NBG_THERMO_NOSEHOOVER ? 1 : 0); }
 

@@ -39,6 +39,8 @@ def lib():
         _lib.oracle_uniform.restype = ctypes.c_double
         _lib.oracle_uniform.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
         _lib.oracle_normals3.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _dp]
+        _lib.oracle_rdf_histogram.argtypes = [_dp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
+                                              ctypes.c_int64, ctypes.c_double, ctypes.c_int32, _dp]
     return _lib
 
 
@@ -118,3 +120,15 @@ def normals3(seed, atom, step):
     out = np.zeros(3)
     lib().oracle_normals3(seed, atom, step, _p(out))
     return out
+
+
+def rdf_histogram(frames, idx, L, maxbin=1000):
+    """rdf's histogram (nbody_simulation_result.jl:664-709) over frames of
+    shape (nframes, ncols, 3) for the atoms idx; float64 counts."""
+    frames = np.ascontiguousarray(frames, dtype=np.float64)
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    hist = np.zeros(maxbin)
+    lib().oracle_rdf_histogram(_p(frames), frames.shape[0], frames.shape[1],
+                               idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(idx), float(L),
+                               int(maxbin), _p(hist))
+    return hist

@@ -123,3 +123,50 @@ def test_philox_streams_distinct(oracle):
     assert 0.45 < us.mean() < 0.55
     zs = np.array([oracle.normals3(7, i, 3) for i in range(2000)]).ravel()
     assert abs(zs.mean()) < 0.06 and abs(zs.std() - 1) < 0.05
+
+
+def _rdf_loops(frames, idx, L, maxbin):
+    """The reference rdf's loops (nbody_simulation_result.jl:672-692) with its
+    minimum image (boundary_conditions.jl:138-165), in plain Python."""
+    hist = [0.0] * maxbin
+    dr = L / maxbin
+    radius = 0.5 * L
+    for cc in frames:
+        for a in range(len(idx)):
+            ri = cc[idx[a]]
+            for b in range(a + 1, len(idx)):
+                rj = cc[idx[b]]
+                d = [float(ri[k]) - float(rj[k]) for k in range(3)]
+                for k in range(3):
+                    while d[k] >= radius:
+                        d[k] -= L
+                    while d[k] < -radius:
+                        d[k] += L
+                r2 = d[0] ** 2 + d[1] ** 2 + d[2] ** 2
+                if r2 < (0.5 * L) ** 2:
+                    bn = math.ceil(math.sqrt(r2) / dr)
+                    if 1 < bn <= maxbin:
+                        hist[bn - 1] += 2
+    return np.array(hist)
+
+
+@pytest.mark.parametrize("maxbin", [1000, 37])
+def test_rdf_histogram_oracle_matches_reference_loops(oracle, maxbin):
+    """The oracle's rdf histogram equals the reference's loops on unwrapped
+    frames, bin-edge distances and a ragged participant subset."""
+    rng = np.random.default_rng(maxbin)
+    L = 3.0
+    frames = rng.uniform(-2 * L, 3 * L, size=(2, 60, 3))
+    dr = L / maxbin
+    frames[0, 1] = frames[0, 0] + [dr * 7, 0.0, 0.0]       # on a bin edge
+    frames[0, 2] = frames[0, 0] + [0.5 * L, 0.0, 0.0]      # half the box
+    frames[1, 3] = frames[1, 4] + [0.0, 11 * dr, 0.0]
+    idx = np.concatenate([np.arange(0, 60, 2), [1, 3]])
+    ref = _rdf_loops(frames, idx, L, maxbin)
+    prev = oracle.lib().oracle_get_threads()
+    try:
+        for nt in (1, 4):
+            oracle.set_threads(nt)
+            assert np.array_equal(oracle.rdf_histogram(frames, idx, L, maxbin), ref)
+    finally:
+        oracle.set_threads(prev)

@@ -49,6 +49,12 @@
 // (L/2)^2 (relative to r^2) in which the FP32 estimate is not trusted; its
 // error is below 6 ulp = 3.6e-7
 #define RDF_MARGIN 2e-6f
+// Plain FP32 box-unit positions (no lo part) for maxbin up to this: each
+// component is then off by at most 3 * 2^-25 box (two roundings of u and one
+// of the difference), |dr| <= 1.6e-7 L, so q is off by <= 1.6e-7 maxbin, and
+// the band gets RDF_MARGIN_ABS * maxbin more; the half-box band doubles.
+#define RDF_PLAIN_MAXBIN 2048
+#define RDF_MARGIN_ABS 8e-7
 // |coordinate| / L from which a participant's pairs are all decided in FP64.
 // Below it the reference's rounding (the difference and up to 2 * 64 wrap
 // steps, each within half an ulp of 128 L) stays under 3e-12 L, far inside the
@@ -70,6 +76,7 @@ struct RdfArgs {
     float inv_dr;             // maxbin / L
     float q2scale;            // maxbin^2: (r / dr)^2 from r^2 in box units
     float hq2_lo, hq2_hi;     // (maxbin / 2)^2 band for the half-box test
+    float half_thr;           // 1/2 - the absolute part of the bin-edge band
     int maxbin;
     unsigned long long* counts;  // [maxbin] the reference's hist
     unsigned* status;
@@ -83,6 +90,7 @@ struct RdfPackArgs {
     double4_32a* raw;
     int64_t ncols, nidx, npad, nframes;
     double L, invL, far, limit;
+    int split;  // hi on the 2^-22 grid and a lo remainder; else plain FP32 u
     unsigned* status;
 };
 
@@ -115,7 +123,7 @@ __global__ void __launch_bounds__(256) k_rdf_pack(RdfPackArgs a)
             if (w < 0.0) w += a.L;
             if (w >= a.L) w -= a.L;
             const double u = w * a.invL;  // box units, [0, 1]
-            const double hq = rint(u * 4194304.0) * (1.0 / 4194304.0);  // the 2^-22 grid
+            const double hq = a.split ? rint(u * 4194304.0) * (1.0 / 4194304.0) : (double)(float)u;  // 2^-22 grid
             h[k] = (float)hq;
             l[k] = (float)(u - hq);
         }
@@ -137,10 +145,11 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
 }
 
 // The decision on one screened pair, without branches. decided: q^2 <= lo
-// (inside half the box) and |D| >= M (clear of a bin edge; D = q - nearest
-// integer, M = RDF_MARGIN q). A decided pair with q > 1 adds w to the shared
-// counter at `slot`. An undecided pair with q^2 < hi, or NaN (a far
-// participant), sets `bit` in amb. SELA: the add always runs, at `dummy` (a
+// (inside half the box) and |E| < T (clear of a bin edge: E = q - 1/2 -
+// floor(q), T = 1/2 - the margin; NaN, a self pair, counts as clear). A
+// decided pair with q > 1 adds w to the shared counter at `slot`, that of
+// bin ceil(q). An undecided pair with q^2 < hi, or NaN (a far participant),
+// sets `bit` in amb. SELA: the add always runs, at `dummy` (a
 // counter of this lane that is never read) for a pair not counted; otherwise
 // it is predicated.
 template <bool SELA>
@@ -154,7 +163,7 @@ __device__ __forceinline__ void rdf_decide(float Q2, float Q, float D, float M, 
             ".reg .f32 ad;\n\t"
             ".reg .u32 sa;\n\t"
             "abs.f32 ad, %3;\n\t"
-            "setp.ge.f32 pd, ad, %4;\n\t"
+            "setp.ltu.f32 pd, ad, %4;\n\t"
             "setp.le.and.f32 pd, %1, %5, pd;\n\t"
             "setp.gt.and.f32 pc, %2, 0f3F800000, pd;\n\t"
             "setp.ltu.and.f32 pa, %1, %6, !pd;\n\t"
@@ -170,7 +179,7 @@ __device__ __forceinline__ void rdf_decide(float Q2, float Q, float D, float M, 
             ".reg .pred pd, pc, pa;\n\t"
             ".reg .f32 ad;\n\t"
             "abs.f32 ad, %3;\n\t"
-            "setp.ge.f32 pd, ad, %4;\n\t"
+            "setp.ltu.f32 pd, ad, %4;\n\t"
             "setp.le.and.f32 pd, %1, %5, pd;\n\t"
             "setp.gt.and.f32 pc, %2, 0f3F800000, pd;\n\t"
             "setp.ltu.and.f32 pa, %1, %6, !pd;\n\t"
@@ -209,16 +218,17 @@ __device__ __forceinline__ int rdf_bin64(const RdfArgs& a, int64_t f, int64_t i,
 
 // TILE participants per tile (threads per block), UNROLL groups of 4 j in
 // flight, MINB blocks per SM for the register budget, SELA the form of the
-// counting add (rdf_decide). The undecided pairs of
+// counting add (rdf_decide), SPLIT hi/lo positions (else plain FP32). The undecided pairs of
 // an item are decided during the next item's pair loop (two queues in turn),
 // so their FP64 loads overlap the other warps' screening; the next item's
 // positions are loaded into registers during the current one.
-template <int TILE, int UNROLL, int MINB, bool SELA>
+template <int TILE, int UNROLL, int MINB, bool SELA, bool SPLIT>
 __global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
 {
     extern __shared__ unsigned rdf_hist[];  // [maxbin]
-    // the j tile: hi x, y, z, lo x, y, z, q^2 offset (0, or RDF_PAD past nidx)
-    __shared__ __align__(16) float sj[7][TILE];
+    // the j tile: hi x, y, z, (lo x, y, z,) q^2 offset (0, or RDF_PAD past nidx)
+    constexpr int NA = SPLIT ? 7 : 4;
+    __shared__ __align__(16) float sj[NA][TILE];
     __shared__ unsigned queue[2][RDF_QCAP];  // (i in tile) << 16 | (j in tile)
     __shared__ int qn[2];
     __shared__ long long qf[2], qib[2], qjb[2];  // a queue's frame and tile bases
@@ -227,14 +237,17 @@ __global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
     const int t = threadIdx.x;
     for (int b = t; b < a.maxbin; b += TILE) rdf_hist[b] = 0u;
     const float magic = 12582912.0f;  // 1.5 * 2^23: x + magic rounds x to an integer
-    const int magic_bits = __float_as_int(magic);
-    // shared address of counter ceil(q) - 1 = (bits(q + magic) - bits(magic)) - (q below its nearest integer)
-    const unsigned slot0 = (unsigned)__cvta_generic_to_shared(rdf_hist) - 4u * (unsigned)magic_bits;
+    // q + (2^23 - 1/2) rounds to 2^23 + floor(q) for q >= 1/2 off the integers:
+    // the counter of bin ceil(q) = floor(q) + 1 is at 4 bits(that) + slot0
+    const float fl_c = 8388607.5f;
+    const unsigned slot0 = (unsigned)__cvta_generic_to_shared(rdf_hist) - 4u * 0x4b000000u;
     const unsigned dummy = (unsigned)__cvta_generic_to_shared(dummies) + 4u * (unsigned)(t & 31);
     const float2 m1 = make_float2(-1.f, -1.f);
     const float2 mg = make_float2(magic, magic), mmg = make_float2(-magic, -magic);
+    const float2 fc = make_float2(fl_c, fl_c);
     const float2 c2 = make_float2(a.q2scale, a.q2scale);
-    const float2 marg = make_float2(RDF_MARGIN, RDF_MARGIN);
+    const float2 nmarg = make_float2(-RDF_MARGIN, -RDF_MARGIN);
+    const float2 hthr = make_float2(a.half_thr, a.half_thr);
     // item -> (frame, tile pair {ti, tj}), tj = ti + s (mod tiles): every unordered pair once
     auto decode = [&](int64_t item, int64_t& f, int64_t& ti, int64_t& tj, int64_t& s) {
         f = item / a.tile_pairs;
@@ -249,9 +262,11 @@ __global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
         int64_t f, ti, tj, s;
         decode(blockIdx.x, f, ti, tj, s);
         nh = a.hi[f * a.npad + tj * TILE + t];
-        nl = a.lo[f * a.npad + tj * TILE + t];
         ih = a.hi[f * a.npad + ti * TILE + t];
-        il = a.lo[f * a.npad + ti * TILE + t];
+        if (SPLIT) {
+            nl = a.lo[f * a.npad + tj * TILE + t];
+            il = a.lo[f * a.npad + ti * TILE + t];
+        }
     }
     int since_flush = 0, k = 0;
     for (int64_t item = blockIdx.x; item < a.items; item += gridDim.x, ++k) {
@@ -264,10 +279,12 @@ __global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
         sj[0][t] = nh.x;
         sj[1][t] = nh.y;
         sj[2][t] = nh.z;
-        sj[3][t] = nl.x;
-        sj[4][t] = nl.y;
-        sj[5][t] = nl.z;
-        sj[6][t] = (jb + t < a.nidx) ? 0.f : RDF_PAD;
+        if (SPLIT) {
+            sj[3][t] = nl.x;
+            sj[4][t] = nl.y;
+            sj[5][t] = nl.z;
+        }
+        sj[NA - 1][t] = (jb + t < a.nidx) ? 0.f : RDF_PAD;
         if (t == 0) {
             qn[buf] = 0;
             qf[buf] = f;
@@ -281,9 +298,11 @@ __global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
             int64_t f2, ti2, tj2, s2;
             decode(item + gridDim.x, f2, ti2, tj2, s2);
             nh = a.hi[f2 * a.npad + tj2 * TILE + t];
-            nl = a.lo[f2 * a.npad + tj2 * TILE + t];
             ih = a.hi[f2 * a.npad + ti2 * TILE + t];
-            il = a.lo[f2 * a.npad + ti2 * TILE + t];
+            if (SPLIT) {
+                nl = a.lo[f2 * a.npad + tj2 * TILE + t];
+                il = a.lo[f2 * a.npad + ti2 * TILE + t];
+            }
         }
         if (k > 0) {
             // the previous item's undecided pairs, in FP64
@@ -306,38 +325,38 @@ __global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
                 unsigned amb = 0u;
 #pragma unroll UNROLL
                 for (int g = 0; g < RDF_CHUNK; g += 4) {
-                    float4 J[7];
+                    float4 J[NA];
 #pragma unroll
-                    for (int m = 0; m < 7; ++m) J[m] = *reinterpret_cast<const float4*>(&sj[m][c + g]);
+                    for (int m = 0; m < NA; ++m) J[m] = *reinterpret_cast<const float4*>(&sj[m][c + g]);
 #pragma unroll
                     for (int half = 0; half < 2; ++half) {
-                        float2 v[7];
+                        float2 v[NA];
 #pragma unroll
-                        for (int m = 0; m < 7; ++m) v[m] = half ? make_float2(J[m].z, J[m].w) : make_float2(J[m].x, J[m].y);
-                        // hi and lo differences in box units, the image shift s = rint(dh)
+                        for (int m = 0; m < NA; ++m) v[m] = half ? make_float2(J[m].z, J[m].w) : make_float2(J[m].x, J[m].y);
+                        // differences in box units, the image shift s = rint(dh); dh - s is exact
                         const float2 dxh = __ffma2_rn(v[0], m1, hx), dyh = __ffma2_rn(v[1], m1, hy);
                         const float2 dzh = __ffma2_rn(v[2], m1, hz);
-                        const float2 dxl = __ffma2_rn(v[3], m1, lx), dyl = __ffma2_rn(v[4], m1, ly);
-                        const float2 dzl = __ffma2_rn(v[5], m1, lz);
                         const float2 sx = __fadd2_rn(__fadd2_rn(dxh, mg), mmg);
                         const float2 sy = __fadd2_rn(__fadd2_rn(dyh, mg), mmg);
                         const float2 sz = __fadd2_rn(__fadd2_rn(dzh, mg), mmg);
-                        // dh - s is exact (both on the grid); then the lo difference
-                        const float2 dx = __fadd2_rn(__ffma2_rn(sx, m1, dxh), dxl);
-                        const float2 dy = __fadd2_rn(__ffma2_rn(sy, m1, dyh), dyl);
-                        const float2 dz = __fadd2_rn(__ffma2_rn(sz, m1, dzh), dzl);
+                        float2 dx = __ffma2_rn(sx, m1, dxh), dy = __ffma2_rn(sy, m1, dyh), dz = __ffma2_rn(sz, m1, dzh);
+                        if (SPLIT) {  // the lo differences
+                            dx = __fadd2_rn(dx, __ffma2_rn(v[3], m1, lx));
+                            dy = __fadd2_rn(dy, __ffma2_rn(v[4], m1, ly));
+                            dz = __fadd2_rn(dz, __ffma2_rn(v[5], m1, lz));
+                        }
                         const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-                        const float2 q2 = __ffma2_rn(r2, c2, v[6]);  // (r / dr)^2, or past the band for padding
-                        // q = sqrt(q2); q2 = 0 (a self pair) gives NaN, which decides nothing
+                        const float2 q2 = __ffma2_rn(r2, c2, v[NA - 1]);  // (r / dr)^2, or past the band for padding
+                        // q = sqrt(q2); q2 = 0 (a self pair) gives NaN: clear, not counted
                         const float2 q = __fmul2_rn(q2, make_float2(rsqrt_ftz(q2.x), rsqrt_ftz(q2.y)));
-                        const float2 tq = __fadd2_rn(q, mg);
-                        const float2 dq = __ffma2_rn(__fadd2_rn(tq, mmg), m1, q);  // q - nearest integer
-                        const float2 mq = __fmul2_rn(q, marg);
-                        const unsigned sl0 = slot0 + 4u * (unsigned)__float_as_int(tq.x) - ((__float_as_uint(dq.x) >> 29) & 4u);
-                        const unsigned sl1 = slot0 + 4u * (unsigned)__float_as_int(tq.y) - ((__float_as_uint(dq.y) >> 29) & 4u);
+                        const float2 tq = __fadd2_rn(q, fc);                    // 2^23 + floor(q)
+                        const float2 e = __fadd2_rn(q, __ffma2_rn(tq, m1, fc));  // q - 1/2 - floor(q), exact
+                        const float2 thr = __ffma2_rn(q, nmarg, hthr);          // 1/2 - the band
+                        const unsigned sl0 = slot0 + 4u * __float_as_uint(tq.x);
+                        const unsigned sl1 = slot0 + 4u * __float_as_uint(tq.y);
                         const int p0 = g + 2 * half;
-                        rdf_decide<SELA>(q2.x, q.x, dq.x, mq.x, a.hq2_lo, a.hq2_hi, sl0, dummy, w, 1u << p0, amb);
-                        rdf_decide<SELA>(q2.y, q.y, dq.y, mq.y, a.hq2_lo, a.hq2_hi, sl1, dummy, w, 2u << p0, amb);
+                        rdf_decide<SELA>(q2.x, q.x, e.x, thr.x, a.hq2_lo, a.hq2_hi, sl0, dummy, w, 1u << p0, amb);
+                        rdf_decide<SELA>(q2.y, q.y, e.y, thr.y, a.hq2_lo, a.hq2_hi, sl1, dummy, w, 2u << p0, amb);
                     }
                 }
                 if (amb) {  // this chunk's undecided pairs, for the FP64 pass
@@ -392,18 +411,21 @@ __global__ void k_rdf_finish(const unsigned long long* counts, int maxbin, doubl
     if (b < maxbin) hist[b] = (double)counts[b];
 }
 
-// The instantiated forms of k_rdf_pairs; NBG_RDF_FORM=<index> picks one
-// (default 0, the fastest on the 4096-oxygen, 512-frame water trajectory:
-// 5.32 ms against 5.45-6.12 ms for the others).
+// The instantiated forms of k_rdf_pairs, each with plain positions (maxbin up
+// to RDF_PLAIN_MAXBIN) and split ones; NBG_RDF_FORM=<index> picks one
+// (default 0: 4.17 ms on the 4096-oxygen, 512-frame water trajectory against
+// 4.20-4.92 ms for the others).
 struct RdfForm {
-    void (*kernel)(RdfArgs);
+    void (*plain)(RdfArgs);
+    void (*split)(RdfArgs);
     int tile, unroll, minb;
 };
+#define RDF_FORM(T, U, M, S) {k_rdf_pairs<T, U, M, S, false>, k_rdf_pairs<T, U, M, S, true>, T, U, M}
 const RdfForm kRdfForms[] = {
-    {k_rdf_pairs<256, 8, 3, true>, 256, 8, 3},  {k_rdf_pairs<256, 8, 3, false>, 256, 8, 3},
-    {k_rdf_pairs<256, 8, 2, true>, 256, 8, 2},  {k_rdf_pairs<256, 4, 3, true>, 256, 4, 3},
-    {k_rdf_pairs<128, 8, 5, true>, 128, 8, 5},  {k_rdf_pairs<128, 8, 4, false>, 128, 8, 4},
+    RDF_FORM(256, 8, 3, true), RDF_FORM(256, 8, 3, false), RDF_FORM(256, 8, 2, true),
+    RDF_FORM(256, 8, 4, true), RDF_FORM(128, 8, 6, true), RDF_FORM(128, 8, 4, false),
 };
+#undef RDF_FORM
 const int kRdfFormCount = (int)(sizeof(kRdfForms) / sizeof(kRdfForms[0]));
 
 namespace {
@@ -529,18 +551,23 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
                 return NBG_ERR_CUDA;
             }
         cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, device);
-        for (const RdfForm& fm : kRdfForms)
-            cudaFuncSetAttribute(fm.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        for (const RdfForm& fm : kRdfForms) {
+            cudaFuncSetAttribute(fm.plain, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  RDF_MAXBIN * (int)sizeof(unsigned));
+            cudaFuncSetAttribute(fm.split, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 RDF_MAXBIN * (int)sizeof(unsigned));
+        }
         const char* env = std::getenv("NBG_RDF_FORM");
         S.form = env ? std::atoi(env) : 0;
         if (S.form < 0 || S.form >= kRdfFormCount) S.form = 0;
     }
     const RdfForm& form = kRdfForms[S.form];
+    const bool split = maxbin > RDF_PLAIN_MAXBIN;
+    void (*const pairs_kernel)(RdfArgs) = split ? form.split : form.plain;
     if (S.occ_maxbin != maxbin) {
         // a grid of all the blocks that fit at once with this histogram size
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, form.kernel, form.tile, maxbin * sizeof(unsigned));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pairs_kernel, form.tile, maxbin * sizeof(unsigned));
         S.pair_blocks = S.sms * std::max(per_sm, 1);
         S.occ_maxbin = maxbin;
     }
@@ -583,6 +610,7 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
         pa.L = L;
         pa.invL = 1.0 / L;
         pa.far = RDF_FAR_BOXES * L;
+        pa.split = split ? 1 : 0;
         pa.limit = 0.25 * MINIMAGE_MAX_ITERS * L;
         pa.status = S.status;
         const int64_t pack_threads = nframes * npad;
@@ -624,14 +652,16 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
 
         const double qmax = 0.5 * maxbin;  // q = r / dr at r = L / 2
         a.q2scale = (float)((double)maxbin * maxbin);
-        a.hq2_lo = (float)(qmax * qmax * (1.0 - RDF_MARGIN));
-        a.hq2_hi = (float)(qmax * qmax * (1.0 + RDF_MARGIN));
+        const double hband = split ? RDF_MARGIN : 2.0 * RDF_MARGIN;
+        a.hq2_lo = (float)(qmax * qmax * (1.0 - hband));
+        a.hq2_hi = (float)(qmax * qmax * (1.0 + hband));
+        a.half_thr = (float)(0.5 - (split ? 0.0 : RDF_MARGIN_ABS * maxbin));
         a.maxbin = maxbin;
         a.counts = S.counts;
         a.status = S.status;
         const int64_t blocks = std::min<int64_t>(a.items, S.pair_blocks);
         cudaEventRecord(S.ev[2], st);
-        form.kernel<<<(unsigned)blocks, form.tile, maxbin * sizeof(unsigned), st>>>(a);
+        pairs_kernel<<<(unsigned)blocks, form.tile, maxbin * sizeof(unsigned), st>>>(a);
         cudaEventRecord(S.ev[3], st);
     }
     k_rdf_finish<<<(maxbin + 255) / 256, 256, 0, st>>>(S.counts, maxbin, hist_d);

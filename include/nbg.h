@@ -375,13 +375,16 @@ NBG_API int nbg_ml_kernel_times(nbg_ctx* ctx, int32_t reps, double* ms);
    distance r, r^2 < (L/2)^2 and bin = ceil(r / (L / maxbin)) in 2..maxbin,
    hist[bin - 1] += 2: the reference's counts exactly (FP32 screening, FP64
    arithmetic of the reference for every pair near a bin edge). frames and
-   hist may be host or device memory of `device`; 1 <= maxbin <= 16384.
+   hist may be host or device memory of `device` (device frames are read on
+   the legacy default stream); 1 <= maxbin <= 16384.
    NBG_ERR_NONFINITE for a non-finite coordinate, NBG_ERR_RANGE for one more
    than 16384 boxes out. Context-free; calls are serialised. */
 NBG_API int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t ncols, const int32_t* idx,
                               int64_t nidx, double L, int32_t maxbin, int device, double* hist);
 /* Device time (ms, CUDA events on the launching stream) of the last
-   nbg_rdf_histogram call's kernels: [0] position split, [1] pair histogram. */
+   nbg_rdf_histogram call's kernels: [0] position split, [1] pair histogram.
+   For host frames, which go up in chunks with each chunk's kernels running
+   behind its copy, [0] is 0 and [1] spans the whole pipeline. */
 NBG_API int nbg_rdf_kernel_times(double* ms);
 
 #ifdef __cplusplus

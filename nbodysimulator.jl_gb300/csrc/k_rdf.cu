@@ -51,10 +51,11 @@
 #define RDF_MARGIN 2e-6f
 // Plain FP32 box-unit positions (no lo part) for maxbin up to this: each
 // component is then off by at most 3 * 2^-25 box (two roundings of u and one
-// of the difference), |dr| <= 1.6e-7 L, so q is off by <= 1.6e-7 maxbin, and
-// the band gets RDF_MARGIN_ABS * maxbin more; the half-box band doubles.
+// of the difference; the image shift is exact), |dr| <= sqrt(3) 3 2^-25 L =
+// 1.55e-7 L, so q is off by <= 1.55e-7 maxbin, and the band gets
+// RDF_MARGIN_ABS * maxbin more (2.6 times that); the half-box band doubles.
 #define RDF_PLAIN_MAXBIN 2048
-#define RDF_MARGIN_ABS 8e-7
+#define RDF_MARGIN_ABS 4e-7
 // |coordinate| / L from which a participant's pairs are all decided in FP64.
 // Below it the reference's rounding (the difference and up to 2 * 64 wrap
 // steps, each within half an ulp of 128 L) stays under 3e-12 L, far inside the
@@ -64,6 +65,10 @@
 #define RDF_FLUSH_ITEMS 8192
 // q^2 offset of a padding j (beyond any q^2 band)
 #define RDF_PAD 1e30f
+// host frames go up in at most this many chunks of at least RDF_CHUNK_BYTES,
+// each one's kernels starting when it has arrived
+#define RDF_MAX_CHUNKS 16
+#define RDF_CHUNK_BYTES (8u << 20)
 
 struct RdfArgs {
     const float4* hi;        // [nframes][npad] wrapped hi parts (x, y, z, 0)
@@ -71,6 +76,7 @@ struct RdfArgs {
     const double4_32a* raw;  // [nframes][npad] the unwrapped positions (x, y, z, 0)
     const double* thresh;    // [maxbin + 1]: bin > b <=> r^2 >= thresh[b]
     int64_t nidx, npad;
+    int64_t f0;  // first frame of this launch
     int64_t tiles, tile_pairs, items;
     double L, radius, half2;  // FP64 constants of the reference's formula
     float inv_dr;             // maxbin / L
@@ -88,7 +94,8 @@ struct RdfPackArgs {
     float4* hi;
     float4* lo;
     double4_32a* raw;
-    int64_t ncols, nidx, npad, nframes;
+    int64_t ncols, nidx, npad;
+    int64_t f0, nframes;  // the frames of this launch
     double L, invL, far, limit;
     int split;  // hi on the 2^-22 grid and a lo remainder; else plain FP32 u
     unsigned* status;
@@ -96,9 +103,10 @@ struct RdfPackArgs {
 
 __global__ void __launch_bounds__(256) k_rdf_pack(RdfPackArgs a)
 {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= a.nframes * a.npad) return;
-    const int64_t f = t / a.npad, s = t - f * a.npad;
+    const int64_t tl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (tl >= a.nframes * a.npad) return;
+    const int64_t fl = tl / a.npad, s = tl - fl * a.npad;
+    const int64_t f = a.f0 + fl, t = f * a.npad + s;
     float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
     double4_32a r = make_double4_32a(0.0, 0.0, 0.0, 0.0);
     if (s < a.nidx) {
@@ -123,15 +131,19 @@ __global__ void __launch_bounds__(256) k_rdf_pack(RdfPackArgs a)
             if (w < 0.0) w += a.L;
             if (w >= a.L) w -= a.L;
             const double u = w * a.invL;  // box units, [0, 1]
-            const double hq = a.split ? rint(u * 4194304.0) * (1.0 / 4194304.0) : (double)(float)u;  // 2^-22 grid
-            h[k] = (float)hq;
-            l[k] = (float)(u - hq);
+            if (a.split) {
+                const double hq = rint(u * 4194304.0) * (1.0 / 4194304.0);  // the 2^-22 grid
+                h[k] = (float)hq;
+                l[k] = (float)(u - hq);
+            } else {
+                h[k] = (float)u;
+            }
         }
         if (st) atomicOr(a.status, st);
         if (far || st) h[0] = __int_as_float(0x7fc00000);  // NaN: every pair of this one in FP64
     }
     a.hi[t] = make_float4(h[0], h[1], h[2], 0.f);
-    a.lo[t] = make_float4(l[0], l[1], l[2], 0.f);
+    if (a.split) a.lo[t] = make_float4(l[0], l[1], l[2], 0.f);
     a.raw[t] = r;
 }
 
@@ -250,8 +262,9 @@ __global__ void __launch_bounds__(TILE, MINB) k_rdf_pairs(RdfArgs a)
     const float2 hthr = make_float2(a.half_thr, a.half_thr);
     // item -> (frame, tile pair {ti, tj}), tj = ti + s (mod tiles): every unordered pair once
     auto decode = [&](int64_t item, int64_t& f, int64_t& ti, int64_t& tj, int64_t& s) {
-        f = item / a.tile_pairs;
-        const int64_t p = item - f * a.tile_pairs;
+        const int64_t fl = item / a.tile_pairs;
+        const int64_t p = item - fl * a.tile_pairs;
+        f = a.f0 + fl;
         s = p / a.tiles;
         ti = p - s * a.tiles;
         tj = ti + s;
@@ -448,6 +461,8 @@ struct RdfScratch {
     int thresh_maxbin = 0;
     unsigned* status = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // pack start/end, pairs start/end
+    cudaStream_t copy = nullptr, comp = nullptr;  // host frames: chunk uploads, and the kernels behind them
+    cudaEvent_t copied[RDF_MAX_CHUNKS] = {};      // chunk c is on the device
     double last_ms[2] = {0.0, 0.0};                             // the last call's pack, pairs
     int sms = 0;
     int form = 0;        // index into kRdfForms
@@ -462,6 +477,10 @@ void rdf_release(RdfScratch& s)
 {
     for (cudaEvent_t& e : s.ev)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t& e : s.copied)
+        if (e) cudaEventDestroy(e);
+    if (s.copy) cudaStreamDestroy(s.copy);
+    if (s.comp) cudaStreamDestroy(s.comp);
     cudaFree(s.frames);
     cudaFree(s.packed);
     cudaFree(s.idx);
@@ -545,11 +564,14 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
             rdf_release(S);
             return NBG_ERR_NOMEM;
         }
-        for (cudaEvent_t& e : S.ev)
-            if (cudaEventCreate(&e) != cudaSuccess) {
-                rdf_release(S);
-                return NBG_ERR_CUDA;
-            }
+        bool ok = cudaStreamCreateWithFlags(&S.copy, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&S.comp, cudaStreamNonBlocking) == cudaSuccess;
+        for (cudaEvent_t& e : S.ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+        for (cudaEvent_t& e : S.copied) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            rdf_release(S);
+            return NBG_ERR_CUDA;
+        }
         cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, device);
         for (const RdfForm& fm : kRdfForms) {
             cudaFuncSetAttribute(fm.plain, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -571,20 +593,38 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
         S.pair_blocks = S.sms * std::max(per_sm, 1);
         S.occ_maxbin = maxbin;
     }
-    cudaStream_t st = 0;
+    const bool work = nframes > 0 && nidx > 0;
+    // host frames: uploaded in chunks on S.copy, the kernels on S.comp behind
+    // them; device frames: the legacy default stream (ordered after the
+    // caller's work there)
+    const bool host_in = work && !is_device_pointer(frames);
+    cudaStream_t st = host_in ? S.comp : 0;
     const bool dev_out = is_device_pointer(hist);
     double* hist_d = dev_out ? hist : S.hist;
     cudaMemsetAsync(S.counts, 0, maxbin * sizeof(unsigned long long), st);
     cudaMemsetAsync(S.status, 0, sizeof(unsigned), st);
     const int64_t tiles = (nidx + form.tile - 1) / form.tile;
     const int64_t npad = tiles * form.tile;
-    if (nframes > 0 && nidx > 0) {
+    if (work) {
+        const size_t frame_doubles = (size_t)ncols * 3;
+        int64_t per_chunk = nframes;
+        if (host_in) {
+            const double bytes = (double)nframes * frame_doubles * sizeof(double);
+            const int64_t want = std::max<int64_t>(1, std::min<int64_t>(RDF_MAX_CHUNKS, (int64_t)(bytes / RDF_CHUNK_BYTES)));
+            per_chunk = (nframes + want - 1) / want;
+        }
+        const int64_t nchunks = (nframes + per_chunk - 1) / per_chunk;
         const double* frames_d = frames;
-        if (!is_device_pointer(frames)) {
-            const size_t n = (size_t)nframes * (size_t)ncols * 3;
-            if (!grow(S.frames, S.frames_cap, n)) return NBG_ERR_NOMEM;
-            if (cudaMemcpyAsync(S.frames, frames, n * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
-                return NBG_ERR_CUDA;
+        if (host_in) {
+            if (!grow(S.frames, S.frames_cap, (size_t)nframes * frame_doubles)) return NBG_ERR_NOMEM;
+            for (int64_t c = 0; c < nchunks; ++c) {
+                const int64_t f0 = c * per_chunk, fn = std::min(per_chunk, nframes - f0);
+                if (cudaMemcpyAsync(S.frames + f0 * frame_doubles, frames + f0 * frame_doubles,
+                                    (size_t)fn * frame_doubles * sizeof(double), cudaMemcpyHostToDevice,
+                                    S.copy) != cudaSuccess)
+                    return NBG_ERR_CUDA;
+                cudaEventRecord(S.copied[c], S.copy);
+            }
             frames_d = S.frames;
         }
         const size_t nslots = (size_t)nframes * (size_t)npad;
@@ -597,44 +637,6 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
                                 st) != cudaSuccess)
                 return NBG_ERR_CUDA;
         }
-        RdfPackArgs pa;
-        pa.frames = frames_d;
-        pa.idx = S.idx;
-        pa.hi = reinterpret_cast<float4*>(S.packed);
-        pa.lo = pa.hi + nslots;
-        pa.raw = S.packed + nslots;
-        pa.ncols = ncols;
-        pa.nidx = nidx;
-        pa.npad = npad;
-        pa.nframes = nframes;
-        pa.L = L;
-        pa.invL = 1.0 / L;
-        pa.far = RDF_FAR_BOXES * L;
-        pa.split = split ? 1 : 0;
-        pa.limit = 0.25 * MINIMAGE_MAX_ITERS * L;
-        pa.status = S.status;
-        const int64_t pack_threads = nframes * npad;
-        cudaEventRecord(S.ev[0], st);
-        k_rdf_pack<<<(unsigned)((pack_threads + 255) / 256), 256, 0, st>>>(pa);
-        cudaEventRecord(S.ev[1], st);
-        // invalid coordinates end the call here (their pairs would all take
-        // the FP64 path)
-        unsigned pst = 0;
-        if (cudaMemcpyAsync(&pst, S.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaStreamSynchronize(st) != cudaSuccess)
-            return NBG_ERR_CUDA;
-        if (pst & ST_NONFINITE) return NBG_ERR_NONFINITE;
-        if (pst & ST_RANGE) return NBG_ERR_RANGE;
-
-        RdfArgs a;
-        a.hi = pa.hi;
-        a.lo = pa.lo;
-        a.raw = pa.raw;
-        a.nidx = nidx;
-        a.npad = npad;
-        a.tiles = tiles;
-        a.tile_pairs = tiles * (tiles + 1) / 2;
-        a.items = nframes * a.tile_pairs;
         if (S.thresh_L != L || S.thresh_maxbin != maxbin) {
             const double dr = L / maxbin;  // pbc.L / maxbin
             std::vector<double> th(maxbin + 1);
@@ -644,12 +646,35 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
             S.thresh_L = L;
             S.thresh_maxbin = maxbin;
         }
+        RdfPackArgs pa;
+        pa.frames = frames_d;
+        pa.idx = S.idx;
+        pa.hi = reinterpret_cast<float4*>(S.packed);
+        pa.lo = pa.hi + nslots;
+        pa.raw = S.packed + nslots;
+        pa.ncols = ncols;
+        pa.nidx = nidx;
+        pa.npad = npad;
+        pa.L = L;
+        pa.invL = 1.0 / L;
+        pa.far = RDF_FAR_BOXES * L;
+        pa.split = split ? 1 : 0;
+        pa.limit = 0.25 * MINIMAGE_MAX_ITERS * L;
+        pa.status = S.status;
+
+        RdfArgs a;
+        a.hi = pa.hi;
+        a.lo = pa.lo;
+        a.raw = pa.raw;
         a.thresh = S.thresh;
+        a.nidx = nidx;
+        a.npad = npad;
+        a.tiles = tiles;
+        a.tile_pairs = tiles * (tiles + 1) / 2;
         a.L = L;
         a.radius = 0.5 * L;
         a.inv_dr = (float)(maxbin / L);
         a.half2 = (0.5 * L) * (0.5 * L);
-
         const double qmax = 0.5 * maxbin;  // q = r / dr at r = L / 2
         a.q2scale = (float)((double)maxbin * maxbin);
         const double hband = split ? RDF_MARGIN : 2.0 * RDF_MARGIN;
@@ -659,9 +684,32 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
         a.maxbin = maxbin;
         a.counts = S.counts;
         a.status = S.status;
-        const int64_t blocks = std::min<int64_t>(a.items, S.pair_blocks);
-        cudaEventRecord(S.ev[2], st);
-        pairs_kernel<<<(unsigned)blocks, form.tile, maxbin * sizeof(unsigned), st>>>(a);
+
+        for (int64_t c = 0; c < nchunks; ++c) {
+            const int64_t f0 = c * per_chunk, fn = std::min(per_chunk, nframes - f0);
+            if (host_in) cudaStreamWaitEvent(st, S.copied[c], 0);
+            if (c == 0) cudaEventRecord(S.ev[0], st);
+            pa.f0 = f0;
+            pa.nframes = fn;
+            const int64_t pack_threads = fn * npad;
+            k_rdf_pack<<<(unsigned)((pack_threads + 255) / 256), 256, 0, st>>>(pa);
+            if (!host_in) {
+                // device frames, one chunk: invalid coordinates end the call
+                // here (their pairs would all take the FP64 path)
+                cudaEventRecord(S.ev[1], st);
+                unsigned pst = 0;
+                if (cudaMemcpyAsync(&pst, S.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                    cudaStreamSynchronize(st) != cudaSuccess)
+                    return NBG_ERR_CUDA;
+                if (pst & ST_NONFINITE) return NBG_ERR_NONFINITE;
+                if (pst & ST_RANGE) return NBG_ERR_RANGE;
+                cudaEventRecord(S.ev[2], st);
+            }
+            a.f0 = f0;
+            a.items = fn * a.tile_pairs;
+            const int64_t blocks = std::min<int64_t>(a.items, S.pair_blocks);
+            pairs_kernel<<<(unsigned)blocks, form.tile, maxbin * sizeof(unsigned), st>>>(a);
+        }
         cudaEventRecord(S.ev[3], st);
     }
     k_rdf_finish<<<(maxbin + 255) / 256, 256, 0, st>>>(S.counts, maxbin, hist_d);
@@ -674,10 +722,14 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
         return NBG_ERR_CUDA;
     if (cudaGetLastError() != cudaSuccess) return NBG_ERR_CUDA;
     S.last_ms[0] = S.last_ms[1] = 0.0;
-    if (nframes > 0 && nidx > 0) {
+    if (work) {
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, S.ev[0], S.ev[1]) == cudaSuccess) S.last_ms[0] = ms;
-        if (cudaEventElapsedTime(&ms, S.ev[2], S.ev[3]) == cudaSuccess) S.last_ms[1] = ms;
+        if (host_in) {  // the pipelined chunks as a whole
+            if (cudaEventElapsedTime(&ms, S.ev[0], S.ev[3]) == cudaSuccess) S.last_ms[1] = ms;
+        } else {
+            if (cudaEventElapsedTime(&ms, S.ev[0], S.ev[1]) == cudaSuccess) S.last_ms[0] = ms;
+            if (cudaEventElapsedTime(&ms, S.ev[2], S.ev[3]) == cudaSuccess) S.last_ms[1] = ms;
+        }
     }
     if (status & ST_NONFINITE) return NBG_ERR_NONFINITE;
     if (status & ST_RANGE) return NBG_ERR_RANGE;

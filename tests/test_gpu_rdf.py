@@ -139,15 +139,18 @@ def test_rdf_device_buffers(gpu):
 
 def test_rdf_full_size_properties(gpu, oracle):
     """4096 oxygens of the 12,288-atom water box, 64 frames: additivity over
-    frames, invariance under a permutation of the participants, and two
-    frames against the oracle."""
+    frames, host (chunked upload) and device frames alike, invariance under a
+    permutation of the participants, and two frames against the oracle."""
     pos, _, L = nbg.workloads.spcfw_water_box(4096, seed=7)
     rng = np.random.default_rng(9)
     frames = pos[None] + rng.normal(scale=0.02, size=(64,) + pos.shape)
     idx = np.arange(0, pos.shape[0], 3)
-    full = _hist(frames, idx, L)
+    full = _hist(frames, idx, L)  # host frames: uploaded in chunks, each chunk's kernels behind its copy
     halves = _hist(frames[:32], idx, L) + _hist(frames[32:], idx, L)
     assert np.array_equal(full, halves)
+    torch = pytest.importorskip("torch")
+    dev = nbg._abi.rdf_histogram(torch.from_numpy(frames).cuda(), idx, L, 1000)  # device frames: one launch
+    assert np.array_equal(full, dev)
     assert np.array_equal(full, _hist(frames, rng.permutation(idx), L))
     assert full.sum() <= 64 * len(idx) * (len(idx) - 1)
     _check(oracle, frames[[0, 63]], idx, L)

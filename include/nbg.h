@@ -191,7 +191,9 @@ NBG_API int nbg_accel(nbg_ctx* ctx, double* dv, double* v, const double* u, doub
 
 /* Copy a state (3 x n doubles each, 3 x (n+1) with Nose-Hoover) to and from
    the device-resident state. For batches the replicas' columns are
-   concatenated in replica order. */
+   concatenated in replica order. A state set here restarts every schedule
+   that depends on past steps (list builds, the gravity sort), so runs from
+   the same state give the same bits. */
 NBG_API int nbg_set_state(nbg_ctx* ctx, const double* u, const double* v);
 NBG_API int nbg_get_state(nbg_ctx* ctx, double* u, double* v);
 
@@ -214,7 +216,9 @@ NBG_API int nbg_advance(nbg_ctx* ctx, double dt, int64_t nsteps);
  * (and at the end) copy the state into traj_u / traj_v (each of
  * (nsteps/save_every + 1) x 3 x n doubles, frame 0 = the initial state; either
  * may be NULL); download the final state into u, v. save_every <= 0 saves only
- * the first and last frames.
+ * the first and last frames. The steps write the frames into a device buffer
+ * (up to 1 GiB of them at a time), copied out once per such segment: saving
+ * every step costs about one small kernel per step, and no host round trip.
  */
 NBG_API int nbg_run(nbg_ctx* ctx, double* u, double* v, double dt, int64_t nsteps,
             int64_t save_every, double* traj_u, double* traj_v, nbg_run_stats* stats);

@@ -100,7 +100,8 @@ __device__ __forceinline__ void cl_join(float& h, float& e, int o, int width)
 template <int LPA>
 __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s, double* xb, double dt, int nsteps,
                                                               int rebuild_every, int per, int cap, int* lst_g,
-                                                              int* cnt_g, double* xref_g, int* since_g, int reuse)
+                                                              int* cnt_g, double* xref_g, int* since_g, int reuse,
+                                                              int64_t step0, int save)
 {
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
@@ -168,6 +169,10 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     // remote shared-memory access
     cl.sync();
 
+    // the frame sink (trajectory saving): state of time index step0 + st;
+    // its other fields are read at a save point
+    const int64_t sk_every = save && owner ? d.sink->every : 0;
+
     for (int st = 0; st <= nsteps; ++st) {
         // kick of the previous step with the forces its groups left in fsum
         if (owner && st > 0) {
@@ -177,6 +182,20 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
                 if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
                 v[k] = kick1(v[k], a[k], an, dt);
                 a[k] = an;
+            }
+            if (sk_every > 0 && (step0 + st) % sk_every == 0) {
+                const FrameSink* sk = d.sink;
+                const int64_t slot = (step0 + st) / sk_every - sk->first;
+                if (slot >= 0 && slot < sk->cap) {
+                    const size_t o = (size_t)slot * 3 * d.cols + 3 * (size_t)io;
+                    double* fx = sk->x;
+                    double* fv = sk->v;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        fx[o + k] = x[k];
+                        fv[o + k] = v[k];
+                    }
+                }
             }
         }
         if (st == nsteps) break;  // uniform: every thread leaves after the last kick
@@ -343,7 +362,8 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     if (rank == 0 && tid == 0) *since_g = since;
 }
 
-typedef void (*cluster_kernel_t)(Dev, StateView, double*, double, int, int, int, int, int*, int*, double*, int*, int);
+typedef void (*cluster_kernel_t)(Dev, StateView, double*, double, int, int, int, int, int*, int*, double*, int*, int, int64_t,
+                                 int);
 
 static cluster_kernel_t cluster_kernel(int lpa)
 {
@@ -409,7 +429,7 @@ bool cluster_plan(nbg_ctx* c)
     return false;
 }
 
-int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every)
+int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every, int64_t step0)
 {
     cluster_kernel_t k = cluster_kernel(c->cluster_lpa);
     cudaLaunchConfig_t cfg = {};
@@ -427,7 +447,8 @@ int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps,
     prof_begin(c);
     cudaError_t e = cudaLaunchKernelEx(&cfg, k, c->d, s, c->cluster_x, dt, (int)nsteps, rebuild_every,
                                        c->cluster_per, c->cluster_cap, c->cluster_lists, c->cluster_cnt,
-                                       c->cluster_xref, c->cluster_since, c->cluster_lists_valid ? 1 : 0);
+                                       c->cluster_xref, c->cluster_since, c->cluster_lists_valid ? 1 : 0, step0,
+                                       c->sink_on ? 1 : 0);
     prof_end(c);
     if (e != cudaSuccess) return cuda_fail(c, e, "k_cluster_vv launch");
     NBG_LAUNCH_CHECK(c, "k_cluster_vv");

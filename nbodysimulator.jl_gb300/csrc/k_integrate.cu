@@ -406,6 +406,32 @@ int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt)
     return NBG_OK;
 }
 
+// After the step with StepRef sr: when its new time index t is a save point
+// of the sink, copy the state (positions and velocities) into its slot.
+__global__ void k_save_frame(const FrameSink* sink, const double* x, const double* v, int64_t n3, StepRef sr)
+{
+    const int64_t every = sink->every;
+    if (every <= 0) return;
+    const int64_t t = (sr.base ? *sr.base : 0) + sr.off + 1;
+    if (t % every != 0) return;
+    const int64_t slot = t / every - sink->first;
+    if (slot < 0 || slot >= sink->cap) return;
+    double* fx = sink->x + slot * n3;
+    double* fv = sink->v + slot * n3;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
+        fx[i] = x[i];
+        fv[i] = v[i];
+    }
+}
+
+int launch_save_frame(nbg_ctx* c, const StateView& s, StepRef sr)
+{
+    const int64_t n3 = 3 * c->d.cols;
+    k_save_frame<<<grid_for(n3, 256), 256, 0, c->stream>>>(c->d.sink, s.x, s.v, n3, sr);
+    NBG_LAUNCH_CHECK(c, "k_save_frame");
+    return NBG_OK;
+}
+
 __global__ void k_step_advance(int64_t* step, int64_t by) { *step += by; }
 __global__ void k_set_step(int64_t* step, int64_t value) { *step = value; }
 

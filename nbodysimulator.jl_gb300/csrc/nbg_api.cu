@@ -430,6 +430,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     if ((st = dalloc(c, &D.rebuild_flag, 2 * (size_t)nrep))) return st;
     if ((st = dalloc(c, &D.build_count, 1))) return st;
     if ((st = dalloc(c, &D.step_dev, 1))) return st;
+    if ((st = dalloc(c, &D.sink, 1))) return st;  // zeroed: every = 0, nothing saved
     // slices of 256 atoms per replica (the last block adds them in order)
     D.red_slices = (int)std::min<int64_t>(512, std::max<int64_t>(1, (max_rep_n + 255) / 256));
     if ((st = dalloc(c, &D.red_partial, (size_t)nrep * D.red_slices))) return st;
@@ -612,6 +613,9 @@ static void release(nbg_ctx* c)
     prof_drain(c);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
+    if (c->frames) cudaFree(c->frames);
+    c->frames = nullptr;
+    c->frames_cap = 0;
     for (void* p : c->allocs) cudaFree(p);
     c->allocs.clear();
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -836,6 +840,10 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
     c->T_valid = false;
     c->steps_since_build = -1;
     c->cluster_lists_valid = false;
+    // the gravity sort schedule restarts too: runs from the same state give
+    // the same bits
+    c->grav_evals = 0;
+    c->grav_perm_valid = false;
     return NBG_OK;
 }
 
@@ -977,9 +985,9 @@ static int step_em(nbg_ctx* c, double dt, StepRef sr)
 
 static int step_any(nbg_ctx* c, double dt, StepRef sr)
 {
-    if (is_em(c)) return step_em(c, dt, sr);
-    if (c->baoab) return step_baoab(c, dt, sr);
-    return step_vv(c, dt, sr);
+    int st = is_em(c) ? step_em(c, dt, sr) : c->baoab ? step_baoab(c, dt, sr) : step_vv(c, dt, sr);
+    if (st == NBG_OK && c->sink_on) st = launch_save_frame(c, c->st, sr);
+    return st;
 }
 
 static int step_direct(nbg_ctx* c, double dt)
@@ -1048,6 +1056,7 @@ static int capture_graph(nbg_ctx* c, double dt)
         return cuda_fail(c, e, "graph instantiate");
     }
     c->graph_steps = G;
+    c->graph_sink = c->sink_on;
     c->graph_launches = c->launches - launches0;
     c->launches = launches0;
     c->graph_dt = dt;
@@ -1069,6 +1078,10 @@ static int replay_graph(nbg_ctx* c)
     }
     return NBG_OK;
 }
+
+// device bytes of trajectory frames (positions and velocities) nbg_run keeps
+// before copying them out
+#define RUN_FRAME_BYTES ((size_t)1 << 30)
 
 static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
 {
@@ -1121,7 +1134,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
             if (c->cluster_ok) {
                 // the whole chunk in one persistent cluster launch (its lists
                 // live in shared memory: the global ones are rebuilt later)
-                if ((st = launch_cluster_vv(c, c->st, dt, k - s, c->desc.rebuild_every))) break;
+                if ((st = launch_cluster_vv(c, c->st, dt, k - s, c->desc.rebuild_every, c->step))) break;
                 c->cluster_lists_valid = true;
                 c->step += k - s;
                 c->steps_since_build = -1;
@@ -1130,7 +1143,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
             }
             c->cluster_lists_valid = false;  // the graph or direct steps below move the state
             if (graphs && graph_aligned(c) && k - s >= graph_period(c)) {
-                if (!c->graph || c->graph_dt != dt) {
+                if (!c->graph || c->graph_dt != dt || c->graph_sink != c->sink_on) {
                     if ((st = capture_graph(c, dt))) break;
                 }
                 if (!counter_set) {
@@ -1203,19 +1216,56 @@ extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nste
     c->step = 0;
     if (c->path == PATH_LIST) CK(cudaMemcpyAsync(&builds0, c->d.build_count, 8, cudaMemcpyDeviceToHost, c->stream), "builds");
     size_t fb = state_bytes(c);
+    const int64_t n3 = 3 * c->cols;
     int64_t frame = 0;
     if (traj_u) memcpy(traj_u, u, fb);
     if (traj_v) memcpy(traj_v, v, fb);
     ++frame;
+    // frames at the multiples of save_every are written by the steps into a
+    // device buffer (up to RUN_FRAME_BYTES of them at a time) and copied out
+    // once per segment; a last partial interval ends with the final state
+    const bool traj = traj_u || traj_v;
+    const int64_t aligned = traj && save_every > 0 ? nsteps / save_every : 0;
+    int64_t cap = 0;
+    if (aligned > 0) {
+        cap = std::max<int64_t>(1, std::min<int64_t>(aligned, (int64_t)(RUN_FRAME_BYTES / (2 * fb))));
+        if (c->frames_cap < cap) {
+            if (c->frames) cudaFree(c->frames);
+            c->frames = nullptr;
+            c->frames_cap = 0;
+            cudaError_t e = cudaMalloc(&c->frames, 2 * (size_t)cap * fb);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                c->frames = nullptr;
+                return fail(c, NBG_ERR_NOMEM, "trajectory frames: cudaMalloc failed");
+            }
+            c->frames_cap = cap;
+        }
+    }
     int64_t done = 0;
     while (done < nsteps) {
-        int64_t k = save_every > 0 ? std::min<int64_t>(save_every, nsteps - done) : nsteps - done;
-        if ((st = advance_impl(c, dt, k))) return st;
-        done += k;
-        if (traj_u || traj_v) {
-            if (traj_u) CK(cudaMemcpyAsync(traj_u + frame * 3 * c->cols, c->st.x, fb, cudaMemcpyDeviceToHost, c->stream), "traj");
-            if (traj_v) CK(cudaMemcpyAsync(traj_v + frame * 3 * c->cols, c->st.v, fb, cudaMemcpyDeviceToHost, c->stream), "traj");
-            ++frame;
+        if (done / std::max<int64_t>(save_every, 1) < aligned) {
+            const int64_t j0 = done / save_every + 1;  // the segment's first frame
+            const int64_t nf = std::min<int64_t>(cap, aligned - (j0 - 1));
+            const FrameSink h{c->frames, c->frames + (size_t)c->frames_cap * n3, save_every, j0, nf};
+            CK(cudaMemcpy(c->d.sink, &h, sizeof h, cudaMemcpyHostToDevice), "frame sink");
+            c->sink_on = true;
+            st = advance_impl(c, dt, nf * save_every);
+            c->sink_on = false;
+            if (st) return st;
+            if (traj_u) CK(cudaMemcpyAsync(traj_u + j0 * n3, h.x, nf * fb, cudaMemcpyDeviceToHost, c->stream), "traj");
+            if (traj_v) CK(cudaMemcpyAsync(traj_v + j0 * n3, h.v, nf * fb, cudaMemcpyDeviceToHost, c->stream), "traj");
+            done += nf * save_every;
+            frame = j0 + nf;
+        } else {
+            const int64_t k = nsteps - done;
+            if ((st = advance_impl(c, dt, k))) return st;
+            done += k;
+            if (traj) {
+                if (traj_u) CK(cudaMemcpyAsync(traj_u + frame * n3, c->st.x, fb, cudaMemcpyDeviceToHost, c->stream), "traj");
+                if (traj_v) CK(cudaMemcpyAsync(traj_v + frame * n3, c->st.v, fb, cudaMemcpyDeviceToHost, c->stream), "traj");
+                ++frame;
+            }
         }
     }
     CK(cudaMemcpyAsync(u, c->st.x, fb, cudaMemcpyDeviceToHost, c->stream), "u download");

@@ -64,6 +64,15 @@ struct RepDev {
 };
 
 // Everything a kernel needs, passed by value.
+// Where the step loop leaves saved frames (device memory): the state after
+// step t goes to slot t / every - first when t is a multiple of every and the
+// slot is below cap. every = 0: nothing is saved.
+struct FrameSink {
+    double* x;  // [cap][3 cols] positions
+    double* v;  // [cap][3 cols] velocities
+    int64_t every, first, cap;
+};
+
 struct Dev {
     int64_t n;          // atoms (all replicas)
     int64_t cols;       // state columns (n, +1 with Nose-Hoover)
@@ -105,6 +114,7 @@ struct Dev {
     unsigned long long* build_count;
     unsigned* status;
     int64_t* step_dev;          // step counter read by graph-captured kernels
+    FrameSink* sink;            // trajectory frames kept on the device (nbg_run)
     // reductions
     double* red_partial;
     double* red_T;      // per replica temperature of the current velocities
@@ -203,7 +213,12 @@ struct nbg_ctx {
     int64_t graph_steps = 0;     // steps per replay
     int64_t graph_launches = 0;  // kernels per replay
     double graph_dt = 0.0;
+    bool graph_sink = false;     // the captured steps save frames
     bool use_graphs = true;
+    // trajectory frames on the device: the steps save them while sink_on
+    bool sink_on = false;
+    double* frames = nullptr;    // [2][frames_cap][3 cols]: positions, then velocities
+    int64_t frames_cap = 0;
     bool baoab = false;          // Langevin by BAOAB instead of Euler-Maruyama
     double baoab_dt = -1.0;      // dt of the BAOAB coefficients in the replica table
     // temperature folded into the kick (single system, Berendsen / Nose-Hoover)
@@ -260,7 +275,8 @@ struct StepRef {
 int launch_pack(nbg_ctx* c, const StateView& s);
 int launch_gravity(nbg_ctx* c, const StateView& s);
 bool cluster_plan(nbg_ctx* c);
-int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every);
+// step0: the time index of the state at the launch (for the frame sink)
+int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every, int64_t step0);
 int launch_allpairs(nbg_ctx* c, const StateView& s);
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
 int launch_force_list(nbg_ctx* c, const StateView& s);
@@ -274,6 +290,7 @@ int launch_step_advance(nbg_ctx* c, int64_t by);
 int launch_baoab_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt);
 int launch_set_step(nbg_ctx* c, int64_t value);
+int launch_save_frame(nbg_ctx* c, const StateView& s, StepRef sr);
 int launch_rhs_thermostat(nbg_ctx* c, const StateView& s);
 int gravity_plan_chunks(nbg_ctx* c, int64_t npad);
 size_t gravity_sort_bytes(int64_t n);

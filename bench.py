@@ -630,6 +630,8 @@ def main():
     ap.add_argument("--no-flush", action="store_true", help="time all steps back to back (no L2 flush)")
     ap.add_argument("--ref-sample", type=int, default=2048)
     ap.add_argument("--ref-frames", type=int, default=16, help="rdf: whole frames per reference step")
+    ap.add_argument("--save-every", type=int, default=0,
+                    help="also time nbg_run with trajectory frames every N steps (single systems)")
     ap.add_argument("--n", type=int, default=None, help="gravity body count (smaller profiling captures)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--grav-plain", action="store_true", help="gravity with plain FP32 positions")
@@ -776,6 +778,21 @@ def main():
                "path": "nbg_run: host state uploaded, K steps, host state downloaded", "steps": args.steps}
 
     u_end, v_end = eng.get_state()
+    traj = None
+    if args.save_every > 0 and not batch:
+        # run_simulation's frames (nbg_run from host buffers): saved every
+        # save_every steps, against the same run without frames
+        traj_steps = max(args.save_every, min(args.steps, 1000))
+        eng.run(u0, v0, dt, 20, 0, save_trajectory=False)
+        t0 = time.perf_counter()
+        eng.run(u0, v0, dt, traj_steps, 0, save_trajectory=False)
+        t_none = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        _, _, tu, _, _ = eng.run(u0, v0, dt, traj_steps, args.save_every)
+        t_frames = time.perf_counter() - t0
+        traj = {"save_every": args.save_every, "steps": traj_steps, "frames": len(tu),
+                "us_per_step": 1e6 * t_frames / traj_steps, "us_per_step_no_frames": 1e6 * t_none / traj_steps,
+                "path": "nbg_run from host buffers, positions and velocities saved (run_simulation)"}
     work, unit, bound = algorithmic_work(args.workload, n, eng)
     avg_kern = kern_ms / max(kern_n, 1)
     if cluster is not None:
@@ -814,6 +831,8 @@ def main():
             "dtype": "f32 pair forces, f64 state" + ("+bonded" if args.workload == "water" else ""),
             "data": "synthetic (seeded generator, no dataset)", "config": config,
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+    if traj is not None:
+        line["trajectory"] = traj
     if not batch:
         e_end = eng.energy(u_end, v_end)
         drift_key = "gravity" if args.workload == "gravity" else "potential"

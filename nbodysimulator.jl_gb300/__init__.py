@@ -30,6 +30,8 @@ from .simulation import (BAOAB, EM, NBodySimulation, SecondOrderODEProblem,
                          system_descriptor, temperature, total_energy, kb_SI)
 from .systems import (ChargedParticles, GravitationalSystem,
                       PotentialNBodySystem, WaterSPCFw)
+from .pdb import (extract_from_pdb, load_water_molecules_from_pdb,
+                  save_to_pdb, write_pdb_data)
 from . import workloads
 
 __all__ = [n for n in dir() if not n.startswith("_")]

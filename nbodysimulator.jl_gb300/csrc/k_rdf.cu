@@ -614,35 +614,45 @@ extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t 
             per_chunk = (nframes + want - 1) / want;
         }
         const int64_t nchunks = (nframes + per_chunk - 1) / per_chunk;
+        const size_t nslots = (size_t)nframes * (size_t)npad;
+        // every allocation before the first asynchronous copy from the
+        // caller's frames, so that no early return leaves one in flight
+        if (!grow(S.packed, S.packed_cap, 2 * nslots)) return NBG_ERR_NOMEM;
+        if (S.idx_cap < (size_t)nidx) {
+            S.idx_host.clear();  // a new buffer: upload the columns again
+            if (!grow(S.idx, S.idx_cap, (size_t)nidx)) return NBG_ERR_NOMEM;
+        }
+        if (host_in && !grow(S.frames, S.frames_cap, (size_t)nframes * frame_doubles)) return NBG_ERR_NOMEM;
+        // an error after the uploads started waits for them before returning
+        auto bail = [&](int code) {
+            if (host_in) cudaStreamSynchronize(S.copy);
+            return code;
+        };
         const double* frames_d = frames;
         if (host_in) {
-            if (!grow(S.frames, S.frames_cap, (size_t)nframes * frame_doubles)) return NBG_ERR_NOMEM;
             for (int64_t c = 0; c < nchunks; ++c) {
                 const int64_t f0 = c * per_chunk, fn = std::min(per_chunk, nframes - f0);
                 if (cudaMemcpyAsync(S.frames + f0 * frame_doubles, frames + f0 * frame_doubles,
                                     (size_t)fn * frame_doubles * sizeof(double), cudaMemcpyHostToDevice,
                                     S.copy) != cudaSuccess)
-                    return NBG_ERR_CUDA;
+                    return bail(NBG_ERR_CUDA);
                 cudaEventRecord(S.copied[c], S.copy);
             }
             frames_d = S.frames;
         }
-        const size_t nslots = (size_t)nframes * (size_t)npad;
-        if (!grow(S.packed, S.packed_cap, 2 * nslots)) return NBG_ERR_NOMEM;
         if (S.idx_host.size() != (size_t)nidx ||
             std::memcmp(S.idx_host.data(), idx, (size_t)nidx * sizeof(int32_t)) != 0) {
-            if (!grow(S.idx, S.idx_cap, (size_t)nidx)) return NBG_ERR_NOMEM;
             S.idx_host.assign(idx, idx + nidx);
             if (cudaMemcpyAsync(S.idx, S.idx_host.data(), (size_t)nidx * sizeof(int32_t), cudaMemcpyHostToDevice,
                                 st) != cudaSuccess)
-                return NBG_ERR_CUDA;
+                return bail(NBG_ERR_CUDA);
         }
         if (S.thresh_L != L || S.thresh_maxbin != maxbin) {
             const double dr = L / maxbin;  // pbc.L / maxbin
             std::vector<double> th(maxbin + 1);
             for (int b = 0; b <= maxbin; ++b) th[b] = rdf_threshold(dr, b);
             if (cudaMemcpy(S.thresh, th.data(), th.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
-                return NBG_ERR_CUDA;
+                return bail(NBG_ERR_CUDA);
             S.thresh_L = L;
             S.thresh_maxbin = maxbin;
         }

@@ -612,9 +612,13 @@ def run_rdf(args, rank, world):
         line["parity_two_frames_exact"] = bool(np.array_equal(gsub, oracle.rdf_histogram(frames[pick], idx, L,
                                                                                           maxbin)))
         rate, done, el = rdf_cpu_rate(oracle, frames, idx, L, maxbin, 10.0)
+        oracle.set_threads(1)
+        rate1, done1, el1 = rdf_cpu_rate(oracle, frames, idx, L, maxbin, 3.0)
+        oracle.set_threads(cores)
         line["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "cores": cores, "kind": "port",
                                 "sample": f"{done} whole frames ({len(idx)} oxygens each) in {el:.1f} s: the FP64 "
-                                          "restatement of the reference rdf's loops"}
+                                          "restatement of the reference rdf's loops",
+                                "value_1thread": rate1, "sample_1thread": f"{done1} whole frames on 1 thread"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

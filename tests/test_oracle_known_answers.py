@@ -170,3 +170,48 @@ def test_rdf_histogram_oracle_matches_reference_loops(oracle, maxbin):
             assert np.array_equal(oracle.rdf_histogram(frames, idx, L, maxbin), ref)
     finally:
         oracle.set_threads(prev)
+
+
+def test_charge_orbit_closure(oracle):
+    """electrostatics_test.jl:7-40: a light negative charge on a circular
+    orbit around a heavy positive one returns to its start after one period,
+    within 0.1 r (the reference integrates with its default adaptive method;
+    velocity Verlet at T / 2000 here)."""
+    k, r, q1, q2, m1, m2 = 9.0e9, 100.0, 1.0e-3, -1.0e-3, 100.0, 0.1
+    v2 = math.sqrt(abs(k * q1 * q2 / m2 / r))
+    period = 2 * math.pi * r / v2
+    p1 = nbg.ChargedParticle((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), m1, q1)
+    p2 = nbg.ChargedParticle((r, 0.0, 0.0), (0.0, v2, 0.0), m2, q2)
+    sim = nbg.NBodySimulation(nbg.ChargedParticles([p1, p2], k), (0.0, period))
+    desc, keep, u0, v0, u, v = _run(oracle, sim, period / 2000, 2000)
+    assert np.abs(u - u0).max() <= 0.1 * r
+
+
+def test_five_body_choreography_closure(oracle):
+    """gravitational_test.jl:72-101: the 5-body choreography returns to its
+    start after t = 2 pi within 0.01 (the reference integrates with Tsit5 at
+    1e-10 tolerances; velocity Verlet at 2 pi / 200000 here: the six-digit
+    initial conditions leave ~0.005 at t = 2 pi for any fine step)."""
+    rs = [(1.657666, 0.0, 0.0), (0.439775, -0.169717, 0.0), (-1.268608, -0.267651, 0.0),
+          (-1.268608, 0.267651, 0.0), (0.439775, 0.169717, 0.0)]
+    vs = [(0.0, -0.593786, 0.0), (1.822785, 0.128248, 0.0), (1.271564, 0.168645, 0.0),
+          (-1.271564, 0.168645, 0.0), (-1.822785, 0.128248, 0.0)]
+    bodies = [nbg.MassBody(r, v, 1.0) for r, v in zip(rs, vs)]
+    sim = nbg.NBodySimulation(nbg.GravitationalSystem(bodies, 1.0), (0.0, 2 * math.pi))
+    desc, keep, u0, v0, u, v = _run(oracle, sim, 2 * math.pi / 200000, 200000)
+    assert np.abs(u - u0).max() <= 0.01
+
+
+def test_repelling_magnetic_dipoles(oracle):
+    """magnetostaic_test.jl:5-32: two parallel dipoles 1 cm apart, 100 VV
+    steps of 0.01 s: the speed from energy conservation within 1e-3."""
+    d1, m1, rho, M, mu_4pi = 0.01, 5.0e-6, 7800.0, 1.2e6, 1.0e-7
+    mm = (0.0, 0.0, M * m1 / rho)
+    p1 = nbg.MagneticParticle((-d1 / 2, 0.0, 0.0), (0.0, 0.0, 0.0), m1, mm)
+    p2 = nbg.MagneticParticle((d1 / 2, 0.0, 0.0), (0.0, 0.0, 0.0), m1, mm)
+    system = nbg.PotentialNBodySystem([p1, p2], {"magnetostatic": nbg.MagnetostaticParameters(mu_4pi)})
+    sim = nbg.NBodySimulation(system, (0.0, 1.0))
+    desc, keep, u0, v0, u, v = _run(oracle, sim, 0.01, 100)
+    d2 = np.linalg.norm(u[1] - u[0])
+    v_expected = math.sqrt(mu_4pi * (np.dot(mm, mm) * (1 / d1 ** 3 - 1 / d2 ** 3)) / m1)
+    assert abs(np.linalg.norm(v[1]) - v_expected) <= 0.001

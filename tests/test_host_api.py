@@ -141,3 +141,32 @@ def test_library_exports_every_header_symbol():
     loaded = nbg.load_library()
     assert loaded.nbg_abi_version() == nbg._abi.NBG_ABI_VERSION
     assert b"sm_103a" in loaded.nbg_version()
+
+
+def test_result_analysis_at_saved_times():
+    """gravitational_test.jl:26-41: get_position / get_velocity of body 1 at
+    the first saved time are its initial values exactly, get_masses the
+    bodies' masses; and electrostatics_test.jl:31-39: the charges and masses
+    the descriptor carries (obtain_data_for_electrostatic_interaction). The
+    result here is hand-made, so no kernel runs."""
+    sim = S.figure8()
+    u0, v0 = S.state(sim)
+    res = nbg.SimulationResult(nbg.simulation.Solution([0.0, 1.0], [u0, u0 + 0.5], [v0, v0 - 0.5], 1), sim)
+    r1 = nbg.get_position(res, 0.0, 1)
+    v1 = nbg.get_velocity(res, 0.0, 1)
+    for i, (r, v) in enumerate(zip((-0.995492, 0.0, 0.0), (-0.347902, -0.53393, 0.0))):
+        assert r1[i] == r and v1[i] == v
+    assert list(nbg.get_masses(sim.system)) == [1.0, 1.0, 1.0]
+    assert np.array_equal(nbg.get_position(res, 1.0, 2), u0[1] + 0.5)
+    assert np.array_equal(nbg.get_position(res, 1.0), (u0 + 0.5).T)
+
+    k, q1, q2, m1, m2 = 9.0e9, 1.0e-3, -1.0e-3, 100.0, 0.1
+    p1 = nbg.ChargedParticle((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), m1, q1)
+    p2 = nbg.ChargedParticle((100.0, 0.0, 0.0), (0.0, 1.0, 0.0), m2, q2)
+    sim = nbg.NBodySimulation(nbg.ChargedParticles([p1, p2], k), (0.0, 1.0))
+    desc, keep = nbg.system_descriptor(sim)
+    qs = np.ctypeslib.as_array(desc.charge, shape=(2,))
+    ms = np.ctypeslib.as_array(desc.mass, shape=(2,))
+    assert qs[0] == q1 and qs[1] == q2
+    assert ms[0] == m1 and ms[1] == m2
+    assert desc.el_k == k

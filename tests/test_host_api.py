@@ -170,3 +170,29 @@ def test_result_analysis_at_saved_times():
     assert qs[0] == q1 and qs[1] == q2
     assert ms[0] == m1 and ms[1] == m2
     assert desc.el_k == k
+
+
+def test_rdf_histogram_argument_checks():
+    """nbg_rdf_histogram refuses bad arguments before any device work
+    (NBG_ERR_ARG = -1): bin counts outside 1..16384, a column outside the
+    frame, a non-positive or non-finite box, missing buffers."""
+    lib = nbg.load_library()
+    frames = np.zeros((2, 10, 3))
+    hist = np.zeros(16385)
+    idx = np.arange(10, dtype=np.int32)
+    ip = idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+    def call(idx_p=ip, nidx=10, L=2.0, maxbin=100, fr=frames.ctypes.data, out=hist.ctypes.data):
+        return lib.nbg_rdf_histogram(fr, 2, 10, idx_p, nidx, L, maxbin, 0, out)
+
+    assert call(maxbin=0) == -1
+    assert call(maxbin=16385) == -1
+    assert call(L=0.0) == -1 and call(L=-1.0) == -1 and call(L=float("inf")) == -1
+    bad = np.array([0, 10], dtype=np.int32)
+    assert call(idx_p=bad.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), nidx=2) == -1
+    neg = np.array([-1], dtype=np.int32)
+    assert call(idx_p=neg.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), nidx=1) == -1
+    assert call(out=None) == -1
+    assert call(fr=None) == -1
+    assert call(idx_p=None) == -1
+    assert lib.nbg_rdf_kernel_times(None) == -1

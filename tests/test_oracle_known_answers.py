@@ -215,3 +215,95 @@ def test_repelling_magnetic_dipoles(oracle):
     d2 = np.linalg.norm(u[1] - u[0])
     v_expected = math.sqrt(mu_4pi * (np.dot(mm, mm) * (1 / d1 ** 3 - 1 / d2 ** 3)) / m1)
     assert abs(np.linalg.norm(v[1]) - v_expected) <= 0.001
+
+
+def _ref_energies(sim, u, v):
+    """The reference's energy loops (nbody_simulation_result.jl:209-212,
+    281-397) in plain Python: kinetic sum(m v^2 / 2); LJ 4 eps sum_{i<j}
+    (s12 - s6) with r^2 clamped to R^2 beyond the cutoff; electrostatics
+    k sum_{i<j, not excluded} q_i q_j / r (or / R beyond); bonds sum k d^2 / 4
+    over both ends; angles sum k (theta - theta0)^2 / 2."""
+    sysm = sim.system
+    bc = sim.boundary_conditions
+    L = bc.L if isinstance(bc, nbg.CubicPeriodicBoundaryConditions) else None
+
+    def dist2(i, j):
+        d = [float(u[i][k]) - float(u[j][k]) for k in range(3)]
+        if L is not None:
+            for k in range(3):
+                while d[k] >= 0.5 * L:
+                    d[k] -= L
+                while d[k] < -0.5 * L:
+                    d[k] += L
+        return d[0] ** 2 + d[1] ** 2 + d[2] ** 2
+
+    ms = nbg.get_masses(sysm)
+    out = {"kinetic": sum(float(np.dot(v[i], v[i])) * (ms[i] / 2) for i in range(len(ms)))}
+    water = isinstance(sysm, nbg.WaterSPCFw)
+    if water:
+        lj, el = sysm.lj_parameters, sysm.e_parameters
+        n = 3 * len(sysm.bodies)
+        lj_idx = list(range(0, n, 3))
+        qs = [sysm.qO, sysm.qH, sysm.qH] * len(sysm.bodies)
+        excluded = lambda i, j: i // 3 == j // 3
+    else:
+        lj = sysm.potentials.get("lennard_jones")
+        el = sysm.potentials.get("electrostatic")
+        n = len(sysm.bodies)
+        lj_idx = list(range(n))
+        qs = [getattr(b, "q", 0.0) for b in sysm.bodies]
+        excluded = lambda i, j: i == j
+    e = 0
+    if lj is not None:
+        for a in range(len(lj_idx)):
+            for b in range(a + 1, len(lj_idx)):
+                r2 = dist2(lj_idx[a], lj_idx[b])
+                if not r2 < lj.R2:
+                    r2 = lj.R2
+                s6 = (lj.sigma2 / r2) ** 3
+                e += s6 ** 2 - s6
+        out["lennard_jones"] = 4 * lj.eps * e
+    if el is not None:
+        e_el = 0.0
+        for i in range(n):
+            e_i = 0.0
+            for j in range(i + 1, n):
+                if not excluded(i, j):
+                    r2 = dist2(i, j)
+                    e_i += qs[j] / math.sqrt(r2) if r2 < el.R2 else qs[j] / el.R
+            e_el += e_i * qs[i]
+        out["electrostatic"] = e_el * el.k
+    if water:
+        p = sysm.scpfw_parameters
+        eb, ea = 0, 0
+        for m in range(len(sysm.bodies)):
+            o, h1, h2 = 3 * m, 3 * m + 1, 3 * m + 2
+            for a, b in ((o, h1), (o, h2), (h1, o), (h2, o)):
+                eb += (float(np.linalg.norm(u[a] - u[b])) - p.rOH) ** 2 * p.kb
+            ba, bc_ = u[h1] - u[o], u[h2] - u[o]
+            ang = math.acos(float(np.dot(ba, bc_)) / (float(np.linalg.norm(ba)) * float(np.linalg.norm(bc_))))
+            ea += p.ka * (ang - p.aHOH) ** 2
+        out["bonds"], out["angles"] = eb / 4, ea / 2
+    return out
+
+
+@pytest.mark.parametrize("which", ["lj", "charges", "water"])
+def test_oracle_energies_match_reference_loops(oracle, which):
+    """Each energy term of the oracle against a plain restatement of the
+    reference's loops, on a thermalised LJ liquid (pairs beyond the cutoff
+    clamped), eight charges with a cutoff, and three water molecules."""
+    if which == "lj":
+        sim = S.lj_liquid(64, seed=5, jitter=0.05)
+    elif which == "charges":
+        sim, _ = S.charges8()
+    else:
+        sim, _, _ = S.water3()
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    rng = np.random.default_rng(6)
+    u = u0 + rng.normal(scale=0.01, size=u0.shape) * (0.02 if which == "water" else 1.0)
+    v = v0 + rng.normal(scale=0.1, size=v0.shape)
+    got = oracle.energy(desc, u, v)
+    ref = _ref_energies(sim, u, v)
+    for key, val in ref.items():
+        assert got[key] == pytest.approx(val, rel=1e-12, abs=1e-12 * (abs(val) + 1e-300)), key

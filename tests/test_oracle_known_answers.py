@@ -307,3 +307,127 @@ def test_oracle_energies_match_reference_loops(oracle, which):
     ref = _ref_energies(sim, u, v)
     for key, val in ref.items():
         assert got[key] == pytest.approx(val, rel=1e-12, abs=1e-12 * (abs(val) + 1e-300)), key
+
+
+def _ref_accel(sim, u):
+    """The reference's acceleration functions (basic_potentials.jl:240-433)
+    in plain Python, summed per atom as soode_system! does for an NVE system
+    (nbody_to_ode.jl:471-536): LJ over the LJ participants, electrostatics
+    outside the exclusions, gravity, magnetic dipoles, and for water the
+    bonds and the H-O-H angle."""
+    sysm = sim.system
+    bc = sim.boundary_conditions
+    L = bc.L if isinstance(bc, nbg.CubicPeriodicBoundaryConditions) else None
+
+    def rij(i, j):
+        d = [float(u[i][k]) - float(u[j][k]) for k in range(3)]
+        if L is not None:
+            for k in range(3):
+                while d[k] >= 0.5 * L:
+                    d[k] -= L
+                while d[k] < -0.5 * L:
+                    d[k] += L
+        return np.array(d), d[0] ** 2 + d[1] ** 2 + d[2] ** 2
+
+    water = isinstance(sysm, nbg.WaterSPCFw)
+    ms = nbg.get_masses(sysm)
+    n = len(ms)
+    dv = np.zeros((n, 3))
+    if water:
+        lj, el, grav, mag = sysm.lj_parameters, sysm.e_parameters, None, None
+        lj_idx = list(range(0, n, 3))
+        qs = [sysm.qO, sysm.qH, sysm.qH] * len(sysm.bodies)
+        excluded = lambda i, j: i // 3 == j // 3
+    else:
+        pots = getattr(sysm, "potentials", {})
+        lj, el = pots.get("lennard_jones"), pots.get("electrostatic")
+        mag = pots.get("magnetostatic")
+        grav = sysm if isinstance(sysm, nbg.GravitationalSystem) else pots.get("gravitational")
+        lj_idx = list(range(n))
+        qs = [getattr(b, "q", 0.0) for b in sysm.bodies]
+        excluded = lambda i, j: i == j
+    for i in range(n):
+        if lj is not None and i in lj_idx:
+            f = np.zeros(3)
+            for j in lj_idx:
+                if j != i:
+                    d, r2 = rij(i, j)
+                    if r2 < lj.R2:
+                        s6 = (lj.sigma2 / r2) ** 3
+                        f += (2 * s6 ** 2 - s6) / r2 * d
+            dv[i] += 24 * lj.eps / ms[i] * f
+        if el is not None:
+            f = np.zeros(3)
+            for j in range(n):
+                if not excluded(i, j):
+                    d, r2 = rij(i, j)
+                    if r2 < el.R2:
+                        f += qs[j] / (math.sqrt(r2) * r2) * d
+            dv[i] += el.k * qs[i] / ms[i] * f
+        if grav is not None:
+            for j in range(n):
+                if j != i:
+                    d = u[i] - u[j]
+                    dv[i] += -grav.G * sysm.bodies[j].m / np.linalg.norm(d) ** 3 * d
+        if mag is not None:
+            f = np.zeros(3)
+            mi = np.asarray(sysm.bodies[i].mm, dtype=float)
+            for j in range(n):
+                if j != i:
+                    mj = np.asarray(sysm.bodies[j].mm, dtype=float)
+                    d = u[i] - u[j]
+                    r = d / np.linalg.norm(d)
+                    mir, mij = np.dot(mi, r), np.dot(mj, r)
+                    f += (mi * mij + mj * mir + r * np.dot(mi, mj) - 5 * r * mir * mij) / np.dot(d, d) ** 2
+            dv[i] += 3 * mag.mu_4pi / sysm.bodies[i].m * f
+    if water:
+        p = sysm.scpfw_parameters
+        for m in range(len(sysm.bodies)):
+            o, h1, h2 = 3 * m, 3 * m + 1, 3 * m + 2
+            for i, nbrs in ((o, (h1, h2)), (h1, (o,)), (h2, (o,))):
+                for j in nbrs:
+                    d = u[i] - u[j]
+                    r = np.linalg.norm(d)
+                    dv[i] += -(r - p.rOH) * p.kb / r * d / ms[i]
+            rba, rbc, rcb = u[h1] - u[o], u[h2] - u[o], u[o] - u[h2]
+            x = np.cross(rba, rbc)
+            pa = np.cross(rba, x)
+            pa = pa / np.linalg.norm(pa)
+            pc = np.cross(rcb, x)
+            pc = pc / np.linalg.norm(pc)
+            c = min(1.0, max(-1.0, float(np.dot(rba, rbc)) / (np.linalg.norm(rba) * np.linalg.norm(rbc))))
+            force = -p.ka * (math.acos(c) - p.aHOH)
+            fa = pa * force / np.linalg.norm(rba)
+            fc = pc * force / np.linalg.norm(rbc)
+            dv[h1] += fa / ms[h1]
+            dv[o] += -(fa + fc) / ms[o]
+            dv[h2] += fc / ms[h2]
+    return dv
+
+
+@pytest.mark.parametrize("which", ["lj", "charges", "gravity", "magnetic", "water"])
+def test_oracle_accelerations_match_reference_loops(oracle, which):
+    """The oracle's right-hand side against a plain restatement of the
+    reference's acceleration functions, to 1e-10 of the largest component."""
+    rng = np.random.default_rng(8)
+    if which == "lj":
+        sim = S.lj_liquid(64, seed=5, jitter=0.05)
+    elif which == "charges":
+        sim, _ = S.charges8()
+    elif which == "gravity":
+        sim = S.plummer(32)
+    elif which == "magnetic":
+        bodies = [nbg.MagneticParticle(rng.uniform(-1, 1, 3), (0, 0, 0), 1.0 + rng.random(), rng.normal(size=3))
+                  for _ in range(6)]
+        sim = nbg.NBodySimulation(nbg.PotentialNBodySystem(bodies, {"magnetostatic": nbg.MagnetostaticParameters(1.0)}),
+                                  (0.0, 1.0))
+    else:
+        sim, _, _ = S.water3()
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    u = u0 + rng.normal(scale=0.01 if which != "water" else 0.002, size=u0.shape)
+    dv, _ = oracle.accel(desc, v0, u)
+    ref = _ref_accel(sim, u)
+    scale = np.abs(ref).max()
+    assert scale > 0
+    assert np.abs(dv[: len(ref)] - ref).max() <= 1e-10 * scale

@@ -431,3 +431,44 @@ def test_oracle_accelerations_match_reference_loops(oracle, which):
     scale = np.abs(ref).max()
     assert scale > 0
     assert np.abs(dv[: len(ref)] - ref).max() <= 1e-10 * scale
+
+
+@pytest.mark.parametrize("which", ["lj_berendsen", "lj_nosehoover", "water_berendsen", "water_nosehoover"])
+def test_oracle_thermostat_terms_match_reference(oracle, which):
+    """The simultaneous thermostat terms of soode_system! against the
+    reference (thermostats.jl:76-128, data nbody_to_ode.jl:392-433):
+    T = sum m v^2 / (kb (3N - Nc)) (no 1/2; Nc = 2 per water molecule);
+    Berendsen dv += gamma (T0 / T - 1) v, gamma = 0.5 / tau; Nose-Hoover
+    dv -= zeta v with zeta = u[3N+1], dv of the extra column 0, and
+    v[3N+1] = tau^-2 (T / T0 - (ndf + 1) / ndf)."""
+    rng = np.random.default_rng(9)
+    T0, tau = (1.0, 0.3) if which.startswith("lj") else (300.0, 0.1)
+    th = (nbg.BerendsenThermostat(T0, tau) if which.endswith("berendsen") else nbg.NoseHooverThermostat(T0, tau))
+    if which.startswith("lj"):
+        sim = S.lj_liquid(64, seed=5, jitter=0.05, thermostat=th)
+        kb, N, Nc = 1.0, 64, 0
+    else:
+        sim = S.water_box(8, seed=2, thermostat=th)
+        kb, N, Nc = S.KB_KJ, 24, 16
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    u = u0.copy()
+    u[:N] += rng.normal(scale=0.002, size=(N, 3))
+    v = v0 + rng.normal(scale=0.05, size=v0.shape)
+    nh = which.endswith("nosehoover")
+    if nh:
+        assert u.shape[0] == N + 1
+        u[N] = (0.37, 0.0, 0.0)  # zeta
+        v[N] = (0.0, 0.0, 0.0)
+    dv, v_out = oracle.accel(desc, v.copy(), u)
+    ms = nbg.get_masses(sim.system)
+    forces = _ref_accel(sim, u[:N])
+    T = float(sum(ms[i] * np.dot(v[i], v[i]) for i in range(N))) / (kb * (3 * N - Nc))
+    if nh:
+        zeta = u[N][0]
+        ref = np.vstack([forces - zeta * v[:N], np.zeros((1, 3))])
+        ndf = 3 * N - Nc
+        assert v_out[N][0] == pytest.approx(tau ** -2 * (T / T0 - (ndf + 1) / ndf), rel=1e-12)
+    else:
+        ref = forces + (0.5 / tau) * (T0 / T - 1) * v[:N]
+    assert np.abs(dv - ref).max() <= 1e-10 * np.abs(ref).max()

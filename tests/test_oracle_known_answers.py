@@ -472,3 +472,21 @@ def test_oracle_thermostat_terms_match_reference(oracle, which):
     else:
         ref = forces + (0.5 / tau) * (T0 / T - 1) * v[:N]
     assert np.abs(dv - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_oracle_langevin_drift_matches_reference():
+    """SDEProblem for a potential system (nbody_to_ode.jl:567-598): the drift
+    is du = v, dv = a(u) - gamma v, and Euler-Maruyama steps X' = X + dt f(X)
+    + g dW. At T = 0 the noise amplitude sqrt(2 gamma kb T / m) vanishes, so
+    one oracle step must equal the drift step exactly as restated here."""
+    import __graft_entry__ as g
+    oracle = g.load_oracle()
+    gamma, dt = 0.7, 0.004
+    sim = S.lj_liquid(64, seed=5, jitter=0.05, thermostat=nbg.LangevinThermostat(0.0, gamma))
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    u1, v1 = oracle.run(desc, u0, v0, dt, 1)
+    a = _ref_accel(sim, u0)
+    assert np.abs(u1 - (u0 + dt * v0)).max() <= 1e-14 * np.abs(u0).max()
+    ref_v = v0 + dt * (a - gamma * v0)
+    assert np.abs(v1 - ref_v).max() <= 1e-10 * np.abs(ref_v).max()

@@ -3,9 +3,32 @@
 Positions and velocities are length-3 float64 arrays, as the reference's
 SVector{3} fields.
 """
+import decimal
+import fractions
 import math
 
 import numpy as np
+
+
+def is_wide(x):
+    """True for an element type wider than float64, the counterpart of the
+    reference's BigFloat (and exact Rational) support: Decimal, Fraction,
+    mpmath numbers, numpy longdouble, or a container holding one. Such
+    problems have no GPU kernel; float32 and float64 inputs are computed in
+    float64."""
+    if isinstance(x, (decimal.Decimal, fractions.Fraction)):
+        return True
+    if type(x).__module__.split(".")[0] == "mpmath":
+        return True
+    if isinstance(x, np.ndarray):
+        if x.dtype == object:
+            return any(is_wide(e) for e in x.flat)
+        return (x.dtype.kind == "f" and x.dtype.itemsize > 8) or (x.dtype.kind == "c" and x.dtype.itemsize > 16)
+    if isinstance(x, np.generic):
+        return is_wide(np.asarray(x))
+    if isinstance(x, (list, tuple)):
+        return any(is_wide(e) for e in x)
+    return False
 
 
 def _vec3(x):
@@ -21,6 +44,7 @@ class MassBody(Body):
     """MassBody(r, v, m) (bodies.jl:37)."""
 
     def __init__(self, r, v, m):
+        self.wide = is_wide(r) or is_wide(v) or is_wide(m)
         self.r = _vec3(r)
         self.v = _vec3(v)
         self.m = float(m)
@@ -30,6 +54,7 @@ class ChargedParticle(Body):
     """ChargedParticle(r, v, m, q) (bodies.jl:68)."""
 
     def __init__(self, r, v, m, q):
+        self.wide = is_wide(r) or is_wide(v) or is_wide(m) or is_wide(q)
         self.r = _vec3(r)
         self.v = _vec3(v)
         self.m = float(m)
@@ -40,6 +65,7 @@ class MagneticParticle(Body):
     """MagneticParticle(r, v, m, mm) with magnetic moment mm (bodies.jl:102-107)."""
 
     def __init__(self, r, v, m, mm):
+        self.wide = is_wide(r) or is_wide(v) or is_wide(m) or is_wide(mm)
         self.r = _vec3(r)
         self.v = _vec3(v)
         self.m = float(m)
@@ -53,6 +79,7 @@ class WaterMolecule(Body):
         self.O = O
         self.H1 = H1
         self.H2 = H2
+        self.wide = any(getattr(b, "wide", False) for b in (O, H1, H2))
 
 
 def generate_bodies_in_cell_nodes(n, m, v_dev, L, rng=None):

@@ -8,7 +8,7 @@ import numbers
 import numpy as np
 
 from . import _abi
-from .bodies import MassBody, WaterMolecule
+from .bodies import MassBody, WaterMolecule, is_wide
 from .engine import Engine
 from .parameters import (AndersenThermostat, BerendsenThermostat,
                          CubicPeriodicBoundaryConditions, InfiniteBox,
@@ -47,6 +47,8 @@ class NBodySimulation:
         bc = InfiniteBox()
         thermostat = NullThermostat()
         kb_pos = None
+        # arbitrary-precision time span or kb (system_descriptor refuses them)
+        self.wide = is_wide(tuple(tspan)) or is_wide(kb) or any(is_wide(a) for a in args)
         for a in args:
             if isinstance(a, (InfiniteBox, CubicPeriodicBoundaryConditions, PeriodicBoundaryConditions)):
                 bc = a
@@ -147,9 +149,25 @@ def gather_bodies_initial_coordinates(simulation):
     return u0, v0, n
 
 
+def _has_wide_elements(simulation):
+    """Any arbitrary-precision element (is_wide) in the simulation's bodies,
+    parameters, time span or kb."""
+    sysm = simulation.system
+    if getattr(simulation, "wide", False) or any(getattr(b, "wide", False) for b in sysm.bodies):
+        return True
+    params = list(getattr(sysm, "potentials", {}).values())
+    params += [getattr(sysm, a) for a in ("lj_parameters", "e_parameters", "scpfw_parameters") if hasattr(sysm, a)]
+    scalars = [getattr(sysm, a) for a in ("mH", "mO", "qH", "qO", "G") if hasattr(sysm, a)]
+    return any(is_wide(x) for x in scalars) or any(is_wide(x) for p in params for x in vars(p).values())
+
+
 def system_descriptor(simulation):
     """Build the nbg_system_desc of a simulation (what the reference's
-    obtain_data_for_* functions extract). Returns (desc, keepalive)."""
+    obtain_data_for_* functions extract). Returns (desc, keepalive).
+    Arbitrary-precision elements (the reference's BigFloat) are refused with
+    NBG_ERR_UNSUPPORTED: the caller keeps such a problem on the CPU."""
+    if _has_wide_elements(simulation):
+        raise _abi.EngineError(-6, "arbitrary-precision elements (BigFloat-like) have no GPU kernel")
     sysm = simulation.system
     d = _abi.NbgSystemDesc()
     d.abi_version = _abi.NBG_ABI_VERSION

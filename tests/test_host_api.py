@@ -196,3 +196,41 @@ def test_rdf_histogram_argument_checks():
     assert call(fr=None) == -1
     assert call(idx_p=None) == -1
     assert lib.nbg_rdf_kernel_times(None) == -1
+
+
+def test_element_types():
+    """interface_test.jl: the reference runs BigFloat and Float32 problems.
+    Here float32 input is accepted and computed in float64; arbitrary
+    precision (Decimal, Fraction, numpy longdouble standing in for BigFloat)
+    has no GPU kernel and the descriptor builder refuses it with
+    NBG_ERR_UNSUPPORTED (-6), so the caller keeps it on the CPU."""
+    from decimal import Decimal
+    from fractions import Fraction
+
+    f32 = np.float32
+    b1 = nbg.MassBody(np.array([1, 0, 0], dtype=f32), np.array([0, 0.5, 0], dtype=f32), f32(1))
+    b2 = nbg.MassBody(np.array([-1, 0, 0], dtype=f32), np.array([0, -0.5, 0], dtype=f32), f32(1))
+    sim = nbg.NBodySimulation(nbg.GravitationalSystem([b1, b2], f32(1)), (f32(0), f32(1)), nbg.InfiniteBox(),
+                              f32(1.38e-23))
+    desc, keep = nbg.system_descriptor(sim)
+    assert desc.n == 2 and desc.grav_G == 1.0
+
+    def refused(make):
+        with pytest.raises(nbg.EngineError) as e:
+            nbg.system_descriptor(make())
+        assert e.value.status == -6
+
+    big = lambda x: Decimal(str(x))
+    refused(lambda: nbg.NBodySimulation(
+        nbg.GravitationalSystem([nbg.MassBody((big(1), big(0), big(0)), (big(0), big(0.5), big(0)), big(1)),
+                                 nbg.MassBody((big(-1), big(0), big(0)), (big(0), big(-0.5), big(0)), big(1))],
+                                big(1)), (0.0, 1.0)))
+    p0 = nbg.MassBody((0, 0, 0), (0, 0, 0), 1.0)
+    p1 = nbg.MassBody((2, 0, 0), (0, 0, 0), 1.0)
+    refused(lambda: nbg.NBodySimulation(nbg.PotentialNBodySystem(
+        [p0, p1], {"lennard_jones": nbg.LennardJonesParameters(big(1), big(1), big(2.5))}), (0.0, 0.1)))
+    refused(lambda: nbg.NBodySimulation(nbg.GravitationalSystem([p0, p1], 1.0), (Fraction(0), Fraction(1, 10))))
+    if np.dtype(np.longdouble).itemsize > 8:
+        ld = np.longdouble
+        refused(lambda: nbg.NBodySimulation(nbg.GravitationalSystem(
+            [nbg.MassBody(np.array([1, 0, 0], dtype=ld), (0, 0, 0), 1.0), p1], 1.0), (0.0, 1.0)))

@@ -8,32 +8,35 @@
 // The counts are integers, so parity is bit-exact:
 //
 //   k_rdf_pack    one thread per (frame, participant): wraps the position
-//                 into the box, scales it to box units u in [0, 1) and splits
-//                 u into an FP32 hi part on the grid 2^-22 and an FP32 lo
-//                 remainder (the image shift of a hi difference, rint of it,
-//                 is then exact), and keeps the unwrapped FP64 position
-//                 contiguous per frame;
+//                 into the box, scales it to box units u in [0, 1) and keeps
+//                 FP32 u (plain positions, up to RDF_PLAIN_MAXBIN bins) or
+//                 splits u into an FP32 hi part on the grid 2^-22 and an FP32
+//                 lo remainder (split positions); the image shift of a
+//                 difference, rint of it, is exact either way. It also keeps
+//                 the unwrapped FP64 position contiguous per frame;
 //   k_rdf_pairs   a grid-stride loop over (frame, tile pair) items of
 //                 TILE x TILE participants, one i per thread, the j tile in
 //                 shared memory as structure-of-arrays float4 groups, two j
-//                 per packed FP32x2 instruction. The split difference gives
-//                 q = r / dr to ~6 ulp. A pair whose q lies within
-//                 RDF_MARGIN * q of an integer, or whose r^2 lies within
-//                 RDF_MARGIN of (L/2)^2, is undecided: a bit in a per-thread
-//                 mask over 32 j, queued in shared memory once per 32 j, and
-//                 decided by the whole block with the reference's FP64
-//                 arithmetic on the unwrapped positions (the loop minimum
-//                 image, r^2, then bin > b <=> r^2 >= thresh[b], a table the
-//                 host builds with IEEE sqrt and division: the reference's
-//                 ceil(sqrt(r^2) / dr) exactly). All other pairs are counted
-//                 in a per-block shared histogram by predicated atomics:
-//                 weight 2 for an off-diagonal tile pair (each unordered pair
-//                 once), weight 1 on a diagonal tile, which runs the full
-//                 square (each unordered pair twice; a self pair has r = 0,
-//                 bin 0). A participant with a coordinate beyond
-//                 RDF_FAR_BOXES boxes has a NaN hi part, so all its pairs take
-//                 the FP64 path: there the rounding of the reference's long
-//                 wrap loops can exceed the band;
+//                 per packed FP32x2 instruction. q = r / dr is good to
+//                 1.55e-7 maxbin plus ~6 ulp (plain) or ~6 ulp (split). A
+//                 pair is undecided when q lies within RDF_MARGIN * q (plus
+//                 RDF_MARGIN_ABS * maxbin for plain positions) of an
+//                 integer, or r^2 within RDF_MARGIN (plain: twice that) of
+//                 (L/2)^2: a bit in a per-thread mask over 32 j, queued in
+//                 shared memory once per 32 j, and decided during the next
+//                 item by the block with the reference's FP64 arithmetic on
+//                 the unwrapped positions (the loop minimum image, r^2, then
+//                 bin > b <=> r^2 >= thresh[b], a table the host builds with
+//                 IEEE sqrt and division: the reference's ceil(sqrt(r^2) /
+//                 dr) exactly). All other pairs go to a per-block shared
+//                 histogram by a branch-free add: weight 2 for an
+//                 off-diagonal tile pair (each unordered pair once), weight
+//                 1 on a diagonal tile, which runs the full square (each
+//                 unordered pair twice; a self pair has r = 0, bin 0). A
+//                 participant with a coordinate beyond RDF_FAR_BOXES boxes
+//                 has a NaN hi part, so all its pairs take the FP64 path:
+//                 there the rounding of the reference's long wrap loops can
+//                 exceed the band;
 //   k_rdf_finish  hist[b] = counts[b].
 #include <cstdlib>
 #include <cstring>

@@ -490,3 +490,44 @@ def test_oracle_langevin_drift_matches_reference():
     assert np.abs(u1 - (u0 + dt * v0)).max() <= 1e-14 * np.abs(u0).max()
     ref_v = v0 + dt * (a - gamma * v0)
     assert np.abs(v1 - ref_v).max() <= 1e-10 * np.abs(ref_v).max()
+
+
+def _adaptive(oracle, sim):
+    """run_simulation(sim)'s host adaptive integration (simulation.py
+    _adaptive_run) with the oracle's right-hand side in place of nbg_accel."""
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    rhs = lambda v, u, t: oracle.accel(desc, v, u, t)[0]
+    return nbg.simulation._adaptive_run(rhs, u0, v0, sim.tspan, 1e-6, 1e-3, True)
+
+
+def test_default_adaptive_run_closes_the_figure_eight(oracle):
+    """gravitational_test.jl:8-24: run_simulation(simulation) with the default
+    adaptive method returns the figure-eight to its start after 2 pi within
+    0.1; the saved times are the accepted steps from 0 to 2 pi."""
+    t, tu, tv, nacc = _adaptive(oracle, S.figure8())
+    assert t[0] == 0.0 and t[-1] == pytest.approx(2 * math.pi) and nacc == len(t) - 1 > 10
+    assert np.abs(tu[-1] - tu[0]).max() <= 0.1
+
+
+def test_default_adaptive_run_closes_the_charge_orbit(oracle):
+    """electrostatics_test.jl:7-29, with run_simulation(simulation)'s default
+    adaptive method: back at the start after one period within 0.1 r."""
+    k, r, q1, q2, m1, m2 = 9.0e9, 100.0, 1.0e-3, -1.0e-3, 100.0, 0.1
+    v2 = math.sqrt(abs(k * q1 * q2 / m2 / r))
+    p1 = nbg.ChargedParticle((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), m1, q1)
+    p2 = nbg.ChargedParticle((r, 0.0, 0.0), (0.0, v2, 0.0), m2, q2)
+    sim = nbg.NBodySimulation(nbg.ChargedParticles([p1, p2], k), (0.0, 2 * math.pi * r / v2))
+    t, tu, tv, nacc = _adaptive(oracle, sim)
+    assert np.abs(tu[-1] - tu[0]).max() <= 0.1 * r
+
+
+def test_default_adaptive_run_refuses_stateful_thermostats():
+    """Nose-Hoover writes zeta into v inside the right-hand side, Andersen is
+    a callback and Langevin an SDE: run_simulation(sim) without dt refuses
+    them (NBG_ERR_UNSUPPORTED) before touching the GPU."""
+    for th in (nbg.NoseHooverThermostat(1.0, 0.1), nbg.AndersenThermostat(1.0, 0.1), nbg.LangevinThermostat(1.0, 1.0)):
+        sim = S.lj_liquid(64, seed=1, thermostat=th)
+        with pytest.raises(nbg.EngineError) as e:
+            nbg.run_simulation(sim)
+        assert e.value.status == -6

@@ -114,3 +114,23 @@ def test_rdf_peak_and_msd(gpu):
     assert d2[0] < d2[-1]
     rs, gr = nbg.rdf(res)
     assert abs(rs[int(np.argmax(gr))] / sigma - 1.0) <= 1.0
+
+
+def test_default_run_simulation_is_adaptive(gpu):
+    """gravitational_test.jl:8-24 and electrostatics_test.jl:7-29 call
+    run_simulation(simulation) with the default adaptive method: the
+    figure-eight back at its start after 2 pi within 0.1, a charge orbit after
+    one period within 0.1 r (host DOP853 over the GPU right-hand side)."""
+    sim = S.figure8()
+    res = nbg.run_simulation(sim)
+    u = res.solution.u
+    assert res.solution.t[-1] == pytest.approx(2 * math.pi)
+    assert np.abs(u[-1] - u[0]).max() <= 0.1
+    k, r, q1, q2, m1, m2 = 9.0e9, 100.0, 1.0e-3, -1.0e-3, 100.0, 0.1
+    v2 = math.sqrt(abs(k * q1 * q2 / m2 / r))
+    p1 = nbg.ChargedParticle((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), m1, q1)
+    p2 = nbg.ChargedParticle((r, 0.0, 0.0), (0.0, v2, 0.0), m2, q2)
+    sim = nbg.NBodySimulation(nbg.ChargedParticles([p1, p2], k), (0.0, 2 * math.pi * r / v2))
+    res = nbg.run_simulation(sim)
+    u = res.solution.u
+    assert np.abs(u[-1] - u[0]).max() <= 0.1 * r

@@ -197,6 +197,18 @@ NBG_API int nbg_accel(nbg_ctx* ctx, double* dv, double* v, const double* u, doub
 NBG_API int nbg_set_state(nbg_ctx* ctx, const double* u, const double* v);
 NBG_API int nbg_get_state(nbg_ctx* ctx, double* u, double* v);
 
+/* The context's step counter: steps taken on the resident state since the
+   context was created or the counter was last set. It keys the Philox noise
+   of the Andersen and Langevin thermostats (counter (atom, step)), and it
+   keeps running across nbg_advance / nbg_run calls, so that every run draws
+   fresh noise, as each run_simulation call of the reference does
+   (nbody_simulation_result.jl:504-540, nbody_to_ode.jl:567-598). A
+   checkpoint is nbg_get_state + nbg_get_step; nbg_set_state + nbg_set_step
+   resume it. Resuming at a multiple of rebuild_every (where the uninterrupted
+   run rebuilds its lists too) continues the run bit for bit. */
+NBG_API int nbg_get_step(nbg_ctx* ctx, int64_t* step);
+NBG_API int nbg_set_step(nbg_ctx* ctx, int64_t step);
+
 /* Accelerations of the resident state into the resident acceleration buffer
    (no host traffic); the unit the force roofline is measured on. */
 NBG_API int nbg_compute_forces(nbg_ctx* ctx);
@@ -274,7 +286,10 @@ NBG_API int nbg_cluster_shape(nbg_ctx* ctx, int32_t* ctas, int32_t* lanes);
  * share the array: calls that overlap on the GPU (other streams or threads)
  * race and must be serialised by the caller. Synchronous on `stream` (a
  * cudaStream_t, NULL for the default stream). Errors are described by
- * nbg_last_error(NULL).
+ * nbg_last_error(NULL). The looked-up address is kept for the life of the
+ * process: the entry point assumes each device's primary context (the CUDA
+ * runtime's) throughout, so do not call it after cudaDeviceReset or from a
+ * non-primary driver context on the same device.
  */
 NBG_API int nbg_gravity_accel_noalloc(const double* x, const double* mass, int64_t n, double G, double* a,
                                       void* stream);

@@ -20,7 +20,7 @@ from .parameters import (AndersenThermostat, BerendsenThermostat,
                          NoseHooverThermostat, NullThermostat,
                          PeriodicBoundaryConditions, PotentialParameters,
                          SPCFwParameters)
-from .simulation import (BAOAB, EM, NBodySimulation, SecondOrderODEProblem, Tsit5,
+from .simulation import (BAOAB, DOP853, EM, NBodySimulation, SecondOrderODEProblem, Tsit5,
                          SimulationResult, VelocityVerlet,
                          gather_bodies_initial_coordinates, get_masses,
                          get_degrees_of_freedom, get_position, get_velocity,

@@ -129,6 +129,8 @@ SIGNATURES = {
     "nbg_accel": (ctypes.c_int, [_vp, _dp, _dp, _dp, ctypes.c_double]),
     "nbg_set_state": (ctypes.c_int, [_vp, _dp, _dp]),
     "nbg_get_state": (ctypes.c_int, [_vp, _dp, _dp]),
+    "nbg_get_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64)]),
+    "nbg_set_step": (ctypes.c_int, [_vp, ctypes.c_int64]),
     "nbg_compute_forces": (ctypes.c_int, [_vp]),
     "nbg_get_accel": (ctypes.c_int, [_vp, _dp]),
     "nbg_advance": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int64]),

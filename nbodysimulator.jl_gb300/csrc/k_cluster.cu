@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     // the frame sink (trajectory saving): state of time index step0 + st;
     // its other fields are read at a save point
     const int64_t sk_every = save && owner ? d.sink->every : 0;
+    const int64_t sk_t0 = save && owner ? d.sink->t0 : 0;
 
     for (int st = 0; st <= nsteps; ++st) {
         // kick of the previous step with the forces its groups left in fsum
@@ -183,9 +184,9 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
                 v[k] = kick1(v[k], a[k], an, dt);
                 a[k] = an;
             }
-            if (sk_every > 0 && (step0 + st) % sk_every == 0) {
+            if (sk_every > 0 && (step0 + st - sk_t0) % sk_every == 0) {
                 const FrameSink* sk = d.sink;
-                const int64_t slot = (step0 + st) / sk_every - sk->first;
+                const int64_t slot = (step0 + st - sk_t0) / sk_every - sk->first;
                 if (slot >= 0 && slot < sk->cap) {
                     const size_t o = (size_t)slot * 3 * d.cols + 3 * (size_t)io;
                     double* fx = sk->x;

@@ -412,7 +412,7 @@ __global__ void k_save_frame(const FrameSink* sink, const double* x, const doubl
 {
     const int64_t every = sink->every;
     if (every <= 0) return;
-    const int64_t t = (sr.base ? *sr.base : 0) + sr.off + 1;
+    const int64_t t = (sr.base ? *sr.base : 0) + sr.off + 1 - sink->t0;
     if (t % every != 0) return;
     const int64_t slot = t / every - sink->first;
     if (slot < 0 || slot >= sink->cap) return;

@@ -857,6 +857,21 @@ extern "C" int nbg_get_state(nbg_ctx* c, double* u, double* v)
     return NBG_OK;
 }
 
+extern "C" int nbg_get_step(nbg_ctx* c, int64_t* step)
+{
+    if (!c || !step) return NBG_ERR_ARG;
+    *step = c->step;
+    return NBG_OK;
+}
+
+extern "C" int nbg_set_step(nbg_ctx* c, int64_t step)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (step < 0) return fail(c, NBG_ERR_ARG, "the step counter must be >= 0");
+    c->step = step;
+    return NBG_OK;
+}
+
 extern "C" int nbg_compute_forces(nbg_ctx* c)
 {
     if (!c) return NBG_ERR_ARG;
@@ -1213,7 +1228,10 @@ extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nste
     unsigned long long builds0 = 0;
     int st;
     if ((st = nbg_set_state(c, u, v))) return st;
-    c->step = 0;
+    // the step counter keys the Philox noise (Andersen, Langevin): it keeps
+    // running across runs, so every run draws fresh noise, as the
+    // reference's run_simulation does; nbg_set_step restarts or restores it
+    const int64_t t0 = c->step;
     if (c->path == PATH_LIST) CK(cudaMemcpyAsync(&builds0, c->d.build_count, 8, cudaMemcpyDeviceToHost, c->stream), "builds");
     size_t fb = state_bytes(c);
     const int64_t n3 = 3 * c->cols;
@@ -1247,7 +1265,7 @@ extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nste
         if (done / std::max<int64_t>(save_every, 1) < aligned) {
             const int64_t j0 = done / save_every + 1;  // the segment's first frame
             const int64_t nf = std::min<int64_t>(cap, aligned - (j0 - 1));
-            const FrameSink h{c->frames, c->frames + (size_t)c->frames_cap * n3, save_every, j0, nf};
+            const FrameSink h{c->frames, c->frames + (size_t)c->frames_cap * n3, save_every, j0, nf, t0};
             CK(cudaMemcpy(c->d.sink, &h, sizeof h, cudaMemcpyHostToDevice), "frame sink");
             c->sink_on = true;
             st = advance_impl(c, dt, nf * save_every);

@@ -64,13 +64,16 @@ struct RepDev {
 };
 
 // Everything a kernel needs, passed by value.
-// Where the step loop leaves saved frames (device memory): the state after
-// step t goes to slot t / every - first when t is a multiple of every and the
-// slot is below cap. every = 0: nothing is saved.
+// Where the step loop leaves saved frames (device memory): with t the step
+// index counted from the run's first step t0 (the context's step counter
+// keeps running across runs), the state after step t goes to slot
+// t / every - first when t is a multiple of every and the slot is below cap.
+// every = 0: nothing is saved.
 struct FrameSink {
     double* x;  // [cap][3 cols] positions
     double* v;  // [cap][3 cols] velocities
     int64_t every, first, cap;
+    int64_t t0;  // absolute step index of the run's initial state
 };
 
 struct Dev {

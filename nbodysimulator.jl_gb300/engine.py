@@ -93,9 +93,23 @@ class Engine:
     def advance(self, dt, nsteps):
         self._chk(self.lib.nbg_advance(self.ctx, float(dt), int(nsteps)))
 
-    def run(self, u, v, dt, nsteps, save_every=0, save_trajectory=True):
+    @property
+    def step(self):
+        """The step counter that keys the Andersen / Langevin noise; it keeps
+        running across runs (every run draws fresh noise)."""
+        out = ctypes.c_int64()
+        self._chk(self.lib.nbg_get_step(self.ctx, ctypes.byref(out)))
+        return out.value
+
+    def set_step(self, step):
+        self._chk(self.lib.nbg_set_step(self.ctx, int(step)))
+
+    def run(self, u, v, dt, nsteps, save_every=0, save_trajectory=True, step=None):
         """Upload (u, v), run, download. Returns (u, v, traj_u, traj_v, stats);
-        traj arrays have shape (frames, cols, 3)."""
+        traj arrays have shape (frames, cols, 3). step: set the noise step
+        counter first (None continues it)."""
+        if step is not None:
+            self.set_step(step)
         u = _f64(u).copy()
         v = _f64(v).copy()
         nframes = (nsteps // save_every + 1 if save_every > 0 else 1) + 1

@@ -30,15 +30,22 @@ class EM:
     """Euler-Maruyama (StochasticDiffEq.EM), used with LangevinThermostat."""
 
 
-class Tsit5:
-    """The reference's default method (OrdinaryDiffEqTsit5.Tsit5, adaptive
-    5(4) Runge-Kutta, nbody_simulation_result.jl:480): here a host adaptive
-    integrator over the GPU right-hand side nbg_accel, at SciML's default
-    tolerances (abstol 1e-6, reltol 1e-3). The method is scipy's DOP853
-    (Dormand-Prince 8(5,3)): at these tolerances scipy's RK45 misses the
-    reference's own closure tests (a charge orbit back within 0.1 r), DOP853
-    meets them. Only the right-hand side runs on the GPU; the fused loops are
-    VelocityVerlet, EM and BAOAB."""
+class DOP853:
+    """Adaptive Dormand-Prince 8(5,3) (scipy's DOP853) on the host over the
+    GPU right-hand side nbg_accel, at SciML's default tolerances (abstol 1e-6,
+    reltol 1e-3): what run_simulation(sim) without dt runs. At these
+    tolerances scipy's RK45 misses the reference's own closure tests (a charge
+    orbit back within 0.1 r); DOP853 meets them. Only the right-hand side runs
+    on the GPU; the fused loops are VelocityVerlet, EM and BAOAB."""
+
+
+class Tsit5(DOP853):
+    """The reference's default method name (OrdinaryDiffEqTsit5.Tsit5,
+    nbody_simulation_result.jl:480), accepted as an alias of DOP853. Tsit5
+    itself is not implemented: the saved times and the accepted-step count
+    ("Time steps" in show()) are DOP853's, not the reference's Tsit5 step
+    sequence; the states at the saved times agree with the reference within
+    the tolerances."""
 
 
 class BAOAB:
@@ -319,8 +326,11 @@ class Solution:
 
     def __init__(self, t, u, v, naccept):
         self.t = np.asarray(t, dtype=np.float64)
-        self.u = u
-        self.v = v
+        # every path (fused steps or the host adaptive integrator) stores
+        # frames as one (frames, cols, 3) array, so that msd / rdf / the
+        # interpolation index them alike
+        self.u = np.asarray(u, dtype=np.float64)
+        self.v = np.asarray(v, dtype=np.float64)
         self.naccept = naccept
 
 
@@ -450,10 +460,11 @@ def run_simulation(simulation, alg=None, dt=None, save_everystep=True, save_ever
     on the GPU. The state is saved every step (the reference's default) unless
     save_everystep=False (first and last frame) or save_every=k.
 
-    run_simulation(sim) without dt, or with alg Tsit5(), is the reference's
-    default adaptive call: DOP853 on the host over the GPU right-hand side
-    (see Tsit5), for systems without a thermostat or with Berendsen."""
-    if isinstance(alg, Tsit5) or (alg is None and dt is None):
+    run_simulation(sim) without dt, or with alg DOP853() (or its alias
+    Tsit5()), is the reference's default adaptive call: DOP853 on the host
+    over the GPU right-hand side, for systems without a thermostat or with
+    Berendsen."""
+    if isinstance(alg, DOP853) or (alg is None and dt is None):
         if not isinstance(simulation.thermostat, (NullThermostat, BerendsenThermostat)):
             raise _abi.EngineError(-6, f"{type(simulation.thermostat).__name__} is not integrated adaptively "
                                        "here; use VelocityVerlet (or EM for Langevin) with dt")

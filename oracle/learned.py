@@ -77,11 +77,14 @@ def min_image(d, L):
     return d - L * np.round(d / L)
 
 
-def neighbours(u, L, i):
-    """(j, rij vector j - i, r) of atoms of other molecules within RD."""
+def neighbours(u, L, i, ids=None):
+    """(j, rij vector j - i, r) of atoms of other molecules within RD. ids:
+    the atom indices of u's rows when u holds a subset of the system (rows
+    of the whole system by default); j indexes u's rows."""
+    ids = np.arange(len(u)) if ids is None else ids
     d = min_image(u - u[i], L)
     r = np.sqrt((d * d).sum(axis=1))
-    m = (r < RD) & (np.arange(len(u)) // 3 != i // 3)
+    m = (r < RD) & (ids // 3 != ids[i] // 3)
     j = np.nonzero(m)[0]
     return j, d[j], r[j]
 
@@ -90,10 +93,11 @@ def species(j):
     return np.where(j % 3 == 0, 0, 1)
 
 
-def descriptor(u, L, i):
+def descriptor(u, L, i, ids=None):
     """D (64,) and the moments (p[2,4,3], Q[2,4,3,3]) of atom i."""
-    j, d, r = neighbours(u, L, i)
-    s = species(j)
+    ids = np.arange(len(u)) if ids is None else ids
+    j, d, r = neighbours(u, L, i, ids)
+    s = species(ids[j])
     f = fc(r)
     mu = R0 + W * np.arange(NK)
     G = np.zeros((2, NK))
@@ -135,44 +139,79 @@ def forces(u, L, thetas):
     F = np.zeros_like(u)
     Etot = 0.0
     for i in range(n):
-        D, p, Q = descriptor(u, L, i)
-        E, dD = mlp(thetas[0 if i % 3 == 0 else 1], D)
+        E, j, grad = atom_energy_grad(u, L, thetas, i)
         Etot += E
-        j, d, r = neighbours(u, L, i)
-        s = species(j)
-        f, df = fc(r), dfc(r)
-        rh = d / r[:, None]
-        mu = R0 + W * np.arange(NK)
-        g = np.exp(-((r[:, None] - mu[None, :]) ** 2) / (2 * W * W))
-        # radial: dG/dr = g' fc + g fc'
-        dgr = (g * (-(r[:, None] - mu[None, :]) / (W * W)) * f[:, None] + g * df[:, None])
-        coef = np.where(s[:, None] == 0, dD[None, :NK], dD[None, NK:2 * NK])
-        dEdr = (coef * dgr).sum(axis=1)
-        grad = dEdr[:, None] * rh  # dE_i / d r_j  (radial part)
-        for a, rho in enumerate(RHO):
-            e = np.exp(-r * r / (2 * rho * rho))
-            psi = f * e
-            dpsi = df * e + f * e * (-r / (rho * rho))
-            for sp in (0, 1):
-                m = s == sp
-                if not m.any():
-                    continue
-                cA1 = dD[48 + 4 * sp + a]
-                cA2 = dD[56 + 4 * sp + a]
-                pv = p[sp, a]
-                Qm = Q[sp, a]
-                rr = rh[m]
-                pr = rr @ pv
-                # d|p|^2/dr_j = 2 [psi' (p.rh) rh + psi/r (p - (p.rh) rh)]
-                g1 = 2 * (dpsi[m, None] * pr[:, None] * rr + (psi[m] / r[m])[:, None] * (pv[None] - pr[:, None] * rr))
-                Qr = rr @ Qm
-                rQr = (Qr * rr).sum(axis=1)
-                # d|Q|^2/dr_j = 2 [psi' rQr rh + psi 2/r (Q rh - rQr rh)]
-                g2 = 2 * (dpsi[m, None] * rQr[:, None] * rr + (2 * psi[m] / r[m])[:, None] * (Qr - rQr[:, None] * rr))
-                grad[m] += cA1 * g1 + cA2 * g2
         F[j] -= grad
         F[i] += grad.sum(axis=0)
     return Etot, F
+
+
+def local_rows(u, L, i, radius):
+    """Indices of the atoms within `radius` of atom i (minimum image), i first."""
+    d = min_image(u - u[i], L)
+    near = np.nonzero((d * d).sum(axis=1) < radius * radius)[0]
+    return np.concatenate([[i], near[near != i]])
+
+
+def forces_on(u, L, thetas, idx):
+    """Learned forces -d(sum_k E_k)/dx_i of the atoms idx only (FP64), from
+    local neighbourhoods: only atoms k within RD of i have E_k depend on x_i,
+    and their own neighbours lie within 2 RD of i, so each force needs the
+    atoms within 2 RD of i (a sample of a large box, without all atoms)."""
+    out = np.zeros((len(idx), 3))
+    for t, i in enumerate(idx):
+        rows = local_rows(u, L, i, 2 * RD + 1e-6)
+        sub = u[rows]
+        j0, _, _ = neighbours(sub, L, 0, rows)
+        f = np.zeros(3)
+        _, jj, grad = atom_energy_grad(sub, L, thetas, 0, rows)
+        f += grad.sum(axis=0)  # dE_i/dx_i = -sum_j dE_i/dx_j
+        for k in j0:
+            _, jk, gk = atom_energy_grad(sub, L, thetas, k, rows)
+            f -= gk[jk == 0].sum(axis=0)  # dE_k/dx_i
+        out[t] = f
+    return out
+
+
+def atom_energy_grad(u, L, thetas, i, ids=None):
+    """Energy E_i of atom i and dE_i/dr_j for its neighbours j (rows of u,
+    as neighbours() returns them); dE_i/dr_i is minus their sum."""
+    ids = np.arange(len(u)) if ids is None else ids
+    D, p, Q = descriptor(u, L, i, ids)
+    E, dD = mlp(thetas[0 if ids[i] % 3 == 0 else 1], D)
+    j, d, r = neighbours(u, L, i, ids)
+    s = species(ids[j])
+    f, df = fc(r), dfc(r)
+    rh = d / r[:, None]
+    mu = R0 + W * np.arange(NK)
+    g = np.exp(-((r[:, None] - mu[None, :]) ** 2) / (2 * W * W))
+    # radial: dG/dr = g' fc + g fc'
+    dgr = (g * (-(r[:, None] - mu[None, :]) / (W * W)) * f[:, None] + g * df[:, None])
+    coef = np.where(s[:, None] == 0, dD[None, :NK], dD[None, NK:2 * NK])
+    dEdr = (coef * dgr).sum(axis=1)
+    grad = dEdr[:, None] * rh  # dE_i / d r_j  (radial part)
+    for a, rho in enumerate(RHO):
+        e = np.exp(-r * r / (2 * rho * rho))
+        psi = f * e
+        dpsi = df * e + f * e * (-r / (rho * rho))
+        for sp in (0, 1):
+            m = s == sp
+            if not m.any():
+                continue
+            cA1 = dD[48 + 4 * sp + a]
+            cA2 = dD[56 + 4 * sp + a]
+            pv = p[sp, a]
+            Qm = Q[sp, a]
+            rr = rh[m]
+            pr = rr @ pv
+            # d|p|^2/dr_j = 2 [psi' (p.rh) rh + psi/r (p - (p.rh) rh)]
+            g1 = 2 * (dpsi[m, None] * pr[:, None] * rr + (psi[m] / r[m])[:, None] * (pv[None] - pr[:, None] * rr))
+            Qr = rr @ Qm
+            rQr = (Qr * rr).sum(axis=1)
+            # d|Q|^2/dr_j = 2 [psi' rQr rh + psi 2/r (Q rh - rQr rh)]
+            g2 = 2 * (dpsi[m, None] * rQr[:, None] * rr + (2 * psi[m] / r[m])[:, None] * (Qr - rQr[:, None] * rr))
+            grad[m] += cA1 * g1 + cA2 * g2
+    return E, j, grad
 
 
 def smoothstep(r):
@@ -184,10 +223,14 @@ def smoothstep(r):
 
 def short_range_labels(u, L, q, lj_eps, lj_sigma, k_el):
     """Per-atom short-range energies E_i and the exact short-range forces."""
-    n = len(u)
-    E = np.zeros(n)
-    F = np.zeros_like(u)
-    for i in range(n):
+    return labels_on(u, L, q, lj_eps, lj_sigma, k_el, np.arange(len(u)))
+
+
+def labels_on(u, L, q, lj_eps, lj_sigma, k_el, idx):
+    """short_range_labels of the atoms idx only: (E[len(idx)], F[len(idx), 3])."""
+    E = np.zeros(len(idx))
+    F = np.zeros((len(idx), 3))
+    for t, i in enumerate(idx):
         j, d, r = neighbours(u, L, i)
         S, dS = smoothstep(r)
         kqq = k_el * q[i] * q[j]
@@ -199,10 +242,10 @@ def short_range_labels(u, L, q, lj_eps, lj_sigma, k_el):
             sr6 = (lj_sigma / r[o]) ** 6
             phi[o] += 4 * lj_eps * (sr6 * sr6 - sr6)
             dphi[o] += 4 * lj_eps * (-12 * sr6 * sr6 + 6 * sr6) / r[o]
-        E[i] = 0.5 * (phi * S).sum()
+        E[t] = 0.5 * (phi * S).sum()
         # dE_total/dr_j for the pair (counted once per ordered pair with the 1/2)
         fpair = (dphi * S + phi * dS)[:, None] * (d / r[:, None])
-        F[i] += fpair.sum(axis=0)
+        F[t] += fpair.sum(axis=0)
     return E, F
 
 

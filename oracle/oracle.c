@@ -302,7 +302,10 @@ static double norm3(const double* a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a
 
 /* valence_angle_potential_acceleration! :395-433, called with
    (a, b, c) = (H1, O, H2) by get_group_accelerating_function (nbody_to_ode.jl:244-261). */
-static void angle_accel(double* dv, const double* rs, int64_t mol, const nbg_system_desc* d)
+/* The H1-O-H2 angle forces of molecule mol on its atoms a = H1, b = O,
+   c = H2 (fa, fb, fc), then divided by the masses into dv. */
+static void angle_forces(const double* rs, int64_t mol, const nbg_system_desc* d, double fa[3], double fb[3],
+                         double fc[3])
 {
     int64_t b = 3 * mol, a = b + 1, c = b + 2;
     const double *ra = rs + 3 * a, *rb = rs + 3 * b, *rc = rs + 3 * c;
@@ -323,12 +326,18 @@ static void angle_accel(double* dv, const double* rs, int64_t mol, const nbg_sys
     else if (cosine < -1.0) cosine = -1.0;
     double ang = acos(cosine);
     double force = -d->water_ka * (ang - d->water_aHOH);
-    double fa[3], fc[3], fb[3];
     for (int k = 0; k < 3; ++k) {
         fa[k] = pa[k] * force / nba;
         fc[k] = pc[k] * force / nbc;
         fb[k] = -(fa[k] + fc[k]);
     }
+}
+
+static void angle_accel(double* dv, const double* rs, int64_t mol, const nbg_system_desc* d)
+{
+    int64_t b = 3 * mol, a = b + 1, c = b + 2;
+    double fa[3], fb[3], fc[3];
+    angle_forces(rs, mol, d, fa, fb, fc);
     for (int k = 0; k < 3; ++k) {
         dv[3 * a + k] += fa[k] / d->mass[a];
         dv[3 * b + k] += fb[k] / d->mass[b];
@@ -833,7 +842,10 @@ int64_t oracle_pair_list(const nbg_system_desc* d, const double* u, int32_t whic
 }
 
 /* Accelerations of a subset of atoms [i0, i1) (bench CPU-baseline sample of
-   the all-pairs work; same per-atom loops as body_accelerations). */
+   the all-pairs work, and the sampled parity checks at full size; same
+   per-atom loops as body_accelerations). For water, with i0 and i1 on
+   molecule boundaries the angle terms (:526-531) of the molecules inside are
+   added too, so the rows equal body_accelerations' rows. */
 void oracle_partial_accel(const nbg_system_desc* d, const double* u, double* dv, int64_t i0, int64_t i1)
 {
 #pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads)
@@ -846,6 +858,18 @@ void oracle_partial_accel(const nbg_system_desc* d, const double* u, double* dv,
             if (i % 3 == 0) lj_accel(a, u, i, d);
         } else {
             potential_terms(a, u, i, d);
+        }
+    }
+    if (is_water(d) && i0 % 3 == 0 && i1 % 3 == 0) {
+        for (int64_t m = i0 / 3; m < i1 / 3; ++m) {
+            double fa[3], fb[3], fc[3];
+            angle_forces(u, m, d, fa, fb, fc);
+            double* ab = dv + 3 * (3 * m - i0);
+            for (int k = 0; k < 3; ++k) {
+                ab[3 + k] += fa[k] / d->mass[3 * m + 1];
+                ab[k] += fb[k] / d->mass[3 * m];
+                ab[6 + k] += fc[k] / d->mass[3 * m + 2];
+            }
         }
     }
 }

@@ -49,17 +49,17 @@ def test_run_frames_match_unsaved_runs(gpu, kind, every):
         assert eng.cluster_shape() is None
     u0, v0 = S.state(sim)
     nsteps = 25
-    u, v, tu, tv, _ = eng.run(u0, v0, dt, nsteps, every)
+    u, v, tu, tv, _ = eng.run(u0, v0, dt, nsteps, every, step=0)
     nf = nsteps // every + 1 + (1 if nsteps % every else 0)
     assert len(tu) == nf and len(tv) == nf
     assert np.array_equal(tu[0], u0) and np.array_equal(tv[0], v0)
     assert np.array_equal(tu[-1], u) and np.array_equal(tv[-1], v)
     # saving changes nothing: the same run without frames
-    u1, v1, _, _, _ = eng.run(u0, v0, dt, nsteps, 0, save_trajectory=False)
+    u1, v1, _, _, _ = eng.run(u0, v0, dt, nsteps, 0, save_trajectory=False, step=0)
     assert np.array_equal(u1, u) and np.array_equal(v1, v)
     # frame j is the state after j * every steps
     for j in sorted({1, 2, nsteps // every}):
-        uj, vj, _, _, _ = eng.run(u0, v0, dt, j * every, 0, save_trajectory=False)
+        uj, vj, _, _, _ = eng.run(u0, v0, dt, j * every, 0, save_trajectory=False, step=0)
         assert np.array_equal(tu[j], uj), (kind, every, j)
         assert np.array_equal(tv[j], vj), (kind, every, j)
     eng.close()
@@ -70,9 +70,33 @@ def test_run_frames_long_run(gpu):
     48 MB): a frame in the middle matches the end of a run without frames."""
     sim, eng, dt = _engine("lj_cluster")
     u0, v0 = S.state(sim)
-    u, v, tu, tv, st = eng.run(u0, v0, dt, 2000, 1)
+    u, v, tu, tv, st = eng.run(u0, v0, dt, 2000, 1, step=0)
     assert len(tu) == 2001
-    uj, _, _, _, _ = eng.run(u0, v0, dt, 1234, 0, save_trajectory=False)
+    uj, _, _, _, _ = eng.run(u0, v0, dt, 1234, 0, save_trajectory=False, step=0)
     assert np.array_equal(tu[1234], uj)
     assert np.array_equal(tu[-1], u)
+    eng.close()
+
+
+@pytest.mark.parametrize("kind", ["lj_cluster", "lj_graph", "water", "gravity", "langevin"])
+def test_run_frames_match_oracle_frames(gpu, oracle, kind):
+    """save_every frames of nbg_run against the oracle's frames of the same
+    run (the reference's saved solution, nbody_simulation_result.jl:480-487):
+    positions within the trajectory tolerance of the parity tests (1e-8 of
+    the coordinate scale after 20 steps; 1e-7 for Langevin), velocities
+    within 1e-5 relative RMS (FP32 pair forces); the Langevin frames use the
+    same Philox draws."""
+    sim, eng, dt = _engine(kind)
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    nsteps, every = 20, 5
+    u, v, tu, tv, _ = eng.run(u0, v0, dt, nsteps, every, step=0)
+    uo, vo, tuo, tvo = oracle.run(desc, u0, v0, dt, nsteps, every, trajectory=True)
+    assert len(tu) == len(tuo) == nsteps // every + 1
+    scale = max(np.abs(tuo).max(), 1.0)
+    # Euler-Maruyama's FP32 Box-Muller normals add ~1e-7 relative noise errors
+    tol = 1e-7 if kind == "langevin" else 1e-8
+    for j in range(len(tu)):
+        assert np.abs(tu[j] - tuo[j]).max() <= tol * scale, (kind, j, np.abs(tu[j] - tuo[j]).max())
+        assert S.rel_rmse(tv[j], tvo[j]) <= 1e-5, (kind, j, S.rel_rmse(tv[j], tvo[j]))
     eng.close()

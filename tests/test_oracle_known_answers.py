@@ -510,6 +510,23 @@ def test_default_adaptive_run_closes_the_figure_eight(oracle):
     assert np.abs(tu[-1] - tu[0]).max() <= 0.1
 
 
+def test_adaptive_frames_feed_msd_and_interpolation(oracle):
+    """The adaptive path's frames are one (frames, cols, 3) array like the
+    fused path's, so msd (nbody_simulation_result.jl:730-783) and the
+    interpolation between saved times work on its result."""
+    sim = S.figure8()
+    t, tu, tv, nacc = _adaptive(oracle, sim)
+    sr = nbg.SimulationResult(nbg.simulation.Solution(t, tu, tv, nacc), sim)
+    assert sr.solution.u.shape == (len(t), 3, 3)
+    ts, m = nbg.msd(sr)
+    U = np.stack(tu)
+    ref = ((U - U[0]) ** 2).sum(axis=2).mean(axis=1)
+    assert np.array_equal(ts, t) and m[0] == 0.0 and np.allclose(m, ref, rtol=0, atol=0)
+    mid = 0.5 * (t[3] + t[4])
+    p = nbg.get_position(sr, mid)
+    assert p.shape == (3, 3) and np.all(np.isfinite(p))
+
+
 def test_default_adaptive_run_closes_the_charge_orbit(oracle):
     """electrostatics_test.jl:7-29, with run_simulation(simulation)'s default
     adaptive method: back at the start after one period within 0.1 r."""

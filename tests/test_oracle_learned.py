@@ -79,3 +79,32 @@ def test_training_gradient_is_loss_gradient():
         tm[p] -= h
         fd = (LO.train_gradients(tp, X, y)[0] - LO.train_gradients(tm, X, y)[0]) / (2 * h)
         assert abs(fd - grad[p]) <= 1e-6 * max(1.0, abs(grad[p])), (p, fd, grad[p])
+
+
+def test_sampled_forces_and_labels_equal_full_rows(small_box):
+    """forces_on / labels_on (the sampled forms the full-size GPU checks use)
+    give the rows of forces / short_range_labels of the whole box."""
+    u, L, q = small_box
+    D = np.array([LO.descriptor(u, L, i)[0] for i in range(len(u))])
+    E, F = LO.short_range_labels(u, L, q, 0.650299, 0.3165492, 138.935458)
+    th = [_params(7, D, E), _params(8, D, E)]
+    _, Ff = LO.forces(u, L, th)
+    idx = np.array([0, 1, 2, 50, 97, 191])
+    Fs = LO.forces_on(u, L, th, idx)
+    assert np.abs(Fs - Ff[idx]).max() <= 1e-10 * np.abs(Ff).max()
+    Es, Fl = LO.labels_on(u, L, q, 0.650299, 0.3165492, 138.935458, idx)
+    assert np.array_equal(Es, E[idx]) and np.array_equal(Fl, F[idx])
+
+
+def test_oracle_partial_accel_rows_of_water(small_box):
+    """oracle_partial_accel over whole molecules (with their angle terms)
+    equals the rows of the full right-hand side."""
+    import systems as S
+    sim = S.water_box(64, seed=5)
+    desc, keep = S.nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    oracle = g.load_oracle()
+    a, _ = oracle.accel(desc, v.copy(), u)
+    for i0, i1 in ((0, 30), (99, 192)):
+        p = oracle.partial_accel(desc, u, i0, i1)
+        assert np.abs(p - a[i0:i1]).max() <= 1e-12 * np.abs(a).max()

@@ -294,6 +294,13 @@ NBG_API int nbg_cluster_shape(nbg_ctx* ctx, int32_t* ctas, int32_t* lanes);
 NBG_API int nbg_gravity_accel_noalloc(const double* x, const double* mass, int64_t n, double G, double* a,
                                       void* stream);
 
+/* The Verlet-list force kernel's current form (no reference counterpart):
+   *lanes = lanes per atom (1: a thread per atom), *fixed_point = 1 when the
+   fixed-point kernel with its lists staged into shared memory by the tensor
+   memory accelerator runs, 0 for the split-position kernels. Either pointer
+   may be NULL. NBG_ERR_UNSUPPORTED off the list path. */
+NBG_API int nbg_force_form(nbg_ctx* ctx, int32_t* lanes, int32_t* fixed_point);
+
 /* Measured FP32 FMA throughput of a device in TFLOP/s (an FMA counts 2):
    the roofline denominator of the FP32-bound gravity kernel. */
 NBG_API int nbg_probe_fp32_peak(int device, double* tflops);

@@ -8,7 +8,7 @@
 // (:353-372); angles sum k (theta - theta0)^2 / 2 (:374-397); gravity
 // -G sum_{i<j} m_i m_j / r (this project's; the reference has none).
 // Per-block partials are summed by the host in block order (deterministic).
-#include "nbg_internal.cuh"
+#include "fx_pair.cuh"
 
 #define EB 128
 
@@ -242,20 +242,40 @@ int launch_energy(nbg_ctx* c, const StateView& s, double* out_host)
 }
 
 // Pair-set export: every ordered pair the force kernels count as inside the
-// cutoff of `which` (NBG_POT_LJ or NBG_POT_EL), same classification code.
-__global__ void k_pairs(Dev d, StateView s, int which, int use_list, int* out_j, int* out_cnt, int64_t cap)
+// cutoff of `which` (NBG_POT_LJ or NBG_POT_EL), same classification code
+// (fx: the fixed-point kernel's, fx_pair.cuh; else pair_cutoff's).
+__global__ void k_pairs(Dev d, StateView s, int which, int use_list, int fx, int* out_j, int* out_cnt, int64_t cap)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
         const RepDev& R = d.reps[d.rep_of[i]];
         float4 hi = d.phi[i], lo = d.plo[i];
         int64_t cnt = 0;
         int64_t m = use_list ? d.nbr_count[i] : (R.atom0 + R.n);
+        const bool water = d.kind == NBG_SYSTEM_WATER;
+        const bool lj_i = (d.pots & NBG_POT_LJ) && (!water || (i % 3) == 0);
         for (int64_t k = use_list ? 0 : R.atom0; k < m; ++k) {
             int64_t j = use_list ? d.nbr[k * d.nbr_kstride + i * d.nbr_istride] : k;
             if (j == i) continue;
-            PairOut o = pair_cutoff(d, R, PairK(R), i, j, hi, lo, d.phi[j], d.plo[j], 0.0f, s.x);
-            if (o.range_err) status_set(d.status, ST_RANGE);
-            bool in = which == NBG_POT_LJ ? o.lj_in : o.el_in;
+            bool in;
+            if (fx) {
+                const bool lp = lj_i && (!water || fx_oxygen((int)j));
+                const bool ep = (d.pots & NBG_POT_EL) != 0;
+                float dx, dy, dz;
+                const float r2 = fx_r2(d.pfx[i], d.pfx[j], dx, dy, dz);
+                bool lj_in, el_in, amb;
+                fx_classify(r2, lp, ep, R.fx_lj_lo, R.fx_lj_hi, R.fx_el_lo, R.fx_el_hi, lj_in, el_in, amb);
+                if (amb) {
+                    const FxPair o = fx_pair_fallback(d, s.x, i, j, lp, ep);
+                    if (o.range_err) status_set(d.status, ST_RANGE);
+                    lj_in = o.lj_in;
+                    el_in = o.el_in;
+                }
+                in = which == NBG_POT_LJ ? lj_in : el_in;
+            } else {
+                PairOut o = pair_cutoff(d, R, PairK(R), i, j, hi, lo, d.phi[j], d.plo[j], 0.0f, s.x);
+                if (o.range_err) status_set(d.status, ST_RANGE);
+                in = which == NBG_POT_LJ ? o.lj_in : o.el_in;
+            }
             if (in) {
                 if (cnt < cap) out_j[i * cap + cnt] = (int)j;
                 ++cnt;
@@ -267,8 +287,8 @@ __global__ void k_pairs(Dev d, StateView s, int which, int use_list, int* out_j,
 
 int launch_pairs(nbg_ctx* c, const StateView& s, int which, int* out_j, int* out_cnt, int64_t cap_per_atom)
 {
-    k_pairs<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s, which, c->path == PATH_LIST ? 1 : 0, out_j, out_cnt,
-                                                        cap_per_atom);
+    k_pairs<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s, which, c->path == PATH_LIST ? 1 : 0,
+                                                        c->fx_ready ? 1 : 0, out_j, out_cnt, cap_per_atom);
     NBG_LAUNCH_CHECK(c, "k_pairs");
     return NBG_OK;
 }

@@ -689,6 +689,7 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
 
 int launch_force_list(nbg_ctx* c, const StateView& s)
 {
+    if (c->fx_ready) return launch_force_fx(c, s);
     const int lpa = c->list_lpa;
     prof_begin(c);
     if (lpa <= 1) {

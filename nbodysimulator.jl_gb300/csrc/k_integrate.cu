@@ -15,7 +15,7 @@
 __global__ void k_pack(Dev d, const double* X)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x)
-        pack_atom(d, i, X);
+        pack_atom<true>(d, i, X);
 }
 
 int launch_pack(nbg_ctx* c, const StateView& s)

@@ -173,6 +173,23 @@ static void set_list_layout(nbg_ctx* c)
     }
 }
 
+// The list force kernel's form for the current lanes per atom and list
+// buffer: the fixed-point kernel where it fits, and whether the steps must
+// also keep the split positions current (the split-form kernels or the
+// learned model read them every step). Captured graphs hold the old form.
+static int set_force_form(nbg_ctx* c)
+{
+    set_list_layout(c);
+    int st = fx_prepare(c);
+    if (st) return st;
+    c->d.split_on = (!c->fx_ready || c->ml_on) ? 1 : 0;
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    return NBG_OK;
+}
+
 static int alloc_lists(nbg_ctx* c, int cell_cap, int nbr_cap)
 {
     int st;
@@ -184,8 +201,7 @@ static int alloc_lists(nbg_ctx* c, int cell_cap, int nbr_cap)
     if ((st = dalloc(c, &c->d.nbr, (size_t)c->n * nbr_cap))) return st;
     c->d.cell_cap = cell_cap;
     c->d.nbr_cap = nbr_cap;
-    set_list_layout(c);
-    return NBG_OK;
+    return set_force_form(c);
 }
 
 static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
@@ -250,6 +266,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         D.el_crf = std::isfinite(d0->el_cutoff) ? 1.0 / d0->el_cutoff : 0.0;
     }
     D.el_krf2 = (float)(2.0 * D.el_krf);
+    D.split_on = 1;
     D.G = d0->grav_G;
     D.mu4pi = d0->mag_mu_4pi;
     D.kb = d0->kb;
@@ -301,6 +318,27 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
             double R2 = d0->el_cutoff * d0->el_cutoff;
             R.el_lo = f_down(std::min(R2 * (1.0 - m), img2));
             R.el_hi = f_up(R2 * (1.0 + m));
+        }
+        if (d->bc == NBG_BC_CUBIC) {
+            // fixed-point box units u = L / 2^32 (the same bands, in u^2)
+            const double L = d->box[0];
+            const double u = L / 4294967296.0, iu2 = 1.0 / (u * u);
+            R.fx_scale = 4294967296.0 / L;
+            const double hb = 2147483648.0 * (1.0 - m), img2b = hb * hb;
+            if (pots & NBG_POT_LJ) {
+                const double R2 = d0->lj_cutoff * d0->lj_cutoff * iu2;
+                R.fx_lj_lo = f_down(std::min(R2 * (1.0 - m), img2b));
+                R.fx_lj_hi = f_up(R2 * (1.0 + m));
+                R.fx_sig2 = (float)(d0->lj_sigma * d0->lj_sigma * iu2);
+                R.fx_ljf = (float)(24.0 * d0->lj_epsilon / u);
+            }
+            if (pots & NBG_POT_EL) {
+                const double R2 = d0->el_cutoff * d0->el_cutoff * iu2;
+                R.fx_el_lo = f_down(std::min(R2 * (1.0 - m), img2b));
+                R.fx_el_hi = f_up(R2 * (1.0 + m));
+                R.fx_el1 = (float)iu2;
+                R.fx_el2 = (float)(2.0 * D.el_krf * u);
+            }
         }
         if (c->path == PATH_LIST) {
             double rl = list_radius(d);
@@ -441,6 +479,20 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     if ((st = dalloc(c, &c->kick_counter, 1))) return st;
 
     if (c->path == PATH_LIST) {
+        // fixed-point positions, w = the FP32 charge (static)
+        if (n < ((int64_t)1 << 31) && !getenv("NBG_NO_FX")) {
+            if ((st = dalloc(c, &D.pfx, n))) return st;
+            std::vector<uint4> q(n);
+            for (int64_t i = 0; i < n; ++i) {
+                const float qf = (float)c->charge_h[i];
+                uint32_t w;
+                memcpy(&w, &qf, sizeof w);
+                q[i] = make_uint4(0u, 0u, 0u, w);
+            }
+            CK(cudaMemcpy(D.pfx, q.data(), sizeof(uint4) * n, cudaMemcpyHostToDevice), "pfx init");
+        } else {
+            c->fx_disabled = true;
+        }
         if ((st = dalloc(c, &D.cell_count, D.ncell_total))) return st;
         if ((st = dalloc(c, &D.cell_n, D.ncell_total))) return st;
         if ((st = dalloc(c, &D.nbr_count, n))) return st;
@@ -597,6 +649,15 @@ extern "C" int nbg_force_kernel_time(nbg_ctx* c, double* total_ms, int64_t* laun
     *launches = c->prof_count;
     c->prof_ms = 0.0;
     c->prof_count = 0;
+    return NBG_OK;
+}
+
+extern "C" int nbg_force_form(nbg_ctx* c, int32_t* lanes, int32_t* fixed_point)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (c->path != PATH_LIST) return fail(c, NBG_ERR_UNSUPPORTED, "the force form applies to the Verlet-list path");
+    if (lanes) *lanes = c->list_lpa;
+    if (fixed_point) *fixed_point = c->fx_ready ? 1 : 0;
     return NBG_OK;
 }
 
@@ -1449,6 +1510,7 @@ extern "C" int nbg_ml_enable(nbg_ctx* c)
     if ((st = dalloc(c, &c->ml_judge, 2 * c->ml_judge_cap))) return st;
     if ((st = launch_mlp_attrs(c))) return st;
     c->ml_on = true;
+    if ((st = set_force_form(c))) return st;  // the learned kernels read the split positions every step
     for (int s = 0; s < 2; ++s)
         if ((st = launch_ml_pack(c, s))) return st;
     CK(cudaStreamSynchronize(c->stream), "ml enable sync");
@@ -2005,7 +2067,7 @@ extern "C" int nbg_autotune(nbg_ctx* c, int32_t reps, int32_t* lpa_out, double* 
     int st = NBG_OK;
     for (int k = 0; k < 5 && st == NBG_OK; ++k) {
         c->list_lpa = cands[k];
-        set_list_layout(c);
+        if ((st = set_force_form(c))) break;
         if ((st = clear_status(c))) break;
         if ((st = launch_pack(c, c->st))) break;
         if ((st = launch_list_build(c, c->st, true, StepRef{c->step, nullptr}))) break;
@@ -2034,12 +2096,9 @@ extern "C" int nbg_autotune(nbg_ctx* c, int32_t reps, int32_t* lpa_out, double* 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->list_lpa = st == NBG_OK ? best : keep;
-    set_list_layout(c);
+    const int st2 = set_force_form(c);  // (drops captured launches of the previous form)
+    if (st == NBG_OK) st = st2;
     resident_dirty(c);  // the next step rebuilds the list in the chosen layout
-    if (c->graph) {     // captured launches hold the previous form
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-    }
     if (lpa_out) *lpa_out = c->list_lpa;
     return st;
 }

@@ -61,6 +61,15 @@ struct RepDev {
     double sigma_num;   // sqrt(2 gamma kb T) (water)
     double ndf;         // 3N - Nc
     uint64_t seed;
+    // fixed-point box coordinates (list path, cubic): q = x / L * 2^32 mod 2^32,
+    // so a 32-bit wrapping difference is the minimum image in box units
+    // u = L / 2^32; every FP32 constant below is in those units
+    double fx_scale;             // 2^32 / L
+    float fx_lj_lo, fx_lj_hi;    // classification bands of r^2 (as lj_lo / lj_hi)
+    float fx_el_lo, fx_el_hi;
+    float fx_sig2;               // sigma^2 / u^2
+    float fx_ljf;                // 24 eps / u: LJ force = fx_ljf (2 s^12 - s^6) / r^2 d
+    float fx_el1, fx_el2;        // 1 / u^2 and 2 k_rf u: EL force = k q_i q_j (rinv^3 el1 - el2) d
 };
 
 // Everything a kernel needs, passed by value.
@@ -99,6 +108,10 @@ struct Dev {
     const RepDev* reps;
     float4* phi;
     float4* plo;
+    // fixed-point positions (x, y, z as 32-bit box fractions, w the charge's
+    // FP32 bits) for the list force kernel; null where it is not used
+    uint4* pfx;
+    int split_on;       // the steps also refresh phi / plo (their per-step readers run)
     // lists
     int* cell_count;
     int* cell_n;
@@ -197,6 +210,13 @@ struct nbg_ctx {
     float grav_far2 = 256.f;    // a tile pair is far when (F g)^2 >= max|r|^2, F = 16
     double grav_m0 = 0.0;
     int list_lpa = 0;         // lanes per atom of k_force_list (1 = thread per atom)
+    // the fixed-point, list-staged force kernel (k_force_fx.cu): its tensor
+    // map of the list, grid and shared memory for the current form
+    alignas(64) unsigned char fx_map[128];
+    bool fx_ready = false;     // it runs (else the split-form kernels do)
+    bool fx_disabled = false;  // NBG_NO_FX: the split-form kernels only
+    int fx_grid = 0, fx_nbox = 0;
+    size_t fx_smem = 0;
     double* grav_part = nullptr;
     // compensated gravity: bodies re-sorted along a Morton curve every 8th
     // evaluation; far tile pairs take the plain FP32 difference
@@ -283,6 +303,8 @@ int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps,
 int launch_allpairs(nbg_ctx* c, const StateView& s);
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
 int launch_force_list(nbg_ctx* c, const StateView& s);
+int fx_prepare(nbg_ctx* c);
+int launch_force_fx(nbg_ctx* c, const StateView& s);
 int launch_bonded(nbg_ctx* c, const StateView& s);
 int launch_drift(nbg_ctx* c, const StateView& s, double dt, StepRef pos);
 int launch_temperature(nbg_ctx* c, const double* v);
@@ -562,9 +584,33 @@ __device__ __forceinline__ void split_position_image(const RepDev& R, const doub
     }
 }
 
+// Fixed-point box coordinate: x / L * 2^32 rounded, modulo 2^32 (the wrap
+// into the box is the integer truncation; exact to 2^-21 of a unit for
+// positions within 1024 boxes of the origin).
+__device__ __forceinline__ unsigned fx_coord(double x, double scale)
+{
+    return (unsigned)(unsigned long long)__double2ll_rn(__dmul_rn(x, scale));
+}
+
+__device__ __forceinline__ void pack_fx(const Dev& d, const RepDev& R, int64_t i, const double* X)
+{
+    uint4 q;
+    q.x = fx_coord(X[3 * i], R.fx_scale);
+    q.y = fx_coord(X[3 * i + 1], R.fx_scale);
+    q.z = fx_coord(X[3 * i + 2], R.fx_scale);
+    q.w = d.pfx[i].w;
+    d.pfx[i] = q;
+}
+
+// ALL: refresh every position form (on-demand evaluations); otherwise the
+// steps write the fixed-point form and the split form only when its per-step
+// readers run (split_on).
+template <bool ALL = false>
 __device__ __forceinline__ void pack_atom(const Dev& d, int64_t i, const double* X)
 {
     const RepDev& R = d.reps[d.rep_of[i]];
+    if (d.pfx) pack_fx(d, R, i, X);
+    if (!ALL && !d.split_on) return;
     const double p[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
     float h[3], l[3];
     if (d.img && d.bc == NBG_BC_CUBIC) split_position_image(R, p, d.img + 3 * i, h, l);

@@ -156,6 +156,16 @@ class Engine:
             self._chk(used)
         return (ctas.value, lanes.value) if used == 1 else None
 
+    def force_form(self):
+        """(lanes per atom, fixed-point list-staged kernel?) of the Verlet-list
+        force kernel, or None off the list path."""
+        lanes, fx = ctypes.c_int32(), ctypes.c_int32()
+        st = self.lib.nbg_force_form(self.ctx, ctypes.byref(lanes), ctypes.byref(fx))
+        if st == -6:  # NBG_ERR_UNSUPPORTED: not on the list path
+            return None
+        self._chk(st)
+        return lanes.value, bool(fx.value)
+
     def force_kernel_time(self):
         """(summed ms, launches) of the dominant force kernel since the last call."""
         ms = ctypes.c_double()

@@ -2,6 +2,7 @@
 same seeded inputs: forces within the relative-RMSE tolerance of 1e-5, the
 cutoff pair sets bit for bit, energies, thermostat terms and trajectories."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -74,8 +75,11 @@ def test_lj_forces_and_pair_set(gpu, oracle, flags):
     assert pg.shape == po.shape and np.array_equal(pg, po)
 
 
-def test_lj_pair_set_at_cutoff_boundary(gpu, oracle):
-    """Pairs placed within a few ulps of r = R: the FP64 re-check decides."""
+@pytest.mark.parametrize("lanes", [None, "4", "32"])
+def test_lj_pair_set_at_cutoff_boundary(gpu, oracle, lanes):
+    """Pairs placed within a few ulps of r = R: the FP64 re-check decides
+    (the split-position classification of a thread per atom, and the
+    fixed-point one of the lanes-per-atom kernel)."""
     R = 2.5
     L = 10.0
     eps = np.finfo(np.float64).eps
@@ -91,10 +95,21 @@ def test_lj_pair_set_at_cutoff_boundary(gpu, oracle):
     sim = nbg.NBodySimulation(system, (0.0, 1.0), nbg.CubicPeriodicBoundaryConditions(L), kb=1.0, skin=0.3)
     desc, keep = nbg.system_descriptor(sim)
     u, v = S.state(sim)
-    eng = nbg.Engine(desc, 0)
+    if lanes:
+        os.environ["NBG_LIST_LPA"] = lanes
+    try:
+        eng = nbg.Engine(desc, 0)
+    finally:
+        os.environ.pop("NBG_LIST_LPA", None)
+    form = eng.force_form()
+    assert form == ((int(lanes), True) if lanes else (1, False)), form
     pg = eng.pair_list(u, nbg._abi.NBG_POT_LJ)
     po = oracle.pair_list(desc, u, nbg._abi.NBG_POT_LJ)
     assert np.array_equal(pg, po)
+    # the forces count exactly those pairs
+    ag = eng.accel(v.copy(), u)
+    ar, _ = oracle.accel(desc, v.copy(), u)
+    assert np.abs(ag - ar).max() <= 1e-5 * np.abs(ar).max()
 
 
 def test_coulomb_unbounded_forces(gpu, oracle):

@@ -95,7 +95,8 @@ def _ref_water_langevin(T0=275.0, gamma=100.0, n_mol=216, seed=5):
     v_dev = (S.KB_KJ * w["T"] / mH2O) ** 0.5
     bodies = nbg.generate_bodies_in_cell_nodes(n_mol, mH2O, v_dev, L, rng=np.random.default_rng(seed))
     water = nbg.WaterSPCFw(bodies, w["mH"], w["mO"], w["qH"], w["qO"], lj, el, spc)
-    return nbg.NBodySimulation(water, (0.0, 200 * w["tau"]), nbg.CubicPeriodicBoundaryConditions(L),
+    # t2 = 200 tau' with tau' = 0.5e-4 ps, stepped at dt = tau = 0.5e-3 ps: 20 steps
+    return nbg.NBodySimulation(water, (0.0, 200 * 0.5e-4), nbg.CubicPeriodicBoundaryConditions(L),
                                nbg.LangevinThermostat(T0, gamma), S.KB_KJ), w["tau"]
 
 
@@ -113,7 +114,8 @@ def test_water_langevin_em_matches_oracle(gpu, oracle):
 
 def test_water_langevin_thermostating(gpu):
     """test/water_test.jl:136-153: 216 molecules, LangevinThermostat(275, 100),
-    EM at dt = tau for 200 steps: |T(t2) - T0| / T0 within 1."""
+    EM at dt = tau = 0.5 fs up to t2 = 10 fs (20 steps): |T(t2) - T0| / T0
+    within 1."""
     sim, tau = _ref_water_langevin()
     result = nbg.run_simulation(sim, nbg.EM(), dt=tau)
     T2 = nbg.temperature(result, sim.tspan[1])

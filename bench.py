@@ -759,19 +759,37 @@ def main():
         e2e_steps = max(3, min(args.steps, 50 if args.workload == "gravity" else 200))
         eng.accel(vh, uh, out=ah)
         torch.cuda.synchronize()
+        # the host loop of SciML's velocity Verlet around the drop-in: numpy
+        # in-place passes over the pinned arrays (no temporaries), one
+        # nbg_accel per step through the C ABI
+        tmp = np.empty_like(uh)
+        accel = eng.lib.nbg_accel
+        ctx = eng.ctx
+        p_v, p_u = nbg._abi.as_dptr(vh), nbg._abi.as_dptr(uh)
+        p_a = [nbg._abi.as_dptr(ah), nbg._abi.as_dptr(anh)]
+        arrs = [ah, anh]
+        hdt, hdt2 = 0.5 * dt, 0.5 * dt * dt
         t0 = time.perf_counter()
+        cur = 0
         for s in range(e2e_steps):
-            # u += dt v + dt^2/2 a ; a' = accel(u) ; v += dt/2 (a + a'): in-place
-            # passes over the pinned host arrays on torch's CPU threads
-            ut.add_(vt, alpha=dt).add_(at, alpha=0.5 * dt * dt)
-            eng.accel(vh, uh, out=anh)
-            vt.add_(at, alpha=0.5 * dt).add_(ant, alpha=0.5 * dt)
-            at, ant, ah, anh = ant, at, anh, ah
+            a_old, a_new = arrs[cur], arrs[cur ^ 1]
+            # u += dt v + dt^2/2 a ; a' = accel(u) ; v += dt/2 (a + a')
+            np.multiply(vh, dt, out=tmp)
+            np.add(uh, tmp, out=uh)
+            np.multiply(a_old, hdt2, out=tmp)
+            np.add(uh, tmp, out=uh)
+            st = accel(ctx, p_a[cur ^ 1], p_v, p_u, 0.0)
+            if st != 0:
+                raise nbg.EngineError(st, "nbg_accel")
+            np.add(a_old, a_new, out=tmp)
+            np.multiply(tmp, hdt, out=tmp)
+            np.add(vh, tmp, out=vh)
+            cur ^= 1
         e2e_s = time.perf_counter() - t0
         e2e = {"value": n * e2e_steps * world / e2e_s, "unit": "atom-steps/s",
                "h2d_bytes_per_step": (2 if v_read else 1) * uh.nbytes, "d2h_bytes_per_step": ah.nbytes,
                "path": "nbg_accel (RHS drop-in) per step from pinned host buffers, velocity-Verlet update on host",
-               "host_threads": torch.get_num_threads(), "steps": e2e_steps}
+               "host_update": "numpy in place, one thread", "steps": e2e_steps}
     elif not args.no_e2e and batch:
         # the batch's public call: nbg_run from (pageable) host buffers, state in and out
         t0 = time.perf_counter()

@@ -219,9 +219,18 @@ NBG_API int nbg_get_accel(nbg_ctx* ctx, double* dv);
  * (run_simulation(sim, VelocityVerlet(), dt=dt), nbody_simulation_result.jl:
  * 468-487), applying the thermostat. With NBG_THERMO_LANGEVIN it advances the
  * first-order SDE with Euler-Maruyama instead (calculate_simulation_sde,
- * :489-492). No host traffic; asynchronous on the context's stream.
+ * :489-492). No host traffic; asynchronous on the context's stream: the call
+ * returns once its steps are queued, without waiting for them. Steps run in
+ * chunks of 512 whose status word is read before the next chunk; the last
+ * chunk's status is read by the next call on the context (or nbg_sync), which
+ * returns that chunk's error, or, after a list overflow, undoes the chunk,
+ * grows the lists and runs it again before doing its own work.
  */
 NBG_API int nbg_advance(nbg_ctx* ctx, double dt, int64_t nsteps);
+
+/* Wait for the context's queued work and return the status of its last
+   nbg_advance (see there). */
+NBG_API int nbg_sync(nbg_ctx* ctx);
 
 /*
  * Host-buffer driver: upload u, v; take nsteps steps; every save_every steps

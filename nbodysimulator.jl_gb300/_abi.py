@@ -134,6 +134,7 @@ SIGNATURES = {
     "nbg_compute_forces": (ctypes.c_int, [_vp]),
     "nbg_get_accel": (ctypes.c_int, [_vp, _dp]),
     "nbg_advance": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int64]),
+    "nbg_sync": (ctypes.c_int, [_vp]),
     "nbg_run": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int64, ctypes.c_int64,
                                _dp, _dp, ctypes.POINTER(NbgRunStats)]),
     "nbg_energy": (ctypes.c_int, [_vp, _dp, _dp, ctypes.POINTER(NbgEnergies)]),

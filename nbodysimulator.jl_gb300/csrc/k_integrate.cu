@@ -442,6 +442,20 @@ int launch_step_advance(nbg_ctx* c, int64_t by)
     return NBG_OK;
 }
 
+int launch_counter_advance(nbg_ctx* c, int64_t* counter, int64_t by)
+{
+    k_step_advance<<<1, 1, 0, c->stream>>>(counter, by);
+    NBG_LAUNCH_CHECK(c, "k_step_advance");
+    return NBG_OK;
+}
+
+int launch_pack_disp(nbg_ctx* c, const double* X, StepRef pos)
+{
+    k_pack_disp<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, X, c->path == PATH_LIST ? 1 : 0, pos);
+    NBG_LAUNCH_CHECK(c, "k_pack_disp");
+    return NBG_OK;
+}
+
 int launch_set_step(nbg_ctx* c, int64_t value)
 {
     k_set_step<<<1, 1, 0, c->stream>>>(c->d.step_dev, value);

@@ -41,6 +41,14 @@ static int fail(nbg_ctx* c, int code, const std::string& msg)
     } while (0)
 
 static int plan_cluster(nbg_ctx* c);
+static int settle(nbg_ctx* c);
+// entry of a context call: the device current, any deferred step status read
+#define NBG_ENTER(c)                           \
+    do {                                       \
+        cudaSetDevice((c)->device);            \
+        int _settled = settle(c);              \
+        if (_settled) return _settled;         \
+    } while (0)
 
 template <typename T>
 static int dalloc(nbg_ctx* c, T** p, size_t count)
@@ -187,6 +195,11 @@ static int set_force_form(nbg_ctx* c)
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;
     }
+    if (c->accel_graph) {
+        cudaGraphExecDestroy(c->accel_graph);
+        c->accel_graph = nullptr;
+    }
+    c->accel_lists_valid = false;
     return NBG_OK;
 }
 
@@ -399,10 +412,12 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     // state
     StateView* views[2] = {&c->st, &c->ev};
     for (StateView* sv : views) {
-        if ((st = dalloc(c, &sv->x, 3 * c->cols))) return st;
-        if ((st = dalloc(c, &sv->v, 3 * c->cols))) return st;
-        if ((st = dalloc(c, &sv->a_old, 3 * c->cols))) return st;
-        if ((st = dalloc(c, &sv->a_new, 3 * c->cols))) return st;
+        double* blk = nullptr;  // x, v, a_old, a_new in one allocation (one-copy backups)
+        if ((st = dalloc(c, &blk, 12 * (size_t)c->cols))) return st;
+        sv->x = blk;
+        sv->v = blk + 3 * c->cols;
+        sv->a_old = blk + 6 * c->cols;
+        sv->a_new = blk + 9 * c->cols;
     }
     // gravity bodies padded to a multiple of the largest i-block (4 x 128)
     c->npad = c->path == PATH_GRAVITY ? ((n + 511) / 512) * 512 : n;
@@ -632,7 +647,7 @@ static void prof_drain(nbg_ctx* c)
 extern "C" int nbg_set_profiling(nbg_ctx* c, int on)
 {
     if (!c) return NBG_ERR_ARG;
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     prof_drain(c);
     c->profiling = on != 0;
     c->prof_ms = 0.0;
@@ -643,7 +658,7 @@ extern "C" int nbg_set_profiling(nbg_ctx* c, int on)
 extern "C" int nbg_force_kernel_time(nbg_ctx* c, double* total_ms, int64_t* launches)
 {
     if (!c || !total_ms || !launches) return NBG_ERR_ARG;
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     prof_drain(c);
     *total_ms = c->prof_ms;
     *launches = c->prof_count;
@@ -674,6 +689,10 @@ static void release(nbg_ctx* c)
     prof_drain(c);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
+    if (c->accel_graph) cudaGraphExecDestroy(c->accel_graph);
+    c->accel_graph = nullptr;
+    if (c->hst) cudaFreeHost(c->hst);
+    c->hst = nullptr;
     if (c->frames) cudaFree(c->frames);
     c->frames = nullptr;
     c->frames_cap = 0;
@@ -745,6 +764,7 @@ extern "C" void nbg_destroy(nbg_ctx* c)
 {
     if (!c) return;
     cudaSetDevice(c->device);
+    if (c->pending) cudaStreamSynchronize(c->stream);  // queued steps end before the buffers go
     if (c->stream) cudaStreamSynchronize(c->stream);
     release(c);
     delete c;
@@ -753,6 +773,7 @@ extern "C" void nbg_destroy(nbg_ctx* c)
 extern "C" int nbg_set_stream(nbg_ctx* c, void* s)
 {
     if (!c) return NBG_ERR_ARG;
+    NBG_ENTER(c);  // deferred steps on the previous stream settle first
     c->stream = s ? (cudaStream_t)s : c->own_stream;
     return NBG_OK;
 }
@@ -814,7 +835,7 @@ static int grow_lists(nbg_ctx* c, unsigned st)
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;
     }
-    int rc = alloc_lists(c, cell_cap, nbr_cap);
+    int rc = alloc_lists(c, cell_cap, nbr_cap);  // (drops the right-hand-side graph too)
     if (rc) return rc;
     return plan_cluster(c);  // the lists' shared-memory share grew
 }
@@ -851,15 +872,104 @@ static void resident_dirty(nbg_ctx* c)
     c->cluster_lists_valid = false;
 }
 
+// The list path's right-hand side as one captured graph: status clear, the
+// upload of u (and v) from the pinned staging, the packing with the
+// displacement check against the positions of the last build, the list
+// kernels (which rebuild only when flagged), the force kernels, the
+// thermostat term, and the downloads of dv (and the Nose-Hoover rate) and of
+// the status word; a last node advances the call counter whose parity picks
+// the rebuild flags.
+static int accel_graph_capture(nbg_ctx* c, bool v_read)
+{
+    const size_t sb = state_bytes(c);
+    if (!c->hst) {
+        cudaError_t e = cudaMallocHost(&c->hst, 3 * sb + 64);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c->hst = nullptr;
+            return fail(c, NBG_ERR_NOMEM, "pinned staging of the right-hand side: cudaMallocHost failed");
+        }
+    }
+    int st;
+    if (!c->accel_step && (st = dalloc(c, &c->accel_step, 1))) return st;
+    double* hu = c->hst;
+    double* hv = c->hst + 3 * c->cols;
+    double* hdv = c->hst + 6 * c->cols;
+    unsigned* hstat = reinterpret_cast<unsigned*>(c->hst + 9 * c->cols);
+    const int64_t launches0 = c->launches;
+    const StepRef pos{0, c->accel_step};
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "accel capture begin");
+    st = NBG_OK;
+    auto q = [&](cudaError_t e) {
+        if (e != cudaSuccess && st == NBG_OK) st = cuda_fail(c, e, "accel capture");
+    };
+    q(cudaMemsetAsync(c->d.status, 0, sizeof(unsigned), c->stream));
+    q(cudaMemcpyAsync(c->ev.x, hu, sb, cudaMemcpyHostToDevice, c->stream));
+    if (v_read) q(cudaMemcpyAsync(c->ev.v, hv, sb, cudaMemcpyHostToDevice, c->stream));
+    q(cudaMemsetAsync(c->ev.a_new, 0, sb, c->stream));
+    if (st == NBG_OK) st = launch_pack_disp(c, c->ev.x, pos);
+    if (st == NBG_OK) st = forces(c, c->ev, false, pos);
+    if (st == NBG_OK) st = launch_rhs_thermostat(c, c->ev);
+    q(cudaMemcpyAsync(hdv, c->ev.a_new, sb, cudaMemcpyDeviceToHost, c->stream));
+    if (c->d.therm == NBG_THERMO_NOSEHOOVER)
+        q(cudaMemcpyAsync(hv + 3 * c->n, c->ev.v + 3 * c->n, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    q(cudaMemcpyAsync(hstat, c->d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    if (st == NBG_OK) st = launch_counter_advance(c, c->accel_step, 1);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->accel_graph_launches = c->launches - launches0;
+    c->launches = launches0;
+    c->accel_lists_valid = false;  // nothing ran yet: the first replay builds
+    if (st != NBG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "accel capture");
+    e = cudaGraphInstantiate(&c->accel_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->accel_graph = nullptr;
+        return cuda_fail(c, e, "accel graph instantiate");
+    }
+    return NBG_OK;
+}
+
 extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
 {
     (void)t;
     if (!c || !dv || !v || !u) return NBG_ERR_ARG;
-    cudaSetDevice(c->device);
-    CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    NBG_ENTER(c);
     // only the Berendsen and Nose-Hoover terms of the right-hand side read v
-    if (c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER)
-        CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
+    const bool v_read = c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER;
+    if (c->path == PATH_LIST && c->use_graphs && !c->profiling) {
+        resident_dirty(c);
+        c->T_valid = false;
+        for (int attempt = 0; attempt < 6; ++attempt) {
+            int st;
+            if (!c->accel_graph && (st = accel_graph_capture(c, v_read))) return st;
+            const size_t sb = state_bytes(c);
+            memcpy(c->hst, u, sb);
+            if (v_read) memcpy(c->hst + 3 * c->cols, v, sb);
+            if (!c->accel_lists_valid)  // lists of other positions: every replica rebuilds
+                CK(cudaMemsetAsync(c->d.rebuild_flag, 0xff, 2 * sizeof(int) * (size_t)c->nrep, c->stream), "flags");
+            CK(cudaGraphLaunch(c->accel_graph, c->stream), "accel graph launch");
+            c->launches += c->accel_graph_launches;
+            CK(cudaStreamSynchronize(c->stream), "accel sync");
+            const unsigned w = *reinterpret_cast<const unsigned*>(c->hst + 9 * c->cols);
+            if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+            if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
+                if ((st = grow_lists(c, w))) return st;  // (drops the graph: captured again above)
+                continue;
+            }
+            memcpy(dv, c->hst + 6 * c->cols, sb);
+            if (c->d.therm == NBG_THERMO_NOSEHOOVER) v[3 * c->n] = c->hst[3 * c->cols + 3 * c->n];
+            c->accel_lists_valid = true;
+            return status_error(c, w);
+        }
+        return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
+    }
+    CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
+    if (v_read) CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     resident_dirty(c);
     c->T_valid = false;  // the RHS reduces T of its own velocities into red_T
     // the whole evaluation, the download and the status word in one stream
@@ -892,7 +1002,7 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
 extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
 {
     if (!c || !u || !v) return NBG_ERR_ARG;
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     CK(cudaMemcpyAsync(c->st.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
     CK(cudaMemcpyAsync(c->st.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     c->state_valid = true;
@@ -911,7 +1021,7 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
 extern "C" int nbg_get_state(nbg_ctx* c, double* u, double* v)
 {
     if (!c || (!u && !v)) return NBG_ERR_ARG;
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     if (u) CK(cudaMemcpyAsync(u, c->st.x, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "u download");
     if (v) CK(cudaMemcpyAsync(v, c->st.v, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "v download");
     CK(cudaStreamSynchronize(c->stream), "state sync");
@@ -928,6 +1038,7 @@ extern "C" int nbg_get_step(nbg_ctx* c, int64_t* step)
 extern "C" int nbg_set_step(nbg_ctx* c, int64_t step)
 {
     if (!c) return NBG_ERR_ARG;
+    NBG_ENTER(c);
     if (step < 0) return fail(c, NBG_ERR_ARG, "the step counter must be >= 0");
     c->step = step;
     return NBG_OK;
@@ -937,7 +1048,7 @@ extern "C" int nbg_compute_forces(nbg_ctx* c)
 {
     if (!c) return NBG_ERR_ARG;
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     int st;
     if ((st = launch_pack(c, c->st))) return st;
     if ((st = forces(c, c->st, c->steps_since_build < 0, StepRef{c->step, nullptr}))) return st;
@@ -948,7 +1059,7 @@ extern "C" int nbg_compute_forces(nbg_ctx* c)
 extern "C" int nbg_get_accel(nbg_ctx* c, double* dv)
 {
     if (!c || !dv) return NBG_ERR_ARG;
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     CK(cudaMemcpyAsync(dv, c->st.a_new, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "a download");
     CK(cudaStreamSynchronize(c->stream), "accel sync");
     unsigned w = 0;
@@ -960,25 +1071,20 @@ extern "C" int nbg_get_accel(nbg_ctx* c, double* dv)
 // ---------------------------------------------------------------------
 // the step loop
 // ---------------------------------------------------------------------
-struct Backup {
-    double *x = nullptr, *v = nullptr, *a = nullptr;
-};
-
-static int backup_alloc(nbg_ctx* c, Backup& b)
+// The step loop's backup buffer (allocated once per context).
+static int ensure_backup(nbg_ctx* c)
 {
-    int st;
-    if ((st = dalloc(c, &b.x, 3 * c->cols))) return st;
-    if ((st = dalloc(c, &b.v, 3 * c->cols))) return st;
-    if ((st = dalloc(c, &b.a, 3 * c->cols))) return st;
-    return NBG_OK;
+    return c->bk ? NBG_OK : dalloc(c, &c->bk, 12 * (size_t)c->cols);
 }
 
-static void backup_free(nbg_ctx* c, Backup& b)
+// x, v, a_old of the resident state to or from the backup (one copy each way)
+static int backup_state(nbg_ctx* c, bool restore)
 {
-    dfree(c, b.x);
-    dfree(c, b.v);
-    dfree(c, b.a);
-    b = Backup{};
+    const size_t bytes = 3 * sizeof(double) * 3 * (size_t)c->cols;
+    CK(cudaMemcpyAsync(restore ? c->st.x : c->bk, restore ? c->bk : c->st.x, bytes, cudaMemcpyDeviceToDevice,
+                       c->stream),
+       restore ? "restore" : "backup");
+    return NBG_OK;
 }
 
 // EM is the reference's Langevin integrator; BAOAB (flag) and velocity
@@ -1159,12 +1265,42 @@ static int replay_graph(nbg_ctx* c)
 // before copying them out
 #define RUN_FRAME_BYTES ((size_t)1 << 30)
 
-static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
+static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer = false);
+
+// Read the status word of a deferred nbg_advance chunk. After a list
+// overflow the chunk is undone (backup), the lists grow, and it runs again
+// (synchronously); a non-finite, range or timeout status is returned here.
+static int settle(nbg_ctx* c)
+{
+    if (!c->pending) return NBG_OK;
+    c->pending = false;
+    unsigned w = 0;
+    int st;
+    if ((st = read_status(c, &w))) return st;
+    if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
+    if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
+        if ((st = grow_lists(c, w))) return st;
+        if ((st = backup_state(c, true))) return st;
+        c->step = c->pend_step0;
+        c->steps_since_build = -1;
+        c->cluster_lists_valid = false;
+        c->T_valid = false;
+        if ((st = clear_status(c))) return st;
+        if ((st = launch_pack(c, c->st))) return st;
+        return advance_impl(c, c->pend_dt, c->pend_steps, false);
+    }
+    return status_error(c, w);
+}
+
+// defer: leave the status of the last chunk unread (no host synchronisation);
+// the next call on the context settles it.
+static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
 {
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
     if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
     int st;
     c->respa_valid = false;  // a_old becomes the velocity-Verlet acceleration
+    c->accel_lists_valid = false;  // the steps rebuild the lists for the resident positions
     if (c->baoab && c->baoab_dt != dt) {
         // per-replica BAOAB coefficients for this dt (host FP64, uploaded before any capture)
         for (int r = 0; r < c->nrep; ++r) {
@@ -1192,18 +1328,13 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
     const int64_t chunk = can_overflow ? 512 : nsteps;
     // graphs pay off for short steps; events around kernels (profiling) stay direct
     const bool graphs = c->use_graphs && !c->profiling && nsteps >= 2 * graph_period(c);
-    Backup b;
-    if (can_overflow && (st = backup_alloc(c, b))) return st;
+    if (can_overflow && (st = ensure_backup(c))) return st;
     int64_t done = 0;
     int retries = 0;
     while (done < nsteps) {
         int64_t k = std::min<int64_t>(chunk > 0 ? chunk : nsteps, nsteps - done);
-        int64_t step0 = c->step;
-        if (can_overflow) {
-            CK(cudaMemcpyAsync(b.x, c->st.x, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
-            CK(cudaMemcpyAsync(b.v, c->st.v, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
-            CK(cudaMemcpyAsync(b.a, c->st.a_old, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "backup");
-        }
+        const int64_t step0 = c->step;
+        if (can_overflow && (st = backup_state(c, false))) return st;
         int64_t s = 0;
         bool counter_set = false;
         while (s < k) {
@@ -1234,45 +1365,49 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps)
                 ++s;
             }
         }
-        if (st) {
-            backup_free(c, b);
-            return st;
+        if (st) return st;
+        if (defer && done + k == nsteps && can_overflow) {
+            // the last chunk's status is read by the next call (settle)
+            c->pending = true;
+            c->pend_dt = dt;
+            c->pend_steps = k;
+            c->pend_step0 = step0;
+            return NBG_OK;
         }
         unsigned w = 0;
-        if ((st = read_status(c, &w))) { backup_free(c, b); return st; }
-        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) {
-            backup_free(c, b);
-            return status_error(c, w);
-        }
+        if ((st = read_status(c, &w))) return st;
+        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
-            if (++retries > 6) {
-                backup_free(c, b);
-                return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
-            }
-            if ((st = grow_lists(c, w))) { backup_free(c, b); return st; }
-            CK(cudaMemcpyAsync(c->st.x, b.x, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
-            CK(cudaMemcpyAsync(c->st.v, b.v, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
-            CK(cudaMemcpyAsync(c->st.a_old, b.a, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream), "restore");
+            if (++retries > 6) return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
+            if ((st = grow_lists(c, w))) return st;
+            if ((st = backup_state(c, true))) return st;
             c->step = step0;
             c->steps_since_build = -1;
             c->cluster_lists_valid = false;
             c->T_valid = false;
-            if ((st = clear_status(c))) { backup_free(c, b); return st; }
-            if ((st = launch_pack(c, c->st))) { backup_free(c, b); return st; }
+            if ((st = clear_status(c))) return st;
+            if ((st = launch_pack(c, c->st))) return st;
             continue;
         }
-        if ((st = status_error(c, w))) { backup_free(c, b); return st; }
+        if ((st = status_error(c, w))) return st;
         done += k;
     }
-    backup_free(c, b);
     return NBG_OK;
 }
 
 extern "C" int nbg_advance(nbg_ctx* c, double dt, int64_t nsteps)
 {
     if (!c) return NBG_ERR_ARG;
-    cudaSetDevice(c->device);
-    return advance_impl(c, dt, nsteps);
+    NBG_ENTER(c);
+    return advance_impl(c, dt, nsteps, true);
+}
+
+extern "C" int nbg_sync(nbg_ctx* c)
+{
+    if (!c) return NBG_ERR_ARG;
+    NBG_ENTER(c);
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    return NBG_OK;
 }
 
 extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nsteps, int64_t save_every,
@@ -1280,7 +1415,7 @@ extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nste
 {
     if (!c || !u || !v) return NBG_ERR_ARG;
     if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     int64_t launches0 = c->launches;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");
@@ -1370,7 +1505,7 @@ extern "C" int nbg_energy(nbg_ctx* c, const double* u, const double* v, nbg_ener
 {
     if (!c || !u || !v || !out) return NBG_ERR_ARG;
     if (c->nrep != 1) return fail(c, NBG_ERR_UNSUPPORTED, "energies are per system (create one context per replica)");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
     CK(cudaMemcpyAsync(c->ev.v, v, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "v upload");
     int st;
@@ -1405,7 +1540,7 @@ extern "C" int nbg_pair_list(nbg_ctx* c, const double* u, int32_t which, int32_t
     if (!c || !u || !count || (which != NBG_POT_LJ && which != NBG_POT_EL)) return NBG_ERR_ARG;
     if (!(c->d.pots & which)) return fail(c, NBG_ERR_ARG, "potential not present");
     if (c->path == PATH_GRAVITY) return fail(c, NBG_ERR_UNSUPPORTED, "gravity has no pair list");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     CK(cudaMemcpyAsync(c->ev.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
     resident_dirty(c);
     int st;
@@ -1450,7 +1585,7 @@ static int ml_check(nbg_ctx* c)
 {
     if (!c) return NBG_ERR_ARG;
     if (!c->ml_on) return fail(c, NBG_ERR_ARG, "learned model not enabled (call nbg_ml_enable)");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     return NBG_OK;
 }
 
@@ -1472,7 +1607,7 @@ extern "C" int nbg_ml_enable(nbg_ctx* c)
     if (c->d.kind != NBG_SYSTEM_WATER || c->path != PATH_LIST || c->nrep != 1 || c->d.bc != NBG_BC_CUBIC)
         return fail(c, NBG_ERR_UNSUPPORTED,
                     "the learned model needs one SPC/Fw water system on the Verlet-list path in a cubic box");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     int st;
     if (ml_init_constants() != NBG_OK) return fail(c, NBG_ERR_CUDA, "learned-model constants");
     const int64_t n = c->n;
@@ -1906,17 +2041,11 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
     if (c->d.therm != NBG_THERMO_NULL && c->d.therm != NBG_THERMO_BERENDSEN)
         return fail(c, NBG_ERR_UNSUPPORTED, "r-RESPA supports no thermostat or Berendsen");
     nbg_respa_stats S{};
+    c->accel_lists_valid = false;
     const int64_t chunk = c->ml_judge_cap;
-    Backup b;
-    double* b_slow = nullptr;
-    if ((st = backup_alloc(c, b))) return st;
-    if ((st = dalloc(c, &b_slow, 3 * c->cols))) {
-        backup_free(c, b);
-        return st;
-    }
+    if ((st = ensure_backup(c))) return st;
+    double* b_slow = c->bk + 9 * c->cols;  // the slow acceleration's slot of the backup
     auto done_with = [&](int code) {
-        backup_free(c, b);
-        dfree(c, b_slow);
         c->accel_valid = false;
         if (out) *out = S;
         return code;
@@ -1931,9 +2060,7 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
         const int64_t step0 = c->step;
         const int64_t ssb0 = c->steps_since_build;
         const size_t sb = state_bytes(c);
-        CK(cudaMemcpyAsync(b.x, c->st.x, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
-        CK(cudaMemcpyAsync(b.v, c->st.v, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
-        CK(cudaMemcpyAsync(b.a, c->st.a_old, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
+        if ((st = backup_state(c, false))) return done_with(st);
         CK(cudaMemcpyAsync(b_slow, c->ml_a_slow, sb, cudaMemcpyDeviceToDevice, c->stream), "backup");
         CK(cudaMemsetAsync(c->ml_judge, 0, sizeof(double) * 2 * chunk, c->stream), "judge clear");
         for (int64_t o = 0; o < k && st == NBG_OK; ++o) {
@@ -1947,9 +2074,8 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
            "judge read");
         CK(cudaStreamSynchronize(c->stream), "judge sync");
         auto restore = [&]() -> int {
-            CK(cudaMemcpyAsync(c->st.x, b.x, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
-            CK(cudaMemcpyAsync(c->st.v, b.v, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
-            CK(cudaMemcpyAsync(c->st.a_old, b.a, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
+            int rs = backup_state(c, true);
+            if (rs) return rs;
             CK(cudaMemcpyAsync(c->ml_a_slow, b_slow, sb, cudaMemcpyDeviceToDevice, c->stream), "restore");
             c->step = step0;
             c->steps_since_build = ssb0;
@@ -2001,7 +2127,7 @@ extern "C" int nbg_set_thermostat_target(nbg_ctx* c, int32_t replica, double T)
     if (!c) return NBG_ERR_ARG;
     if (replica < 0 || replica >= c->nrep || !(T >= 0.0) || !std::isfinite(T))
         return fail(c, NBG_ERR_ARG, "replica in range and a finite T >= 0");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     c->reps_h[replica].T0 = T;
     if (replica == 0) c->desc.thermo_T = T;
     c->baoab_dt = -1.0;  // BAOAB noise amplitude follows T0
@@ -2055,7 +2181,7 @@ extern "C" int nbg_autotune(nbg_ctx* c, int32_t reps, int32_t* lpa_out, double* 
     if (!c) return NBG_ERR_ARG;
     if (c->path != PATH_LIST) return fail(c, NBG_ERR_UNSUPPORTED, "autotuning applies to the Verlet-list path");
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
-    cudaSetDevice(c->device);
+    NBG_ENTER(c);
     if (reps < 1) reps = 1;
     const int cands[5] = {1, 4, 8, 16, 32};
     const int keep = c->list_lpa;

@@ -185,6 +185,15 @@ struct nbg_ctx {
     StateView ev{};        // scratch state for nbg_accel / nbg_energy / nbg_pair_list
     bool state_valid = false;
     bool accel_valid = false;
+    // x, v, a_old, a_new of each view are one allocation, in that order
+    // (the step loop backs up x, v, a_old with one copy)
+    double* bk = nullptr;  // backup [4][3 cols]: x, v, a_old, then the r-RESPA slow acceleration
+    // an nbg_advance whose last chunk's status word was not read yet; the
+    // next call on the context settles it (re-running the chunk after a list
+    // overflow, or returning its error)
+    bool pending = false;
+    double pend_dt = 0.0;
+    int64_t pend_steps = 0, pend_step0 = 0;
     int64_t step = 0;      // steps taken on the resident state
     int64_t steps_since_build = 0;
     int64_t list_builds = 0;
@@ -233,6 +242,14 @@ struct nbg_ctx {
     bool profiling = false;
     // captured step graphs (velocity Verlet / Euler-Maruyama)
     cudaGraphExec_t graph = nullptr;
+    // nbg_accel on the list path: the whole right-hand side as one graph on
+    // pinned staging buffers; the lists are rebuilt only when an atom moved
+    // more than skin/2 since they were built for an earlier call's positions
+    cudaGraphExec_t accel_graph = nullptr;
+    double* hst = nullptr;         // pinned [3][3 cols] u, v, dv, then the status word
+    int64_t* accel_step = nullptr; // device counter of the calls (parity of the rebuild flags)
+    bool accel_lists_valid = false;
+    int64_t accel_graph_launches = 0;  // kernels per replay
     int64_t graph_steps = 0;     // steps per replay
     int64_t graph_launches = 0;  // kernels per replay
     double graph_dt = 0.0;
@@ -312,6 +329,8 @@ int launch_kick(nbg_ctx* c, const StateView& s, double dt, bool do_T, bool therm
 int launch_andersen(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_step_advance(nbg_ctx* c, int64_t by);
+int launch_pack_disp(nbg_ctx* c, const double* X, StepRef pos);
+int launch_counter_advance(nbg_ctx* c, int64_t* counter, int64_t by);
 int launch_baoab_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt);
 int launch_set_step(nbg_ctx* c, int64_t value);

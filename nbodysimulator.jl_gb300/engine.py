@@ -91,7 +91,13 @@ class Engine:
         return a
 
     def advance(self, dt, nsteps):
+        """Queue nsteps on the resident state (asynchronous: the last chunk's
+        status is read by the next call, or by sync())."""
         self._chk(self.lib.nbg_advance(self.ctx, float(dt), int(nsteps)))
+
+    def sync(self):
+        """Wait for the queued steps; raises the error of the last advance."""
+        self._chk(self.lib.nbg_sync(self.ctx))
 
     @property
     def step(self):

@@ -388,7 +388,11 @@ def run_mts(args, rank, world):
     sim, pos, vel = mts_sim(nbg, n_mol, seed=rank)
     n = 3 * n_mol
     eng = sim.engine()
-    stream = torch.cuda.current_stream()
+    # a stream of torch's, current for the flush and the events, on which
+    # the library launches (its handle is not the legacy default stream's 0,
+    # which nbg_set_stream would read as "the context's own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
     eng.set_state(pos, vel)
     t_setup = time.perf_counter()
@@ -677,7 +681,12 @@ def main():
     u0, v0, n = wl.u0, wl.v0, wl.n
     dt = w["dt"]
     eng = nbg.Engine(wl.descs, device)
-    stream = torch.cuda.current_stream()
+    # a stream of torch's, current for the flush and the events, on which
+    # the library launches (nbg_advance returns without waiting, so the
+    # events must be on the library's stream; the legacy default stream's
+    # handle 0 would select the context's own stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
     batch = len(wl.descs) > 1
     # the ensemble's working set (~0.5 GB) exceeds L2 by itself

@@ -27,6 +27,8 @@
 //     which keeps its x, v, a in registers for the whole launch, kicks the
 //     velocity at the start of the next step.
 // Every thread of every CTA passes the same cluster barriers (no early exit).
+#include <algorithm>
+
 #include <cooperative_groups.h>
 
 #include "nbg_internal.cuh"
@@ -101,7 +103,7 @@ template <int LPA>
 __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s, double* xb, double dt, int nsteps,
                                                               int rebuild_every, int per, int cap, int* lst_g,
                                                               int* cnt_g, double* xref_g, int* since_g, int reuse,
-                                                              int64_t step0, int save)
+                                                              int64_t step0, int save, int drop_step)
 {
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
@@ -115,7 +117,8 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     __shared__ unsigned flag[2];  // rebuild requests of the step of each parity
     __shared__ int build_s;
     __shared__ __align__(8) unsigned long long mbar[2];  // other CTAs' positions of each parity arrived
-    __shared__ int wait_failed;
+    __shared__ int wait_failed;  // a bounded wait of this CTA ran out (this step)
+    __shared__ int abort_s;      // some CTA's wait ran out: every CTA leaves after the next cluster barrier
     const RepDev& R = d.reps[0];
     const PairK K(R);
     const int tid = threadIdx.x;
@@ -161,6 +164,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     if (tid < 2) flag[tid] = 0u;
     if (tid == 0) {
         wait_failed = 0;
+        abort_s = 0;
         mbar_init(smem_addr(&mbar[0]), 1);
         mbar_init(smem_addr(&mbar[1]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -231,7 +235,9 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
         if (tid == 0) {
             const unsigned mb = smem_addr(&mbar[par]);
             mbar_arrive_expect_tx(mb, (unsigned)(n - na) * 32u);
-            if (na > 0) {
+            // (drop_step: a host-set test of the timeout path; no CTA sends
+            // that step's positions, so its waits run out with nothing in flight)
+            if (na > 0 && st != drop_step) {
                 const unsigned sh = smem_addr(ph + a0), sl = smem_addr(pl + a0), bytes = (unsigned)na * 16u;
                 for (int r = 0; r < C; ++r) {
                     if (r == rank) continue;
@@ -243,23 +249,35 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
         }
         if (any_moved && tid < C) *cl.map_shared_rank(&flag[par], tid) = 1u;
         // arrive (release) / wait (acquire) at cluster scope: the rebuild
-        // flags and the FP64 copies X are visible past it
+        // flags, the FP64 copies X and an abort raised in the previous step
+        // are visible past it
         cl.sync();
+        const unsigned mb_cur = smem_addr(&mbar[par]), phase_cur = (unsigned)((st >> 1) & 1);
+        if (abort_s) {
+            // every CTA saw the same flag after the same barrier: leave the
+            // step loop together, once this step's incoming copies (sent
+            // before the barrier) have landed (bounded)
+            unsigned tries = 0;
+            while (!mbar_try_wait(mb_cur, phase_cur) && ++tries < CL_WAIT_TRIES) {
+            }
+            break;
+        }
         // the other CTAs' positions of this step: the k-th use of mbar[par]
-        // completes phase k (bounded wait; after a timeout the launch stops
-        // waiting and reports ST_TIMEOUT)
+        // completes phase k (bounded wait; a timeout is reported as
+        // ST_TIMEOUT and ends the launch at the next cluster barrier)
         {
-            const unsigned mb = smem_addr(&mbar[par]), phase = (unsigned)((st >> 1) & 1);
-            if (!wait_failed) {
-                unsigned tries = 0;
-                while (!mbar_try_wait(mb, phase)) {
-                    if (++tries >= CL_WAIT_TRIES) {
-                        wait_failed = 1;
-                        status_set(d.status, ST_TIMEOUT);
-                        break;
-                    }
+            unsigned tries = 0;
+            while (!mbar_try_wait(mb_cur, phase_cur)) {
+                if (++tries >= CL_WAIT_TRIES) {
+                    wait_failed = 1;
+                    break;
                 }
             }
+        }
+        __syncthreads();
+        if (tid == 0 && wait_failed) {
+            status_set(d.status, ST_TIMEOUT);
+            for (int r = 0; r < C; ++r) *cl.map_shared_rank(&abort_s, r) = 1;
         }
         if (tid == 0) {
             build_s = ((st == 0 && !reuse) || flag[par] != 0u || (rebuild_every > 0 && since >= rebuild_every)) ? 1 : 0;
@@ -364,7 +382,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
 }
 
 typedef void (*cluster_kernel_t)(Dev, StateView, double*, double, int, int, int, int, int*, int*, double*, int*, int, int64_t,
-                                 int);
+                                 int, int);
 
 static cluster_kernel_t cluster_kernel(int lpa)
 {
@@ -445,11 +463,18 @@ int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps,
     cfg.stream = c->stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    // a one-shot test of the timeout path (NBG_TEST_CLUSTER_DROP at context
+    // creation): the launch drops the position copies of one step
+    int drop = -2;
+    if (c->cluster_test_drop != -2) {
+        drop = c->cluster_test_drop < 0 ? (int)nsteps - 1 : std::min<int>(c->cluster_test_drop, (int)nsteps - 1);
+        c->cluster_test_drop = -2;
+    }
     prof_begin(c);
     cudaError_t e = cudaLaunchKernelEx(&cfg, k, c->d, s, c->cluster_x, dt, (int)nsteps, rebuild_every,
                                        c->cluster_per, c->cluster_cap, c->cluster_lists, c->cluster_cnt,
                                        c->cluster_xref, c->cluster_since, c->cluster_lists_valid ? 1 : 0, step0,
-                                       c->sink_on ? 1 : 0);
+                                       c->sink_on ? 1 : 0, drop);
     prof_end(c);
     if (e != cudaSuccess) return cuda_fail(c, e, "k_cluster_vv launch");
     NBG_LAUNCH_CHECK(c, "k_cluster_vv");

@@ -175,17 +175,34 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
         const uint4 qi = d.pfx[ia];
         const int cnt = active ? min(min(d.nbr_count[ia], d.nbr_cap), s_nbox[st] * 32) : 0;
         const bool lj_i = HAS_LJ && (POT != FX_WATER || (ia % 3) == 0);
-        const float kqi = HAS_EL ? (float)(d.el_k_d * d.charge[ia]) : 0.0f;
+        // k q_i / (u^2 fscale): rinv^3 in box units times this is the
+        // electrostatic factor in the units of the LJ sum
+        const float kqi = HAS_EL ? (float)(d.el_k_d * d.charge[ia] * (R.fx_scale * R.fx_scale) / R.fx_fscale) : 0.0f;
         const float lj_lo = R.fx_lj_lo, lj_hi = R.fx_lj_hi, el_lo = R.fx_el_lo, el_hi = R.fx_el_hi;
-        const float sig2 = R.fx_sig2, ljf = R.fx_ljf, el1 = R.fx_el1, el2 = R.fx_el2;
+        const float sig2h = R.fx_sig2_hi, sig2l = R.fx_sig2_lo, krf = R.fx_krf;
         float2 px = make_float2(0.f, 0.f), py = px, pz = px;
+        // the next iteration's entries and gathers are issued before this
+        // iteration's arithmetic (two neighbours ahead per lane)
+        int jn0 = 0, jn1 = 0;
+        uint4 qn0 = qi, qn1 = qi;
+        if (lane < cnt) {
+            jn0 = fx_entry(stage, A, a, lane);
+            jn1 = lane + LPA < cnt ? fx_entry(stage, A, a, lane + LPA) : jn0;
+            qn0 = __ldg(&d.pfx[jn0]);
+            qn1 = __ldg(&d.pfx[jn1]);
+        }
         for (int k0 = lane; k0 < cnt; k0 += 2 * LPA) {
             const int k1 = k0 + LPA;
             const bool v1 = k1 < cnt;
-            const int j0 = fx_entry(stage, A, a, k0);
-            const int j1 = v1 ? fx_entry(stage, A, a, k1) : j0;
-            const uint4 q0 = __ldg(&d.pfx[j0]);
-            const uint4 q1 = __ldg(&d.pfx[j1]);
+            const int j0 = jn0, j1 = jn1;
+            const uint4 q0 = qn0, q1 = qn1;
+            const int kn = k0 + 2 * LPA;
+            if (kn < cnt) {
+                jn0 = fx_entry(stage, A, a, kn);
+                jn1 = kn + LPA < cnt ? fx_entry(stage, A, a, kn + LPA) : jn0;
+                qn0 = __ldg(&d.pfx[jn0]);
+                qn1 = __ldg(&d.pfx[jn1]);
+            }
             float2 dx = make_float2(fx_diff(qi.x, q0.x), fx_diff(qi.x, q1.x));
             float2 dy = make_float2(fx_diff(qi.y, q0.y), fx_diff(qi.y, q1.y));
             float2 dz = make_float2(fx_diff(qi.z, q0.z), fx_diff(qi.z, q1.z));
@@ -220,19 +237,19 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
             float2 f = make_float2(0.f, 0.f);
             if (HAS_LJ) {
                 const float2 ri = make_float2(__fdividef(1.0f, r2.x), __fdividef(1.0f, r2.y));
-                const float2 s2 = __fmul2_rn(make_float2(sig2, sig2), ri);
+                // s^2 = sigma^2 / r^2 with sigma^2 / u^2 as hi + lo
+                const float2 s2 = __ffma2_rn(make_float2(sig2h, sig2h), ri, __fmul2_rn(make_float2(sig2l, sig2l), ri));
                 const float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
                 // (2 s^12 - s^6) / r^2 = (2 s^6 - 1) s^6 / r^2
                 const float2 fl = __fmul2_rn(__fmul2_rn(__ffma2_rn(make_float2(2.f, 2.f), s6, make_float2(-1.f, -1.f)), s6),
-                                             __fmul2_rn(ri, make_float2(ljf, ljf)));
+                                             ri);
                 f = make_float2(lj0 ? fl.x : 0.f, lj1 ? fl.y : 0.f);
             }
             if (HAS_EL) {
                 const float qj0 = __int_as_float((int)q0.w), qj1 = __int_as_float((int)q1.w);
                 const float2 rb = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
                 const float2 r3 = __fmul2_rn(__fmul2_rn(rb, rb), rb);
-                const float2 fe = __fmul2_rn(make_float2(kqi * qj0, kqi * qj1),
-                                             __ffma2_rn(r3, make_float2(el1, el1), make_float2(-el2, -el2)));
+                const float2 fe = __fmul2_rn(make_float2(kqi * qj0, kqi * qj1), __fadd2_rn(r3, make_float2(-krf, -krf)));
                 f = make_float2(el0 ? f.x + fe.x : f.x, el1b ? f.y + fe.y : f.y);
             }
             px = __ffma2_rn(f, dx, px);
@@ -249,7 +266,7 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
             fx_join(hz, ez, o, LPA);
         }
         if (active && lane == 0) {
-            const double im = d.inv_mass[i];
+            const double im = d.inv_mass[i] * R.fx_fscale;
             const double a0 = ((double)hx + (double)ex) * im, a1 = ((double)hy + (double)ey) * im,
                          a2 = ((double)hz + (double)ez) * im;
             if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);

@@ -338,19 +338,20 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
             const double u = L / 4294967296.0, iu2 = 1.0 / (u * u);
             R.fx_scale = 4294967296.0 / L;
             const double hb = 2147483648.0 * (1.0 - m), img2b = hb * hb;
+            R.fx_fscale = (pots & NBG_POT_LJ) ? 24.0 * d0->lj_epsilon / u : 1.0;
             if (pots & NBG_POT_LJ) {
                 const double R2 = d0->lj_cutoff * d0->lj_cutoff * iu2;
                 R.fx_lj_lo = f_down(std::min(R2 * (1.0 - m), img2b));
                 R.fx_lj_hi = f_up(R2 * (1.0 + m));
-                R.fx_sig2 = (float)(d0->lj_sigma * d0->lj_sigma * iu2);
-                R.fx_ljf = (float)(24.0 * d0->lj_epsilon / u);
+                const double s2 = d0->lj_sigma * d0->lj_sigma * iu2;
+                R.fx_sig2_hi = (float)s2;
+                R.fx_sig2_lo = (float)(s2 - (double)R.fx_sig2_hi);
             }
             if (pots & NBG_POT_EL) {
                 const double R2 = d0->el_cutoff * d0->el_cutoff * iu2;
                 R.fx_el_lo = f_down(std::min(R2 * (1.0 - m), img2b));
                 R.fx_el_hi = f_up(R2 * (1.0 + m));
-                R.fx_el1 = (float)iu2;
-                R.fx_el2 = (float)(2.0 * D.el_krf * u);
+                R.fx_krf = (float)(2.0 * D.el_krf * u * u * u);
             }
         }
         if (c->path == PATH_LIST) {
@@ -561,6 +562,11 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     }
     if (getenv("NBG_NO_GRAPHS")) c->use_graphs = false;  // direct launches, for comparisons
     if (getenv("NBG_NO_CLUSTER")) c->cluster_disabled = true;  // the graph step loop for small systems too
+    // a test of the cluster loop's bounded waits: the first launch drops the
+    // position copies of one step ("last" or a step index), so that the
+    // receivers' waits run out with no copy in flight
+    if (const char* td = getenv("NBG_TEST_CLUSTER_DROP"))
+        c->cluster_test_drop = strcmp(td, "last") == 0 ? -1 : std::max(0, atoi(td));
     if ((st = plan_cluster(c))) return st;
     if (c->path == PATH_GRAVITY) {
         const char* gv = getenv("NBG_GRAVITY_VARIANT");  // kernel-form override for tuning sweeps
@@ -1277,7 +1283,15 @@ static int settle(nbg_ctx* c)
     unsigned w = 0;
     int st;
     if ((st = read_status(c, &w))) return st;
-    if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
+    if (w & ST_TIMEOUT) {
+        if ((st = backup_state(c, true))) return st;  // the chunk ended early: back to its start
+        c->step = c->pend_step0;
+        c->steps_since_build = -1;
+        c->cluster_lists_valid = false;
+        c->T_valid = false;
+        return status_error(c, ST_TIMEOUT);
+    }
+    if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
     if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
         if ((st = grow_lists(c, w))) return st;
         if ((st = backup_state(c, true))) return st;
@@ -1376,6 +1390,16 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
         }
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
+        if ((w & ST_TIMEOUT) && can_overflow) {
+            // a launch that gave up waiting ended early: the state goes back
+            // to the chunk's start, and the error is returned
+            if ((st = backup_state(c, true))) return st;
+            c->step = step0;
+            c->steps_since_build = -1;
+            c->cluster_lists_valid = false;
+            c->T_valid = false;
+            return status_error(c, ST_TIMEOUT);  // (whatever else the abandoned steps flagged)
+        }
         if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if (++retries > 6) return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");

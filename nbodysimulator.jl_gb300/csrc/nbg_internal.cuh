@@ -67,9 +67,15 @@ struct RepDev {
     double fx_scale;             // 2^32 / L
     float fx_lj_lo, fx_lj_hi;    // classification bands of r^2 (as lj_lo / lj_hi)
     float fx_el_lo, fx_el_hi;
-    float fx_sig2;               // sigma^2 / u^2
-    float fx_ljf;                // 24 eps / u: LJ force = fx_ljf (2 s^12 - s^6) / r^2 d
-    float fx_el1, fx_el2;        // 1 / u^2 and 2 k_rf u: EL force = k q_i q_j (rinv^3 el1 - el2) d
+    // The kernel sums, per pair, (2 s^6 - 1) s^6 / r^2 d for LJ and
+    // kq_i q_j (rinv^3 - krf) d for electrostatics (box units, s^2 =
+    // sigma^2 / r^2, kq_i = k q_i / (u^2 fscale)) and multiplies the sums by
+    // fscale (24 eps / u with LJ, else 1) in FP64: the FP32 constants of the
+    // pair loop carry no systematic rounding beyond sigma^2's (kept as a
+    // hi + lo pair) and the charges'.
+    float fx_sig2_hi, fx_sig2_lo;  // sigma^2 / u^2
+    float fx_krf;                  // 2 k_rf u^3
+    double fx_fscale;
 };
 
 // Everything a kernel needs, passed by value.
@@ -215,6 +221,9 @@ struct nbg_ctx {
     double* cluster_xref = nullptr;  // [3n] positions at the cluster lists' build
     int* cluster_since = nullptr;
     bool cluster_lists_valid = false;
+    // test of the cluster loop's timeout path: the next launch drops the
+    // position copies of this step (-1: its last step; -2: none)
+    int cluster_test_drop = -2;
     bool grav_uniform = false;  // every body has mass grav_m0: the reduction applies G m
     float grav_far2 = 256.f;    // a tile pair is far when (F g)^2 >= max|r|^2, F = 16
     double grav_m0 = 0.0;

@@ -450,3 +450,30 @@ def test_cluster_step_loop_list_regrowth(gpu, oracle):
     err, err_ref = np.abs(ug - uo).max(), np.abs(ur - uo).max()
     assert err <= max(1e-8 * L, 3.0 * err_ref), (err, err_ref)
     assert eng.cluster_shape() is not None  # still on the cluster path, with the larger lists
+
+
+@pytest.mark.parametrize("drop", ["last", "5"])
+def test_cluster_loop_timeout_is_reported_and_recovers(gpu, oracle, drop):
+    """The persistent cluster loop's bounded waits: with a host-set test flag
+    (NBG_TEST_CLUSTER_DROP, read at creation, used by the first launch only)
+    no CTA sends its positions in one step, so every receiver's wait runs
+    out with no copy in flight. The launch leaves the step loop together at
+    the next cluster barrier, the call returns NBG_ERR_TIMEOUT with the state
+    back at the chunk's start, and the next run on the same context is
+    normal (against the oracle)."""
+    sim = S.lj_liquid(1000, seed=21)
+    desc, keep = nbg.system_descriptor(sim)
+    u, v = S.state(sim)
+    os.environ["NBG_TEST_CLUSTER_DROP"] = drop
+    try:
+        eng = nbg.Engine(desc, 0)
+    finally:
+        os.environ.pop("NBG_TEST_CLUSTER_DROP", None)
+    assert eng.cluster_shape() is not None
+    with pytest.raises(nbg.EngineError) as e:
+        eng.run(u, v, 0.005, 20, 0, save_trajectory=False)
+    assert e.value.status == -5  # NBG_ERR_TIMEOUT
+    ug, vg, _, _, _ = eng.run(u, v, 0.005, 20, 0, save_trajectory=False)
+    uo, vo = oracle.run(desc, u, v, 0.005, 20)
+    assert np.abs(ug - uo).max() <= 1e-8 * np.abs(uo).max()
+    eng.close()

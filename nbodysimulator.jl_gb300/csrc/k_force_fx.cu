@@ -292,6 +292,239 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
     }
 }
 
+// The same pair arithmetic with the staging per warp: a warp owns tiles of
+// AW = 32 / LPA atoms in turn and streams their list rows as 32-entry boxes
+// (AW rows x 128 B) through a ring of FXW_SLOTS shared-memory slots, each
+// with its own mbarrier; lane 0 keeps up to FXW_SLOTS boxes in flight ahead
+// of the lanes, across tile ends. No block barrier: the warps of a block
+// run independently, and a tile costs the boxes of its own largest list.
+#define FXW_WARPS 8
+#define FXW_SLOTS 4
+
+// One packed pair step (entries k0 and k0 + LPA of atom row a) of the
+// fixed-point kernels: classification, FP64 fallback, LJ and reaction-field
+// factors in the units of the LJ sum, accumulated into (px, py, pz).
+template <int POT>
+__device__ __forceinline__ void fx_pair2(const Dev& d, const double* X, int64_t ia, bool lj_i, float kqi,
+                                         const uint4& qi, int j0, int j1, bool v1, const uint4& q0,
+                                         const uint4& q1, float lj_lo, float lj_hi, float el_lo, float el_hi,
+                                         float sig2h, float sig2l, float krf, float2& px, float2& py, float2& pz,
+                                         bool& range_err)
+{
+    constexpr bool HAS_LJ = POT == FX_LJ || POT == FX_LJEL || POT == FX_WATER;
+    constexpr bool HAS_EL = POT == FX_EL || POT == FX_LJEL || POT == FX_WATER;
+    float2 dx = make_float2(fx_diff(qi.x, q0.x), fx_diff(qi.x, q1.x));
+    float2 dy = make_float2(fx_diff(qi.y, q0.y), fx_diff(qi.y, q1.y));
+    float2 dz = make_float2(fx_diff(qi.z, q0.z), fx_diff(qi.z, q1.z));
+    float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+    const bool lp0 = HAS_LJ && lj_i && (POT != FX_WATER || fx_oxygen(j0));
+    const bool lp1 = HAS_LJ && v1 && lj_i && (POT != FX_WATER || fx_oxygen(j1));
+    const bool ep0 = HAS_EL, ep1 = HAS_EL && v1;
+    bool lj0, lj1, el0, el1b, amb0, amb1;
+    fx_classify(r2.x, lp0, ep0, lj_lo, lj_hi, el_lo, el_hi, lj0, el0, amb0);
+    fx_classify(r2.y, lp1, ep1, lj_lo, lj_hi, el_lo, el_hi, lj1, el1b, amb1);
+    if (amb0 | amb1) {
+        if (amb0) {
+            const FxPair o = fx_pair_fallback(d, X, ia, j0, lp0, ep0);
+            lj0 = o.lj_in;
+            el0 = o.el_in;
+            dx.x = o.dx, dy.x = o.dy, dz.x = o.dz, r2.x = o.r2;
+            range_err |= o.range_err != 0;
+        }
+        if (amb1) {
+            const FxPair o = fx_pair_fallback(d, X, ia, j1, lp1, ep1);
+            lj1 = o.lj_in;
+            el1b = o.el_in;
+            dx.y = o.dx, dy.y = o.dy, dz.y = o.dz, r2.y = o.r2;
+            range_err |= o.range_err != 0;
+        }
+    }
+    const bool in0 = lj0 || el0, in1 = lj1 || el1b;
+    r2 = make_float2(in0 ? r2.x : 1.0f, in1 ? r2.y : 1.0f);
+    float2 f = make_float2(0.f, 0.f);
+    if (HAS_LJ) {
+        const float2 ri = make_float2(__fdividef(1.0f, r2.x), __fdividef(1.0f, r2.y));
+        const float2 s2 = __ffma2_rn(make_float2(sig2h, sig2h), ri, __fmul2_rn(make_float2(sig2l, sig2l), ri));
+        const float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
+        const float2 fl =
+            __fmul2_rn(__fmul2_rn(__ffma2_rn(make_float2(2.f, 2.f), s6, make_float2(-1.f, -1.f)), s6), ri);
+        f = make_float2(lj0 ? fl.x : 0.f, lj1 ? fl.y : 0.f);
+    }
+    if (HAS_EL) {
+        const float qj0 = __int_as_float((int)q0.w), qj1 = __int_as_float((int)q1.w);
+        const float2 rb = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        const float2 r3 = __fmul2_rn(__fmul2_rn(rb, rb), rb);
+        const float2 fe = __fmul2_rn(make_float2(kqi * qj0, kqi * qj1), __fadd2_rn(r3, make_float2(-krf, -krf)));
+        f = make_float2(el0 ? f.x + fe.x : f.x, el1b ? f.y + fe.y : f.y);
+    }
+    px = __ffma2_rn(f, dx, px);
+    py = __ffma2_rn(f, dy, py);
+    pz = __ffma2_rn(f, dz, pz);
+}
+
+// entry c (< 32) of row a of one swizzled box
+__device__ __forceinline__ int fxw_entry(const unsigned char* box, int a, int c)
+{
+    return *reinterpret_cast<const int*>(box + a * 128 + ((((c >> 2) ^ (a & 7))) << 4) + ((c & 3) << 2));
+}
+
+template <int LPA, int POT>
+__global__ void __launch_bounds__(FXW_WARPS * 32, 3) k_force_fxw(Dev d, StateView s,
+                                                                 const __grid_constant__ CUtensorMap map)
+{
+    static_assert(LPA >= 4 && LPA <= 16, "two entries per lane per box step");
+    constexpr int AW = 32 / LPA;    // atoms per warp tile (rows of a box)
+    constexpr int IT = 16 / LPA;    // packed steps per box (32 entries / (2 LPA))
+    constexpr bool HAS_LJ = POT == FX_LJ || POT == FX_LJEL || POT == FX_WATER;
+    constexpr bool HAS_EL = POT == FX_EL || POT == FX_LJEL || POT == FX_WATER;
+    __shared__ __align__(8) unsigned long long mbar[FXW_WARPS][FXW_SLOTS];
+    extern __shared__ unsigned char fxw_dyn[];
+    const int warp = threadIdx.x >> 5, lane_w = threadIdx.x & 31;
+    const int lane = lane_w % LPA, a = lane_w / LPA;
+    const unsigned dyn = fx_smem(fxw_dyn);
+    const unsigned base = ((dyn + 1023u) & ~1023u) + (unsigned)warp * FXW_SLOTS * 1024u;  // slot k: base + 1024 k
+    const unsigned char* const slot0 = fxw_dyn + (base - dyn);
+    const int64_t ntiles = (d.n + AW - 1) / AW;
+    const int64_t nwarps = (int64_t)gridDim.x * FXW_WARPS;
+    const int64_t gw = (int64_t)blockIdx.x * FXW_WARPS + warp;
+    if (lane_w < FXW_SLOTS) fx_mbar_init(fx_smem(&mbar[warp][lane_w]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+
+    // boxes of a tile: its largest count in 32-entry boxes (warp-uniform)
+    auto boxes_of = [&](int64_t t) -> int {
+        int c = 0;
+        if (lane_w < AW) {
+            const int64_t i = t * AW + lane_w;
+            if (i < d.n) c = min(d.nbr_count[i], d.nbr_cap);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_xor_sync(0xffffffffu, c, o));
+        return (c + 31) >> 5;
+    };
+    // the producer's next box: box pb of the pnb boxes of tile pt
+    int64_t pt = gw;
+    int pb = 0, pnb = 0;
+    while (pt < ntiles && (pnb = boxes_of(pt)) == 0) pt += nwarps;
+    unsigned issued = 0, consumed = 0;
+    auto refill = [&]() {
+        while (pt < ntiles && issued - consumed < FXW_SLOTS) {
+            if (lane_w == 0) {
+                const unsigned sl = issued % FXW_SLOTS;
+                const unsigned mb = fx_smem(&mbar[warp][sl]);
+                // the slot was last read by generic loads (ordered by __syncwarp)
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                fx_mbar_expect(mb, AW * 128u);
+                fx_tma_box(base + sl * 1024u, &map, pb * 32, (int)(pt * AW), mb);
+            }
+            ++issued;
+            if (++pb >= pnb) {
+                pb = 0;
+                pt += nwarps;
+                while (pt < ntiles && (pnb = boxes_of(pt)) == 0) pt += nwarps;
+            }
+        }
+    };
+    refill();
+
+    bool range_err = false, timeout = false;
+    for (int64_t t = gw; t < ntiles; t += nwarps) {
+        const int nb = boxes_of(t);
+        const int64_t i = t * AW + a;
+        const bool active = i < d.n;
+        const int64_t ia = active ? i : 0;
+        const RepDev& R = d.reps[d.rep_of[ia]];
+        const uint4 qi = d.pfx[ia];
+        const int cnt = active ? min(d.nbr_count[ia], d.nbr_cap) : 0;
+        const bool lj_i = HAS_LJ && (POT != FX_WATER || (ia % 3) == 0);
+        const float kqi =
+            HAS_EL ? (float)(d.el_k_d * d.charge[ia] * (R.fx_scale * R.fx_scale) / R.fx_fscale) : 0.0f;
+        const float lj_lo = R.fx_lj_lo, lj_hi = R.fx_lj_hi, el_lo = R.fx_el_lo, el_hi = R.fx_el_hi;
+        const float sig2h = R.fx_sig2_hi, sig2l = R.fx_sig2_lo, krf = R.fx_krf;
+        float2 px = make_float2(0.f, 0.f), py = px, pz = px;
+        for (int b = 0; b < nb; ++b) {
+            const unsigned sl = consumed % FXW_SLOTS;
+            const unsigned mb = fx_smem(&mbar[warp][sl]);
+            const unsigned parity = (consumed / FXW_SLOTS) & 1u;
+            unsigned tries = 0;
+            bool late = false;
+            while (!fx_mbar_try(mb, parity)) {
+                if (++tries > FX_WAIT_TRIES) {
+                    late = true;
+                    break;
+                }
+            }
+            if (__any_sync(0xffffffffu, late)) {
+                timeout = true;
+                break;
+            }
+            const unsigned char* box = slot0 + sl * 1024u;
+            const int kb = 32 * b;
+            // this box's entries of the lane: kb + lane + 2 m LPA (+ LPA), the
+            // next step's entries and gathers issued before this step's arithmetic
+            int jn0 = 0, jn1 = 0;
+            uint4 qn0 = qi, qn1 = qi;
+            if (kb + lane < cnt) {
+                jn0 = fxw_entry(box, a, lane);
+                jn1 = kb + lane + LPA < cnt ? fxw_entry(box, a, lane + LPA) : jn0;
+                qn0 = __ldg(&d.pfx[jn0]);
+                qn1 = __ldg(&d.pfx[jn1]);
+            }
+#pragma unroll
+            for (int m = 0; m < IT; ++m) {
+                const int c0 = lane + 2 * m * LPA;
+                const bool v0 = kb + c0 < cnt, v1 = kb + c0 + LPA < cnt;
+                const int j0 = jn0, j1 = jn1;
+                const uint4 q0 = qn0, q1 = qn1;
+                if (m + 1 < IT) {
+                    const int cn = c0 + 2 * LPA;
+                    if (kb + cn < cnt) {
+                        jn0 = fxw_entry(box, a, cn);
+                        jn1 = kb + cn + LPA < cnt ? fxw_entry(box, a, cn + LPA) : jn0;
+                        qn0 = __ldg(&d.pfx[jn0]);
+                        qn1 = __ldg(&d.pfx[jn1]);
+                    }
+                }
+                if (v0)
+                    fx_pair2<POT>(d, s.x, ia, lj_i, kqi, qi, j0, j1, v1, q0, q1, lj_lo, lj_hi, el_lo, el_hi, sig2h,
+                                  sig2l, krf, px, py, pz, range_err);
+            }
+            __syncwarp();  // every lane is done with the slot
+            ++consumed;
+            refill();
+        }
+        if (timeout) break;
+        float hx = __fadd_rn(px.x, px.y), hy = __fadd_rn(py.x, py.y), hz = __fadd_rn(pz.x, pz.y);
+        float ex = 0.f, ey = 0.f, ez = 0.f;
+#pragma unroll
+        for (int o = LPA / 2; o > 0; o >>= 1) {
+            fx_join(hx, ex, o, LPA);
+            fx_join(hy, ey, o, LPA);
+            fx_join(hz, ez, o, LPA);
+        }
+        if (active && lane == 0) {
+            const double im = d.inv_mass[i] * R.fx_fscale;
+            const double a0 = ((double)hx + (double)ex) * im, a1 = ((double)hy + (double)ey) * im,
+                         a2 = ((double)hz + (double)ez) * im;
+            if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
+            s.a_new[3 * i] = a0;
+            s.a_new[3 * i + 1] = a1;
+            s.a_new[3 * i + 2] = a2;
+        }
+    }
+    if (range_err) status_set(d.status, ST_RANGE);
+    if (timeout) {
+        if (lane_w == 0) status_set(d.status, ST_TIMEOUT);
+        // boxes still in flight land in this warp's own slots: wait (bounded)
+        for (unsigned q = consumed; q != issued; ++q) {
+            const unsigned mb = fx_smem(&mbar[warp][q % FXW_SLOTS]);
+            unsigned tries = 0;
+            while (!fx_mbar_try(mb, (q / FXW_SLOTS) & 1u) && ++tries < FX_WAIT_TRIES) {
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------
@@ -309,7 +542,12 @@ static PFN_cuTensorMapEncodeTiled_v12000 fx_encode_fn()
     return fn;
 }
 
-int fx_atoms_per_tile(int lpa) { return FX_THREADS / lpa; }
+// The per-warp form runs for 4, 8 and 16 lanes per atom (NBG_FX_BLOCK keeps
+// the per-block form, for comparisons), the per-block form for 32.
+static bool fx_warp_form(const nbg_ctx* c) { return c->list_lpa <= 16 && !c->fx_block_only; }
+
+// rows (atoms) of one list box of the tensor map
+static int fx_box_rows(const nbg_ctx* c) { return fx_warp_form(c) ? 32 / c->list_lpa : FX_THREADS / c->list_lpa; }
 
 // Tensor map of the row-major list: dims (cap entries, n atoms), boxes of
 // 32 entries x A atoms, 128-byte swizzle; encoded again whenever the list
@@ -324,7 +562,7 @@ int fx_encode_map(nbg_ctx* c)
     CUtensorMap* map = reinterpret_cast<CUtensorMap*>(c->fx_map);
     const cuuint64_t dims[2] = {(cuuint64_t)c->d.nbr_cap, (cuuint64_t)c->n};
     const cuuint64_t strides[1] = {(cuuint64_t)c->d.nbr_cap * sizeof(int)};
-    const cuuint32_t box[2] = {32u, (cuuint32_t)fx_atoms_per_tile(c->list_lpa)};
+    const cuuint32_t box[2] = {32u, (cuuint32_t)fx_box_rows(c)};
     const cuuint32_t estr[2] = {1u, 1u};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_INT32, 2, c->d.nbr, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -341,6 +579,24 @@ int fx_encode_map(nbg_ctx* c)
 template <int LPA, int POT>
 static int fx_prepare_form(nbg_ctx* c)
 {
+    if constexpr (LPA <= 16) {
+        if (fx_warp_form(c)) {
+            const size_t smem = (size_t)FXW_WARPS * FXW_SLOTS * 1024 + 1024;
+            auto kern = k_force_fxw<LPA, POT>;
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+                cudaGetLastError();
+                return NBG_ERR_UNSUPPORTED;
+            }
+            int occ = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, FXW_WARPS * 32, smem);
+            if (occ < 1) return NBG_ERR_UNSUPPORTED;
+            const int64_t ntiles = (c->n + (32 / LPA) - 1) / (32 / LPA);
+            c->fx_grid = (int)std::min<int64_t>((ntiles + FXW_WARPS - 1) / FXW_WARPS, (int64_t)c->sms * occ);
+            c->fx_smem = smem;
+            c->fx_nbox = 0;
+            return NBG_OK;
+        }
+    }
     const int nbox_cap = (c->d.nbr_cap + 31) / 32;
     const size_t smem = 2 * (size_t)nbox_cap * (FX_THREADS / LPA) * 128 + 1024;
     auto kern = k_force_fx<LPA, POT>;
@@ -363,6 +619,12 @@ template <int LPA, int POT>
 static void fx_launch(nbg_ctx* c, const StateView& s)
 {
     const CUtensorMap* map = reinterpret_cast<const CUtensorMap*>(c->fx_map);
+    if constexpr (LPA <= 16) {
+        if (fx_warp_form(c)) {
+            k_force_fxw<LPA, POT><<<(unsigned)c->fx_grid, FXW_WARPS * 32, c->fx_smem, c->stream>>>(c->d, s, *map);
+            return;
+        }
+    }
     k_force_fx<LPA, POT><<<(unsigned)c->fx_grid, FX_THREADS, c->fx_smem, c->stream>>>(c->d, s, *map, c->fx_nbox);
 }
 

@@ -562,6 +562,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     }
     if (getenv("NBG_NO_GRAPHS")) c->use_graphs = false;  // direct launches, for comparisons
     if (getenv("NBG_NO_CLUSTER")) c->cluster_disabled = true;  // the graph step loop for small systems too
+    if (getenv("NBG_FX_BLOCK")) c->fx_block_only = true;         // per-block list staging (comparisons)
     // a test of the cluster loop's bounded waits: the first launch drops the
     // position copies of one step ("last" or a step index), so that the
     // receivers' waits run out with no copy in flight

@@ -233,6 +233,7 @@ struct nbg_ctx {
     alignas(64) unsigned char fx_map[128];
     bool fx_ready = false;     // it runs (else the split-form kernels do)
     bool fx_disabled = false;  // NBG_NO_FX: the split-form kernels only
+    bool fx_block_only = false;  // NBG_FX_BLOCK: the per-block staging form for every width
     int fx_grid = 0, fx_nbox = 0;
     size_t fx_smem = 0;
     double* grav_part = nullptr;

@@ -50,15 +50,19 @@ def _systems():
 
 
 @pytest.mark.parametrize("name", ["lj", "ljel", "water", "water_rf"])
-@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
-def test_fixed_point_kernel_matches_oracle_and_split_form(gpu, oracle, name, lanes):
+@pytest.mark.parametrize("lanes,staging", [(4, "warp"), (8, "warp"), (16, "warp"), (4, "block"), (8, "block"),
+                                           (16, "block"), (32, "block")])
+def test_fixed_point_kernel_matches_oracle_and_split_form(gpu, oracle, name, lanes, staging):
+    """Both stagings of the lists (per warp: a ring of 32-entry boxes; per
+    block: whole tiles, double-buffered) at every width."""
     sim = _systems()[name]
     desc, keep = nbg.system_descriptor(sim)
     u, v = S.state(sim)
-    eng = _engine(desc, NBG_LIST_LPA=lanes, NBG_NO_CLUSTER=1)
+    extra = {"NBG_FX_BLOCK": 1} if staging == "block" and lanes < 32 else {}
+    eng = _engine(desc, NBG_LIST_LPA=lanes, NBG_NO_CLUSTER=1, **extra)
     # water's ~580-entry list rows for 64 atoms of 4 lanes overflow the two
-    # shared-memory stages: that form stays on the split-position kernel
-    assert eng.force_form() == (lanes, not (name.startswith("water") and lanes == 4))
+    # per-block shared-memory stages: that form stays on the split-position kernel
+    assert eng.force_form() == (lanes, not (name.startswith("water") and lanes == 4 and staging == "block"))
     ref = _engine(desc, NBG_LIST_LPA=lanes, NBG_NO_CLUSTER=1, NBG_NO_FX=1)
     assert ref.force_form() == (lanes, False)
     a_fx = _forces(eng, u, v)

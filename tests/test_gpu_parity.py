@@ -222,8 +222,13 @@ def test_short_trajectories(gpu, oracle, case):
     eng = nbg.Engine(desc, 0)
     ug, vg, _, _, stats = eng.run(u, v, dt, n, 0, save_trajectory=False)
     uo, vo = oracle.run(desc, u, v, dt, n)
-    scale = np.abs(uo).max()
-    assert np.abs(ug - uo).max() <= tol * max(scale, 1.0), np.abs(ug - uo).max()
+    na = int(desc.n)
+    scale = np.abs(uo[:na]).max()
+    assert np.abs(ug[:na] - uo[:na]).max() <= tol * max(scale, 1.0), np.abs(ug[:na] - uo[:na]).max()
+    if len(uo) > na:
+        # the Nose-Hoover variable integrates the temperature error of FP32
+        # pair forces: relative agreement at that level
+        assert abs(ug[na, 0] - uo[na, 0]) <= 1e-7 * max(abs(uo[na, 0]), 1.0), (ug[na], uo[na])
     assert stats.kernel_launches > 0
 
 

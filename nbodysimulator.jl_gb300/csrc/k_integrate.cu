@@ -442,6 +442,60 @@ int launch_step_advance(nbg_ctx* c, int64_t by)
     return NBG_OK;
 }
 
+// The right-hand side's first node: u (and v) read from the caller-facing
+// pinned staging (host memory the GPU reads directly), stored into the
+// scratch state, packed, and checked for displacement against the positions
+// of the last list build (rebuild flag of the call counter's parity); the
+// status word starts clean.
+__global__ void k_accel_import(Dev d, StateView s, const double* __restrict__ hu, const double* __restrict__ hv,
+                               int v_read, StepRef pos)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d.status = 0u;
+    const int parity = (int)(step_of(pos) & 1);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.cols; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int k = 0; k < 3; ++k) {
+            s.x[3 * i + k] = hu[3 * i + k];
+            if (v_read) s.v[3 * i + k] = hv[3 * i + k];
+        }
+        if (i >= d.n) continue;
+        pack_atom(d, i, s.x);
+        const double dx = s.x[3 * i] - d.xref[3 * i];
+        const double dy = s.x[3 * i + 1] - d.xref[3 * i + 1];
+        const double dz = s.x[3 * i + 2] - d.xref[3 * i + 2];
+        if (!(dx * dx + dy * dy + dz * dz <= d.skin_half2)) d.rebuild_flag[parity * d.nrep + d.rep_of[i]] = 1;
+    }
+}
+
+// The right-hand side's last node: dv (and the Nose-Hoover rate) and the
+// status word written straight into the pinned staging; the call counter
+// advances.
+__global__ void k_accel_export(Dev d, StateView s, double* __restrict__ hdv, double* __restrict__ hv, unsigned* hstat,
+                               int64_t* counter, int nh)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * d.cols; e += (int64_t)gridDim.x * blockDim.x)
+        hdv[e] = s.a_new[e];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (nh) hv[3 * d.n] = s.v[3 * d.n];
+        *hstat = *d.status;
+        *counter += 1;
+    }
+}
+
+int launch_accel_import(nbg_ctx* c, const StateView& s, const double* hu, const double* hv, bool v_read, StepRef pos)
+{
+    k_accel_import<<<grid_for(c->cols, 256), 256, 0, c->stream>>>(c->d, s, hu, hv, v_read ? 1 : 0, pos);
+    NBG_LAUNCH_CHECK(c, "k_accel_import");
+    return NBG_OK;
+}
+
+int launch_accel_export(nbg_ctx* c, const StateView& s, double* hdv, double* hv, unsigned* hstat, int64_t* counter)
+{
+    k_accel_export<<<grid_for(3 * c->cols, 256), 256, 0, c->stream>>>(c->d, s, hdv, hv, hstat, counter,
+                                                                      c->d.therm == NBG_THERMO_NOSEHOOVER ? 1 : 0);
+    NBG_LAUNCH_CHECK(c, "k_accel_export");
+    return NBG_OK;
+}
+
 int launch_counter_advance(nbg_ctx* c, int64_t* counter, int64_t by)
 {
     k_step_advance<<<1, 1, 0, c->stream>>>(counter, by);

@@ -879,50 +879,39 @@ static void resident_dirty(nbg_ctx* c)
     c->cluster_lists_valid = false;
 }
 
-// The list path's right-hand side as one captured graph: status clear, the
-// upload of u (and v) from the pinned staging, the packing with the
-// displacement check against the positions of the last build, the list
-// kernels (which rebuild only when flagged), the force kernels, the
-// thermostat term, and the downloads of dv (and the Nose-Hoover rate) and of
-// the status word; a last node advances the call counter whose parity picks
-// the rebuild flags.
+// The list path's right-hand side as one captured graph of kernels only:
+// an import node reads u (and v) from the pinned staging (mapped host
+// memory, read by the GPU over the CPU-GPU link), stores and packs them,
+// checks the displacement against the last build and clears the status;
+// the list kernels rebuild only when flagged; the force kernels and the
+// thermostat term; an export node writes dv (and the Nose-Hoover rate) and
+// the status word back into the staging and advances the call counter
+// whose parity picks the rebuild flags.
 static int accel_graph_capture(nbg_ctx* c, bool v_read)
 {
     const size_t sb = state_bytes(c);
     if (!c->hst) {
-        cudaError_t e = cudaMallocHost(&c->hst, 3 * sb + 64);
+        cudaError_t e = cudaHostAlloc((void**)&c->hst, 3 * sb + 64, cudaHostAllocMapped);
         if (e != cudaSuccess) {
             cudaGetLastError();
             c->hst = nullptr;
-            return fail(c, NBG_ERR_NOMEM, "pinned staging of the right-hand side: cudaMallocHost failed");
+            return fail(c, NBG_ERR_NOMEM, "pinned staging of the right-hand side: cudaHostAlloc failed");
         }
     }
+    double* dst = nullptr;
+    CK(cudaHostGetDevicePointer((void**)&dst, c->hst, 0), "staging device pointer");
     int st;
     if (!c->accel_step && (st = dalloc(c, &c->accel_step, 1))) return st;
-    double* hu = c->hst;
-    double* hv = c->hst + 3 * c->cols;
-    double* hdv = c->hst + 6 * c->cols;
-    unsigned* hstat = reinterpret_cast<unsigned*>(c->hst + 9 * c->cols);
     const int64_t launches0 = c->launches;
     const StepRef pos{0, c->accel_step};
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "accel capture begin");
-    st = NBG_OK;
-    auto q = [&](cudaError_t e) {
-        if (e != cudaSuccess && st == NBG_OK) st = cuda_fail(c, e, "accel capture");
-    };
-    q(cudaMemsetAsync(c->d.status, 0, sizeof(unsigned), c->stream));
-    q(cudaMemcpyAsync(c->ev.x, hu, sb, cudaMemcpyHostToDevice, c->stream));
-    if (v_read) q(cudaMemcpyAsync(c->ev.v, hv, sb, cudaMemcpyHostToDevice, c->stream));
-    q(cudaMemsetAsync(c->ev.a_new, 0, sb, c->stream));
-    if (st == NBG_OK) st = launch_pack_disp(c, c->ev.x, pos);
+    st = launch_accel_import(c, c->ev, dst, dst + 3 * c->cols, v_read, pos);
     if (st == NBG_OK) st = forces(c, c->ev, false, pos);
     if (st == NBG_OK) st = launch_rhs_thermostat(c, c->ev);
-    q(cudaMemcpyAsync(hdv, c->ev.a_new, sb, cudaMemcpyDeviceToHost, c->stream));
-    if (c->d.therm == NBG_THERMO_NOSEHOOVER)
-        q(cudaMemcpyAsync(hv + 3 * c->n, c->ev.v + 3 * c->n, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    q(cudaMemcpyAsync(hstat, c->d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-    if (st == NBG_OK) st = launch_counter_advance(c, c->accel_step, 1);
+    if (st == NBG_OK)
+        st = launch_accel_export(c, c->ev, dst + 6 * c->cols, dst + 3 * c->cols,
+                                 reinterpret_cast<unsigned*>(dst + 9 * c->cols), c->accel_step);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->accel_graph_launches = c->launches - launches0;
     c->launches = launches0;

@@ -256,7 +256,7 @@ struct nbg_ctx {
     // pinned staging buffers; the lists are rebuilt only when an atom moved
     // more than skin/2 since they were built for an earlier call's positions
     cudaGraphExec_t accel_graph = nullptr;
-    double* hst = nullptr;         // pinned [3][3 cols] u, v, dv, then the status word
+    double* hst = nullptr;         // pinned, mapped [3][3 cols] u, v, dv, then the status word (the GPU reads and writes it)
     int64_t* accel_step = nullptr; // device counter of the calls (parity of the rebuild flags)
     bool accel_lists_valid = false;
     int64_t accel_graph_launches = 0;  // kernels per replay
@@ -340,6 +340,8 @@ int launch_andersen(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_em(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_step_advance(nbg_ctx* c, int64_t by);
 int launch_pack_disp(nbg_ctx* c, const double* X, StepRef pos);
+int launch_accel_import(nbg_ctx* c, const StateView& s, const double* hu, const double* hv, bool v_read, StepRef pos);
+int launch_accel_export(nbg_ctx* c, const StateView& s, double* hdv, double* hv, unsigned* hstat, int64_t* counter);
 int launch_counter_advance(nbg_ctx* c, int64_t* counter, int64_t by);
 int launch_baoab_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt);

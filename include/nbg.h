@@ -310,6 +310,26 @@ NBG_API int nbg_gravity_accel_noalloc(const double* x, const double* mass, int64
    may be NULL. NBG_ERR_UNSUPPORTED off the list path. */
 NBG_API int nbg_force_form(nbg_ctx* ctx, int32_t* lanes, int32_t* fixed_point);
 
+/* Replica ensembles (no reference counterpart: the reference runs one
+   simulation per call). A batch of potential systems under cubic boundaries
+   with the Langevin thermostat integrated by BAOAB, or without thermostat,
+   and replicas of at most 9216 atoms, advances as one persistent launch per
+   chunk of steps: a CTA per replica (largest first) runs the replica's whole
+   step loop (integration, in-launch Verlet-list rebuilds from a
+   shared-memory cell sort, pair forces gathering neighbours from shared
+   memory), synchronising only its own threads. nbg_ensemble_form returns 1
+   and the form (lanes per atom, threads per replica, cells: 1 = of at least
+   the list radius over 3^3 cells, 2 = of half of it over 5^3) when the batch
+   runs it, 0 otherwise (any pointer may be NULL). NBG_NO_ENSEMBLE_LOOP at
+   creation keeps a batch on the step graphs. */
+NBG_API int nbg_ensemble_form(nbg_ctx* ctx, int32_t* lanes, int32_t* threads, int32_t* cells);
+/* Autotuner of the loop: forms f = 0..11 (lanes 4 or 8 = f / 6; threads 512,
+   768, 1024 = (f / 2) % 3; cells 1 or 2 = 1 + f % 2) each run `steps` steps
+   from the resident state, timed (ms per step into ms[12], may be NULL); the
+   state and the step counter are restored after each, and the fastest form
+   is kept and written to form[3] (lanes, threads, cells). */
+NBG_API int nbg_ensemble_tune(nbg_ctx* ctx, int32_t steps, int32_t* form, double* ms);
+
 /* Measured FP32 FMA throughput of a device in TFLOP/s (an FMA counts 2):
    the roofline denominator of the FP32-bound gravity kernel. */
 NBG_API int nbg_probe_fp32_peak(int device, double* tflops);

@@ -143,6 +143,9 @@ SIGNATURES = {
     "nbg_set_profiling": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbg_force_kernel_time": (ctypes.c_int, [_vp, _dp, ctypes.POINTER(ctypes.c_int64)]),
     "nbg_force_form": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "nbg_ensemble_form": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32)]),
+    "nbg_ensemble_tune": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp]),
     "nbg_probe_fp32_peak": (ctypes.c_int, [ctypes.c_int, _dp]),
     "nbg_gravity_accel_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_double, _vp, _vp]),
     "nbg_ml_param_count": (ctypes.c_int, []),

@@ -394,6 +394,7 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_list_build_warps(Dev d, ListC
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos)
 {
     c->accel_lists_valid = false;  // the lists follow other positions now
+    c->ens_lists_valid = false;
     ListCtl L{pos, force ? 1 : 0};
     k_cell_fill<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, L, s.x);
     NBG_LAUNCH_CHECK(c, "k_cell_fill");

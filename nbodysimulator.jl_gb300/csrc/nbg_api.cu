@@ -220,6 +220,8 @@ static int alloc_lists(nbg_ctx* c, int cell_cap, int nbr_cap)
 static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
 {
     const nbg_system_desc* d0 = &descs[0];
+    // read before the list buffers (and the force kernel's form) are set up
+    if (getenv("NBG_FX_BLOCK")) c->fx_block_only = true;  // per-block list staging (comparisons)
     c->desc = *d0;
     c->desc.mass = c->desc.charge = c->desc.dipole = nullptr;
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
@@ -347,6 +349,10 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
                 R.fx_sig2_hi = (float)s2;
                 R.fx_sig2_lo = (float)(s2 - (double)R.fx_sig2_hi);
             }
+            const double rlb = list_radius(d);
+            R.fx_rl2 = f_up(rlb * rlb * (1.0 + 1e-5) * iu2);
+            const double sh = 0.5 * std::max(d->skin, 0.0);
+            R.fx_disp2 = f_down(sh * sh * iu2 * (1.0 - 1e-4));
             if (pots & NBG_POT_EL) {
                 const double R2 = d0->el_cutoff * d0->el_cutoff * iu2;
                 R.fx_el_lo = f_down(std::min(R2 * (1.0 - m), img2b));
@@ -562,13 +568,22 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     }
     if (getenv("NBG_NO_GRAPHS")) c->use_graphs = false;  // direct launches, for comparisons
     if (getenv("NBG_NO_CLUSTER")) c->cluster_disabled = true;  // the graph step loop for small systems too
-    if (getenv("NBG_FX_BLOCK")) c->fx_block_only = true;         // per-block list staging (comparisons)
     // a test of the cluster loop's bounded waits: the first launch drops the
     // position copies of one step ("last" or a step index), so that the
     // receivers' waits run out with no copy in flight
     if (const char* td = getenv("NBG_TEST_CLUSTER_DROP"))
         c->cluster_test_drop = strcmp(td, "last") == 0 ? -1 : std::max(0, atoi(td));
     if ((st = plan_cluster(c))) return st;
+    if (getenv("NBG_NO_ENSEMBLE_LOOP")) c->ens_disabled = true;  // batches on the step graphs (comparisons)
+    if (ensemble_plan(c)) {
+        std::vector<int> ord(nrep);
+        for (int r = 0; r < nrep; ++r) ord[r] = r;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return c->reps_h[a].n > c->reps_h[b].n; });
+        if ((st = dalloc(c, &c->ens_order, nrep))) return st;
+        CK(cudaMemcpy(c->ens_order, ord.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice), "replica order");
+        if ((st = dalloc(c, &c->ens_since, nrep))) return st;
+        if ((st = dalloc(c, &c->ens_pref, n))) return st;
+    }
     if (c->path == PATH_GRAVITY) {
         const char* gv = getenv("NBG_GRAVITY_VARIANT");  // kernel-form override for tuning sweeps
         if (gv) c->grav_variant = atoi(gv);
@@ -603,6 +618,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
 static int plan_cluster(nbg_ctx* c)
 {
     c->cluster_lists_valid = false;
+    c->ens_lists_valid = false;
     if (!cluster_plan(c)) return NBG_OK;
     int st;
     if (!c->cluster_x && (st = dalloc(c, &c->cluster_x, 6 * (size_t)c->n))) return st;
@@ -681,6 +697,15 @@ extern "C" int nbg_force_form(nbg_ctx* c, int32_t* lanes, int32_t* fixed_point)
     if (lanes) *lanes = c->list_lpa;
     if (fixed_point) *fixed_point = c->fx_ready ? 1 : 0;
     return NBG_OK;
+}
+
+extern "C" int nbg_ensemble_form(nbg_ctx* c, int32_t* lanes, int32_t* threads, int32_t* cells)
+{
+    if (!c) return NBG_ERR_ARG;
+    if (lanes) *lanes = c->ens_ok ? c->ens_lpa : 0;
+    if (threads) *threads = c->ens_ok ? c->ens_threads : 0;
+    if (cells) *cells = c->ens_ok ? (c->ens_cells == 2 ? 2 : 1) : 0;
+    return c->ens_ok ? 1 : 0;
 }
 
 extern "C" int nbg_cluster_shape(nbg_ctx* c, int32_t* ctas, int32_t* lanes)
@@ -877,6 +902,7 @@ static void resident_dirty(nbg_ctx* c)
     c->steps_since_build = -1;
     c->respa_valid = false;
     c->cluster_lists_valid = false;
+    c->ens_lists_valid = false;
 }
 
 // The list path's right-hand side as one captured graph of kernels only:
@@ -1007,6 +1033,7 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
     c->T_valid = false;
     c->steps_since_build = -1;
     c->cluster_lists_valid = false;
+    c->ens_lists_valid = false;
     // the gravity sort schedule restarts too: runs from the same state give
     // the same bits
     c->grav_evals = 0;
@@ -1278,6 +1305,7 @@ static int settle(nbg_ctx* c)
         c->step = c->pend_step0;
         c->steps_since_build = -1;
         c->cluster_lists_valid = false;
+        c->ens_lists_valid = false;
         c->T_valid = false;
         return status_error(c, ST_TIMEOUT);
     }
@@ -1288,6 +1316,7 @@ static int settle(nbg_ctx* c)
         c->step = c->pend_step0;
         c->steps_since_build = -1;
         c->cluster_lists_valid = false;
+        c->ens_lists_valid = false;
         c->T_valid = false;
         if ((st = clear_status(c))) return st;
         if ((st = launch_pack(c, c->st))) return st;
@@ -1342,6 +1371,16 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
         int64_t s = 0;
         bool counter_set = false;
         while (s < k) {
+            if (c->ens_ok && !is_em(c)) {
+                // every replica's steps of the chunk in one launch (a CTA per
+                // replica; its lists stay with it between launches)
+                if ((st = launch_ensemble(c, c->st, dt, k - s, c->step))) break;
+                c->ens_lists_valid = true;
+                c->step += k - s;
+                c->steps_since_build = -1;
+                s = k;
+                continue;
+            }
             if (c->cluster_ok) {
                 // the whole chunk in one persistent cluster launch (its lists
                 // live in shared memory: the global ones are rebuilt later)
@@ -1352,7 +1391,8 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
                 s = k;
                 continue;
             }
-            c->cluster_lists_valid = false;  // the graph or direct steps below move the state
+            c->cluster_lists_valid = false;
+            c->ens_lists_valid = false;  // the graph or direct steps below move the state
             if (graphs && graph_aligned(c) && k - s >= graph_period(c)) {
                 if (!c->graph || c->graph_dt != dt || c->graph_sink != c->sink_on) {
                     if ((st = capture_graph(c, dt))) break;
@@ -1387,6 +1427,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
             c->step = step0;
             c->steps_since_build = -1;
             c->cluster_lists_valid = false;
+            c->ens_lists_valid = false;
             c->T_valid = false;
             return status_error(c, ST_TIMEOUT);  // (whatever else the abandoned steps flagged)
         }
@@ -1398,6 +1439,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
             c->step = step0;
             c->steps_since_build = -1;
             c->cluster_lists_valid = false;
+            c->ens_lists_valid = false;
             c->T_valid = false;
             if ((st = clear_status(c))) return st;
             if ((st = launch_pack(c, c->st))) return st;
@@ -2240,5 +2282,88 @@ extern "C" int nbg_autotune(nbg_ctx* c, int32_t reps, int32_t* lpa_out, double* 
     if (st == NBG_OK) st = st2;
     resident_dirty(c);  // the next step rebuilds the list in the chosen layout
     if (lpa_out) *lpa_out = c->list_lpa;
+    return st;
+}
+
+// Autotuner of the persistent ensemble loop: every form (lanes per atom 4 or
+// 8; 512, 768 or 1024 threads per replica; cells of rl over 3^3 or of rl/2
+// over 5^3) runs `steps` steps from the resident state (lists built afresh,
+// so every form pays one build), timed by CUDA events; the state and the
+// step counter are put back after each, and the fastest form is kept.
+extern "C" int nbg_ensemble_tune(nbg_ctx* c, int32_t steps, int32_t* form, double* ms_out)
+{
+    if (!c) return NBG_ERR_ARG;
+    NBG_ENTER(c);
+    if (!c->ens_ok) return fail(c, NBG_ERR_UNSUPPORTED, "the batch does not run the persistent ensemble loop");
+    if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
+    if (steps < 1) steps = 1;
+    int st;
+    if (!c->accel_valid && (st = init_accel(c))) return st;
+    if ((st = ensure_backup(c))) return st;
+    if ((st = backup_state(c, false))) return st;
+    const double dt = c->baoab_dt > 0.0 ? c->baoab_dt : 0.005;
+    if (c->baoab && c->baoab_dt <= 0.0) {
+        for (int r = 0; r < c->nrep; ++r) {
+            RepDev& R = c->reps_h[r];
+            R.bc1 = std::exp(-R.tparam * dt);
+            R.bsd = std::sqrt(1.0 - R.bc1 * R.bc1) * std::sqrt(c->d.kb * R.T0);
+        }
+        CK(cudaMemcpy(const_cast<RepDev*>(c->d.reps), c->reps_h.data(), sizeof(RepDev) * c->nrep,
+                      cudaMemcpyHostToDevice), "replica upload");
+        c->baoab_dt = dt;
+    }
+    const int64_t step0 = c->step;
+    const int keep[3] = {c->ens_lpa, c->ens_threads, c->ens_cells};
+    int best = -1;
+    double best_ms = INFINITY;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    static const int lanes_of[2] = {4, 8}, threads_of[3] = {512, 768, 1024};
+    for (int f = 0; f < 12 && st == NBG_OK; ++f) {
+        c->ens_lpa = lanes_of[f / 6];
+        c->ens_threads = threads_of[(f / 2) % 3];
+        c->ens_cells = 1 + f % 2;
+        double ms = INFINITY;
+        if (ensemble_plan(c)) {
+            c->ens_lists_valid = false;
+            if ((st = clear_status(c))) break;
+            cudaEventRecord(e0, c->stream);
+            if ((st = launch_ensemble(c, c->st, dt, steps, step0))) break;
+            cudaEventRecord(e1, c->stream);
+            unsigned w = 0;
+            if ((st = read_status(c, &w))) break;
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (!(w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT))) ms = (double)t / steps;
+            if ((st = backup_state(c, true))) break;
+        }
+        if (ms_out) ms_out[f] = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = f;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st == NBG_OK && best >= 0) {
+        c->ens_lpa = lanes_of[best / 6];
+        c->ens_threads = threads_of[(best / 2) % 3];
+        c->ens_cells = 1 + best % 2;
+    } else {
+        c->ens_lpa = keep[0];
+        c->ens_threads = keep[1];
+        c->ens_cells = keep[2];
+    }
+    ensemble_plan(c);
+    c->ens_lists_valid = false;
+    c->steps_since_build = -1;
+    int st2 = clear_status(c);
+    if (st == NBG_OK) st = st2;
+    if (form) {
+        form[0] = c->ens_lpa;
+        form[1] = c->ens_threads;
+        form[2] = c->ens_cells == 2 ? 2 : 1;
+    }
     return st;
 }

@@ -76,6 +76,12 @@ struct RepDev {
     float fx_sig2_hi, fx_sig2_lo;  // sigma^2 / u^2
     float fx_krf;                  // 2 k_rf u^3
     double fx_fscale;
+    float fx_rl2;                  // list radius^2 (inflated), box units
+    float fx_disp2;                // (skin/2)^2 in box units, slightly inside (rebuild trigger)
+    // cell grid of the persistent ensemble loop's in-kernel list build, per
+    // cell-width choice [0]: cells of >= rl over 3^3 cells, [1]: >= rl/2 over
+    // 5^3; nc = 1 (ns = 0): one cell holds the replica
+    int ens_nc[2], ens_ns[2];
 };
 
 // Everything a kernel needs, passed by value.
@@ -221,6 +227,15 @@ struct nbg_ctx {
     double* cluster_xref = nullptr;  // [3n] positions at the cluster lists' build
     int* cluster_since = nullptr;
     bool cluster_lists_valid = false;
+    // replica ensembles: one persistent launch per chunk of steps, a CTA per
+    // replica (k_ensemble.cu)
+    bool ens_ok = false, ens_disabled = false;
+    bool ens_lists_valid = false;  // the lists, their reference positions and step counts are the loop's
+    int ens_lpa = 4, ens_threads = 768, ens_cells = 0;  // form: lanes per atom, threads, cell width (0 = as planned, 1 = rl, 2 = rl/2)
+    size_t ens_smem = 0;
+    int* ens_order = nullptr;     // replicas, largest first (CTA b runs replica order[b])
+    int* ens_since = nullptr;     // per replica: steps since its list build
+    uint4* ens_pref = nullptr;    // per atom: fixed-point position at its replica's last build
     // test of the cluster loop's timeout path: the next launch drops the
     // position copies of this step (-1: its last step; -2: none)
     int cluster_test_drop = -2;
@@ -327,6 +342,9 @@ int launch_gravity(nbg_ctx* c, const StateView& s);
 bool cluster_plan(nbg_ctx* c);
 // step0: the time index of the state at the launch (for the frame sink)
 int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every, int64_t step0);
+// replica ensembles on the persistent per-replica loop (k_ensemble.cu)
+bool ensemble_plan(nbg_ctx* c);
+int launch_ensemble(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int64_t step0);
 int launch_allpairs(nbg_ctx* c, const StateView& s);
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
 int launch_force_list(nbg_ctx* c, const StateView& s);

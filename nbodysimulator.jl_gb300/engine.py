@@ -172,6 +172,23 @@ class Engine:
         self._chk(st)
         return lanes.value, bool(fx.value)
 
+    def ensemble_form(self):
+        """(lanes per atom, threads per replica, cells) of the persistent
+        ensemble loop, or None when the context does not run it."""
+        a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        used = self.lib.nbg_ensemble_form(self.ctx, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        if used < 0:
+            self._chk(used)
+        return (a.value, b.value, c.value) if used == 1 else None
+
+    def ensemble_tune(self, steps=5):
+        """Time every form of the ensemble loop and keep the fastest; returns
+        ((lanes, threads, cells), ms per step of the 12 forms)."""
+        form = (ctypes.c_int32 * 3)()
+        ms = np.zeros(12)
+        self._chk(self.lib.nbg_ensemble_tune(self.ctx, int(steps), form, _abi.as_dptr(ms)))
+        return (form[0], form[1], form[2]), ms
+
     def force_kernel_time(self):
         """(summed ms, launches) of the dominant force kernel since the last call."""
         ms = ctypes.c_double()

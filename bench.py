@@ -701,9 +701,15 @@ def main():
     eng.set_state(u0, v0)
     e_start = None if batch else eng.energy(u0, v0)
     tuned = None
+    ens_tuned = None
     if args.workload in ("lj", "water", "ensemble"):
         # the list force kernel's lanes per atom, timed on this state (untimed here)
         tuned = eng.autotune(5)
+    if batch and eng.ensemble_form() is not None:
+        # the persistent ensemble loop's form (lanes, threads per replica,
+        # cell width), timed on this state (untimed here)
+        eng.advance(dt, 1)  # the BAOAB coefficients of this dt
+        ens_tuned = eng.ensemble_tune(5)
     eng.advance(dt, args.warmup)
     torch.cuda.synchronize()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
@@ -747,6 +753,7 @@ def main():
     # small systems run the persistent cluster step loop: one launch per
     # chunk of steps, timed whole
     cluster = None if batch else eng.cluster_shape()
+    ens = eng.ensemble_form() if batch else None
     eng.set_profiling(False)
     total_ms = max_over_ranks(float(sum(step_ms)), dist, f"cuda:{device}")
     if dist is not None:
@@ -826,7 +833,7 @@ def main():
                 "path": "nbg_run from host buffers, positions and velocities saved (run_simulation)"}
     work, unit, bound = algorithmic_work(args.workload, n, eng)
     avg_kern = kern_ms / max(kern_n, 1)
-    if cluster is not None:
+    if cluster is not None or ens is not None:
         avg_kern = kern_ms / prof_steps  # per step of the multi-step launches
     achieved = work / (avg_kern / 1e3) / (1e12 if unit == "TFLOP/s" else 1e9)
     peaks = measured_peaks()
@@ -836,7 +843,8 @@ def main():
     else:
         peak = peaks.get("hbm_gbs", 6800.0)
         peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    kernel_name = "k_gravity" if args.workload == "gravity" else ("k_cluster_vv" if cluster else "k_force_list")
+    kernel_name = ("k_gravity" if args.workload == "gravity" else "k_cluster_vv" if cluster else
+                   "k_ensemble" if ens else "k_force_list")
     traffic = profile_traffic(f"{kernel_name}:{w['name']}")
     roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
                 "frac": (achieved / peak) if peak else None, "traffic": traffic, "kernel": kernel_name,
@@ -844,6 +852,9 @@ def main():
     if cluster is not None:
         roofline["kernel_ms_is"] = f"per step: {prof_steps} steps in {kern_n} launch(es) of the whole step loop"
         roofline["cluster"] = {"ctas": cluster[0], "lanes_per_atom": cluster[1]}
+    if ens is not None:
+        roofline["kernel_ms_is"] = (f"per step: {prof_steps} steps in {kern_n} launch(es) of the whole step loop "
+                                    "(a CTA per replica); achieved = 406 B per atom-step of algorithmic traffic")
     config = {"workload": w["name"], "N": n, "dt": dt, "integrator": "velocity Verlet",
               "l2": ("512 MB buffer written between timed steps (L2 flushed)" if flush_steps else
                      "working set larger than L2" if batch else "no flush (state L2-resident across steps)"),
@@ -856,6 +867,13 @@ def main():
     if batch:
         config.update(integrator="BAOAB Langevin (gamma=1)", replicas=len(wl.sizes),
                       atoms_min=int(min(wl.sizes)), atoms_max=int(max(wl.sizes)))
+        config["step_loop"] = ("persistent: one launch per chunk of steps, a CTA per replica" if ens else
+                               "CUDA graphs of per-step kernels")
+    if ens_tuned is not None:
+        form, ms = ens_tuned
+        config["ensemble_form"] = {"lanes_per_atom": form[0], "threads_per_replica": form[1],
+                                   "cells": "list radius, 3x3x3" if form[2] == 1 else "half list radius, 5x5x5"}
+        config["ensemble_autotune_ms_per_step"] = [round(float(x), 4) for x in ms]
     line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -161,6 +161,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
         const bool build = __syncthreads_or(moved ? 1 : 0) || since < 0 ||
                            (A.rebuild_every > 0 && since + 1 >= A.rebuild_every);
         if (build) {
+            if (tid == 0) atomicAdd(d.build_count, 1ull);  // the replica's builds, as the graph path counts them
             // counting sort of the atoms into cells, each cell in index order
             for (int c = tid; c < ncell; c += THREADS) ccur[c] = 0;
             __syncthreads();

@@ -446,11 +446,16 @@ def run_mts(args, rank, world):
     ms_ml, l_ml, st_ml = timed(lambda warm: eng.respa_run(dt, inner, outer if warm is None else warm, 0.02))
     ms_ex, l_ex, _ = timed(lambda warm: eng.respa_run(dt, inner, outer if warm is None else warm, 0.0,
                                                         exact_split=True))
+    # the scheme's own cost: the same outer steps with no fast non-bonded
+    # force at all (bonded terms only), the ceiling of any fast model here
+    ms_sk, l_sk, _ = timed(lambda warm: eng.respa_run(dt, inner, outer if warm is None else warm, 0.0,
+                                                        no_fast_force=True))
     clocks = sampler.stop()
     fs_per_day = lambda ms, fs: fs / (ms / 1e3) * 86400 / 1e6  # ns/day
     ns_plain = fs_per_day(ms_plain, K * dt * 1e3)
     ns_ml = fs_per_day(ms_ml, K * dt * 1e3)
     ns_ex = fs_per_day(ms_ex, K * dt * 1e3)
+    ns_sk = fs_per_day(ms_sk, K * dt * 1e3)
 
     # end to end through the public call: host state in, r-RESPA, host state out
     uh = torch.from_numpy(u0).pin_memory().numpy()
@@ -492,6 +497,9 @@ def run_mts(args, rank, world):
                                     "final_loss_std_units": list(loss2), "train_s": t_train}},
             "plain_ns_per_day": ns_plain, "exact_split_ns_per_day": ns_ex,
             "speedup_vs_plain": ns_ml / ns_plain, "exact_split_speedup_vs_plain": ns_ex / ns_plain,
+            "no_fast_force_ns_per_day": ns_sk, "no_fast_force_speedup_vs_plain": ns_sk / ns_plain,
+            "ms_per_outer_step": {"plain_4_steps": 4 * ms_plain / K, "learned": inner * ms_ml / K,
+                                  "exact_split": inner * ms_ex / K, "no_fast_force": inner * ms_sk / K},
             "atom_steps_per_s": {"plain": n * K / (ms_plain / 1e3), "learned_respa": n * K / (ms_ml / 1e3),
                                  "exact_split_respa": n * K / (ms_ex / 1e3)},
             "learned_force_rel_rmse": force_rmse,

@@ -403,6 +403,11 @@ NBG_API int nbg_ml_batch_gradient(nbg_ctx* ctx, int32_t species, const float* x,
    NBG_RESPA_EXACT_SPLIT the fast force uses the exact short-range force in
    place of the learned one (the classical split the model stands in for). */
 #define NBG_RESPA_EXACT_SPLIT 1
+/* With NBG_RESPA_NO_FAST_FORCE the fast force is the bonded terms alone and
+   the slow force all of the non-bonded one: the integrator's own cost per
+   outer step, an upper bound of the speed of any fast non-bonded model in
+   this scheme (the dynamics is not meant to be accurate). */
+#define NBG_RESPA_NO_FAST_FORCE 2
 NBG_API int nbg_respa_run(nbg_ctx* ctx, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,
                           nbg_respa_stats* stats);
 

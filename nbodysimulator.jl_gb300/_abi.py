@@ -104,6 +104,7 @@ class NbgRespaStats(ctypes.Structure):
 NBG_ML_NPARAM = 25091
 NBG_ML_NTRAIN = 24961
 NBG_RESPA_EXACT_SPLIT = 1
+NBG_RESPA_NO_FAST_FORCE = 2
 
 
 class EngineError(RuntimeError):

@@ -105,10 +105,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
     int* sorted = ccur + ncell;                            // [n] atoms in cell order
     __shared__ int warp_tot[THREADS / 32];
     const int tid = threadIdx.x, lane = tid % LPA, g = tid / LPA;
-    const unsigned gshift = (unsigned)((tid & 31) / LPA * LPA);
-    // the group's lanes within the warp (groups of one warp may loop
-    // different numbers of times: votes are per group)
-    const unsigned gmask = (LPA == 32 ? 0xffffffffu : ((1u << LPA) - 1u)) << gshift;
     const double dt = A.dt, hdt = 0.5 * dt, dtsq = dt * dt;
     const double c1 = R.bc1;
     const int cap = d.nbr_cap;
@@ -188,54 +184,57 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
                 }
             }
             __syncthreads();
-            // list rows: a group of LPA lanes per atom scans the stencil
-            // cells in order, entries kept in scan order (ballot compaction)
-            const int w = 2 * ns + 1;
-            for (int i0 = 0; i0 < n; i0 += G) {
-                const int i = i0 + g;
-                const bool active = i < n;
-                const uint4 qi = pos[active ? i : 0];
-                const int cx = ns > 0 ? (int)__umulhi(qi.x, (unsigned)nc) : 0;
-                const int cy = ns > 0 ? (int)__umulhi(qi.y, (unsigned)nc) : 0;
-                const int cz = ns > 0 ? (int)__umulhi(qi.z, (unsigned)nc) : 0;
-                const int64_t gi = a0 + (active ? i : 0);
-                int cnt = 0;
-                for (int qc = 0; qc < w * w * w; ++qc) {
-                    int nx = cx + qc / (w * w) - ns, ny = cy + (qc / w) % w - ns, nz = cz + qc % w - ns;
-                    nx += nx < 0 ? nc : 0;
-                    nx -= nx >= nc ? nc : 0;
-                    ny += ny < 0 ? nc : 0;
-                    ny -= ny >= nc ? nc : 0;
-                    nz += nz < 0 ? nc : 0;
-                    nz -= nz >= nc ? nc : 0;
-                    const int cell = (nx * nc + ny) * nc + nz;
-                    const int b0 = cstart[cell], m = cstart[cell + 1] - b0;
-                    for (int k0 = 0; k0 < m; k0 += LPA) {
-                        const int k = k0 + lane;
-                        bool take = false;
-                        int j = 0;
-                        if (active && k < m) {
-                            j = sorted[b0 + k];
-                            if (j != i) {
-                                float ddx, ddy, ddz;
-                                take = fx_r2(qi, pos[j], ddx, ddy, ddz) < R.fx_rl2;
+            // list rows: a warp per cell, lane = one of the cell's atoms (32
+            // at a time); the stencil cells' atoms are read once per warp as
+            // shared-memory broadcasts, in stencil then index order, and each
+            // lane appends those within the list radius to its own row
+            {
+                const int wid = tid >> 5, wl = tid & 31;
+                for (int c = wid; c < ncell; c += THREADS / 32) {
+                    const int cx = ns > 0 ? c / (nc * nc) : 0, cy = ns > 0 ? (c / nc) % nc : 0,
+                              cz = ns > 0 ? c % nc : 0;
+                    const int c0 = cstart[c], c1 = cstart[c + 1];
+                    for (int a0c = c0; a0c < c1; a0c += 32) {
+                        const bool active = a0c + wl < c1;
+                        const int i = active ? sorted[a0c + wl] : 0;
+                        const uint4 qi = pos[i];
+                        const int64_t gi = a0 + i;
+                        int* row = d.nbr + gi * d.nbr_istride;
+                        int cnt = 0;
+                        for (int ox = -ns; ox <= ns; ++ox) {
+                            int nx = cx + ox;
+                            nx += nx < 0 ? nc : 0;
+                            nx -= nx >= nc ? nc : 0;
+                            for (int oy = -ns; oy <= ns; ++oy) {
+                                int ny = cy + oy;
+                                ny += ny < 0 ? nc : 0;
+                                ny -= ny >= nc ? nc : 0;
+                                for (int oz = -ns; oz <= ns; ++oz) {
+                                    int nz = cz + oz;
+                                    nz += nz < 0 ? nc : 0;
+                                    nz -= nz >= nc ? nc : 0;
+                                    const int cq = (nx * nc + ny) * nc + nz;
+                                    const int q1 = cstart[cq + 1];
+                                    for (int k = cstart[cq]; k < q1; ++k) {
+                                        const int j = sorted[k];
+                                        float ddx, ddy, ddz;
+                                        if (active && j != i && fx_r2(qi, pos[j], ddx, ddy, ddz) < R.fx_rl2) {
+                                            if (cnt < cap) row[(int64_t)cnt * d.nbr_kstride] = (int)(a0 + j);
+                                            ++cnt;
+                                        }
+                                    }
+                                }
                             }
                         }
-                        const unsigned bal = (__ballot_sync(gmask, take) & gmask) >> gshift;
-                        if (take) {
-                            const int p = cnt + __popc(bal & ((1u << lane) - 1u));
-                            if (p < cap) d.nbr[(int64_t)p * d.nbr_kstride + gi * d.nbr_istride] = (int)(a0 + j);
+                        if (active) {
+                            if (cnt > cap) {
+                                status_set(d.status, ST_NBR_OVERFLOW);
+                                cnt = cap;
+                            }
+                            d.nbr_count[gi] = cnt;
+                            A.pref[gi] = qi;
                         }
-                        cnt += __popc(bal);
                     }
-                }
-                if (active && lane == 0) {
-                    if (cnt > cap) {
-                        status_set(d.status, ST_NBR_OVERFLOW);
-                        cnt = cap;
-                    }
-                    d.nbr_count[gi] = cnt;
-                    A.pref[gi] = qi;
                 }
             }
             since = 0;

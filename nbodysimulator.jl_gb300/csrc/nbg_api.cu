@@ -2014,21 +2014,29 @@ extern "C" int nbg_ml_rows(nbg_ctx* c, int64_t* rows)
 // and ml_a_slow = slow (exact non-bonded - learned) accelerations.
 // The fast non-bonded acceleration into a: learned (fixed-point forces, then
 // converted) or exact short-range (written directly).
-static int respa_inner_force(nbg_ctx* c, StepRef pos, bool force_short, bool exact, double* a)
+// Fast-force modes of r-RESPA: 0 the learned model, 1 the exact short-range
+// force (the classical split), 2 none (bonded terms only: the integrator's
+// own cost, a ceiling for any fast non-bonded model).
+static int respa_inner_force(nbg_ctx* c, StepRef pos, bool force_short, int mode, double* a)
 {
-    if (exact) return launch_sr_inner(c, pos, force_short, a);
+    if (mode == 1) return launch_sr_inner(c, pos, force_short, a);
+    if (mode == 2) {
+        CK(cudaMemsetAsync(a, 0, state_bytes(c), c->stream), "fast force clear");
+        return NBG_OK;
+    }
     int st = ml_forces(c, pos, force_short, false);
     if (st) return st;
     return launch_ml_accel(c, 0, a);
 }
 
 // a -= the fast non-bonded acceleration of the last respa_inner_force
-static int respa_sub_fast(nbg_ctx* c, bool exact, double* a)
+static int respa_sub_fast(nbg_ctx* c, int mode, double* a)
 {
-    return exact ? launch_sr_accel(c, -1, a) : launch_ml_accel(c, -1, a);
+    if (mode == 2) return NBG_OK;
+    return mode == 1 ? launch_sr_accel(c, -1, a) : launch_ml_accel(c, -1, a);
 }
 
-static int respa_init(nbg_ctx* c, bool exact)
+static int respa_init(nbg_ctx* c, int exact)
 {
     int st;
     const StateView& s = c->st;
@@ -2046,7 +2054,7 @@ static int respa_init(nbg_ctx* c, bool exact)
     if ((st = respa_sub_fast(c, exact, c->ml_a_slow))) return st;
     if (c->d.therm == NBG_THERMO_BERENDSEN && (st = launch_temperature(c, s.v))) return st;  // T for the first kick
     c->respa_valid = true;
-    c->respa_exact = exact;
+    c->respa_mode = exact;
     c->accel_valid = false;  // a_old no longer holds the velocity-Verlet acceleration
     c->T_valid = false;
     return NBG_OK;
@@ -2056,7 +2064,7 @@ static int respa_init(nbg_ctx* c, bool exact)
 // velocity-Verlet steps of the fast force, the exact force at the new
 // positions (slow force and judge), slow half kick. sr.off: step index of
 // the outer step's start, counted in inner steps.
-static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, bool exact)
+static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, int exact)
 {
     int st;
     const StateView& s = c->st;
@@ -2078,7 +2086,7 @@ static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, bool exact)
     ss.a_new = c->ml_a_slow;
     if ((st = launch_force_list(c, ss))) return st;
     if ((st = respa_sub_fast(c, exact, c->ml_a_slow))) return st;
-    if (!exact) {
+    if (exact == 0) {
         // r-RESPA error check: the learned against the exact short-range force at these positions
         if ((st = launch_sr_exact(c, nullptr, c->ml_fsr))) return st;
         if ((st = launch_ml_judge(c, StepRef{sr.off + inner, sr.base}, inner, c->ml_judge_cap))) return st;
@@ -2089,7 +2097,8 @@ static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, bool exact)
 extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,
                              nbg_respa_stats* out)
 {
-    const bool exact = (flags & NBG_RESPA_EXACT_SPLIT) != 0;
+    // (named `exact` for the fast-force mode: see respa_inner_force)
+    const int exact = (flags & NBG_RESPA_NO_FAST_FORCE) ? 2 : (flags & NBG_RESPA_EXACT_SPLIT) ? 1 : 0;
     int st = ml_check(c);
     if (st) return st;
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
@@ -2112,7 +2121,7 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
     std::vector<double> judge(2 * (size_t)chunk);
     while (done < outer) {
         const int64_t k = std::min<int64_t>(chunk, outer - done);
-        if ((!c->respa_valid || c->respa_exact != exact) && (st = respa_init(c, exact))) return done_with(st);
+        if ((!c->respa_valid || c->respa_mode != exact) && (st = respa_init(c, exact))) return done_with(st);
         const int64_t step0 = c->step;
         const int64_t ssb0 = c->steps_since_build;
         const size_t sb = state_bytes(c);

@@ -317,7 +317,7 @@ struct nbg_ctx {
     int ml_judge_cap = 0;
     double* ml_a_slow = nullptr;  // r-RESPA slow acceleration (exact non-bonded - learned)
     bool respa_valid = false;     // a_old holds the fast and ml_a_slow the slow acceleration of st
-    bool respa_exact = false;     // fast force of respa_valid: exact short-range (true) or learned
+    int respa_mode = 0;           // fast force of respa_valid: 0 learned, 1 exact short-range, 2 none
     std::vector<cudaEvent_t> prof_events;  // start/stop pairs not yet read
     double prof_ms = 0.0;
     int64_t prof_count = 0;

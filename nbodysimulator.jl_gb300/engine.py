@@ -277,11 +277,14 @@ class Engine:
                                                  int(len(y)), _abi.as_fptr(g), ctypes.byref(loss)))
         return loss.value, g
 
-    def respa_run(self, dt, inner, outer, threshold=0.02, exact_split=False):
+    def respa_run(self, dt, inner, outer, threshold=0.02, exact_split=False, no_fast_force=False):
         """Advance the resident state by `outer` r-RESPA steps; returns the
-        stats struct. exact_split: exact short-range force as the fast force."""
+        stats struct. exact_split: exact short-range force as the fast force;
+        no_fast_force: bonded terms only (the integrator's own cost, a ceiling)."""
         stats = _abi.NbgRespaStats()
         flags = _abi.NBG_RESPA_EXACT_SPLIT if exact_split else 0
+        if no_fast_force:
+            flags = _abi.NBG_RESPA_NO_FAST_FORCE
         self._chk(self.lib.nbg_respa_run(self.ctx, float(dt), int(inner), int(outer), float(threshold), flags,
                                          ctypes.byref(stats)))
         return stats

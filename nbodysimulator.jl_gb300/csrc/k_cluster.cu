@@ -27,6 +27,13 @@
 //     which keeps its x, v, a in registers for the whole launch, kicks the
 //     velocity at the start of the next step.
 // Every thread of every CTA passes the same cluster barriers (no early exit).
+//
+// The same kernel with ACCEL evaluates the right-hand side alone (nbg_accel):
+// the positions come from src (pinned host memory read over the CPU-GPU
+// link, or device memory), one step of the loop without drift or kick runs
+// (exchange, displacement check, list build when needed, forces), and the
+// accelerations go to dst; the lists it keeps are its own, built for earlier
+// calls' positions, and the resident state is not touched.
 #include <algorithm>
 
 #include <cooperative_groups.h>
@@ -99,11 +106,13 @@ __device__ __forceinline__ void cl_join(float& h, float& e, int o, int width)
 // own atoms' positions at the last list build [per][3] (double), their lists
 // [per][cap], counts [per] (int) and force partials [per][6] (float: h, e per
 // component).
-template <int LPA>
+template <int LPA, bool ACCEL>
 __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s, double* xb, double dt, int nsteps,
                                                               int rebuild_every, int per, int cap, int* lst_g,
                                                               int* cnt_g, double* xref_g, int* since_g, int reuse,
-                                                              int64_t step0, int save, int drop_step)
+                                                              int64_t step0, int save, int drop_step,
+                                                              double* __restrict__ bk,
+                                                              const double* __restrict__ src, double* __restrict__ dst)
 {
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
@@ -138,11 +147,22 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     double x[3], v[3], a[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        x[k] = owner ? s.x[3 * io + k] : 0.0;
-        v[k] = owner ? s.v[3 * io + k] : 0.0;
-        a[k] = owner ? s.a_old[3 * io + k] : 0.0;
+        x[k] = owner ? (ACCEL ? src[3 * io + k] : s.x[3 * io + k]) : 0.0;
+        v[k] = owner && !ACCEL ? s.v[3 * io + k] : 0.0;
+        a[k] = owner && !ACCEL ? s.a_old[3 * io + k] : 0.0;
     }
     const double im_o = owner ? d.inv_mass[io] : 0.0;
+    if (owner && !ACCEL) {
+        // the backup of the launch's start (x, v, a_old segments of 3 cols):
+        // a timed-out or overflowed launch is undone from it
+        const size_t seg = 3 * (size_t)d.cols;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            bk[3 * io + k] = x[k];
+            bk[seg + 3 * io + k] = v[k];
+            bk[2 * seg + 3 * io + k] = a[k];
+        }
+    }
 
     // the static w parts (charge, atom flags) of every atom in both parities
     for (int j = tid; j < n; j += CL_THREADS) {
@@ -180,7 +200,17 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
 
     for (int st = 0; st <= nsteps; ++st) {
         // kick of the previous step with the forces its groups left in fsum
-        if (owner && st > 0) {
+        if constexpr (ACCEL) {
+            if (owner && st > 0) {
+                // the right-hand side: the acceleration of the source positions
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const double an = ((double)fsum[6 * ko + 2 * k] + (double)fsum[6 * ko + 2 * k + 1]) * im_o;
+                    if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+                    dst[3 * io + k] = an;
+                }
+            }
+        } else if (owner && st > 0) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const double an = ((double)fsum[6 * ko + 2 * k] + (double)fsum[6 * ko + 2 * k + 1]) * im_o;
@@ -213,7 +243,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
         if (owner) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                x[k] = drift1(x[k], v[k], a[k], dt, dtsq);
+                if (!ACCEL) x[k] = drift1(x[k], v[k], a[k], dt, dtsq);
                 X[3 * io + k] = x[k];
             }
             float h[3], l[3];
@@ -364,7 +394,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     // every CTA has waited for all copies into its shared memory, so after
     // this barrier no copy reads a CTA's shared memory any more: all may exit
     cl.sync();
-    if (owner) {
+    if (owner && !ACCEL) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             s.x[3 * io + k] = x[k];
@@ -378,19 +408,19 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     for (int t = tid; t < 3 * na; t += CL_THREADS) xref_g[3 * (size_t)a0 + t] = xref_s[t];
     for (int t = tid; t < na * cap; t += CL_THREADS) lst_g[(size_t)rank * per * cap + t] = lst[t];
     for (int t = tid; t < na; t += CL_THREADS) cnt_g[(size_t)rank * per + t] = cnt[t];
-    if (rank == 0 && tid == 0) *since_g = since;
+    if (!ACCEL && rank == 0 && tid == 0) *since_g = since;
 }
 
 typedef void (*cluster_kernel_t)(Dev, StateView, double*, double, int, int, int, int, int*, int*, double*, int*, int, int64_t,
-                                 int, int);
+                                 int, int, double*, const double*, double*);
 
-static cluster_kernel_t cluster_kernel(int lpa)
+static cluster_kernel_t cluster_kernel(int lpa, bool accel = false)
 {
     switch (lpa) {
-    case 4: return k_cluster_vv<4>;
-    case 8: return k_cluster_vv<8>;
-    case 16: return k_cluster_vv<16>;
-    default: return k_cluster_vv<32>;
+    case 4: return accel ? k_cluster_vv<4, true> : k_cluster_vv<4, false>;
+    case 8: return accel ? k_cluster_vv<8, true> : k_cluster_vv<8, false>;
+    case 16: return accel ? k_cluster_vv<16, true> : k_cluster_vv<16, false>;
+    default: return accel ? k_cluster_vv<32, true> : k_cluster_vv<32, false>;
     }
 }
 
@@ -415,9 +445,15 @@ bool cluster_plan(nbg_ctx* c)
         const size_t bytes = sizeof(float4) * 4 * (size_t)n + sizeof(double) * 3 * (size_t)per +
                              sizeof(int) * ((size_t)per * cap + per) + sizeof(float) * 6 * (size_t)per;
         if (bytes > 200 * 1024) continue;
-        cluster_kernel_t k = cluster_kernel(lpa);
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess ||
-            (C > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
+        cluster_kernel_t k = cluster_kernel(lpa), ka = cluster_kernel(lpa, true);
+        bool attrs_ok = true;
+        for (cluster_kernel_t f : {k, ka}) {
+            attrs_ok = attrs_ok &&
+                       cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess &&
+                       (C <= 8 || cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                                      cudaSuccess);
+        }
+        if (!attrs_ok) {
             cudaGetLastError();
             continue;
         }
@@ -448,7 +484,8 @@ bool cluster_plan(nbg_ctx* c)
     return false;
 }
 
-int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every, int64_t step0)
+int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every, int64_t step0,
+                      unsigned* status)
 {
     cluster_kernel_t k = cluster_kernel(c->cluster_lpa);
     cudaLaunchConfig_t cfg = {};
@@ -466,17 +503,52 @@ int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps,
     // a one-shot test of the timeout path (NBG_TEST_CLUSTER_DROP at context
     // creation): the launch drops the position copies of one step
     int drop = -2;
-    if (c->cluster_test_drop != -2) {
+    if (c->cluster_test_drop != -2 && c->cluster_test_skip > 0) {
+        --c->cluster_test_skip;
+    } else if (c->cluster_test_drop != -2) {
         drop = c->cluster_test_drop < 0 ? (int)nsteps - 1 : std::min<int>(c->cluster_test_drop, (int)nsteps - 1);
         c->cluster_test_drop = -2;
     }
+    Dev d = c->d;
+    d.status = status;
     prof_begin(c);
-    cudaError_t e = cudaLaunchKernelEx(&cfg, k, c->d, s, c->cluster_x, dt, (int)nsteps, rebuild_every,
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k, d, s, c->cluster_x, dt, (int)nsteps, rebuild_every,
                                        c->cluster_per, c->cluster_cap, c->cluster_lists, c->cluster_cnt,
                                        c->cluster_xref, c->cluster_since, c->cluster_lists_valid ? 1 : 0, step0,
-                                       c->sink_on ? 1 : 0, drop);
+                                       c->sink_on ? 1 : 0, drop, c->bk, (const double*)nullptr, (double*)nullptr);
     prof_end(c);
     if (e != cudaSuccess) return cuda_fail(c, e, "k_cluster_vv launch");
+    NBG_LAUNCH_CHECK(c, "k_cluster_vv");
+    return NBG_OK;
+}
+
+// The right-hand side of a small system (nbg_accel) as one cluster launch:
+// positions from u, accelerations to dv (device addresses: pinned host
+// memory mapped into the device's space, or device memory), the launch's
+// own lists reused while no atom moved more than skin/2 from their build.
+int launch_cluster_accel(nbg_ctx* c, const double* u, double* dv, unsigned* status)
+{
+    cluster_kernel_t k = cluster_kernel(c->cluster_lpa, true);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = c->cluster_size;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(c->cluster_size);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = c->cluster_bytes;
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    Dev d = c->d;
+    d.status = status;
+    prof_begin(c);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k, d, c->st, c->cluster_x, 0.0, 1, 0, c->cluster_per, c->cluster_cap,
+                                       c->cla_lists, c->cla_cnt, c->cla_xref, c->cluster_since,
+                                       c->cla_valid ? 1 : 0, (int64_t)0, 0, -2, c->bk, u, dv);
+    prof_end(c);
+    if (e != cudaSuccess) return cuda_fail(c, e, "k_cluster_vv (right-hand side) launch");
     NBG_LAUNCH_CHECK(c, "k_cluster_vv");
     return NBG_OK;
 }

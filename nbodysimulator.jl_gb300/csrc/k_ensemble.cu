@@ -383,7 +383,7 @@ bool ensemble_plan(nbg_ctx* c)
     return true;
 }
 
-int launch_ensemble(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int64_t step0)
+int launch_ensemble(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int64_t step0, unsigned* status)
 {
     EnsArgs A;
     A.order = c->ens_order;
@@ -397,8 +397,10 @@ int launch_ensemble(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, i
     A.step0 = step0;
     A.save = c->sink_on ? 1 : 0;
     A.baoab = c->baoab ? 1 : 0;
+    Dev d = c->d;
+    d.status = status;
     prof_begin(c);
-    ens_kernel(c)<<<(unsigned)c->nrep, (unsigned)c->ens_threads, c->ens_smem, c->stream>>>(c->d, s, A);
+    ens_kernel(c)<<<(unsigned)c->nrep, (unsigned)c->ens_threads, c->ens_smem, c->stream>>>(d, s, A);
     prof_end(c);
     NBG_LAUNCH_CHECK(c, "k_ensemble");
     return NBG_OK;

@@ -568,11 +568,14 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
     }
     if (getenv("NBG_NO_GRAPHS")) c->use_graphs = false;  // direct launches, for comparisons
     if (getenv("NBG_NO_CLUSTER")) c->cluster_disabled = true;  // the graph step loop for small systems too
-    // a test of the cluster loop's bounded waits: the first launch drops the
-    // position copies of one step ("last" or a step index), so that the
-    // receivers' waits run out with no copy in flight
-    if (const char* td = getenv("NBG_TEST_CLUSTER_DROP"))
-        c->cluster_test_drop = strcmp(td, "last") == 0 ? -1 : std::max(0, atoi(td));
+    // a test of the cluster loop's bounded waits: one launch (the first, or
+    // the one after ":k" more) drops the position copies of one step ("last"
+    // or a step index), so that the receivers' waits run out with no copy in
+    // flight
+    if (const char* td = getenv("NBG_TEST_CLUSTER_DROP")) {
+        c->cluster_test_drop = strncmp(td, "last", 4) == 0 ? -1 : std::max(0, atoi(td));
+        if (const char* k = strchr(td, ':')) c->cluster_test_skip = std::max(0, atoi(k + 1));
+    }
     if ((st = plan_cluster(c))) return st;
     if (getenv("NBG_NO_ENSEMBLE_LOOP")) c->ens_disabled = true;  // batches on the step graphs (comparisons)
     if (ensemble_plan(c)) {
@@ -619,18 +622,22 @@ static int plan_cluster(nbg_ctx* c)
 {
     c->cluster_lists_valid = false;
     c->ens_lists_valid = false;
+    c->cla_valid = false;
     if (!cluster_plan(c)) return NBG_OK;
     int st;
     if (!c->cluster_x && (st = dalloc(c, &c->cluster_x, 6 * (size_t)c->n))) return st;
-    if (c->cluster_lists) dfree(c, c->cluster_lists);
-    if (c->cluster_cnt) dfree(c, c->cluster_cnt);
-    c->cluster_lists = nullptr;
-    c->cluster_cnt = nullptr;
+    for (int** p : {&c->cluster_lists, &c->cluster_cnt, &c->cla_lists, &c->cla_cnt}) {
+        if (*p) dfree(c, *p);
+        *p = nullptr;
+    }
     const size_t slots = (size_t)c->cluster_size * c->cluster_per;
     if ((st = dalloc(c, &c->cluster_lists, slots * c->cluster_cap))) return st;
     if ((st = dalloc(c, &c->cluster_cnt, slots))) return st;
+    if ((st = dalloc(c, &c->cla_lists, slots * c->cluster_cap))) return st;
+    if ((st = dalloc(c, &c->cla_cnt, slots))) return st;
     if (!c->cluster_since && (st = dalloc(c, &c->cluster_since, 1))) return st;
     if (!c->cluster_xref && (st = dalloc(c, &c->cluster_xref, 3 * (size_t)c->n))) return st;
+    if (!c->cla_xref && (st = dalloc(c, &c->cla_xref, 3 * (size_t)c->n))) return st;
     return NBG_OK;
 }
 
@@ -725,6 +732,10 @@ static void release(nbg_ctx* c)
     c->accel_graph = nullptr;
     if (c->hst) cudaFreeHost(c->hst);
     c->hst = nullptr;
+    if (c->hw) cudaFreeHost(c->hw);
+    c->hw = c->hw_d = nullptr;
+    if (c->pend_ev) cudaEventDestroy(c->pend_ev);
+    c->pend_ev = nullptr;
     if (c->frames) cudaFree(c->frames);
     c->frames = nullptr;
     c->frames_cap = 0;
@@ -826,6 +837,23 @@ static int clear_status(nbg_ctx* c)
     return NBG_OK;
 }
 
+// The pinned, mapped status word and the event that follows a deferred chunk
+// (allocated once per context).
+static int ensure_hw(nbg_ctx* c)
+{
+    if (c->hw) return NBG_OK;
+    unsigned* h = nullptr;
+    if (cudaHostAlloc((void**)&h, 64, cudaHostAllocMapped) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, NBG_ERR_NOMEM, "pinned status word: cudaHostAlloc failed");
+    }
+    *h = 0u;
+    c->hw = h;
+    CK(cudaHostGetDevicePointer((void**)&c->hw_d, h, 0), "status word device pointer");
+    CK(cudaEventCreateWithFlags(&c->pend_ev, cudaEventDisableTiming), "pending event");
+    return NBG_OK;
+}
+
 static int status_error(nbg_ctx* c, unsigned st)
 {
     if (st & ST_NONFINITE) return fail(c, NBG_ERR_NONFINITE, "non-finite acceleration (NaN/Inf state or coincident bodies)");
@@ -913,20 +941,25 @@ static void resident_dirty(nbg_ctx* c)
 // thermostat term; an export node writes dv (and the Nose-Hoover rate) and
 // the status word back into the staging and advances the call counter
 // whose parity picks the rebuild flags.
-static int accel_graph_capture(nbg_ctx* c, bool v_read)
+static int ensure_staging(nbg_ctx* c, double** dev)
 {
-    const size_t sb = state_bytes(c);
     if (!c->hst) {
-        cudaError_t e = cudaHostAlloc((void**)&c->hst, 3 * sb + 64, cudaHostAllocMapped);
+        cudaError_t e = cudaHostAlloc((void**)&c->hst, 3 * state_bytes(c) + 64, cudaHostAllocMapped);
         if (e != cudaSuccess) {
             cudaGetLastError();
             c->hst = nullptr;
             return fail(c, NBG_ERR_NOMEM, "pinned staging of the right-hand side: cudaHostAlloc failed");
         }
     }
+    CK(cudaHostGetDevicePointer((void**)dev, c->hst, 0), "staging device pointer");
+    return NBG_OK;
+}
+
+static int accel_graph_capture(nbg_ctx* c, bool v_read)
+{
     double* dst = nullptr;
-    CK(cudaHostGetDevicePointer((void**)&dst, c->hst, 0), "staging device pointer");
     int st;
+    if ((st = ensure_staging(c, &dst))) return st;
     if (!c->accel_step && (st = dalloc(c, &c->accel_step, 1))) return st;
     const int64_t launches0 = c->launches;
     const StepRef pos{0, c->accel_step};
@@ -956,6 +989,63 @@ static int accel_graph_capture(nbg_ctx* c, bool v_read)
     return NBG_OK;
 }
 
+// The device address of a host buffer of `bytes` that the device can read
+// and write in place (page-locked, mapped, one piece from its first to its
+// last byte), else null.
+static void* mapped_address(const void* p, size_t bytes)
+{
+    cudaPointerAttributes a0{}, a1{};
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || !a0.devicePointer) return nullptr;
+    if (cudaPointerGetAttributes(&a1, static_cast<const char*>(p) + bytes - 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a1.type != cudaMemoryTypeHost ||
+        static_cast<char*>(a1.devicePointer) - static_cast<char*>(a0.devicePointer) != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a0.devicePointer;
+}
+
+// nbg_accel of a small system (the cluster path): one launch reads u and
+// writes dv in place when they are page-locked host buffers, else through
+// the pinned staging; the status word comes back through the mapped word.
+// Returns 1 when the cluster path no longer applies (lists grew past it).
+static int accel_cluster(nbg_ctx* c, double* dv, const double* u)
+{
+    int st;
+    double* stage = nullptr;
+    if ((st = ensure_hw(c))) return st;
+    const size_t sb = sizeof(double) * 3 * (size_t)c->n;
+    const double* ud = static_cast<const double*>(mapped_address(u, sb));
+    double* dvd = static_cast<double*>(mapped_address(dv, sb));
+    if ((!ud || !dvd) && (st = ensure_staging(c, &stage))) return st;
+    if (!ud) {
+        memcpy(c->hst, u, sb);
+        ud = stage;
+    }
+    double* out = dvd ? dvd : stage + 6 * c->cols;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        *(volatile unsigned*)c->hw = 0u;
+        if ((st = launch_cluster_accel(c, ud, out, c->hw_d))) return st;
+        CK(cudaStreamSynchronize(c->stream), "accel sync");
+        const unsigned w = *(volatile unsigned*)c->hw;
+        c->cla_valid = w == 0u;
+        if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
+            if ((st = grow_lists(c, w))) return st;
+            if (!c->cluster_ok) return 1;
+            continue;
+        }
+        if (w) return status_error(c, w);
+        if (!dvd) memcpy(dv, c->hst + 6 * c->cols, sb);
+        return NBG_OK;
+    }
+    return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
+}
+
 extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
 {
     (void)t;
@@ -963,6 +1053,11 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
     NBG_ENTER(c);
     // only the Berendsen and Nose-Hoover terms of the right-hand side read v
     const bool v_read = c->d.therm == NBG_THERMO_BERENDSEN || c->d.therm == NBG_THERMO_NOSEHOOVER;
+    if (c->path == PATH_LIST && c->cluster_ok) {
+        // (no thermostat term: the cluster path serves plain systems only)
+        const int st = accel_cluster(c, dv, u);
+        if (st != 1) return st;
+    }
     if (c->path == PATH_LIST && c->use_graphs && !c->profiling) {
         resident_dirty(c);
         c->T_valid = false;
@@ -1100,13 +1195,28 @@ static int ensure_backup(nbg_ctx* c)
     return c->bk ? NBG_OK : dalloc(c, &c->bk, 12 * (size_t)c->cols);
 }
 
-// x, v, a_old of the resident state to or from the backup (one copy each way)
+// x, v, a_old of the resident state to the backup (one copy), or the n atoms'
+// rows of each back (one strided copy: the cluster loop writes the backup of
+// its atoms itself, not the padding)
 static int backup_state(nbg_ctx* c, bool restore)
 {
-    const size_t bytes = 3 * sizeof(double) * 3 * (size_t)c->cols;
-    CK(cudaMemcpyAsync(restore ? c->st.x : c->bk, restore ? c->bk : c->st.x, bytes, cudaMemcpyDeviceToDevice,
-                       c->stream),
-       restore ? "restore" : "backup");
+    const size_t seg = 3 * sizeof(double) * (size_t)c->cols;
+    if (restore) {
+        CK(cudaMemcpy2DAsync(c->st.x, seg, c->bk, seg, 3 * sizeof(double) * (size_t)c->n, 3,
+                             cudaMemcpyDeviceToDevice, c->stream),
+           "restore");
+    } else {
+        CK(cudaMemcpyAsync(c->bk, c->st.x, 3 * seg, cudaMemcpyDeviceToDevice, c->stream), "backup");
+    }
+    return NBG_OK;
+}
+
+// The status of the chunk just launched (synchronises the stream).
+static int chunk_status(nbg_ctx* c, unsigned* w)
+{
+    if (!c->chunk_hw) return read_status(c, w);
+    CK(cudaStreamSynchronize(c->stream), "stream sync");
+    *w = *(volatile unsigned*)c->hw;
     return NBG_OK;
 }
 
@@ -1297,9 +1407,10 @@ static int settle(nbg_ctx* c)
 {
     if (!c->pending) return NBG_OK;
     c->pending = false;
-    unsigned w = 0;
+    // the chunk alone (its status word was set or copied before the event)
+    CK(cudaEventSynchronize(c->pend_ev), "pending chunk");
+    const unsigned w = *(volatile unsigned*)c->hw;
     int st;
-    if ((st = read_status(c, &w))) return st;
     if (w & ST_TIMEOUT) {
         if ((st = backup_state(c, true))) return st;  // the chunk ended early: back to its start
         c->step = c->pend_step0;
@@ -1350,31 +1461,40 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
             c->graph = nullptr;
         }
     }
-    if ((st = clear_status(c))) return st;
     const bool em = is_em(c);
+    const bool can_overflow = c->path == PATH_LIST;
+    if (can_overflow && ((st = ensure_backup(c)) || (st = ensure_hw(c)))) return st;
+    // chunks run as one launch (cluster or ensemble loop) on a state whose
+    // acceleration is known report to the host word: the device word is
+    // neither cleared nor read in this call
+    const bool hw_ok = can_overflow && !em && c->accel_valid && (c->cluster_ok || c->ens_ok);
+    if (!hw_ok && (st = clear_status(c))) return st;
     if (!em && !c->accel_valid) {
         if ((st = init_accel(c))) return st;
     } else if (em) {
         if ((st = launch_pack(c, c->st))) return st;
     }
-    const bool can_overflow = c->path == PATH_LIST;
     const int64_t chunk = can_overflow ? 512 : nsteps;
     // graphs pay off for short steps; events around kernels (profiling) stay direct
     const bool graphs = c->use_graphs && !c->profiling && nsteps >= 2 * graph_period(c);
-    if (can_overflow && (st = ensure_backup(c))) return st;
     int64_t done = 0;
     int retries = 0;
     while (done < nsteps) {
         int64_t k = std::min<int64_t>(chunk > 0 ? chunk : nsteps, nsteps - done);
         const int64_t step0 = c->step;
-        if (can_overflow && (st = backup_state(c, false))) return st;
+        // (a retry below clears the device word, so a chunk that falls back
+        // from the one-launch loops to graphs reads a clean word)
+        c->chunk_hw = hw_ok && (c->cluster_ok || c->ens_ok);
+        if (c->chunk_hw) *(volatile unsigned*)c->hw = 0u;  // no launch that sets it is in flight
+        // the cluster loop writes the backup of its atoms itself
+        if (can_overflow && !(c->chunk_hw && c->cluster_ok) && (st = backup_state(c, false))) return st;
         int64_t s = 0;
         bool counter_set = false;
         while (s < k) {
             if (c->ens_ok && !is_em(c)) {
                 // every replica's steps of the chunk in one launch (a CTA per
                 // replica; its lists stay with it between launches)
-                if ((st = launch_ensemble(c, c->st, dt, k - s, c->step))) break;
+                if ((st = launch_ensemble(c, c->st, dt, k - s, c->step, c->chunk_hw ? c->hw_d : c->d.status))) break;
                 c->ens_lists_valid = true;
                 c->step += k - s;
                 c->steps_since_build = -1;
@@ -1384,7 +1504,9 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
             if (c->cluster_ok) {
                 // the whole chunk in one persistent cluster launch (its lists
                 // live in shared memory: the global ones are rebuilt later)
-                if ((st = launch_cluster_vv(c, c->st, dt, k - s, c->desc.rebuild_every, c->step))) break;
+                if ((st = launch_cluster_vv(c, c->st, dt, k - s, c->desc.rebuild_every, c->step,
+                                             c->chunk_hw ? c->hw_d : c->d.status)))
+                    break;
                 c->cluster_lists_valid = true;
                 c->step += k - s;
                 c->steps_since_build = -1;
@@ -1412,6 +1534,11 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
         if (st) return st;
         if (defer && done + k == nsteps && can_overflow) {
             // the last chunk's status is read by the next call (settle)
+            if (!c->chunk_hw) {
+                CK(cudaMemcpyAsync(c->hw, c->d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream),
+                   "status copy");
+            }
+            CK(cudaEventRecord(c->pend_ev, c->stream), "pending event");
             c->pending = true;
             c->pend_dt = dt;
             c->pend_steps = k;
@@ -1419,7 +1546,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
             return NBG_OK;
         }
         unsigned w = 0;
-        if ((st = read_status(c, &w))) return st;
+        if ((st = chunk_status(c, &w))) return st;
         if ((w & ST_TIMEOUT) && can_overflow) {
             // a launch that gave up waiting ended early: the state goes back
             // to the chunk's start, and the error is returned
@@ -2338,7 +2465,7 @@ extern "C" int nbg_ensemble_tune(nbg_ctx* c, int32_t steps, int32_t* form, doubl
             c->ens_lists_valid = false;
             if ((st = clear_status(c))) break;
             cudaEventRecord(e0, c->stream);
-            if ((st = launch_ensemble(c, c->st, dt, steps, step0))) break;
+            if ((st = launch_ensemble(c, c->st, dt, steps, step0, c->d.status))) break;
             cudaEventRecord(e1, c->stream);
             unsigned w = 0;
             if ((st = read_status(c, &w))) break;

@@ -206,6 +206,15 @@ struct nbg_ctx {
     bool pending = false;
     double pend_dt = 0.0;
     int64_t pend_steps = 0, pend_step0 = 0;
+    // the status of a chunk reaches the host through a pinned, mapped word:
+    // a chunk run as one launch (cluster or ensemble loop, chunk_hw) sets its
+    // bits there directly, any other deferred chunk copies the device word
+    // there; pend_ev follows the chunk, so settling waits for the chunk
+    // alone, not for work queued on the stream after it
+    unsigned* hw = nullptr;
+    unsigned* hw_d = nullptr;  // its device address
+    bool chunk_hw = false;
+    cudaEvent_t pend_ev = nullptr;
     int64_t step = 0;      // steps taken on the resident state
     int64_t steps_since_build = 0;
     int64_t list_builds = 0;
@@ -227,6 +236,12 @@ struct nbg_ctx {
     double* cluster_xref = nullptr;  // [3n] positions at the cluster lists' build
     int* cluster_since = nullptr;
     bool cluster_lists_valid = false;
+    // nbg_accel's cluster launches keep lists of their own (same shapes),
+    // valid for any positions within skin/2 of cla_xref
+    int* cla_lists = nullptr;
+    int* cla_cnt = nullptr;
+    double* cla_xref = nullptr;
+    bool cla_valid = false;
     // replica ensembles: one persistent launch per chunk of steps, a CTA per
     // replica (k_ensemble.cu)
     bool ens_ok = false, ens_disabled = false;
@@ -236,9 +251,11 @@ struct nbg_ctx {
     int* ens_order = nullptr;     // replicas, largest first (CTA b runs replica order[b])
     int* ens_since = nullptr;     // per replica: steps since its list build
     uint4* ens_pref = nullptr;    // per atom: fixed-point position at its replica's last build
-    // test of the cluster loop's timeout path: the next launch drops the
-    // position copies of this step (-1: its last step; -2: none)
+    // test of the cluster loop's timeout path: the launch after
+    // cluster_test_skip others drops the position copies of this step (-1:
+    // its last step; -2: none)
     int cluster_test_drop = -2;
+    int cluster_test_skip = 0;
     bool grav_uniform = false;  // every body has mass grav_m0: the reduction applies G m
     float grav_far2 = 256.f;    // a tile pair is far when (F g)^2 >= max|r|^2, F = 16
     double grav_m0 = 0.0;
@@ -341,10 +358,14 @@ int launch_pack(nbg_ctx* c, const StateView& s);
 int launch_gravity(nbg_ctx* c, const StateView& s);
 bool cluster_plan(nbg_ctx* c);
 // step0: the time index of the state at the launch (for the frame sink)
-int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every, int64_t step0);
+// (status: the word the launch sets its bits in; the cluster loop also
+// writes x, v, a_old of its atoms to the backup before its first step)
+int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int rebuild_every, int64_t step0,
+                      unsigned* status);
 // replica ensembles on the persistent per-replica loop (k_ensemble.cu)
 bool ensemble_plan(nbg_ctx* c);
-int launch_ensemble(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int64_t step0);
+int launch_ensemble(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int64_t step0, unsigned* status);
+int launch_cluster_accel(nbg_ctx* c, const double* u, double* dv, unsigned* status);
 int launch_allpairs(nbg_ctx* c, const StateView& s);
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
 int launch_force_list(nbg_ctx* c, const StateView& s);

@@ -182,14 +182,19 @@ def measured_peaks():
         return {}
 
 
-def profile_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+def profile_value(kernel, table="traffic.json"):
+    """A per-launch figure of `kernel` from a committed ncu summary table, if
+    any: traffic.json holds DRAM bytes, issue.json warp instructions."""
+    path = os.path.join(ROOT, "profiles", table)
     try:
         with open(path) as f:
             return json.load(f).get(kernel)
     except (OSError, ValueError):
         return None
+
+
+def profile_traffic(kernel):
+    return profile_value(kernel)
 
 
 def cpu_baseline(oracle, wl, target_s=8.0):
@@ -853,13 +858,33 @@ def main():
         peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     kernel_name = ("k_gravity" if args.workload == "gravity" else "k_cluster_vv" if cluster else
                    "k_ensemble" if ens else "k_force_list")
+    form = eng.force_form() if kernel_name == "k_force_list" else None
+    if form is not None and form[1]:
+        # the fixed-point kernel: per-warp list staging up to 16 lanes per atom
+        kernel_name = "k_force_fxw" if form[0] <= 16 and not os.environ.get("NBG_FX_BLOCK") else "k_force_fx"
     traffic = profile_traffic(f"{kernel_name}:{w['name']}")
     roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
                 "frac": (achieved / peak) if peak else None, "traffic": traffic, "kernel": kernel_name,
                 "kernel_ms": avg_kern, "kernel_launches": kern_n, "peak_source": peak_src}
     if cluster is not None:
+        # a few kB per step stay on chip: the bound is the issue rate of the
+        # cluster's SMs (4 warp instructions per clock each) for the step's
+        # warp instructions (ncu), at the sampled SM clock
+        inst = profile_value(f"k_cluster_vv:{w['name']}", "issue.json")
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+        floor_us = inst / (cluster[0] * 4 * mhz) if inst else None
+        step_us = 1e3 * avg_kern
+        roofline.update(bound="issue", achieved=step_us, peak=floor_us, unit="us/step",
+                        frac=(floor_us / step_us) if floor_us else None,
+                        peak_source=(f"issue floor: {inst} warp instructions per step (ncu) / "
+                                     f"({cluster[0]} SMs x 4 per clock x {mhz:.0f} MHz)"),
+                        algorithmic_bytes_per_step=work, hbm_frac=achieved / peak if peak else None)
         roofline["kernel_ms_is"] = f"per step: {prof_steps} steps in {kern_n} launch(es) of the whole step loop"
         roofline["cluster"] = {"ctas": cluster[0], "lanes_per_atom": cluster[1]}
+        # the per-call floor: an empty kernel of the same launch shape (after the timed region)
+        lf = eng.cluster_launch_floor()
+        if lf is not None:
+            roofline["launch_floor_us"] = {"one_at_a_time": lf[0], "back_to_back": lf[1]}
     if ens is not None:
         roofline["kernel_ms_is"] = (f"per step: {prof_steps} steps in {kern_n} launch(es) of the whole step loop "
                                     "(a CTA per replica); achieved = 406 B per atom-step of algorithmic traffic")

@@ -185,7 +185,9 @@ NBG_API int64_t nbg_kernel_launches(const nbg_ctx* ctx);
  * (3 x (n+1) with Nose-Hoover). As in the reference, the Nose-Hoover term
  * writes the thermostat rate into v[3n] (thermostats.jl:126): v is the only
  * input that is modified. Replaces one call of the closure SciML's solvers
- * make per stage.
+ * make per stage. Page-locked u and dv (cudaHostAlloc / cudaHostRegister
+ * memory, mapped) are read and written by the device in place on the
+ * small-system path; other buffers go through the context's pinned staging.
  */
 NBG_API int nbg_accel(nbg_ctx* ctx, double* dv, double* v, const double* u, double t);
 
@@ -279,6 +281,13 @@ NBG_API int nbg_force_kernel_time(nbg_ctx* ctx, double* total_ms, int64_t* launc
  * keeps such a system on the graph step loop.
  */
 NBG_API int nbg_cluster_shape(nbg_ctx* ctx, int32_t* ctas, int32_t* lanes);
+
+/* The launch floor of that cluster shape (measurement): an empty kernel with
+ * the same CTAs, threads, shared memory and cluster, which passes one
+ * cluster barrier, timed with CUDA events on the context's stream: 200
+ * launches back to back (*us_per_launch) and 200 one at a time with the host
+ * waiting for each (*us_single). NBG_ERR_UNSUPPORTED off the cluster path. */
+NBG_API int nbg_cluster_launch_floor(nbg_ctx* ctx, double* us_single, double* us_per_launch);
 
 /*
  * All-pairs gravity accelerations that allocate no device memory. It has no

@@ -169,6 +169,7 @@ SIGNATURES = {
     "nbg_ml_kernel_times": (ctypes.c_int, [_vp, ctypes.c_int32, _dp]),
     "nbg_autotune": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp]),
     "nbg_cluster_shape": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "nbg_cluster_launch_floor": (ctypes.c_int, [_vp, _dp, _dp]),
     "nbg_rdf_histogram": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
                                          ctypes.c_int64, ctypes.c_double, ctypes.c_int32, ctypes.c_int, _vp]),
     "nbg_rdf_kernel_times": (ctypes.c_int, [_dp]),

@@ -103,7 +103,7 @@ __device__ __forceinline__ void cl_join(float& h, float& e, int o, int width)
 }
 
 // Shared memory (dynamic): split positions [parity][hi, lo][n] (float4), the
-// own atoms' positions at the last list build [per][3] (double), their lists
+// own atoms' positions at the last list build [per][3] (double, padded to a 16-byte end), their lists
 // [per][cap], counts [per] (int) and force partials [per][6] (float: h, e per
 // component).
 template <int LPA, bool ACCEL>
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
     const int n = (int)d.n;
     extern __shared__ float4 cl_pos[];
     double* xref_s = reinterpret_cast<double*>(cl_pos + 4 * (size_t)n);
-    int* lst = reinterpret_cast<int*>(xref_s + 3 * (size_t)per);
+    int* lst = reinterpret_cast<int*>(xref_s + 3 * (size_t)per + ((3 * per) & 1));  // 16-byte aligned
     int* cnt = lst + (size_t)per * cap;
     float* fsum = reinterpret_cast<float*>(cnt + per);
     __shared__ unsigned flag[2];  // rebuild requests of the step of each parity
@@ -173,10 +173,15 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
         }
     }
     int since = 0;
+    bool built = false;  // a list build ran in this launch (the same in every CTA)
     if (reuse) {
         // the lists, their reference positions and the steps since their
         // build, as the previous launch left them
-        for (int t = tid; t < na * cap; t += CL_THREADS) lst[t] = lst_g[(size_t)rank * per * cap + t];
+        // (cap is a multiple of 4: whole 16-byte rows, several loads in flight per thread)
+        const int4* src4 = reinterpret_cast<const int4*>(lst_g + (size_t)rank * per * cap);
+        int4* dst4 = reinterpret_cast<int4*>(lst);
+#pragma unroll 4
+        for (int t = tid; t < na * cap / 4; t += CL_THREADS) dst4[t] = src4[t];
         for (int t = tid; t < na; t += CL_THREADS) cnt[t] = cnt_g[(size_t)rank * per + t];
         for (int t = tid; t < 3 * na; t += CL_THREADS) xref_s[t] = xref_g[3 * (size_t)a0 + t];
         since = *since_g;
@@ -353,6 +358,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
                 for (int k = 0; k < 3; ++k) xref_s[3 * ko + k] = x[k];
             }
             since = 0;
+            built = true;
             __syncthreads();
         }
         ++since;
@@ -403,11 +409,17 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             d.xref[3 * io + k] = xref_s[3 * ko + k];
         }
     }
-    // the lists for the next launch (with their own reference positions:
-    // d.xref also serves the global lists, which other calls rebuild)
-    for (int t = tid; t < 3 * na; t += CL_THREADS) xref_g[3 * (size_t)a0 + t] = xref_s[t];
-    for (int t = tid; t < na * cap; t += CL_THREADS) lst_g[(size_t)rank * per * cap + t] = lst[t];
-    for (int t = tid; t < na; t += CL_THREADS) cnt_g[(size_t)rank * per + t] = cnt[t];
+    // the lists for the next launch, if this one built them (with their own
+    // reference positions: d.xref also serves the global lists, which other
+    // calls rebuild)
+    if (built) {
+        for (int t = tid; t < 3 * na; t += CL_THREADS) xref_g[3 * (size_t)a0 + t] = xref_s[t];
+        int4* dst4 = reinterpret_cast<int4*>(lst_g + (size_t)rank * per * cap);
+        const int4* src4 = reinterpret_cast<const int4*>(lst);
+#pragma unroll 4
+        for (int t = tid; t < na * cap / 4; t += CL_THREADS) dst4[t] = src4[t];
+        for (int t = tid; t < na; t += CL_THREADS) cnt_g[(size_t)rank * per + t] = cnt[t];
+    }
     if (!ACCEL && rank == 0 && tid == 0) *since_g = since;
 }
 
@@ -435,14 +447,15 @@ bool cluster_plan(nbg_ctx* c)
     if (c->cluster_disabled || c->path != PATH_LIST || c->nrep != 1 || c->d.kind != NBG_SYSTEM_POTENTIAL ||
         c->d.bc != NBG_BC_CUBIC || c->d.therm != NBG_THERMO_NULL || c->baoab || c->n < 64 || c->n > 2048)
         return false;
-    const int n = (int)c->n, cap = c->d.nbr_cap;
+    // (the cluster lists' rows are whole 16-byte units: cap rounded up to 4)
+    const int n = (int)c->n, cap = (c->d.nbr_cap + 3) & ~3;
     for (int C = CL_MAX; C >= 8; C /= 2) {
         const int per = (n + C - 1) / C;
         if (per > 128) continue;  // owner threads: 4 warps x 32 lanes
         int lpa = 32;
         while (lpa > 4 && per * lpa > CL_THREADS) lpa /= 2;
         if (per * lpa > CL_THREADS) continue;
-        const size_t bytes = sizeof(float4) * 4 * (size_t)n + sizeof(double) * 3 * (size_t)per +
+        const size_t bytes = sizeof(float4) * 4 * (size_t)n + sizeof(double) * (3 * (size_t)per + ((3 * per) & 1)) +
                              sizeof(int) * ((size_t)per * cap + per) + sizeof(float) * 6 * (size_t)per;
         if (bytes > 200 * 1024) continue;
         cluster_kernel_t k = cluster_kernel(lpa), ka = cluster_kernel(lpa, true);
@@ -552,3 +565,71 @@ int launch_cluster_accel(nbg_ctx* c, const double* u, double* dv, unsigned* stat
     NBG_LAUNCH_CHECK(c, "k_cluster_vv");
     return NBG_OK;
 }
+
+// The launch floor of the cluster loop's shape: a kernel with the same CTAs,
+// threads, shared memory and cluster that only passes one cluster barrier.
+__global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_empty(int* sink)
+{
+    extern __shared__ float4 ce_s[];
+    cg::cluster_group cl = cg::this_cluster();
+    if (threadIdx.x == 0) ce_s[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    cl.sync();
+    if (threadIdx.x == 0 && ce_s[0].x != 0.f) *sink = 1;  // never: keeps the store live
+}
+
+int cluster_launch_floor(nbg_ctx* c, double* us_single, double* us_per_launch)
+{
+    if (!c->cluster_ok) return NBG_ERR_UNSUPPORTED;
+    if (cudaFuncSetAttribute(k_cluster_empty, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->cluster_bytes) !=
+            cudaSuccess ||
+        (c->cluster_size > 8 &&
+         cudaFuncSetAttribute(k_cluster_empty, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess))
+        return cuda_fail(c, cudaGetLastError(), "k_cluster_empty attributes");
+    int* sink = nullptr;
+    if (cudaMalloc(&sink, sizeof(int)) != cudaSuccess) return cuda_fail(c, cudaGetLastError(), "probe sink");
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = c->cluster_size;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(c->cluster_size);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = c->cluster_bytes;
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 20 && e == cudaSuccess; ++k) e = cudaLaunchKernelEx(&cfg, k_cluster_empty, sink);
+    const int reps = 200;
+    float ms = 0.f, single = 0.f;
+    if (e == cudaSuccess) {
+        // back to back
+        cudaEventRecord(e0, c->stream);
+        for (int k = 0; k < reps && e == cudaSuccess; ++k) e = cudaLaunchKernelEx(&cfg, k_cluster_empty, sink);
+        cudaEventRecord(e1, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    }
+    // one at a time, the host waiting for each
+    for (int k = 0; k < reps && e == cudaSuccess; ++k) {
+        float m1 = 0.f;
+        cudaEventRecord(e0, c->stream);
+        e = cudaLaunchKernelEx(&cfg, k_cluster_empty, sink);
+        cudaEventRecord(e1, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&m1, e0, e1);
+        single += m1;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cluster launch floor");
+    if (us_per_launch) *us_per_launch = 1e3 * ms / reps;
+    if (us_single) *us_single = 1e3 * single / reps;
+    return NBG_OK;
+}
+

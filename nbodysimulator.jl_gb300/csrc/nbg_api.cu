@@ -715,6 +715,13 @@ extern "C" int nbg_ensemble_form(nbg_ctx* c, int32_t* lanes, int32_t* threads, i
     return c->ens_ok ? 1 : 0;
 }
 
+extern "C" int nbg_cluster_launch_floor(nbg_ctx* c, double* us_single, double* us_per_launch)
+{
+    if (!c) return NBG_ERR_ARG;
+    NBG_ENTER(c);
+    return cluster_launch_floor(c, us_single, us_per_launch);
+}
+
 extern "C" int nbg_cluster_shape(nbg_ctx* c, int32_t* ctas, int32_t* lanes)
 {
     if (!c) return NBG_ERR_ARG;

@@ -366,6 +366,7 @@ int launch_cluster_vv(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps,
 bool ensemble_plan(nbg_ctx* c);
 int launch_ensemble(nbg_ctx* c, const StateView& s, double dt, int64_t nsteps, int64_t step0, unsigned* status);
 int launch_cluster_accel(nbg_ctx* c, const double* u, double* dv, unsigned* status);
+int cluster_launch_floor(nbg_ctx* c, double* us_single, double* us_per_launch);
 int launch_allpairs(nbg_ctx* c, const StateView& s);
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
 int launch_force_list(nbg_ctx* c, const StateView& s);

@@ -153,6 +153,16 @@ class Engine:
     def set_profiling(self, on=True):
         self._chk(self.lib.nbg_set_profiling(self.ctx, 1 if on else 0))
 
+    def cluster_launch_floor(self):
+        """(µs one launch at a time, µs per launch back to back) of an empty
+        kernel with the cluster loop's launch shape, or None off that path."""
+        single, b2b = ctypes.c_double(), ctypes.c_double()
+        st = self.lib.nbg_cluster_launch_floor(self.ctx, ctypes.byref(single), ctypes.byref(b2b))
+        if st == -6:  # NBG_ERR_UNSUPPORTED
+            return None
+        self._chk(st)
+        return single.value, b2b.value
+
     def cluster_shape(self):
         """(CTAs, lanes per atom) of the persistent cluster step loop, or None
         when the context runs the graph step loop."""

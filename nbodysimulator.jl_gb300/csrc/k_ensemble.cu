@@ -257,10 +257,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
                 POT != FX_LJ ? (float)(d.el_k_d * d.charge[gi] * (R.fx_scale * R.fx_scale) / R.fx_fscale) : 0.0f;
             const int* row = d.nbr + gi * d.nbr_istride;
             float2 px = make_float2(0.f, 0.f), py = px, pz = px;
+            // the row entries of the next iteration are loaded before this
+            // iteration's gathers and arithmetic (one iteration ahead)
+            int jn0 = lane < cnt ? __ldg(row + (int64_t)lane * d.nbr_kstride) : (int)a0;
+            int jn1 = lane + LPA < cnt ? __ldg(row + (int64_t)(lane + LPA) * d.nbr_kstride) : jn0;
             for (int k0 = lane; k0 < cnt; k0 += 2 * LPA) {
                 const bool v1 = k0 + LPA < cnt;
-                const int j0 = __ldg(row + (int64_t)k0 * d.nbr_kstride);
-                const int j1 = v1 ? __ldg(row + (int64_t)(k0 + LPA) * d.nbr_kstride) : j0;
+                const int j0 = jn0, j1 = jn1;
+                const int kn = k0 + 2 * LPA;
+                jn0 = kn < cnt ? __ldg(row + (int64_t)kn * d.nbr_kstride) : (int)a0;
+                jn1 = kn + LPA < cnt ? __ldg(row + (int64_t)(kn + LPA) * d.nbr_kstride) : jn0;
                 const uint4 q0 = pos[j0 - a0], q1 = pos[j1 - a0];
                 fx_pair2<POT>(d, s.x, gi, lj_atoms, kqi, qi, j0, j1, v1, q0, q1, lj_lo, lj_hi, el_lo, el_hi, sig2h,
                               sig2l, krf, px, py, pz, range_err);

@@ -899,8 +899,22 @@ def main():
         if lf is not None:
             roofline["launch_floor_us"] = {"one_at_a_time": lf[0], "back_to_back": lf[1]}
     if ens is not None:
+        # the whole step of every replica in one launch: bound by instruction
+        # issue and latency (positions in shared memory, FP64 integration),
+        # not by DRAM: the floor is the step's warp instructions (ncu) over
+        # all SMs at 4 per clock; the HBM fraction of the 406 B per atom-step
+        # of algorithmic traffic is kept beside it
+        inst = profile_value(f"k_ensemble:{w['name']}", "issue.json")
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
+        floor_ms = inst / (sms * 4 * mhz * 1e3) if inst else None
+        roofline.update(bound="issue", achieved=avg_kern, peak=floor_ms, unit="ms/step",
+                        frac=(floor_ms / avg_kern) if floor_ms else None,
+                        peak_source=(f"issue floor: {inst} warp instructions per step (ncu) / "
+                                     f"({sms} SMs x 4 per clock x {mhz:.0f} MHz)"),
+                        algorithmic_bytes_per_step=work, hbm_frac=achieved / peak if peak else None)
         roofline["kernel_ms_is"] = (f"per step: {prof_steps} steps in {kern_n} launch(es) of the whole step loop "
-                                    "(a CTA per replica); achieved = 406 B per atom-step of algorithmic traffic")
+                                    "(a CTA per replica)")
     config = {"workload": w["name"], "N": n, "dt": dt, "integrator": "velocity Verlet",
               "l2": ("512 MB buffer written between timed steps (L2 flushed)" if flush_steps else
                      "working set larger than L2" if batch else "no flush (state L2-resident across steps)"),

@@ -134,3 +134,23 @@ def test_default_run_simulation_is_adaptive(gpu):
     res = nbg.run_simulation(sim)
     u = res.solution.u
     assert np.abs(u[-1] - u[0]).max() <= 0.1 * r
+
+
+def test_adaptive_berendsen_matches_oracle_rhs(gpu, oracle):
+    """The default adaptive call with a Berendsen thermostat (its right-hand
+    side reads v, thermostats.jl:76-83): DOP853 over the GPU right-hand side
+    against the same DOP853 driver over the FP64 oracle's right-hand side.
+    The two step sequences see forces that differ by FP32 rounding only, so
+    the end states agree far inside the integrator's own tolerance."""
+    simmod = nbg.simulation
+    sim = S.lj_liquid(512, seed=9, jitter=0.05, thermostat=nbg.BerendsenThermostat(1.5, 0.1))
+    sim.tspan = (0.0, 0.05)
+    res = nbg.run_simulation(sim)
+    desc, keep = nbg.system_descriptor(sim)
+    u0, v0 = S.state(sim)
+    t, tu, tv, nacc = simmod._adaptive_run(lambda v, u, t: oracle.accel(desc, v, u)[0], u0, v0, sim.tspan,
+                                           1e-6, 1e-3, False)
+    L = desc.box[0]
+    assert res.solution.t[-1] == pytest.approx(0.05)
+    assert np.abs(np.asarray(res.solution.u[-1]) - tu[-1]).max() <= 1e-6 * L
+    assert np.abs(np.asarray(res.solution.v[-1]) - tv[-1]).max() <= 1e-5 * np.abs(tv[-1]).max()

@@ -333,10 +333,13 @@ NBG_API int nbg_force_form(nbg_ctx* ctx, int32_t* lanes, int32_t* fixed_point);
    creation keeps a batch on the step graphs. */
 NBG_API int nbg_ensemble_form(nbg_ctx* ctx, int32_t* lanes, int32_t* threads, int32_t* cells);
 /* Autotuner of the loop: forms f = 0..11 (lanes 4 or 8 = f / 6; threads 512,
-   768, 1024 = (f / 2) % 3; cells 1 or 2 = 1 + f % 2) each run `steps` steps
-   from the resident state, timed (ms per step into ms[12], may be NULL); the
-   state and the step counter are restored after each, and the fastest form
-   is kept and written to form[3] (lanes, threads, cells). */
+   768, 1024 = (f / 2) % 3; cells 1 or 2 = 1 + f % 2) and f = 12, the batch's
+   per-step kernels in CUDA graphs, each run `steps` steps from the resident
+   state with a full list build at the first, timed (ms per step into ms[13],
+   may be NULL); the state and the step counter are restored after each, and
+   the fastest form is kept and written to form[3] (lanes, threads, cells),
+   or {0, 0, 0} when the step graphs win (the batch then leaves the loop
+   until it is tuned again). */
 NBG_API int nbg_ensemble_tune(nbg_ctx* ctx, int32_t steps, int32_t* form, double* ms);
 
 /* Measured FP32 FMA throughput of a device in TFLOP/s (an FMA counts 2):

@@ -245,6 +245,7 @@ struct nbg_ctx {
     // replica ensembles: one persistent launch per chunk of steps, a CTA per
     // replica (k_ensemble.cu)
     bool ens_ok = false, ens_disabled = false;
+    bool ens_tuned_off = false;  // nbg_ensemble_tune chose the step graphs over the loop
     bool ens_lists_valid = false;  // the lists, their reference positions and step counts are the loop's
     int ens_lpa = 4, ens_threads = 768, ens_cells = 0;  // form: lanes per atom, threads, cell width (0 = as planned, 1 = rl, 2 = rl/2)
     size_t ens_smem = 0;

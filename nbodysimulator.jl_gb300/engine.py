@@ -192,12 +192,13 @@ class Engine:
         return (a.value, b.value, c.value) if used == 1 else None
 
     def ensemble_tune(self, steps=5):
-        """Time every form of the ensemble loop and keep the fastest; returns
-        ((lanes, threads, cells), ms per step of the 12 forms)."""
+        """Time every form of the ensemble loop and the batch's per-step
+        graphs, and keep the fastest; returns ((lanes, threads, cells), or
+        None when the graphs win, and the ms per step of the 13 forms)."""
         form = (ctypes.c_int32 * 3)()
-        ms = np.zeros(12)
+        ms = np.zeros(13)
         self._chk(self.lib.nbg_ensemble_tune(self.ctx, int(steps), form, _abi.as_dptr(ms)))
-        return (form[0], form[1], form[2]), ms
+        return ((form[0], form[1], form[2]) if form[0] else None), ms
 
     def force_kernel_time(self):
         """(summed ms, launches) of the dominant force kernel since the last call."""

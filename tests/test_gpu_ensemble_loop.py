@@ -145,7 +145,8 @@ def test_loop_tuner_keeps_results(gpu, oracle):
     eng.set_state(U, V)
     eng.set_step(5)
     form, ms = eng.ensemble_tune(3)
-    assert len(ms) == 12 and np.all(np.isfinite(ms)) and np.all(ms > 0)
+    assert len(ms) == 13 and np.all(np.isfinite(ms)) and np.all(ms > 0)
+    assert (form is None) == (int(np.argmin(ms)) == 12)
     assert eng.step == 5
     u, v = eng.get_state()
     assert np.array_equal(u, U) and np.array_equal(v, V)

@@ -17,9 +17,12 @@
 //   - each CTA keeps the Verlet lists of its own atoms in shared memory,
 //     rebuilt from the shared positions (all atoms scanned, the FP32 superset
 //     test of the list builders) when any atom moved more than skin/2 since
-//     the last build and every rebuild_every steps; a launch stores them (and
-//     the steps since the build) at its end and the next one starts from them
-//     unless the host invalidated them (a new state), else it builds first;
+//     the last build and every rebuild_every steps; a launch that built
+//     them stores them at its end (the steps since the build always), and
+//     the next one starts from them unless the host invalidated them (a new
+//     state), else it builds first;
+//   - at its start a launch writes x, v, a_old of its atoms to the backup,
+//     from which the host undoes a launch that timed out or overflowed;
 //   - LPA lanes per atom evaluate the pairs (pair_cutoff: the exact pair set;
 //     the ambiguous ones read FP64 positions, which the drift also writes to
 //     a global copy of the step's parity, through L2) and join their

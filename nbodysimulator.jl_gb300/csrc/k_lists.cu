@@ -396,11 +396,17 @@ int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos)
     c->accel_lists_valid = false;  // the lists follow other positions now
     c->ens_lists_valid = false;
     ListCtl L{pos, force ? 1 : 0};
-    k_cell_fill<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->d, L, s.x);
+    // The kernels run at every step of a captured graph and skip the atoms
+    // and cells of replicas without a due rebuild. The fill and the sort
+    // loop over their items on a few waves of blocks, so that a step with no
+    // rebuild (or, in a batch, few) does not schedule a block per cell; the
+    // list build keeps a warp per item, whose work is too uneven for a
+    // fixed share per warp.
+    const int64_t wave = (int64_t)c->sms * 8;
+    k_cell_fill<<<(unsigned)std::min<int64_t>(grid_for(c->n, 256), wave), 256, 0, c->stream>>>(c->d, L, s.x);
     NBG_LAUNCH_CHECK(c, "k_cell_fill");
-    int cells = c->d.ncell_total;
-    int gs = cells < 65536 ? cells : 65536;
-    k_cell_sort<<<gs, 128, sizeof(int) * c->d.cell_cap, c->stream>>>(c->d, L);
+    const int64_t cells = c->d.ncell_total;
+    k_cell_sort<<<(unsigned)std::min<int64_t>(cells, 4 * wave), 128, sizeof(int) * c->d.cell_cap, c->stream>>>(c->d, L);
     NBG_LAUNCH_CHECK(c, "k_cell_sort");
     if (c->d.ncell_total >= 2 * c->sms) {
         // warps per cell from the mean occupancy (with margin); fuller cells loop

@@ -90,7 +90,7 @@ __device__ __forceinline__ void grav_tile(const float4* sh_hi, const float4* sh_
         px2[q] = py2[q] = pz2[q] = make_float2(0.f, 0.f);
     }
     const float2 m1 = make_float2(-1.f, -1.f);
-#pragma unroll 4
+#pragma unroll 8
     for (int jj = 0; jj < GB; ++jj) {
         const float4 hj = sh_hi[jj];
         const float2 jx = make_float2(hj.x, hj.x), jy = make_float2(hj.y, hj.y), jz = make_float2(hj.z, hj.z);
@@ -143,7 +143,7 @@ __device__ __forceinline__ void grav_tile(const float4* sh_hi, const float4* sh_
 // basic_potentials.jl:318-324), the j == i term skipped (:318).
 // UNIFORM: every body has the same mass, which the reduction applies.
 template <bool PLAIN, int TI, bool PACKED, bool UNIFORM>
-__global__ void __launch_bounds__(GB, TI == 2 ? 8 : 1) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
+__global__ void __launch_bounds__(GB, TI == 2 ? 7 : 1) k_gravity(const float4* __restrict__ phi, const float4* __restrict__ plo,
                                                 int64_t n, int64_t npad, int jchunks, double* __restrict__ part,
                                                 const float4* __restrict__ box, float far2)
 {

@@ -296,8 +296,10 @@ __device__ __forceinline__ int fxw_entry(const unsigned char* box, int a, int c)
     return *reinterpret_cast<const int*>(box + a * 128 + ((((c >> 2) ^ (a & 7))) << 4) + ((c & 3) << 2));
 }
 
+// (LJ alone at 4 lanes per atom, the short rows of the ensembles: 4 CTAs
+// per SM at 64 registers beat 3 at 80; the long water rows run faster at 3)
 template <int LPA, int POT>
-__global__ void __launch_bounds__(FXW_WARPS * 32, 3) k_force_fxw(Dev d, StateView s,
+__global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4 : 3) k_force_fxw(Dev d, StateView s,
                                                                  const __grid_constant__ CUtensorMap map)
 {
     static_assert(LPA >= 4 && LPA <= 16, "two entries per lane per box step");

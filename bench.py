@@ -23,9 +23,13 @@ e2e      : the same steps through the reference-facing drop-in, nbg_accel
            every step uploads u (and v where the thermostat reads it) and
            reads back dv.
 roofline : the dominant force kernel's algorithmic FLOP/s (20 flop per pair)
-           or bytes against the measured peak; for the LJ workload, which
-           runs as persistent cluster launches of many steps, the whole step
-           loop's time per step.
+           or bytes against the measured peak. The LJ workload runs as
+           persistent cluster launches of many steps: its line gives the step
+           loop's time per step against the issue floor of the cluster's SMs
+           (warp instructions per step from ncu), and the launch floor of the
+           cluster shape. A batch that runs the persistent ensemble loop is
+           reported the same way against all SMs; the ensemble tuner times
+           the loop's forms and the per-step graphs after 100 untimed steps.
 --workload rdf: the radial distribution function's pair histogram
 (nbg_rdf_histogram, 1000 bins) over 512 frames of the 12,288-atom water box,
 its 4096 oxygens (4.3e9 pair distances per step); metric pairs/s.

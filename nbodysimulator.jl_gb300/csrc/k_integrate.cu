@@ -380,6 +380,51 @@ __global__ void k_baoab_drift(Dev d, StateView s, double dt, StepRef sr)
     }
 }
 
+// Inside a captured run of BAOAB steps: the last B of one step (the kick of
+// k_baoab_kick) and the B A O A of the next (k_baoab_drift, step sr) in one
+// pass over the atoms, with the same operations in the same order, so the
+// bits equal the two kernels'. The velocity stays in registers between them.
+__global__ void k_baoab_kick_drift(Dev d, StateView s, double dt, StepRef sr)
+{
+    const int64_t step = step_of(sr);
+    const int parity = (int)((step + 1) & 1);
+    const double hdt = 0.5 * dt;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const RepDev& R = d.reps[d.rep_of[i]];
+        const int64_t li = i - R.atom0;
+        const double c1 = R.bc1;
+        const double sd = __dmul_rn(R.bsd, d.rsqrt_mass[i]);
+        float z[3];
+        philox_normals3<float>(R.seed, (uint64_t)li, (uint64_t)step, z);
+        for (int k = 0; k < 3; ++k) {
+            const int64_t e = 3 * i + k;
+            const double an = s.a_new[e];
+            if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+            const double v = __dadd_rn(s.v[e], __dmul_rn(hdt, an));
+            s.a_old[e] = an;
+            const double vh = fma(hdt, an, v);
+            const double x = fma(hdt, vh, s.x[e]);
+            const double vo = fma(c1, vh, sd * (double)z[k]);
+            s.x[e] = fma(hdt, vo, x);
+            s.v[e] = vo;
+        }
+        pack_atom(d, i, s.x);
+        if (d.xref) {
+            double dx = s.x[3 * i] - d.xref[3 * i];
+            double dy = s.x[3 * i + 1] - d.xref[3 * i + 1];
+            double dz = s.x[3 * i + 2] - d.xref[3 * i + 2];
+            if (!(dx * dx + dy * dy + dz * dz <= d.skin_half2)) d.rebuild_flag[parity * d.nrep + d.rep_of[i]] = 1;
+        }
+    }
+}
+
+int launch_baoab_kick_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step)
+{
+    k_baoab_kick_drift<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->d, s, dt, step);
+    NBG_LAUNCH_CHECK(c, "k_baoab_kick_drift");
+    return NBG_OK;
+}
+
 // BAOAB last B: v += dt/2 a(x'); the new forces become the next step's.
 __global__ void k_baoab_kick(Dev d, StateView s, double dt)
 {

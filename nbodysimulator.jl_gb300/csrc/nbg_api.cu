@@ -1294,6 +1294,20 @@ static int step_baoab(nbg_ctx* c, double dt, StepRef sr)
     return launch_baoab_kick(c, s, dt);
 }
 
+// A BAOAB step inside a captured run of steps: the first drifts alone, the
+// others fold the previous step's kick into their drift, and the last kicks.
+static int step_baoab_fused(nbg_ctx* c, double dt, StepRef sr, bool first, bool last)
+{
+    int st;
+    const StateView& s = c->st;
+    StepRef pos{sr.off + 1, sr.base};
+    if ((st = first ? launch_baoab_drift(c, s, dt, sr) : launch_baoab_kick_drift(c, s, dt, sr))) return st;
+    bool force = rebuild_due(c, true);
+    if ((st = forces(c, s, force, pos))) return st;
+    c->steps_since_build = force ? 0 : c->steps_since_build + 1;
+    return last ? launch_baoab_kick(c, s, dt) : NBG_OK;
+}
+
 static int step_em(nbg_ctx* c, double dt, StepRef sr)
 {
     int st;
@@ -1361,7 +1375,11 @@ static int capture_graph(nbg_ctx* c, double dt)
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
     int st = NBG_OK;
-    for (int64_t k = 0; k < G && st == NBG_OK; ++k) st = step_any(c, dt, StepRef{k, c->d.step_dev});
+    // (BAOAB without frames: each kick folded into the next step's drift)
+    const bool fuse = c->baoab && !is_em(c) && !c->sink_on;
+    for (int64_t k = 0; k < G && st == NBG_OK; ++k)
+        st = fuse ? step_baoab_fused(c, dt, StepRef{k, c->d.step_dev}, k == 0, k == G - 1)
+                  : step_any(c, dt, StepRef{k, c->d.step_dev});
     if (st == NBG_OK) st = launch_step_advance(c, G);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->steps_since_build = ssb0;  // capture only recorded the steps

@@ -386,6 +386,7 @@ int launch_accel_export(nbg_ctx* c, const StateView& s, double* hdv, double* hv,
 int launch_counter_advance(nbg_ctx* c, int64_t* counter, int64_t by);
 int launch_baoab_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_baoab_kick(nbg_ctx* c, const StateView& s, double dt);
+int launch_baoab_kick_drift(nbg_ctx* c, const StateView& s, double dt, StepRef step);
 int launch_set_step(nbg_ctx* c, int64_t value);
 int launch_save_frame(nbg_ctx* c, const StateView& s, StepRef sr);
 int launch_rhs_thermostat(nbg_ctx* c, const StateView& s);

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
             const uint4 qi = pos[active ? i : 0];
             const int cnt = active ? min(d.nbr_count[gi], cap) : 0;
             const float kqi =
-                POT != FX_LJ ? (float)(d.el_k_d * d.charge[gi] * (R.fx_scale * R.fx_scale) / R.fx_fscale) : 0.0f;
+                POT != FX_LJ ? (float)(d.charge[gi] * R.fx_kq) : 0.0f;
             const int* row = d.nbr + gi * d.nbr_istride;
             float2 px = make_float2(0.f, 0.f), py = px, pz = px;
             // the row entries of the next iteration are loaded before this

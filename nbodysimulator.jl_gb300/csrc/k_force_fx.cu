@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
         const bool lj_i = HAS_LJ && (POT != FX_WATER || (ia % 3) == 0);
         // k q_i / (u^2 fscale): rinv^3 in box units times this is the
         // electrostatic factor in the units of the LJ sum
-        const float kqi = HAS_EL ? (float)(d.el_k_d * d.charge[ia] * (R.fx_scale * R.fx_scale) / R.fx_fscale) : 0.0f;
+        const float kqi = HAS_EL ? (float)(d.charge[ia] * R.fx_kq) : 0.0f;
         const float lj_lo = R.fx_lj_lo, lj_hi = R.fx_lj_hi, el_lo = R.fx_el_lo, el_hi = R.fx_el_hi;
         const float sig2h = R.fx_sig2_hi, sig2l = R.fx_sig2_lo, krf = R.fx_krf;
         float2 px = make_float2(0.f, 0.f), py = px, pz = px;
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
         const int cnt = active ? min(d.nbr_count[ia], d.nbr_cap) : 0;
         const bool lj_i = HAS_LJ && (POT != FX_WATER || (ia % 3) == 0);
         const float kqi =
-            HAS_EL ? (float)(d.el_k_d * d.charge[ia] * (R.fx_scale * R.fx_scale) / R.fx_fscale) : 0.0f;
+            HAS_EL ? (float)(d.charge[ia] * R.fx_kq) : 0.0f;
         const float lj_lo = R.fx_lj_lo, lj_hi = R.fx_lj_hi, el_lo = R.fx_el_lo, el_hi = R.fx_el_hi;
         const float sig2h = R.fx_sig2_hi, sig2l = R.fx_sig2_lo, krf = R.fx_krf;
         float2 px = make_float2(0.f, 0.f), py = px, pz = px;

@@ -157,13 +157,20 @@ __global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int
     // Berendsen on a single system: the factor g (T0/T - 1) is the same for
     // every component, so its three FP64 divisions run once per thread (the
     // same operations as thermo_term_T, so the same bits)
+    // (one thread per block computes it: an FP64 division is a long
+    // sequence on this GPU's FP64 pipe)
     const bool hoist = thermo && d.therm == NBG_THERMO_BERENDSEN && d.nrep == 1;
     double bfac = 0.0;
     if (hoist) {
-        const RepDev& R0 = d.reps[0];
-        const double T = do_T ? T_now : d.red_T[0];
-        const double g = 0.5 / R0.tparam;
-        bfac = (1.0 / T == INFINITY) ? g : __dmul_rn(g, __dsub_rn(R0.T0 / T, 1.0));
+        __shared__ double bfac_s;
+        if (threadIdx.x == 0) {
+            const RepDev& R0 = d.reps[0];
+            const double T = do_T ? T_now : d.red_T[0];
+            const double g = 0.5 / R0.tparam;
+            bfac_s = (1.0 / T == INFINITY) ? g : __dmul_rn(g, __dsub_rn(R0.T0 / T, 1.0));
+        }
+        __syncthreads();
+        bfac = bfac_s;
     }
     double acc = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x) {
@@ -239,10 +246,15 @@ __global__ void k_rhs_thermostat(Dev d, StateView s)
     const bool hoist = d.therm == NBG_THERMO_BERENDSEN && d.nrep == 1;
     double bfac = 0.0;
     if (hoist) {
-        const RepDev& R0 = d.reps[0];
-        const double T = d.red_T[0];
-        const double g = 0.5 / R0.tparam;
-        bfac = (1.0 / T == INFINITY) ? g : __dmul_rn(g, __dsub_rn(R0.T0 / T, 1.0));
+        __shared__ double bfac_s;
+        if (threadIdx.x == 0) {
+            const RepDev& R0 = d.reps[0];
+            const double T = d.red_T[0];
+            const double g = 0.5 / R0.tparam;
+            bfac_s = (1.0 / T == INFINITY) ? g : __dmul_rn(g, __dsub_rn(R0.T0 / T, 1.0));
+        }
+        __syncthreads();
+        bfac = bfac_s;
     }
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ncomp; e += (int64_t)gridDim.x * blockDim.x)
         s.a_new[e] = __dadd_rn(s.a_new[e], hoist ? __dmul_rn(bfac, s.v[e]) : thermo_term(d, e / 3, s.v[e], zeta));

@@ -962,13 +962,19 @@ __global__ void __launch_bounds__(256) k_respa_kick(Dev d, double* v, const doub
                                                     unsigned* counter)
 {
     const bool berendsen = d.therm == NBG_THERMO_BERENDSEN;
-    const double T = d.red_T[0];
-    // the Berendsen factor once per thread (its FP64 divisions are slow here)
+    // the Berendsen factor once per block (its FP64 divisions are long
+    // sequences on this GPU's FP64 pipe)
     double fac = 0.0;
     if (berendsen) {
-        const RepDev& R = d.reps[0];
-        const double gm = 0.5 / R.tparam;
-        fac = (1.0 / T == INFINITY) ? gm : gm * (R.T0 / T - 1.0);
+        __shared__ double fac_s;
+        if (threadIdx.x == 0) {
+            const double T = d.red_T[0];
+            const RepDev& R = d.reps[0];
+            const double gm = 0.5 / R.tparam;
+            fac_s = (1.0 / T == INFINITY) ? gm : gm * (R.T0 / T - 1.0);
+        }
+        __syncthreads();
+        fac = fac_s;
     }
     double acc = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * d.n; e += (int64_t)gridDim.x * blockDim.x) {

@@ -341,6 +341,7 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
             R.fx_scale = 4294967296.0 / L;
             const double hb = 2147483648.0 * (1.0 - m), img2b = hb * hb;
             R.fx_fscale = (pots & NBG_POT_LJ) ? 24.0 * d0->lj_epsilon / u : 1.0;
+            R.fx_kq = D.el_k_d * (R.fx_scale * R.fx_scale) / R.fx_fscale;
             if (pots & NBG_POT_LJ) {
                 const double R2 = d0->lj_cutoff * d0->lj_cutoff * iu2;
                 R.fx_lj_lo = f_down(std::min(R2 * (1.0 - m), img2b));

@@ -76,6 +76,7 @@ struct RepDev {
     float fx_sig2_hi, fx_sig2_lo;  // sigma^2 / u^2
     float fx_krf;                  // 2 k_rf u^3
     double fx_fscale;
+    double fx_kq;                  // k / (u^2 fscale), host FP64: the kernels' kq_i = q_i fx_kq
     float fx_rl2;                  // list radius^2 (inflated), box units
     float fx_disp2;                // (skin/2)^2 in box units, slightly inside (rebuild trigger)
     // cell grid of the persistent ensemble loop's in-kernel list build, per

@@ -24,7 +24,8 @@
 // m16n8k16 BF16 tiles (FP32 accumulate): one warp per 16 atoms of one
 // species, weights staged once per block in shared memory (one orientation,
 // ldmatrix / ldmatrix.trans give both), activations kept in registers in the
-// A-fragment layout between layers. Learned forces are scattered to
+// A-fragment layout between layers. k_mlp_tc (NBG_MLP_TCGEN05) runs the same
+// products with tcgen05.mma into tensor memory, 128 atoms per product. Learned forces are scattered to
 // neighbours as 64-bit fixed point (2^-32 units) so the sum does not depend
 // on the order of the atomics. Training runs in FP32 on the CUDA cores.
 #include <cuda_bf16.h>
@@ -563,6 +564,408 @@ __global__ void __launch_bounds__(MLP_WARPS * 32, 2) k_mlp_bf16(MLView m, int64_
 }
 
 // ---------------------------------------------------------------------
+// MLP forward + backward to the input on the fifth-generation tensor cores:
+// tcgen05.mma from shared-memory operands into FP32 accumulators in tensor
+// memory (TMEM), read back by tcgen05.ld for the epilogues.
+// ---------------------------------------------------------------------
+// A block is TC_GROUPS tile groups of 8 warps; each group takes 128-atom
+// tiles of one species in turn. Per tile four products, each issued by one
+// thread of the group and completing on the group's mbarrier:
+//   D1 = X W1 (128 x 128, K 64)     a1 = tanh(D1 + b1)
+//   D2 = a1 W2 (128 x 128, K 128)   a2 = tanh(D2 + b2), E, g2 = sdE w3 (1 - a2^2)
+//   D3 = g2 W2^T                    g1 = D3 (1 - a1^2)
+//   D4 = g1 W1^T (128 x 64)         dE/dD = D4 / sdD
+// Warp w of a group reads TMEM lanes 32 (w % 4) .. + 31 (the lanes a warp
+// may access) and the columns of half w / 4 of each product: a thread owns
+// one tile row and half of its columns, so 1 - a1^2 stays in its registers
+// (half2) from layer 1 to the first backward product, and the two halves of
+// E meet in shared memory. The group's accumulator is 128 TMEM columns,
+// reused by the four products.
+//
+// Operands use the K-major layout without swizzle: 8-row x 16-byte core
+// matrices of 128 contiguous bytes; the core matrix of rows 8p.. and
+// elements 8q.. of a tile with kd elements per row starts at
+// p (16 kd) + 128 q bytes. In the shared-memory descriptor the first stride
+// is the leading-dimension byte offset (128, between core matrices along K)
+// and the second the stride byte offset (16 kd, between 8-row groups); one
+// K step of 16 elements advances the start address by 256 bytes.
+#define TC_GROUPS 2
+#define TC_GT 256  // threads of a tile group
+#define TC_WAIT_TRIES (1u << 24)
+
+__device__ __forceinline__ unsigned ml_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned tc_off(int r, int k, int kd)
+{
+    return (unsigned)((r >> 3) * (kd * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte
+// offset >> 4 (16-29), stride byte offset >> 4 (32-45), descriptor version 1
+// (bits 46-47), base offset 0, no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ unsigned long long tc_sdesc(unsigned saddr, unsigned sbo)
+{
+    return (unsigned long long)((saddr & 0x3FFFFu) >> 4) | ((unsigned long long)(128u >> 4) << 16) |
+           ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A
+// and B (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit
+// 17, M >> 4 at bit 24
+__host__ __device__ constexpr unsigned tc_idesc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(unsigned dtm, unsigned long long ad, unsigned long long bd, unsigned idesc,
+                                       unsigned acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dtm),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(unsigned mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ bool tc_mbar_try(unsigned a, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// OR of a predicate over a tile group's threads at named barrier id
+__device__ __forceinline__ bool tg_any(bool v, int id)
+{
+    unsigned r;
+    asm volatile(
+        "{\n .reg .pred q, p;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(r)
+        : "r"((unsigned)v), "r"(id), "n"(TC_GT)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void tg_sync(int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(TC_GT) : "memory"); }
+
+#define TC_R8(a) "=r"(r[a]), "=r"(r[a + 1]), "=r"(r[a + 2]), "=r"(r[a + 3]), "=r"(r[a + 4]), "=r"(r[a + 5]), \
+                 "=r"(r[a + 6]), "=r"(r[a + 7])
+#define TC_W8(a) "+r"(r[a]), "+r"(r[a + 1]), "+r"(r[a + 2]), "+r"(r[a + 3]), "+r"(r[a + 4]), "+r"(r[a + 5]), \
+                 "+r"(r[a + 6]), "+r"(r[a + 7])
+
+// 32 consecutive FP32 columns of this thread's TMEM lane; the wait names the
+// registers so that no use of them moves above it
+__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32])
+{
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : TC_R8(0), TC_R8(8), TC_R8(16), TC_R8(24)
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : TC_W8(0), TC_W8(8), TC_W8(16), TC_W8(24) : : "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// thread gt's 8 float4 of the descriptors of the tile at species index k0
+// (rows past count are zero)
+__device__ __forceinline__ void tc_load_x(const MLView& m, int sp, int64_t count, int64_t k0, int gt, float4 (&xv)[8])
+{
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int e = gt + TC_GT * i, r = e >> 4, c4 = e & 15;
+        const int64_t kk = k0 + r;
+        xv[i] = kk < count ? __ldg(reinterpret_cast<const float4*>(m.x + species_atom(sp, kk) * ML_ND) + c4)
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+struct TcSmem {
+    __nv_bfloat16 w1t[ML_NH * ML_ND];          // B of X W1:     (n hidden, k input) = W1[k][n]
+    __nv_bfloat16 w2t[ML_NH * ML_NH];          // B of a1 W2:    (n, k) = W2[k][n]
+    __nv_bfloat16 w2[ML_NH * ML_NH];           // B of g2 W2^T:  (n, k) = W2[n][k]
+    __nv_bfloat16 w1[ML_ND * ML_NH];           // B of g1 W1^T:  (n input, k hidden) = W1[n][k]
+    __nv_bfloat16 xs[TC_GROUPS][128 * ML_ND];  // A: the tile's standardised descriptors
+    __nv_bfloat16 hs[TC_GROUPS][128 * ML_NH];  // A: a1, then g2, then g1
+    float b1[ML_NH], b2[ML_NH], w3[ML_NH], sw3[ML_NH], sdinv[ML_ND];  // sw3 = sdE w3
+    float eh[TC_GROUPS][128];                  // the second column half's part of E
+    unsigned long long mbar[TC_GROUPS];
+    unsigned tmem;
+};
+static constexpr size_t TC_SMEM = sizeof(TcSmem) + 1024;  // + alignment of the operands to 1024 B
+
+__global__ void __launch_bounds__(TC_GROUPS * TC_GT, 1) k_mlp_tc(MLView m, int64_t count_o, int64_t count_h,
+                                                                 int blocks_o, unsigned* status)
+{
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>(tc_raw + ((1024u - (ml_smem(tc_raw) & 1023u)) & 1023u));
+    const int sp = blockIdx.x < (unsigned)blocks_o ? 0 : 1;
+    const int64_t count = sp == 0 ? count_o : count_h;
+    const int64_t blk = sp == 0 ? blockIdx.x : blockIdx.x - blocks_o;
+    const int64_t nblk = sp == 0 ? blocks_o : gridDim.x - blocks_o;
+    const float* th = sp == 0 ? m.theta[0] : m.theta[1];  // (no dynamic index into the parameter)
+    const int tid = threadIdx.x, grp = tid / TC_GT, gt = tid % TC_GT, warp = tid >> 5;
+    const int row = (warp & 3) * 32 + (tid & 31);  // tile row = TMEM lane
+    const int hf = (warp >> 2) & 1;                // column half of this warp
+    {
+        // W1 [64][128] and W2 [128][128] as 16-byte chunks of 8 columns, all
+        // loads issued before the first store; a chunk of row k stays a row
+        // of the straight tile and becomes 8 rows of the transposed one
+        constexpr int NT = TC_GROUPS * TC_GT;
+        constexpr int C1 = ML_ND * ML_NH / 8, C2 = ML_NH * ML_NH / 8, PER = (C1 + C2) / NT;
+        static_assert((C1 + C2) % NT == 0 && C1 % NT == 0, "whole chunks per thread");
+        const uint4* g1 = reinterpret_cast<const uint4*>(sp == 0 ? m.w1[0] : m.w1[1]);
+        const uint4* g2 = reinterpret_cast<const uint4*>(sp == 0 ? m.w2[0] : m.w2[1]);
+        uint4 ch[PER];
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int c = tid + i * NT;
+            ch[i] = c < C1 ? __ldg(g1 + c) : __ldg(g2 + (c - C1));
+        }
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int c0 = tid + i * NT;
+            const bool one = c0 < C1;  // uniform over i
+            const int c = one ? c0 : c0 - C1;
+            const int k = c / 16, n0 = (c % 16) * 8;  // W[k][n0 .. n0 + 7]
+            unsigned char* straight = reinterpret_cast<unsigned char*>(one ? S.w1 : S.w2);
+            unsigned char* trans = reinterpret_cast<unsigned char*>(one ? S.w1t : S.w2t);
+            const int kd = one ? ML_ND : ML_NH;  // K extent of the transposed tile
+            *reinterpret_cast<uint4*>(straight + tc_off(k, n0, ML_NH)) = ch[i];
+            const unsigned w4[4] = {ch[i].x, ch[i].y, ch[i].z, ch[i].w};
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<unsigned short*>(trans + tc_off(n0 + j, k, kd)) =
+                    (unsigned short)(w4[j >> 1] >> (16 * (j & 1)));
+        }
+        for (int e = tid; e < ML_NH; e += blockDim.x) {
+            S.b1[e] = th[param_off_b1() + e];
+            S.b2[e] = th[param_off_b2() + e];
+            S.w3[e] = th[param_off_w3() + e];
+            S.sw3[e] = th[param_off_muE() + 1] * th[param_off_w3() + e];
+        }
+        for (int e = tid; e < ML_ND; e += blockDim.x) S.sdinv[e] = 1.0f / th[param_off_sd() + e];
+    }
+    if (tid < TC_GROUPS)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ml_smem(&S.mbar[tid])) : "memory");
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(ml_smem(&S.tmem)),
+                     "r"(TC_GROUPS * 128)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // the weights were written by generic stores and are read by the tensor cores
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tcol = S.tmem + (unsigned)grp * 128u;               // this group's columns
+    const unsigned trow = tcol + (((unsigned)(warp & 3) * 32u) << 16);  // this warp's 32 lanes
+    const unsigned mb = ml_smem(&S.mbar[grp]);
+    const int bar = 1 + grp;
+    const unsigned sx = ml_smem(S.xs[grp]), sh = ml_smem(S.hs[grp]);
+    const unsigned sw1t = ml_smem(S.w1t), sw2t = ml_smem(S.w2t), sw2 = ml_smem(S.w2), sw1 = ml_smem(S.w1);
+    unsigned char* const xs = reinterpret_cast<unsigned char*>(S.xs[grp]);
+    unsigned char* const hs = reinterpret_cast<unsigned char*>(S.hs[grp]);
+    const float b3 = th[param_off_b3()];
+    const float muE = th[param_off_muE()], sdE = th[param_off_muE() + 1];
+    unsigned phase = 0;
+    bool failed = false;
+    // one product: operands written by this group's threads, then issued by
+    // its thread 0 and completing on the group's mbarrier
+    auto issue = [&](unsigned sa, unsigned sbo_a, unsigned sb, unsigned sbo_b, int ksteps, unsigned idesc) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        tg_sync(bar);
+        if (gt == 0) {
+            tc_fence_after();
+            for (int s = 0; s < ksteps; ++s)
+                tc_mma(tcol, tc_sdesc(sa + 256u * s, sbo_a), tc_sdesc(sb + 256u * s, sbo_b), idesc, s > 0);
+            tc_commit(mb);
+        }
+    };
+    // every thread waits (bounded) for the product; false if it did not
+    // complete, decided the same way for the whole group
+    auto done = [&]() {
+        unsigned tries = 0;
+        bool late = false;
+        while (!tc_mbar_try(mb, phase)) {
+            if (++tries > TC_WAIT_TRIES) {
+                late = true;
+                break;
+            }
+        }
+        if (tg_any(late, bar)) return false;
+        phase ^= 1u;
+        tc_fence_after();
+        return true;
+    };
+    // this thread's 8 float4 of a tile's descriptors (rows past count are zero)
+    float4 xv[8];
+    const int64_t ntile = (count + 127) / 128;
+    const int64_t tstride = nblk * TC_GROUPS;
+    if (blk * TC_GROUPS + grp < ntile) tc_load_x(m, sp, count, (blk * TC_GROUPS + grp) * 128, gt, xv);
+    for (int64_t tile = blk * TC_GROUPS + grp; tile < ntile; tile += tstride) {
+        const int64_t k0 = tile * 128;
+        // the tile's descriptors to BF16
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int e = gt + TC_GT * i, r = e >> 4, c4 = e & 15;
+            *reinterpret_cast<uint2*>(xs + tc_off(r, 4 * c4, ML_ND)) =
+                make_uint2(pack_bf16(xv[i].x, xv[i].y), pack_bf16(xv[i].z, xv[i].w));
+        }
+        issue(sx, 16u * ML_ND, sw1t, 16u * ML_ND, ML_ND / 16, tc_idesc(128, ML_NH));
+        if (!done()) {
+            failed = true;
+            break;
+        }
+        // layer 1 epilogue: a1 to the A tile, 1 - a1^2 kept as half2
+        const float2 one2 = make_float2(1.f, 1.f);
+        unsigned d1h[ML_NH / 4];
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc) {
+            float v[32];
+            const int c0 = hf * 64 + 32 * cc;
+            tc_ld32(trow + (unsigned)c0, v);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                unsigned pk[4];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int j = 8 * q + 4 * h;
+                    const float4 bb = *reinterpret_cast<const float4*>(&S.b1[c0 + j]);
+                    const float2 a01 = make_float2(tanh_fast(v[j] + bb.x), tanh_fast(v[j + 1] + bb.y));
+                    const float2 a23 = make_float2(tanh_fast(v[j + 2] + bb.z), tanh_fast(v[j + 3] + bb.w));
+                    pk[2 * h] = pack_bf16(a01.x, a01.y);
+                    pk[2 * h + 1] = pack_bf16(a23.x, a23.y);
+                    const float2 d01 = __ffma2_rn(make_float2(-a01.x, -a01.y), a01, one2);
+                    const float2 d23 = __ffma2_rn(make_float2(-a23.x, -a23.y), a23, one2);
+                    d1h[(32 * cc + j) / 2] = pack_h2(d01.x, d01.y);
+                    d1h[(32 * cc + j) / 2 + 1] = pack_h2(d23.x, d23.y);
+                }
+                *reinterpret_cast<uint4*>(hs + tc_off(row, c0 + 8 * q, ML_NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            }
+        }
+        issue(sh, 16u * ML_NH, sw2t, 16u * ML_NH, ML_NH / 16, tc_idesc(128, ML_NH));
+        if (!done()) {
+            failed = true;
+            break;
+        }
+        // layer 2 epilogue: E (two halves), and g2 = sdE w3 (1 - a2^2) to the A tile
+        float2 erp = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc) {
+            float v[32];
+            const int c0 = hf * 64 + 32 * cc;
+            tc_ld32(trow + (unsigned)c0, v);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                unsigned pk[4];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int j = 8 * q + 4 * h, col = c0 + j;
+                    const float4 bb = *reinterpret_cast<const float4*>(&S.b2[col]);
+                    const float4 ww = *reinterpret_cast<const float4*>(&S.w3[col]);
+                    const float4 sw = *reinterpret_cast<const float4*>(&S.sw3[col]);
+                    const float2 a01 = make_float2(tanh_fast(v[j] + bb.x), tanh_fast(v[j + 1] + bb.y));
+                    const float2 a23 = make_float2(tanh_fast(v[j + 2] + bb.z), tanh_fast(v[j + 3] + bb.w));
+                    erp = __ffma2_rn(a01, make_float2(ww.x, ww.y), erp);
+                    erp = __ffma2_rn(a23, make_float2(ww.z, ww.w), erp);
+                    const float2 g01 = __fmul2_rn(make_float2(sw.x, sw.y),
+                                                  __ffma2_rn(make_float2(-a01.x, -a01.y), a01, one2));
+                    const float2 g23 = __fmul2_rn(make_float2(sw.z, sw.w),
+                                                  __ffma2_rn(make_float2(-a23.x, -a23.y), a23, one2));
+                    pk[2 * h] = pack_bf16(g01.x, g01.y);
+                    pk[2 * h + 1] = pack_bf16(g23.x, g23.y);
+                }
+                *reinterpret_cast<uint4*>(hs + tc_off(row, c0 + 8 * q, ML_NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            }
+        }
+        const float er = erp.x + erp.y;
+        if (hf) S.eh[grp][row] = er;
+        issue(sh, 16u * ML_NH, sw2, 16u * ML_NH, ML_NH / 16, tc_idesc(128, ML_NH));
+        // (the group barrier in issue ordered the second half's part of E)
+        const int64_t atom = k0 + row < count ? species_atom(sp, k0 + row) : -1;
+        if (!hf && atom >= 0) m.e[atom] = sdE * ((er + S.eh[grp][row]) + b3) + muE;
+        if (!done()) {
+            failed = true;
+            break;
+        }
+        // first backward epilogue: g1 = (g2 W2^T) (1 - a1^2) to the A tile
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc) {
+            float v[32];
+            const int c0 = hf * 64 + 32 * cc;
+            tc_ld32(trow + (unsigned)c0, v);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                unsigned pk[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int j = 8 * q + 2 * h;
+                    const float2 g = __fmul2_rn(make_float2(v[j], v[j + 1]), unpack_h2(d1h[(32 * cc + j) / 2]));
+                    pk[h] = pack_bf16(g.x, g.y);
+                }
+                *reinterpret_cast<uint4*>(hs + tc_off(row, c0 + 8 * q, ML_NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            }
+        }
+        issue(sh, 16u * ML_NH, sw1, 16u * ML_NH, ML_NH / 16, tc_idesc(128, ML_ND));
+        // the next tile's descriptors load while the last product runs
+        if (tile + tstride < ntile) tc_load_x(m, sp, count, (tile + tstride) * 128, gt, xv);
+        if (!done()) {
+            failed = true;
+            break;
+        }
+        // second backward epilogue: dE/dD = (g1 W1^T) / sdD, 32 columns per thread
+        {
+            float v[32];
+            const int c0 = hf * 32;
+            tc_ld32(trow + (unsigned)c0, v);
+            if (atom >= 0) {
+                float4* D = reinterpret_cast<float4*>(m.dx + atom * ML_ND + c0);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float4 sd = *reinterpret_cast<const float4*>(&S.sdinv[c0 + 4 * q]);
+                    const float2 lo = __fmul2_rn(make_float2(v[4 * q], v[4 * q + 1]), make_float2(sd.x, sd.y));
+                    const float2 hi = __fmul2_rn(make_float2(v[4 * q + 2], v[4 * q + 3]), make_float2(sd.z, sd.w));
+                    D[q] = make_float4(lo.x, lo.y, hi.x, hi.y);
+                }
+            }
+        }
+    }
+    if (failed) {
+        if (gt == 0) status_set(status, ST_TIMEOUT);
+        // the products still in flight write this block's TMEM: wait (bounded)
+        unsigned tries = 0;
+        while (!tc_mbar_try(mb, phase) && ++tries < TC_WAIT_TRIES) {
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(TC_GROUPS * 128)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------
 // learned forces: F = -dE/dx through the descriptors (thread per atom i,
 // scatter to the neighbours as fixed point)
 // ---------------------------------------------------------------------
@@ -1068,27 +1471,39 @@ int launch_descriptor(nbg_ctx* c, bool raw)
     return NBG_OK;
 }
 
-int launch_mlp(nbg_ctx* c)
+// blocks of one launch over both species, split by their tiles: all of
+// them when they fit in `slots` resident blocks, else `slots` in proportion
+static void mlp_split(int64_t tiles_o, int64_t tiles_h, int64_t per_block, int64_t slots, int64_t& bo, int64_t& bh)
 {
-    if (!c->ml_attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_mlp_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
-        if (e != cudaSuccess) return cuda_fail(c, e, "k_mlp_bf16 shared memory");
-        e = cudaFuncSetAttribute(k_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (ML_ND * ML_NH + ML_NH * ML_NH) * (int)sizeof(float));
-        if (e != cudaSuccess) return cuda_fail(c, e, "k_train_fb shared memory");
-        c->ml_attr = true;
-    }
-    const MLView m = ml_view(c);
-    // two resident blocks per SM, split between the species by their tiles
-    const int64_t count_o = c->n / 3, count_h = 2 * (c->n / 3);
-    const int64_t tiles_o = (count_o + 15) / 16, tiles_h = (count_h + 15) / 16;
-    const int64_t need_o = (tiles_o + MLP_WARPS - 1) / MLP_WARPS, need_h = (tiles_h + MLP_WARPS - 1) / MLP_WARPS;
-    const int64_t slots = (int64_t)c->sms * 2;
-    int64_t bo = need_o, bh = need_h;
+    bo = (tiles_o + per_block - 1) / per_block;
+    bh = (tiles_h + per_block - 1) / per_block;
     if (bo + bh > slots) {
         bo = std::max<int64_t>(1, (slots * tiles_o + (tiles_o + tiles_h) / 2) / (tiles_o + tiles_h));
         bh = std::max<int64_t>(1, slots - bo);
     }
+}
+
+int launch_mlp(nbg_ctx* c)
+{
+    if (!c->ml_attr) {
+        int st = launch_mlp_attrs(c);
+        if (st) return st;
+    }
+    const MLView m = ml_view(c);
+    const int64_t count_o = c->n / 3, count_h = 2 * (c->n / 3);
+    int64_t bo, bh;
+    if (getenv("NBG_MLP_TCGEN05")) {
+        // the tensor-memory form: one block per SM (its shared memory),
+        // 128-atom tiles per group of 8 warps
+        mlp_split((count_o + 127) / 128, (count_h + 127) / 128, TC_GROUPS, (int64_t)c->sms, bo, bh);
+        k_mlp_tc<<<(int)(bo + bh), TC_GROUPS * TC_GT, TC_SMEM, c->stream>>>(m, count_o, count_h, (int)bo,
+                                                                             c->d.status);
+        NBG_LAUNCH_CHECK(c, "k_mlp_tc");
+        return NBG_OK;
+    }
+    // the warp-level form (the faster at these layer sizes): two resident
+    // blocks per SM, 16-atom tiles per warp
+    mlp_split((count_o + 15) / 16, (count_h + 15) / 16, MLP_WARPS, (int64_t)c->sms * 2, bo, bh);
     k_mlp_bf16<<<(int)(bo + bh), MLP_WARPS * 32, sizeof(MlpSmem), c->stream>>>(m, count_o, count_h, (int)bo);
     NBG_LAUNCH_CHECK(c, "k_mlp_bf16");
     return NBG_OK;
@@ -1229,6 +1644,8 @@ int launch_mlp_attrs(nbg_ctx* c)
 {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmem));
     if (e != cudaSuccess) return cuda_fail(c, e, "k_mlp_bf16 shared memory");
+    e = cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e != cudaSuccess) return cuda_fail(c, e, "k_mlp_tc shared memory");
     e = cudaFuncSetAttribute(k_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (ML_ND * ML_NH + ML_NH * ML_NH) * (int)sizeof(float));
     if (e != cudaSuccess) return cuda_fail(c, e, "k_train_fb shared memory");

@@ -918,7 +918,7 @@ static int forces_once(nbg_ctx* c, const StateView& s)
         if ((st = forces(c, s, true, StepRef{0, nullptr}))) return st;
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
-        if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if ((st = grow_lists(c, w))) return st;
             continue;
@@ -1081,7 +1081,7 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
             c->launches += c->accel_graph_launches;
             CK(cudaStreamSynchronize(c->stream), "accel sync");
             const unsigned w = *reinterpret_cast<const unsigned*>(c->hst + 9 * c->cols);
-            if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+            if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
             if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
                 if ((st = grow_lists(c, w))) return st;  // (drops the graph: captured again above)
                 continue;
@@ -1114,7 +1114,7 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
                "v download");
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
-        if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if ((st = grow_lists(c, w))) return st;
             continue;
@@ -1958,7 +1958,7 @@ static int ml_eval_once(nbg_ctx* c, const double* u, int what)
         }
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
-        if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW)) {
             if ((w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && (st = grow_lists(c, w))) return st;
             if ((w & ST_SHORT_OVERFLOW) && (st = ml_alloc_short(c, c->ml_scap + c->ml_scap / 2 + 32))) return st;
@@ -2300,7 +2300,7 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
             c->T_valid = false;
             return clear_status(c);
         };
-        if (w & (ST_NONFINITE | ST_RANGE)) return done_with(status_error(c, w));
+        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return done_with(status_error(c, w));
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW)) {
             if (++retries > 6) return done_with(fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough"));
             if ((w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && (st = grow_lists(c, w))) return done_with(st);

@@ -157,3 +157,164 @@ def test_mlp_tensor_memory_form_matches_warp_form(water, monkeypatch):
     assert rel(e_ws, e_ref) < 1e-2
     e_o, f_o = LO.forces(u, L, [t.astype(np.float64) for t in th])
     assert rel(f_tc, f_o) < 0.05
+
+
+def test_training_reaches_force_target(water, trained):
+    thO, thH, losses, held = trained
+    eng, L = water["eng"], water["L"]
+    (lo0, lh0), (lo1, lh1) = losses
+    assert lo1 < 1e-3 and lh1 < 1e-3, losses
+    eng.ml_set_params(0, thO)
+    eng.ml_set_params(1, thH)
+    u = held[0]
+    _, f_ml = eng.ml_eval(u)
+    _, f_sr = eng.ml_labels(u)
+    err = rel(f_ml, f_sr)
+    assert err < 0.04, err
+    # the GPU model is the FP64 model with these weights, to BF16 accuracy
+    _, f_o = LO.forces(u, L, [thO.astype(np.float64), thH.astype(np.float64)])
+    assert rel(f_ml, f_o) < 0.01
+
+
+def test_respa_with_one_inner_step_is_velocity_verlet(water, trained):
+    """Without a thermostat one inner step per outer step is velocity Verlet
+    with the same total force, to rounding."""
+    eng = _nve(water)
+    eng.ml_set_params(0, trained[0])
+    eng.ml_set_params(1, trained[1])
+    u, v = trained[3]
+    eng.set_state(u, v)
+    eng.advance(DT, 20)
+    ua, va = eng.get_state()
+    eng.set_state(u, v)
+    eng.respa_run(DT, 1, 20, threshold=0.0)
+    ub, vb = eng.get_state()
+    assert np.abs(ua - ub).max() < 1e-11
+    assert np.abs(va - vb).max() < 1e-9
+
+
+def _nve(water):
+    sim, _, _, _ = systems.spcfw_water_rf(N_MOL, thermo=False)
+    eng = sim.engine()
+    eng.ml_enable()
+    return eng
+
+
+def _zero_output(theta):
+    z = theta.copy()
+    o = 64 * 128 + 128 + 128 * 128 + 128
+    z[o:o + 129] = 0.0  # w3 and b3: E_i = mean_E, no learned force
+    return z
+
+
+def test_respa_ablation(water, trained):
+    """Same start, NVE, 2 fs outer step (4 x 0.5 fs): the trained network
+    keeps the energy close to velocity Verlet's; the split without it (fast
+    force = bonded only) drifts far more. The r-RESPA error check measures
+    the learned force against the exact short-range force every outer step."""
+    thO, thH, _, held = trained
+    eng = _nve(water)
+    u, v = held
+    e0 = eng.energy(u, v)["total"]
+    n = len(u)
+
+    def drift():
+        uu, vv = eng.get_state()
+        return abs(eng.energy(uu, vv)["total"] - e0) / n
+
+    eng.set_state(u, v)
+    eng.advance(DT, 800)
+    d_vv = drift()
+    eng.ml_set_params(0, thO)
+    eng.ml_set_params(1, thH)
+    eng.set_state(u, v)
+    st = eng.respa_run(DT, 4, 200, threshold=0.0)
+    d_ml = drift()
+    assert st.outer_mts == 200 and st.outer_fallback == 0
+    assert st.judge_mean < 0.04, st.judge_mean
+    eng.set_state(u, v)
+    eng.respa_run(DT, 4, 200, threshold=0.0, exact_split=True)
+    d_exact = drift()
+    eng.ml_set_params(0, _zero_output(thO))
+    eng.ml_set_params(1, _zero_output(thH))
+    eng.set_state(u, v)
+    st0 = eng.respa_run(DT, 4, 200, threshold=0.0)
+    d_zero = drift()
+    assert st0.judge_mean > 0.99
+    print(f"drift per atom over 400 fs: VV {d_vv:.3g}, exact split {d_exact:.3g}, learned {d_ml:.3g}, "
+          f"no network {d_zero:.3g}")
+    assert d_zero > 10 * d_ml, (d_zero, d_ml)
+    assert d_ml < 2e-3, d_ml
+
+
+def test_respa_judge_falls_back_to_velocity_verlet(water, trained):
+    """With the untrained (zero-output) model every chunk fails the 2 % judge
+    and is integrated again by velocity Verlet: the result is the plain run
+    (up to the FP32 summation order of forces from lists rebuilt at other
+    steps; an r-RESPA step with this model would differ by orders more)."""
+    thO, thH, _, held = trained
+    eng = _nve(water)
+    u, v = held
+    eng.ml_set_params(0, _zero_output(thO))
+    eng.ml_set_params(1, _zero_output(thH))
+    eng.set_state(u, v)
+    st = eng.respa_run(DT, 4, 70, threshold=0.02)
+    ub, vb = eng.get_state()
+    assert st.outer_fallback == 70 and st.outer_mts == 0
+    eng.set_state(u, v)
+    eng.advance(DT, 64 * 4)
+    eng.advance(DT, 6 * 4)
+    ua, va = eng.get_state()
+    assert np.abs(ua - ub).max() < 1e-6
+    assert np.abs(va - vb).max() < 1e-4
+
+
+def test_learned_api_errors(gpu):
+    """The learned model refuses systems it does not model, and the r-RESPA
+    entry point refuses bad arguments and unsupported thermostats."""
+    import systems as S
+    nbg = S.nbg
+    # a Lennard-Jones liquid: not water
+    sim = S.lj_liquid(1000, seed=2)
+    eng = sim.engine()
+    with pytest.raises(nbg.EngineError) as e:
+        eng.ml_enable()
+    assert e.value.status == -6  # NBG_ERR_UNSUPPORTED
+    # calls before nbg_ml_enable
+    sim, pos, vel, L = systems.spcfw_water_rf(1000)
+    eng = sim.engine()
+    with pytest.raises(nbg.EngineError):
+        eng.ml_eval(pos)
+    eng.ml_enable()
+    with pytest.raises(nbg.EngineError):
+        eng.ml_set_params(2, np.zeros(nbg._abi.NBG_ML_NPARAM, dtype=np.float32))
+    with pytest.raises(nbg.EngineError):  # no resident state yet
+        eng.respa_run(DT, 4, 1)
+    eng.set_state(pos, vel)
+    with pytest.raises(nbg.EngineError):
+        eng.respa_run(-DT, 4, 1)
+    with pytest.raises(nbg.EngineError):
+        eng.respa_run(DT, 0, 1)
+    with pytest.raises(nbg.EngineError):  # empty training set
+        eng.ml_train(10)
+    # Andersen is not supported by r-RESPA
+    simA, pos, vel, L = systems.spcfw_water_rf(1000)
+    simA.thermostat = nbg.AndersenThermostat(300.0, 10.0)
+    engA = simA.engine()
+    engA.ml_enable()
+    engA.set_state(pos, vel)
+    with pytest.raises(nbg.EngineError) as e:
+        engA.respa_run(DT, 4, 1)
+    assert e.value.status == -6
+
+
+def test_thermostat_target_moves_temperature(water):
+    """nbg_set_thermostat_target: a Berendsen run re-targeted to 320 K heats up."""
+    sim, pos, vel, L = systems.spcfw_water_rf(1000)
+    eng = sim.engine()
+    eng.set_state(water["u"], water["v"])
+    eng.set_thermostat_target(320.0)
+    eng.advance(DT, 3000)
+    u, v = eng.get_state()
+    T = eng.energy(u, v)["temperature"]
+    assert 305.0 < T < 335.0, T

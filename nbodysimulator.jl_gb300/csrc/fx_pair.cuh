@@ -78,10 +78,12 @@ __device__ __forceinline__ void fx_join(float& h, float& e, int o, int width)
 
 // One packed pair step (entries k0 and k0 + LPA of atom row a) of the
 // fixed-point kernels: classification, FP64 fallback, LJ and reaction-field
-// factors in the units of the LJ sum, accumulated into (px, py, pz).
+// factors in the units of the LJ sum, accumulated into (px, py, pz). An
+// entry with v0 / v1 false adds exactly zero (its partner must be a valid
+// index, e.g. the atom itself).
 template <int POT>
 __device__ __forceinline__ void fx_pair2(const Dev& d, const double* X, int64_t ia, bool lj_i, float kqi,
-                                         const uint4& qi, int j0, int j1, bool v1, const uint4& q0,
+                                         const uint4& qi, int j0, int j1, bool v0, bool v1, const uint4& q0,
                                          const uint4& q1, float lj_lo, float lj_hi, float el_lo, float el_hi,
                                          float sig2h, float sig2l, float krf, float2& px, float2& py, float2& pz,
                                          bool& range_err)
@@ -92,9 +94,9 @@ __device__ __forceinline__ void fx_pair2(const Dev& d, const double* X, int64_t 
     float2 dy = make_float2(fx_diff(qi.y, q0.y), fx_diff(qi.y, q1.y));
     float2 dz = make_float2(fx_diff(qi.z, q0.z), fx_diff(qi.z, q1.z));
     float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-    const bool lp0 = HAS_LJ && lj_i && (POT != FX_WATER || fx_oxygen(j0));
+    const bool lp0 = HAS_LJ && v0 && lj_i && (POT != FX_WATER || fx_oxygen(j0));
     const bool lp1 = HAS_LJ && v1 && lj_i && (POT != FX_WATER || fx_oxygen(j1));
-    const bool ep0 = HAS_EL, ep1 = HAS_EL && v1;
+    const bool ep0 = HAS_EL && v0, ep1 = HAS_EL && v1;
     bool lj0, lj1, el0, el1b, amb0, amb1;
     fx_classify(r2.x, lp0, ep0, lj_lo, lj_hi, el_lo, el_hi, lj0, el0, amb0);
     fx_classify(r2.y, lp1, ep1, lj_lo, lj_hi, el_lo, el_hi, lj1, el1b, amb1);

@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
                 jn0 = kn < cnt ? __ldg(row + (int64_t)kn * d.nbr_kstride) : (int)a0;
                 jn1 = kn + LPA < cnt ? __ldg(row + (int64_t)(kn + LPA) * d.nbr_kstride) : jn0;
                 const uint4 q0 = pos[j0 - a0], q1 = pos[j1 - a0];
-                fx_pair2<POT>(d, s.x, gi, lj_atoms, kqi, qi, j0, j1, v1, q0, q1, lj_lo, lj_hi, el_lo, el_hi, sig2h,
+                fx_pair2<POT>(d, s.x, gi, lj_atoms, kqi, qi, j0, j1, true, v1, q0, q1, lj_lo, lj_hi, el_lo, el_hi, sig2h,
                               sig2l, krf, px, py, pz, range_err);
             }
             float hx = __fadd_rn(px.x, px.y), hy = __fadd_rn(py.x, py.y), hz = __fadd_rn(pz.x, pz.y);

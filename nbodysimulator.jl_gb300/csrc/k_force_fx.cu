@@ -321,8 +321,8 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncwarp();
 
-    // boxes of a tile: its largest count in 32-entry boxes (warp-uniform)
-    auto boxes_of = [&](int64_t t) -> int {
+    // a tile's largest list count (warp-uniform)
+    auto cmax_of = [&](int64_t t) -> int {
         int c = 0;
         if (lane_w < AW) {
             const int64_t i = t * AW + lane_w;
@@ -330,12 +330,12 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_xor_sync(0xffffffffu, c, o));
-        return (c + 31) >> 5;
+        return c;
     };
     // the producer's next box: box pb of the pnb boxes of tile pt
     int64_t pt = gw;
     int pb = 0, pnb = 0;
-    while (pt < ntiles && (pnb = boxes_of(pt)) == 0) pt += nwarps;
+    while (pt < ntiles && (pnb = (cmax_of(pt) + 31) >> 5) == 0) pt += nwarps;
     unsigned issued = 0, consumed = 0;
     auto refill = [&]() {
         while (pt < ntiles && issued - consumed < FXW_SLOTS) {
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
             if (++pb >= pnb) {
                 pb = 0;
                 pt += nwarps;
-                while (pt < ntiles && (pnb = boxes_of(pt)) == 0) pt += nwarps;
+                while (pt < ntiles && (pnb = (cmax_of(pt) + 31) >> 5) == 0) pt += nwarps;
             }
         }
     };
@@ -359,7 +359,8 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
 
     bool range_err = false, timeout = false;
     for (int64_t t = gw; t < ntiles; t += nwarps) {
-        const int nb = boxes_of(t);
+        const int cm = cmax_of(t);
+        const int nb = (cm + 31) >> 5;
         const int64_t i = t * AW + a;
         const bool active = i < d.n;
         const int64_t ia = active ? i : 0;
@@ -391,33 +392,36 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
             const unsigned char* box = slot0 + sl * 1024u;
             const int kb = 32 * b;
             // this box's entries of the lane: kb + lane + 2 m LPA (+ LPA), the
-            // next step's entries and gathers issued before this step's arithmetic
-            int jn0 = 0, jn1 = 0;
-            uint4 qn0 = qi, qn1 = qi;
-            if (kb + lane < cnt) {
-                jn0 = fxw_entry(box, a, lane);
-                jn1 = kb + lane + LPA < cnt ? fxw_entry(box, a, lane + LPA) : jn0;
+            // next step's entries and gathers issued before this step's
+            // arithmetic. No branch per lane: an entry past the row's count
+            // gathers the atom itself and adds zero; steps past the tile's
+            // largest count are skipped (warp-uniform).
+            int jn0, jn1;
+            uint4 qn0, qn1;
+            {
+                const int e0 = fxw_entry(box, a, lane), e1 = fxw_entry(box, a, lane + LPA);
+                jn0 = kb + lane < cnt ? e0 : (int)ia;
+                jn1 = kb + lane + LPA < cnt ? e1 : jn0;
                 qn0 = __ldg(&d.pfx[jn0]);
                 qn1 = __ldg(&d.pfx[jn1]);
             }
 #pragma unroll
             for (int m = 0; m < IT; ++m) {
+                if (kb + 2 * m * LPA >= cm) break;
                 const int c0 = lane + 2 * m * LPA;
                 const bool v0 = kb + c0 < cnt, v1 = kb + c0 + LPA < cnt;
                 const int j0 = jn0, j1 = jn1;
                 const uint4 q0 = qn0, q1 = qn1;
-                if (m + 1 < IT) {
+                if (m + 1 < IT && kb + 2 * (m + 1) * LPA < cm) {
                     const int cn = c0 + 2 * LPA;
-                    if (kb + cn < cnt) {
-                        jn0 = fxw_entry(box, a, cn);
-                        jn1 = kb + cn + LPA < cnt ? fxw_entry(box, a, cn + LPA) : jn0;
-                        qn0 = __ldg(&d.pfx[jn0]);
-                        qn1 = __ldg(&d.pfx[jn1]);
-                    }
+                    const int e0 = fxw_entry(box, a, cn), e1 = fxw_entry(box, a, cn + LPA);
+                    jn0 = kb + cn < cnt ? e0 : (int)ia;
+                    jn1 = kb + cn + LPA < cnt ? e1 : jn0;
+                    qn0 = __ldg(&d.pfx[jn0]);
+                    qn1 = __ldg(&d.pfx[jn1]);
                 }
-                if (v0)
-                    fx_pair2<POT>(d, s.x, ia, lj_i, kqi, qi, j0, j1, v1, q0, q1, lj_lo, lj_hi, el_lo, el_hi, sig2h,
-                                  sig2l, krf, px, py, pz, range_err);
+                fx_pair2<POT>(d, s.x, ia, lj_i, kqi, qi, j0, j1, v0, v1, q0, q1, lj_lo, lj_hi, el_lo, el_hi, sig2h,
+                              sig2l, krf, px, py, pz, range_err);
             }
             __syncwarp();  // every lane is done with the slot
             ++consumed;

@@ -155,10 +155,11 @@ def algorithmic_work(workload, n, eng):
     gravity 20 flop per ordered pair; list kernels the bytes a launch must move."""
     if workload == "gravity":
         return 20.0 * n * (n - 1), "TFLOP/s", "fp32"
-    # list kernels: per atom 32 B split position + 24 B acceleration write + 4 B
-    # per list entry + 32 B per neighbour gather (counted once per atom in HBM terms)
+    # the fixed-point list kernel: per atom its 16 B position record (each
+    # neighbour's gather counted once per atom in HBM terms) + 24 B acceleration
+    # write + 4 B per list entry
     nbr = 419.0 if workload == "water" else 73.6  # water: 1.0 nm list; LJ liquids (single and ensemble): 2.8 sigma
-    return n * (32 + 24 + 4 * nbr), "GB/s", "hbm"
+    return n * (16 + 24 + 4 * nbr), "GB/s", "hbm"
 
 
 class ClockSampler:
@@ -938,7 +939,7 @@ def main():
         # the whole step of every replica in one launch: bound by instruction
         # issue and latency (positions in shared memory, FP64 integration),
         # not by DRAM: the floor is the step's warp instructions (ncu) over
-        # all SMs at 4 per clock; the HBM fraction of the 406 B per atom-step
+        # all SMs at 4 per clock; the HBM fraction of the 334 B per atom-step
         # of algorithmic traffic is kept beside it
         inst = profile_value(f"k_ensemble:{w['name']}", "issue.json")
         mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0

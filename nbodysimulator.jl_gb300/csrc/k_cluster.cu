@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const double an = ((double)fsum[6 * ko + 2 * k] + (double)fsum[6 * ko + 2 * k + 1]) * im_o;
-                    if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+                    if (!finite64(an)) status_set(d.status, ST_NONFINITE);
                     dst[3 * io + k] = an;
                 }
             }
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const double an = ((double)fsum[6 * ko + 2 * k] + (double)fsum[6 * ko + 2 * k + 1]) * im_o;
-                if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+                if (!finite64(an)) status_set(d.status, ST_NONFINITE);
                 v[k] = kick1(v[k], a[k], an, dt);
                 a[k] = an;
             }

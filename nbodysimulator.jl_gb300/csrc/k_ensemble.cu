@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
                 const double im = d.inv_mass[gi] * R.fx_fscale;
                 const double an[3] = {((double)hx + (double)ex) * im, ((double)hy + (double)ey) * im,
                                       ((double)hz + (double)ez) * im};
-                if (!isfinite(an[0]) || !isfinite(an[1]) || !isfinite(an[2])) status_set(d.status, ST_NONFINITE);
+                if (!finite64(an[0]) || !finite64(an[1]) || !finite64(an[2])) status_set(d.status, ST_NONFINITE);
                 double* v = s.v + 3 * gi;
                 double* ao = s.a_old + 3 * gi;
 #pragma unroll

@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
             const double im = d.inv_mass[i] * R.fx_fscale;
             const double a0 = ((double)hx + (double)ex) * im, a1 = ((double)hy + (double)ey) * im,
                          a2 = ((double)hz + (double)ez) * im;
-            if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
+            if (!finite64(a0) || !finite64(a1) || !finite64(a2)) status_set(d.status, ST_NONFINITE);
             s.a_new[3 * i] = a0;
             s.a_new[3 * i + 1] = a1;
             s.a_new[3 * i + 2] = a2;
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
             const double im = d.inv_mass[i] * R.fx_fscale;
             const double a0 = ((double)hx + (double)ex) * im, a1 = ((double)hy + (double)ey) * im,
                          a2 = ((double)hz + (double)ez) * im;
-            if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
+            if (!finite64(a0) || !finite64(a1) || !finite64(a2)) status_set(d.status, ST_NONFINITE);
             s.a_new[3 * i] = a0;
             s.a_new[3 * i + 1] = a1;
             s.a_new[3 * i + 2] = a2;

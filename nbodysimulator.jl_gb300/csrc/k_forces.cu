@@ -270,7 +270,7 @@ __global__ void k_gravity_reduce(const double* __restrict__ part, int64_t n, int
         double s = 0.0;
         for (int c = 0; c < jchunks; ++c) s += part[(int64_t)c * 3 * n + e];
         double a = -G * s;
-        if (!isfinite(a)) status_set(status, ST_NONFINITE);
+        if (!finite64(a)) status_set(status, ST_NONFINITE);
         const int64_t slot = e / 3;
         A[perm ? 3 * (int64_t)perm[slot] + (e - 3 * slot) : e] = a;
     }
@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(AT) k_allpairs(Dev d, StateView s)
         a[2] += cm * mz.value();
     }
     for (int k = 0; k < 3; ++k) {
-        if (!isfinite(a[k])) status_set(d.status, ST_NONFINITE);
+        if (!finite64(a[k])) status_set(d.status, ST_NONFINITE);
         s.a_new[3 * i + k] = a[k];
     }
 }
@@ -611,7 +611,7 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
         if (range_err) status_set(d.status, ST_RANGE);
         const double im = d.inv_mass[i];
         double a0 = fx.value() * im, a1 = fy.value() * im, a2 = fz.value() * im;
-        if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
+        if (!finite64(a0) || !finite64(a1) || !finite64(a2)) status_set(d.status, ST_NONFINITE);
         s.a_new[3 * i] = a0;
         s.a_new[3 * i + 1] = a1;
         s.a_new[3 * i + 2] = a2;
@@ -680,7 +680,7 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
         const double im = d.inv_mass[i];
         const double a0 = ((double)px + (double)ex) * im, a1 = ((double)py + (double)ey) * im,
                      a2 = ((double)pz + (double)ez) * im;
-        if (!isfinite(a0) || !isfinite(a1) || !isfinite(a2)) status_set(d.status, ST_NONFINITE);
+        if (!finite64(a0) || !finite64(a1) || !finite64(a2)) status_set(d.status, ST_NONFINITE);
         s.a_new[3 * i] = a0;
         s.a_new[3 * i + 1] = a1;
         s.a_new[3 * i + 2] = a2;

@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256) k_kick(Dev d, StateView s, double dt, int
             an = __dadd_rn(an, __dmul_rn(bfac, v));
         else if (thermo && (d.therm == NBG_THERMO_BERENDSEN || d.therm == NBG_THERMO_NOSEHOOVER))
             an = __dadd_rn(an, thermo_term_T(d, e / 3, v, zeta, do_T ? T_now : d.red_T[d.rep_of[e / 3]]));
-        if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+        if (!finite64(an)) status_set(d.status, ST_NONFINITE);
         double vn = kick1(v, s.a_old[e], an, dt);
         s.v[e] = vn;
         s.a_old[e] = an;
@@ -339,7 +339,7 @@ __global__ void k_em(Dev d, StateView s, double dt, double sqdt, StepRef sr)
             double drift = s.a_new[e];
             if (oxy) drift = __dsub_rn(drift, __dmul_rn(g, v) / d.mass[i]);
             drift = __dsub_rn(drift, __dmul_rn(g, v));
-            if (!isfinite(drift)) status_set(d.status, ST_NONFINITE);
+            if (!finite64(drift)) status_set(d.status, ST_NONFINITE);
             double vn = __dadd_rn(__dadd_rn(v, __dmul_rn(dt, drift)), __dmul_rn(sigma, __dmul_rn(sqdt, (double)z[k])));
             s.x[e] = __dadd_rn(s.x[e], __dmul_rn(dt, v));
             s.v[e] = vn;
@@ -411,7 +411,7 @@ __global__ void k_baoab_kick_drift(Dev d, StateView s, double dt, StepRef sr)
         for (int k = 0; k < 3; ++k) {
             const int64_t e = 3 * i + k;
             const double an = s.a_new[e];
-            if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+            if (!finite64(an)) status_set(d.status, ST_NONFINITE);
             const double v = __dadd_rn(s.v[e], __dmul_rn(hdt, an));
             s.a_old[e] = an;
             const double vh = fma(hdt, an, v);
@@ -443,7 +443,7 @@ __global__ void k_baoab_kick(Dev d, StateView s, double dt)
     const double hdt = 0.5 * dt;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 3 * d.n; e += (int64_t)gridDim.x * blockDim.x) {
         double an = s.a_new[e];
-        if (!isfinite(an)) status_set(d.status, ST_NONFINITE);
+        if (!finite64(an)) status_set(d.status, ST_NONFINITE);
         s.v[e] = __dadd_rn(s.v[e], __dmul_rn(hdt, an));
         s.a_old[e] = an;
     }

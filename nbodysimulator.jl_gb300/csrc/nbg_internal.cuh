@@ -448,6 +448,13 @@ __device__ __forceinline__ int64_t step_of(StepRef r) { return r.off + (r.base ?
 
 __device__ __forceinline__ void status_set(unsigned* st, unsigned bit) { atomicOr(st, bit); }
 
+// x is neither infinite nor NaN (the exponent field is not all ones), by
+// integer operations: FP64 compares issue slowly on this GPU
+__device__ __forceinline__ bool finite64(double x)
+{
+    return (__double_as_longlong(x) & 0x7ff0000000000000ll) != 0x7ff0000000000000ll;
+}
+
 // The reference's get_interparticle_distance in FP64, no contraction
 // (boundary_conditions.jl:111-172). Returns false when a while loop exceeded
 // MINIMAGE_MAX_ITERS (non-finite or absurdly distant coordinates).

@@ -65,6 +65,9 @@ WORKLOADS = {
     "rdf": dict(name="rdf-water-oxygens-4096x512", n=12288, dt=None, steps=20, frames=512, maxbin=1000),
 }
 RDF_FLOP_PER_PAIR = 40.0  # the FP32 screen of one pair (FMA = 2)
+# SPC/Fw constants the water workloads run with, reported in their config
+SPCFW_CONFIG = {"r0_nm": 0.1012, "theta0_deg": 113.24,
+                "bond_k": "463700 kJ/mol/nm^2 (4637 read per square angstrom)", "angle_k": "383 kJ/mol/rad^2"}
 
 
 class Workload:
@@ -525,6 +528,7 @@ def run_mts(args, rank, world):
             "data": "synthetic (seeded generator, no dataset); training frames from this run's plain MD",
             "config": {"workload": w["name"], "N": n, "dt_inner_fs": dt * 1e3, "inner_steps": inner,
                        "dt_outer_fs": dt * inner * 1e3, "electrostatics": "reaction field eps_rf 78.5, 0.9 nm",
+                       "spcfw": SPCFW_CONFIG,
                        "thermostat": "Berendsen 300 K tau 0.1 ps", "l2": "no flush (state L2-resident across steps)",
                        "lanes_per_atom": tuned[0], "autotune_force_ms": tuned[1],
                        "training": {"frames": frames_per_T * len(temps), "temperatures_K": list(temps),
@@ -959,6 +963,8 @@ def main():
     if args.workload == "gravity":
         config["gravity_precision"] = "plain FP32 positions" if args.grav_plain else "hi/lo split positions (compensated)"
     else:
+        if args.workload == "water":
+            config["spcfw"] = SPCFW_CONFIG
         d0 = wl.descs[0]
         re = int(d0.rebuild_every)
         config["verlet_list"] = {"skin": float(d0.skin),

@@ -51,7 +51,8 @@ typedef enum nbg_status {
     NBG_ERR_TIMEOUT = -5,      /* a bounded device-side wait gave up */
     NBG_ERR_UNSUPPORTED = -6,  /* system/option not implemented on the GPU */
     NBG_ERR_RANGE = -7,        /* minimum-image loop exceeded its iteration cap */
-    NBG_ERR_NOMEM = -8         /* device allocation failed */
+    NBG_ERR_NOMEM = -8,        /* device allocation failed */
+    NBG_ERR_INDEX = -9         /* a neighbour or cell index out of range (checked by debug builds only) */
 } nbg_status;
 
 /* Boundary conditions (src/boundary_conditions.jl). */

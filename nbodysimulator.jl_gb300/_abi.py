@@ -9,7 +9,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libnbg.so")
+# NBG_DEBUG=1 selects the debug build (libnbg_debug.so: bounds checks on every
+# neighbour and cell index a kernel reads, reported as NBG_ERR_INDEX)
+LIB_PATH = os.path.join(HERE, "libnbg_debug.so" if os.environ.get("NBG_DEBUG") == "1" else "libnbg.so")
 
 NBG_ABI_VERSION = 1
 
@@ -23,6 +25,7 @@ STATUS_NAMES = {
     -6: "NBG_ERR_UNSUPPORTED",
     -7: "NBG_ERR_RANGE",
     -8: "NBG_ERR_NOMEM",
+    -9: "NBG_ERR_INDEX",
 }
 
 NBG_BC_INFINITE, NBG_BC_CUBIC, NBG_BC_PERIODIC = 0, 1, 2
@@ -185,8 +188,9 @@ def load_library(path: str = LIB_PATH):
         return _lib
     if not os.path.exists(path):
         raise RuntimeError(
-            f"libnbg.so not found at {path}: build it with "
-            "`python -c 'import __graft_entry__ as g; g.build()'` (the engine has no CPU fallback)")
+            f"{os.path.basename(path)} not found at {path}: build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (the debug build with "
+            "`python nbodysimulator.jl_gb300/build.py --debug`; the engine has no CPU fallback)")
     lib = ctypes.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)

@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_vv(Dev d, StateView s
             float px = 0.f, py = 0.f, pz = 0.f;
             bool range_err = false;
             for (int k = lane; k < c; k += LPA) {
-                const int j = lst[g * cap + k];
+                const int j = dbg_index(lst[g * cap + k], d.n, i, d.status);
                 const PairOut o = pair_cutoff<true>(d, R, K, i, j, hi_i, lo_i, ph[j], pl[j], kqi, X);
                 range_err |= o.range_err;
                 px += o.fx;

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(EB) k_energy_list(Dev d, const double* X, doub
         const int cnt = d.nbr_count[i];
         double el_i = 0.0;
         for (int k = 0; k < cnt; ++k) {
-            const int64_t j = d.nbr[(int64_t)k * d.nbr_kstride + i * d.nbr_istride];
+            const int64_t j = dbg_index(d.nbr[(int64_t)k * d.nbr_kstride + i * d.nbr_istride], d.n, (int)i, d.status);
             if (j <= i) continue;
             const bool lj = lj_i && (!water || j % 3 == 0);
             const bool el = (d.pots & NBG_POT_EL) && !el_excluded(d.kind, i, j);
@@ -254,7 +254,7 @@ __global__ void k_pairs(Dev d, StateView s, int which, int use_list, int fx, int
         const bool water = d.kind == NBG_SYSTEM_WATER;
         const bool lj_i = (d.pots & NBG_POT_LJ) && (!water || (i % 3) == 0);
         for (int64_t k = use_list ? 0 : R.atom0; k < m; ++k) {
-            int64_t j = use_list ? d.nbr[k * d.nbr_kstride + i * d.nbr_istride] : k;
+            int64_t j = use_list ? dbg_index(d.nbr[k * d.nbr_kstride + i * d.nbr_istride], d.n, (int)i, d.status) : k;
             if (j == i) continue;
             bool in;
             if (fx) {

@@ -259,14 +259,22 @@ __global__ void __launch_bounds__(THREADS, 1) k_ensemble(Dev d, StateView s, Ens
             float2 px = make_float2(0.f, 0.f), py = px, pz = px;
             // the row entries of the next iteration are loaded before this
             // iteration's gathers and arithmetic (one iteration ahead)
-            int jn0 = lane < cnt ? __ldg(row + (int64_t)lane * d.nbr_kstride) : (int)a0;
-            int jn1 = lane + LPA < cnt ? __ldg(row + (int64_t)(lane + LPA) * d.nbr_kstride) : jn0;
+            // (debug builds: an entry outside the replica's atoms is reported
+            // and replaced by its first atom before it indexes shared memory)
+            int jn0 = lane < cnt ? (int)a0 + dbg_index(__ldg(row + (int64_t)lane * d.nbr_kstride) - (int)a0, n, 0, d.status)
+                                 : (int)a0;
+            int jn1 = lane + LPA < cnt
+                          ? (int)a0 + dbg_index(__ldg(row + (int64_t)(lane + LPA) * d.nbr_kstride) - (int)a0, n, 0, d.status)
+                          : jn0;
             for (int k0 = lane; k0 < cnt; k0 += 2 * LPA) {
                 const bool v1 = k0 + LPA < cnt;
                 const int j0 = jn0, j1 = jn1;
                 const int kn = k0 + 2 * LPA;
-                jn0 = kn < cnt ? __ldg(row + (int64_t)kn * d.nbr_kstride) : (int)a0;
-                jn1 = kn + LPA < cnt ? __ldg(row + (int64_t)(kn + LPA) * d.nbr_kstride) : jn0;
+                jn0 = kn < cnt ? (int)a0 + dbg_index(__ldg(row + (int64_t)kn * d.nbr_kstride) - (int)a0, n, 0, d.status)
+                               : (int)a0;
+                jn1 = kn + LPA < cnt
+                          ? (int)a0 + dbg_index(__ldg(row + (int64_t)(kn + LPA) * d.nbr_kstride) - (int)a0, n, 0, d.status)
+                          : jn0;
                 const uint4 q0 = pos[j0 - a0], q1 = pos[j1 - a0];
                 fx_pair2<POT>(d, s.x, gi, lj_atoms, kqi, qi, j0, j1, true, v1, q0, q1, lj_lo, lj_hi, el_lo, el_hi, sig2h,
                               sig2l, krf, px, py, pz, range_err);

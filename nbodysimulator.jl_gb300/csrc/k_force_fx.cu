@@ -175,8 +175,8 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
         int jn0 = 0, jn1 = 0;
         uint4 qn0 = qi, qn1 = qi;
         if (lane < cnt) {
-            jn0 = fx_entry(stage, A, a, lane);
-            jn1 = lane + LPA < cnt ? fx_entry(stage, A, a, lane + LPA) : jn0;
+            jn0 = dbg_index(fx_entry(stage, A, a, lane), d.n, (int)ia, d.status);
+            jn1 = lane + LPA < cnt ? dbg_index(fx_entry(stage, A, a, lane + LPA), d.n, (int)ia, d.status) : jn0;
             qn0 = __ldg(&d.pfx[jn0]);
             qn1 = __ldg(&d.pfx[jn1]);
         }
@@ -187,8 +187,8 @@ __global__ void __launch_bounds__(FX_THREADS) k_force_fx(Dev d, StateView s, con
             const uint4 q0 = qn0, q1 = qn1;
             const int kn = k0 + 2 * LPA;
             if (kn < cnt) {
-                jn0 = fx_entry(stage, A, a, kn);
-                jn1 = kn + LPA < cnt ? fx_entry(stage, A, a, kn + LPA) : jn0;
+                jn0 = dbg_index(fx_entry(stage, A, a, kn), d.n, (int)ia, d.status);
+                jn1 = kn + LPA < cnt ? dbg_index(fx_entry(stage, A, a, kn + LPA), d.n, (int)ia, d.status) : jn0;
                 qn0 = __ldg(&d.pfx[jn0]);
                 qn1 = __ldg(&d.pfx[jn1]);
             }
@@ -400,8 +400,8 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
             uint4 qn0, qn1;
             {
                 const int e0 = fxw_entry(box, a, lane), e1 = fxw_entry(box, a, lane + LPA);
-                jn0 = kb + lane < cnt ? e0 : (int)ia;
-                jn1 = kb + lane + LPA < cnt ? e1 : jn0;
+                jn0 = kb + lane < cnt ? dbg_index(e0, d.n, (int)ia, d.status) : (int)ia;
+                jn1 = kb + lane + LPA < cnt ? dbg_index(e1, d.n, (int)ia, d.status) : jn0;
                 qn0 = __ldg(&d.pfx[jn0]);
                 qn1 = __ldg(&d.pfx[jn1]);
             }
@@ -415,8 +415,8 @@ __global__ void __launch_bounds__(FXW_WARPS * 32, (LPA <= 4 && POT == FX_LJ) ? 4
                 if (m + 1 < IT && kb + 2 * (m + 1) * LPA < cm) {
                     const int cn = c0 + 2 * LPA;
                     const int e0 = fxw_entry(box, a, cn), e1 = fxw_entry(box, a, cn + LPA);
-                    jn0 = kb + cn < cnt ? e0 : (int)ia;
-                    jn1 = kb + cn + LPA < cnt ? e1 : jn0;
+                    jn0 = kb + cn < cnt ? dbg_index(e0, d.n, (int)ia, d.status) : (int)ia;
+                    jn1 = kb + cn + LPA < cnt ? dbg_index(e1, d.n, (int)ia, d.status) : jn0;
                     qn0 = __ldg(&d.pfx[jn0]);
                     qn1 = __ldg(&d.pfx[jn1]);
                 }

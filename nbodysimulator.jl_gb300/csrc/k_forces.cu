@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
         int jn = 0;
         float4 hn = make_float4(0.f, 0.f, 0.f, 0.f), ln = hn;
         if (cnt > 0) {
-            jn = __ldg(nl);
+            jn = dbg_index(__ldg(nl), d.n, (int)i, d.status);
             hn = __ldg(&d.phi[jn]);
             ln = __ldg(&d.plo[jn]);
         }
@@ -593,7 +593,7 @@ __global__ void __launch_bounds__(128) k_force_list(Dev d, StateView s)
             const int j = jn;
             const float4 hj = hn, lj = ln;
             if (k + 1 < cnt) {
-                jn = __ldg(nl + (int64_t)(k + 1) * d.nbr_kstride);
+                jn = dbg_index(__ldg(nl + (int64_t)(k + 1) * d.nbr_kstride), d.n, (int)i, d.status);
                 hn = __ldg(&d.phi[jn]);
                 ln = __ldg(&d.plo[jn]);
             }
@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(256) k_force_list_lanes(Dev d, StateView s)
     // groups (LJ ensembles); longer lists keep fewer registers (more warps)
     auto pair_loop = [&](const auto& K) {
         for (int k = lane; k < cnt; k += LPA) {
-            int j = __ldg(nl + k);
+            int j = dbg_index(__ldg(nl + k), d.n, (int)ia, d.status);
             float4 hj = __ldg(&d.phi[j]), lj = __ldg(&d.plo[j]);
             PairOut o = pair_cutoff(d, R, K, ia, j, hi_i, lo_i, hj, lj, kqi, s.x);
             range_err |= o.range_err;

@@ -129,7 +129,7 @@ struct Stager {
         while (q < q1 && cnt <= ML_STAGE - 4) {
             int jj[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) jj[u] = (q + u < q1) ? col[(int64_t)(q + u) * n] : -1;
+            for (int u = 0; u < 4; ++u) jj[u] = (q + u < q1) ? dbg_index(col[(int64_t)(q + u) * n], d.n, -1, d.status) : -1;
             float4 hh[4], ll[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256) k_short_list(Dev d, MLView m, StepRef pos
         bool take = false;
         int j = 0;
         if (k < cnt) {
-            j = nl[(int64_t)k * d.nbr_kstride];
+            j = dbg_index(nl[(int64_t)k * d.nbr_kstride], d.n, (int)i, d.status);
             float3 dr = split_diff(hi, lo, d.phi[j], d.plo[j], true, R);
             take = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z < m.rs2;
         }
@@ -218,7 +218,7 @@ struct NbrCursor {
     __device__ __forceinline__ void load(const Dev& d)
     {
         if (q < q1) {
-            jn = col[(int64_t)q * stride];
+            jn = dbg_index(col[(int64_t)q * stride], d.n, 0, d.status);
             hn = d.phi[jn];
             ln = d.plo[jn];
         }

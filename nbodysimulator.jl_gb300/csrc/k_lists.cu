@@ -146,7 +146,7 @@ __global__ void k_list_build(Dev d, ListCtl L, const double* X)
                     int m = d.cell_n[cell];
                     const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
                     for (int k = 0; k < m; ++k) {
-                        int j = atoms[k];
+                        int j = dbg_index(atoms[k], d.n, (int)i, d.status);
                         if (j == (int)i) continue;
                         if (water && (j / 3 == (int)(i / 3))) continue;  // intramolecular: never a pair
                         float4 hj = d.phi[j], lj = d.plo[j];
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(256) k_list_build_lanes(Dev d, ListCtl L, cons
                     bool take = false;
                     int j = 0;
                     if (k < m) {
-                        j = atoms[k];
+                        j = dbg_index(atoms[k], d.n, (int)i, d.status);
                         if (j != (int)i && !(water && (j / 3 == (int)(i / 3)))) {
                             float3 dr = split_diff(hi, lo, d.phi[j], d.plo[j], true, R);
                             float r2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
@@ -320,8 +320,14 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_list_build_warps(Dev d, ListC
         const int* atoms = d.cell_atoms + (int64_t)cell * d.cell_cap;
         for (int a0 = c0; a0 < cnt; a0 += 32 * chunks) {
             const int a = a0 + lane;
+#ifdef NBG_DEBUG
+            const int i_read = a < cnt ? atoms[a] : -1;
+            const bool active = a < cnt && dbg_index(i_read, d.n, -1, d.status) >= 0;
+            const int i = active ? i_read : -1;
+#else
             const bool active = a < cnt;
             const int i = active ? atoms[a] : -1;
+#endif
             const float4 hi = active ? d.phi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
             const int mol0 = water && active ? 3 * (i / 3) : -8;  // first atom of i's molecule
             int* row = d.nbr + (int64_t)(active ? i : 0) * d.nbr_istride;
@@ -335,7 +341,7 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_list_build_warps(Dev d, ListC
             if (q < nnb) {
                 const int cq = nb_code[wid][q] & 0xffffff;
                 if (lane < nb_cnt[wid][q]) {
-                    jn = d.cell_atoms[(int64_t)cq * d.cell_cap + lane];
+                    jn = dbg_index(d.cell_atoms[(int64_t)cq * d.cell_cap + lane], d.n, 0, d.status);
                     hn = d.phi[jn];
                 }
             }
@@ -356,7 +362,7 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_list_build_warps(Dev d, ListC
                     const int cq2 = nb_code[wid][q2] & 0xffffff;
                     jn = -1;
                     if (b2 + lane < nb_cnt[wid][q2]) {
-                        jn = d.cell_atoms[(int64_t)cq2 * d.cell_cap + b2 + lane];
+                        jn = dbg_index(d.cell_atoms[(int64_t)cq2 * d.cell_cap + b2 + lane], d.n, 0, d.status);
                         hn = d.phi[jn];
                     }
                 }
@@ -391,8 +397,26 @@ __global__ void __launch_bounds__(LW_WARPS * 32) k_list_build_warps(Dev d, ListC
     }
 }
 
+#ifdef NBG_DEBUG
+// Debug builds only: entry 0 of atom 0's Verlet-list row (nbr[0] in both
+// layouts) becomes n + k, an index past every per-atom buffer, so that the
+// tests see the list readers' index checks report it (NBG_ERR_INDEX).
+__global__ void k_plant_index(Dev d, int k)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0 && d.nbr_count[0] > 0) d.nbr[0] = (int)(d.n + k);
+}
+
+int launch_plant_index(nbg_ctx* c, int k)
+{
+    k_plant_index<<<1, 32, 0, c->stream>>>(c->d, k);
+    NBG_LAUNCH_CHECK(c, "k_plant_index");
+    return NBG_OK;
+}
+#endif
+
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos)
 {
+    NBG_RANGE("launch_list_build");
     c->accel_lists_valid = false;  // the lists follow other positions now
     c->ens_lists_valid = false;
     ListCtl L{pos, force ? 1 : 0};

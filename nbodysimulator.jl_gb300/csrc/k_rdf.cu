@@ -542,6 +542,7 @@ bool is_device_pointer(const void* p)
 extern "C" int nbg_rdf_histogram(const double* frames, int64_t nframes, int64_t ncols, const int32_t* idx,
                                  int64_t nidx, double L, int32_t maxbin, int device, double* hist)
 {
+    NBG_RANGE("nbg_rdf_histogram");
     if (!hist || nframes < 0 || ncols < 0 || nidx < 0 || !(L > 0.0) || !std::isfinite(L) || maxbin < 1 ||
         maxbin > RDF_MAXBIN || nidx > (int64_t)1 << 30)
         return NBG_ERR_ARG;

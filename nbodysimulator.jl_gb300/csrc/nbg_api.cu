@@ -577,6 +577,9 @@ static int build_context(nbg_ctx* c, const nbg_system_desc* descs, int nrep)
         c->cluster_test_drop = strncmp(td, "last", 4) == 0 ? -1 : std::max(0, atoi(td));
         if (const char* k = strchr(td, ':')) c->cluster_test_skip = std::max(0, atoi(k + 1));
     }
+#ifdef NBG_DEBUG
+    if (const char* pv = getenv("NBG_TEST_PLANT_INDEX")) c->plant_index = std::max(1, atoi(pv));
+#endif
     if ((st = plan_cluster(c))) return st;
     if (getenv("NBG_NO_ENSEMBLE_LOOP")) c->ens_disabled = true;  // batches on the step graphs (comparisons)
     if (ensemble_plan(c)) {
@@ -755,6 +758,7 @@ static void release(nbg_ctx* c)
 
 extern "C" int nbg_create_batch(const nbg_system_desc* descs, int32_t n_replicas, int device, nbg_ctx** out)
 {
+    NBG_RANGE("nbg_create_batch");
     if (!out) return NBG_ERR_ARG;
     *out = nullptr;
     if (!descs || n_replicas < 1) return NBG_ERR_ARG;
@@ -864,6 +868,7 @@ static int ensure_hw(nbg_ctx* c)
 
 static int status_error(nbg_ctx* c, unsigned st)
 {
+    if (st & ST_INDEX) return fail(c, NBG_ERR_INDEX, "a neighbour or cell index out of range (debug build check)");
     if (st & ST_NONFINITE) return fail(c, NBG_ERR_NONFINITE, "non-finite acceleration (NaN/Inf state or coincident bodies)");
     if (st & ST_RANGE) return fail(c, NBG_ERR_RANGE, "minimum-image loop exceeded its iteration cap");
     if (st & ST_TIMEOUT) return fail(c, NBG_ERR_TIMEOUT, "a device-side wait for data from other blocks ran out");
@@ -876,11 +881,22 @@ static int status_error(nbg_ctx* c, unsigned st)
 // pos: time index of the positions in s (its parity picks the rebuild flag).
 static int forces(nbg_ctx* c, const StateView& s, bool force_build, StepRef pos)
 {
+    NBG_RANGE("forces");
     int st = NBG_OK;
     if (c->path == PATH_GRAVITY) {
         st = launch_gravity(c, s);
     } else if (c->path == PATH_LIST) {
         if ((st = launch_list_build(c, s, force_build, pos))) return st;
+#ifdef NBG_DEBUG
+        if (c->plant_index) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            CK(cudaStreamIsCapturing(c->stream, &cs), "capture query");
+            if (cs == cudaStreamCaptureStatusNone) {
+                if ((st = launch_plant_index(c, c->plant_index))) return st;
+                c->plant_index = 0;
+            }
+        }
+#endif
         st = launch_force_list(c, s);
     } else {
         st = launch_allpairs(c, s);
@@ -918,7 +934,7 @@ static int forces_once(nbg_ctx* c, const StateView& s)
         if ((st = forces(c, s, true, StepRef{0, nullptr}))) return st;
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
-        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
+        if (w & ST_FATAL) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if ((st = grow_lists(c, w))) return st;
             continue;
@@ -1056,6 +1072,7 @@ static int accel_cluster(nbg_ctx* c, double* dv, const double* u)
 
 extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, double t)
 {
+    NBG_RANGE("nbg_accel");
     (void)t;
     if (!c || !dv || !v || !u) return NBG_ERR_ARG;
     NBG_ENTER(c);
@@ -1081,7 +1098,7 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
             c->launches += c->accel_graph_launches;
             CK(cudaStreamSynchronize(c->stream), "accel sync");
             const unsigned w = *reinterpret_cast<const unsigned*>(c->hst + 9 * c->cols);
-            if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
+            if (w & ST_FATAL) return status_error(c, w);
             if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
                 if ((st = grow_lists(c, w))) return st;  // (drops the graph: captured again above)
                 continue;
@@ -1114,7 +1131,7 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
                "v download");
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
-        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
+        if (w & ST_FATAL) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if ((st = grow_lists(c, w))) return st;
             continue;
@@ -1126,6 +1143,7 @@ extern "C" int nbg_accel(nbg_ctx* c, double* dv, double* v, const double* u, dou
 
 extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
 {
+    NBG_RANGE("nbg_set_state");
     if (!c || !u || !v) return NBG_ERR_ARG;
     NBG_ENTER(c);
     CK(cudaMemcpyAsync(c->st.x, u, state_bytes(c), cudaMemcpyHostToDevice, c->stream), "u upload");
@@ -1146,6 +1164,7 @@ extern "C" int nbg_set_state(nbg_ctx* c, const double* u, const double* v)
 
 extern "C" int nbg_get_state(nbg_ctx* c, double* u, double* v)
 {
+    NBG_RANGE("nbg_get_state");
     if (!c || (!u && !v)) return NBG_ERR_ARG;
     NBG_ENTER(c);
     if (u) CK(cudaMemcpyAsync(u, c->st.x, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "u download");
@@ -1172,6 +1191,7 @@ extern "C" int nbg_set_step(nbg_ctx* c, int64_t step)
 
 extern "C" int nbg_compute_forces(nbg_ctx* c)
 {
+    NBG_RANGE("nbg_compute_forces");
     if (!c) return NBG_ERR_ARG;
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
     NBG_ENTER(c);
@@ -1184,6 +1204,7 @@ extern "C" int nbg_compute_forces(nbg_ctx* c)
 
 extern "C" int nbg_get_accel(nbg_ctx* c, double* dv)
 {
+    NBG_RANGE("nbg_get_accel");
     if (!c || !dv) return NBG_ERR_ARG;
     NBG_ENTER(c);
     CK(cudaMemcpyAsync(dv, c->st.a_new, state_bytes(c), cudaMemcpyDeviceToHost, c->stream), "a download");
@@ -1446,7 +1467,7 @@ static int settle(nbg_ctx* c)
         c->T_valid = false;
         return status_error(c, ST_TIMEOUT);
     }
-    if (w & (ST_NONFINITE | ST_RANGE)) return status_error(c, w);
+    if (w & (ST_NONFINITE | ST_RANGE | ST_INDEX)) return status_error(c, w);
     if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
         if ((st = grow_lists(c, w))) return st;
         if ((st = backup_state(c, true))) return st;
@@ -1584,7 +1605,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
             c->T_valid = false;
             return status_error(c, ST_TIMEOUT);  // (whatever else the abandoned steps flagged)
         }
-        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
+        if (w & ST_FATAL) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) {
             if (++retries > 6) return fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough");
             if ((st = grow_lists(c, w))) return st;
@@ -1606,6 +1627,7 @@ static int advance_impl(nbg_ctx* c, double dt, int64_t nsteps, bool defer)
 
 extern "C" int nbg_advance(nbg_ctx* c, double dt, int64_t nsteps)
 {
+    NBG_RANGE("nbg_advance");
     if (!c) return NBG_ERR_ARG;
     NBG_ENTER(c);
     return advance_impl(c, dt, nsteps, true);
@@ -1613,6 +1635,7 @@ extern "C" int nbg_advance(nbg_ctx* c, double dt, int64_t nsteps)
 
 extern "C" int nbg_sync(nbg_ctx* c)
 {
+    NBG_RANGE("nbg_sync");
     if (!c) return NBG_ERR_ARG;
     NBG_ENTER(c);
     CK(cudaStreamSynchronize(c->stream), "sync");
@@ -1622,6 +1645,7 @@ extern "C" int nbg_sync(nbg_ctx* c)
 extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nsteps, int64_t save_every,
                        double* traj_u, double* traj_v, nbg_run_stats* stats)
 {
+    NBG_RANGE("nbg_run");
     if (!c || !u || !v) return NBG_ERR_ARG;
     if (!(dt > 0.0) || nsteps < 0) return fail(c, NBG_ERR_ARG, "dt must be > 0 and nsteps >= 0");
     NBG_ENTER(c);
@@ -1712,6 +1736,7 @@ extern "C" int nbg_run(nbg_ctx* c, double* u, double* v, double dt, int64_t nste
 
 extern "C" int nbg_energy(nbg_ctx* c, const double* u, const double* v, nbg_energies* out)
 {
+    NBG_RANGE("nbg_energy");
     if (!c || !u || !v || !out) return NBG_ERR_ARG;
     if (c->nrep != 1) return fail(c, NBG_ERR_UNSUPPORTED, "energies are per system (create one context per replica)");
     NBG_ENTER(c);
@@ -1725,7 +1750,7 @@ extern "C" int nbg_energy(nbg_ctx* c, const double* u, const double* v, nbg_ener
         if ((st = launch_energy(c, c->ev, h))) return st;
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
-        if (attempt < 6 && (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && !(w & (ST_NONFINITE | ST_RANGE))) {
+        if (attempt < 6 && (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && !(w & (ST_NONFINITE | ST_RANGE | ST_INDEX))) {
             if ((st = grow_lists(c, w))) return st;
             continue;
         }
@@ -1746,6 +1771,7 @@ extern "C" int nbg_energy(nbg_ctx* c, const double* u, const double* v, nbg_ener
 
 extern "C" int nbg_pair_list(nbg_ctx* c, const double* u, int32_t which, int32_t* pairs, int64_t cap, int64_t* count)
 {
+    NBG_RANGE("nbg_pair_list");
     if (!c || !u || !count || (which != NBG_POT_LJ && which != NBG_POT_EL)) return NBG_ERR_ARG;
     if (!(c->d.pots & which)) return fail(c, NBG_ERR_ARG, "potential not present");
     if (c->path == PATH_GRAVITY) return fail(c, NBG_ERR_UNSUPPORTED, "gravity has no pair list");
@@ -1958,7 +1984,7 @@ static int ml_eval_once(nbg_ctx* c, const double* u, int what)
         }
         unsigned w = 0;
         if ((st = read_status(c, &w))) return st;
-        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return status_error(c, w);
+        if (w & ST_FATAL) return status_error(c, w);
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW)) {
             if ((w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && (st = grow_lists(c, w))) return st;
             if ((w & ST_SHORT_OVERFLOW) && (st = ml_alloc_short(c, c->ml_scap + c->ml_scap / 2 + 32))) return st;
@@ -1971,6 +1997,7 @@ static int ml_eval_once(nbg_ctx* c, const double* u, int what)
 
 extern "C" int nbg_ml_descriptors(nbg_ctx* c, const double* u, int32_t standardised, float* desc)
 {
+    NBG_RANGE("nbg_ml_descriptors");
     int st = ml_check(c);
     if (st) return st;
     if (!u || !desc) return fail(c, NBG_ERR_ARG, "null argument");
@@ -1982,6 +2009,7 @@ extern "C" int nbg_ml_descriptors(nbg_ctx* c, const double* u, int32_t standardi
 
 extern "C" int nbg_ml_eval(nbg_ctx* c, const double* u, float* energies, double* forces)
 {
+    NBG_RANGE("nbg_ml_eval");
     int st = ml_check(c);
     if (st) return st;
     if (!u) return fail(c, NBG_ERR_ARG, "null positions");
@@ -1999,6 +2027,7 @@ extern "C" int nbg_ml_eval(nbg_ctx* c, const double* u, float* energies, double*
 
 extern "C" int nbg_ml_labels(nbg_ctx* c, const double* u, float* energies, float* forces)
 {
+    NBG_RANGE("nbg_ml_labels");
     int st = ml_check(c);
     if (st) return st;
     if (!u) return fail(c, NBG_ERR_ARG, "null positions");
@@ -2033,6 +2062,7 @@ extern "C" int nbg_ml_reserve(nbg_ctx* c, int64_t frames)
 
 extern "C" int nbg_ml_collect(nbg_ctx* c, int64_t* rows)
 {
+    NBG_RANGE("nbg_ml_collect");
     int st = ml_check(c);
     if (st) return st;
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
@@ -2060,6 +2090,7 @@ extern "C" int nbg_ml_collect(nbg_ctx* c, int64_t* rows)
 
 extern "C" int nbg_ml_normalize(nbg_ctx* c)
 {
+    NBG_RANGE("nbg_ml_normalize");
     int st = ml_check(c);
     if (st) return st;
     if (c->ml_rows[0] < 2 || c->ml_rows[1] < 2) return fail(c, NBG_ERR_ARG, "training set holds fewer than 2 rows");
@@ -2099,6 +2130,7 @@ static int ml_scratch(nbg_ctx* c, int B)
 
 extern "C" int nbg_ml_train(nbg_ctx* c, int64_t steps, int32_t batch, double lr, uint64_t seed, double* loss)
 {
+    NBG_RANGE("nbg_ml_train");
     int st = ml_check(c);
     if (st) return st;
     if (steps < 0 || batch < 1 || !(lr > 0.0)) return fail(c, NBG_ERR_ARG, "steps >= 0, batch >= 1, lr > 0");
@@ -2250,6 +2282,7 @@ static int respa_outer(nbg_ctx* c, double dt, int inner, StepRef sr, int exact)
 extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer, double threshold, int32_t flags,
                              nbg_respa_stats* out)
 {
+    NBG_RANGE("nbg_respa_run");
     // (named `exact` for the fast-force mode: see respa_inner_force)
     const int exact = (flags & NBG_RESPA_NO_FAST_FORCE) ? 2 : (flags & NBG_RESPA_EXACT_SPLIT) ? 1 : 0;
     int st = ml_check(c);
@@ -2300,7 +2333,7 @@ extern "C" int nbg_respa_run(nbg_ctx* c, double dt, int32_t inner, int64_t outer
             c->T_valid = false;
             return clear_status(c);
         };
-        if (w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT)) return done_with(status_error(c, w));
+        if (w & ST_FATAL) return done_with(status_error(c, w));
         if (w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW | ST_SHORT_OVERFLOW)) {
             if (++retries > 6) return done_with(fail(c, NBG_ERR_CAPACITY, "list capacity could not be grown enough"));
             if ((w & (ST_CELL_OVERFLOW | ST_NBR_OVERFLOW)) && (st = grow_lists(c, w))) return done_with(st);
@@ -2396,6 +2429,7 @@ extern "C" int nbg_ml_kernel_times(nbg_ctx* c, int32_t reps, double* ms)
 // and keep the fastest for this context.
 extern "C" int nbg_autotune(nbg_ctx* c, int32_t reps, int32_t* lpa_out, double* ms_out)
 {
+    NBG_RANGE("nbg_autotune");
     if (!c) return NBG_ERR_ARG;
     if (c->path != PATH_LIST) return fail(c, NBG_ERR_UNSUPPORTED, "autotuning applies to the Verlet-list path");
     if (!c->state_valid) return fail(c, NBG_ERR_ARG, "no resident state (call nbg_set_state)");
@@ -2454,6 +2488,7 @@ extern "C" int nbg_autotune(nbg_ctx* c, int32_t reps, int32_t* lpa_out, double* 
 // step counter are put back after each, and the fastest form is kept.
 extern "C" int nbg_ensemble_tune(nbg_ctx* c, int32_t steps, int32_t* form, double* ms_out)
 {
+    NBG_RANGE("nbg_ensemble_tune");
     if (!c) return NBG_ERR_ARG;
     NBG_ENTER(c);
     if (!c->ens_ok && !c->ens_tuned_off)
@@ -2503,7 +2538,7 @@ extern "C" int nbg_ensemble_tune(nbg_ctx* c, int32_t steps, int32_t* form, doubl
             if ((st = read_status(c, &w))) break;
             float t = 0.f;
             cudaEventElapsedTime(&t, e0, e1);
-            if (!(w & (ST_NONFINITE | ST_RANGE | ST_TIMEOUT))) ms = (double)t / steps;
+            if (!(w & ST_FATAL)) ms = (double)t / steps;
             if ((st = backup_state(c, true))) break;
         }
         if (ms_out) ms_out[f] = ms;

@@ -21,7 +21,36 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/nbg.h"
+
+// NVTX ranges in the domain "nbg" around the library's calls and the host
+// side of their phases (list build, forces, integration chunks). Without an
+// attached tool (Nsight Systems, Nsight Compute) a push or pop is one test of
+// a null callback. Inside a stream capture a range marks the capture, not
+// the graph's later replays.
+inline nvtxDomainHandle_t nbg_nvtx_domain()
+{
+    static nvtxDomainHandle_t dom = nvtxDomainCreateA("nbg");
+    return dom;
+}
+
+struct NbgRange {
+    explicit NbgRange(const char* name)
+    {
+        nvtxEventAttributes_t a = {};
+        a.version = NVTX_VERSION;
+        a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+        a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+        a.message.ascii = name;
+        nvtxDomainRangePushEx(nbg_nvtx_domain(), &a);
+    }
+    ~NbgRange() { nvtxDomainRangePop(nbg_nvtx_domain()); }
+    NbgRange(const NbgRange&) = delete;
+    NbgRange& operator=(const NbgRange&) = delete;
+};
+#define NBG_RANGE(name) NbgRange nbg_range_scope_(name)
 
 // device status word bits
 #define ST_CELL_OVERFLOW 1u
@@ -30,6 +59,9 @@
 #define ST_RANGE 8u
 #define ST_SHORT_OVERFLOW 16u  // learned-model short list
 #define ST_TIMEOUT 32u         // a bounded wait in a kernel ran out
+#define ST_INDEX 64u           // debug builds: a neighbour or cell index out of range
+// bits that end a call with an error (the others regrow capacity)
+#define ST_FATAL (ST_NONFINITE | ST_RANGE | ST_TIMEOUT | ST_INDEX)
 
 // atom flags (plo.w bits)
 #define AF_LJ 1
@@ -257,6 +289,10 @@ struct nbg_ctx {
     // cluster_test_skip others drops the position copies of this step (-1:
     // its last step; -2: none)
     int cluster_test_drop = -2;
+    // debug builds: NBG_TEST_PLANT_INDEX=k writes n + k into the first entry
+    // of atom 0's Verlet-list row after the next list build outside a stream
+    // capture (one shot), for the tests of the index checks
+    int plant_index = 0;
     int cluster_test_skip = 0;
     bool grav_uniform = false;  // every body has mass grav_m0: the reduction applies G m
     float grav_far2 = 256.f;    // a tile pair is far when (F g)^2 >= max|r|^2, F = 16
@@ -371,6 +407,9 @@ int launch_cluster_accel(nbg_ctx* c, const double* u, double* dv, unsigned* stat
 int cluster_launch_floor(nbg_ctx* c, double* us_single, double* us_per_launch);
 int launch_allpairs(nbg_ctx* c, const StateView& s);
 int launch_list_build(nbg_ctx* c, const StateView& s, bool force, StepRef pos);
+#ifdef NBG_DEBUG
+int launch_plant_index(nbg_ctx* c, int k);
+#endif
 int launch_force_list(nbg_ctx* c, const StateView& s);
 int fx_prepare(nbg_ctx* c);
 int launch_force_fx(nbg_ctx* c, const StateView& s);
@@ -447,6 +486,24 @@ static inline int grid_for(int64_t work, int block)
 __device__ __forceinline__ int64_t step_of(StepRef r) { return r.off + (r.base ? *r.base : 0); }
 
 __device__ __forceinline__ void status_set(unsigned* st, unsigned bit) { atomicOr(st, bit); }
+
+// Debug builds (nvcc -DNBG_DEBUG, libnbg_debug.so): every neighbour or cell
+// index that a kernel reads from a device table is checked against [0, n)
+// before it is used; one outside sets ST_INDEX (NBG_ERR_INDEX on the host)
+// and is replaced by `safe`, an index known to be valid, so the kernel ends
+// without touching memory outside its buffers. Release builds return j.
+__device__ __forceinline__ int dbg_index(int j, int64_t n, int safe, unsigned* st)
+{
+#ifdef NBG_DEBUG
+    if (j < 0 || (int64_t)j >= n) {
+        status_set(st, ST_INDEX);
+        return safe;
+    }
+#else
+    (void)n, (void)safe, (void)st;
+#endif
+    return j;
+}
 
 // x is neither infinite nor NaN (the exponent field is not all ones), by
 // integer operations: FP64 compares issue slowly on this GPU

@@ -143,6 +143,23 @@ def test_library_exports_every_header_symbol():
     assert b"sm_103a" in loaded.nbg_version()
 
 
+def test_debug_library_builds_and_exports_every_header_symbol():
+    """The debug build (nvcc -DNBG_DEBUG: index checks on every neighbour and
+    cell table read) compiles for sm_103a, loads without a GPU and exports the
+    same functions; NBG_ERR_INDEX is in the header and in the status names."""
+    import __graft_entry__ as g
+    lib_build = g._load_by_path("nbg_lib_build", os.path.join(ROOT, "nbodysimulator.jl_gb300", "build.py"))
+    path = lib_build.build(debug=True)
+    assert path.endswith("libnbg_debug.so")
+    lib = ctypes.CDLL(path)
+    for n in _header_functions():
+        assert hasattr(lib, n), n
+    assert lib.nbg_abi_version() == nbg._abi.NBG_ABI_VERSION
+    with open(os.path.join(ROOT, "include", "nbg.h")) as f:
+        assert re.search(r"NBG_ERR_INDEX\s*=\s*-9", f.read())
+    assert nbg._abi.STATUS_NAMES[-9] == "NBG_ERR_INDEX"
+
+
 def test_result_analysis_at_saved_times():
     """gravitational_test.jl:26-41: get_position / get_velocity of body 1 at
     the first saved time are its initial values exactly, get_masses the

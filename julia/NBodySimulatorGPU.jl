@@ -39,6 +39,7 @@ const NBG_THERMO_NULL, NBG_THERMO_ANDERSEN, NBG_THERMO_BERENDSEN, NBG_THERMO_NOS
       NBG_THERMO_LANGEVIN = Int32(0), Int32(1), Int32(2), Int32(3), Int32(4)
 const NBG_FLAG_LANGEVIN_BAOAB = Int32(4)
 const NBG_ERR_UNSUPPORTED = Cint(-6)
+const NBG_ERR_INDEX = Cint(-9)  # libnbg_debug.so (NBG_LIBRARY): a list or cell index out of range
 
 # layout of nbg_system_desc (include/nbg.h), field for field
 mutable struct NbgSystemDesc
